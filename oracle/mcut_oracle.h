@@ -1,0 +1,59 @@
+/*
+ * CPU oracle for the MCUT intersection front end (test infrastructure only).
+ *
+ * Two implementations fill the same result record:
+ *   - mcut_oracle.c      : a plain-C restatement of the reference algorithm
+ *                          (builds anywhere, including the aarch64 GPU host);
+ *   - ref_harness.cpp    : drives the unmodified reference sources compiled
+ *                          into _ref/libmcut_ref.so (only where the reference
+ *                          checkout exists).
+ * The product library never links, loads or calls either of them.
+ *
+ * Identifiers follow the reference's polygon soup ("ps", kernel.cpp:1593-1732):
+ *   ps vertex ids : source vertices [0, Vs), cut-mesh vertices [Vs, Vs+Vc)
+ *   ps face ids   : source faces [0, Fs),    cut-mesh faces   [Fs, Fs+Fc)
+ *   an edge       : (q, r) = source/target vertex of its primary halfedge,
+ *                   i.e. the orientation it has in the lowest-numbered face
+ *                   that contains it (hmesh.cpp:405-651, add_edge/add_face).
+ */
+#ifndef MCUT_ORACLE_H
+#define MCUT_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (kernel.h:52-92 mapped to the front end) */
+enum {
+    FE_OK = 0,
+    FE_GP_VIOLATION = 1,       /* a touching / on-edge / on-vertex configuration */
+    FE_DEGENERATE_SRC_FACE = 2,/* candidate source face with |Newell n|^2 < 1e-9 */
+    FE_DEGENERATE_CUT_FACE = 3,
+    FE_INVALID_INPUT = 4
+};
+
+/* One dispatch of the front end. All arrays are malloc'd by the producer and
+ * released with the producer's free function. Tests/records are in canonical
+ * order: ascending (q, r, face). */
+typedef struct fe_result {
+    int32_t status;
+    int32_t bad_face;          /* ps face id of a degenerate face, else -1 */
+    double cut_eps;            /* cut-mesh face-box enlargement */
+    int64_t n_pairs;
+    uint32_t *pairs;           /* 2*n_pairs: (source face, cut face), ascending */
+    int64_t n_tests;
+    uint32_t *tests;           /* 3*n_tests: (q, r, face) of each culled edge-face test */
+    int8_t *test_info;         /* 4*n_tests: sign(orient3d q), sign(orient3d r), type char, pip char */
+    int64_t n_records;
+    uint32_t *rec_ids;         /* 3*n_records: (q, r, face) */
+    double *rec_pts;           /* 3*n_records */
+    double *face_boxes;        /* 6*(Fs+Fc): min xyz, max xyz (cut boxes enlarged) */
+    double *src_xyz;           /* 3*Vs recentred coordinates */
+    double *cut_xyz;           /* 3*Vc recentred coordinates */
+} fe_result;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

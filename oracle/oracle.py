@@ -1,0 +1,164 @@
+"""ctypes front for the CPU oracles (test infrastructure only).
+
+    front_end(src, cut, impl="port")  -> dict   plain-C restatement (liboracle.so)
+    front_end(src, cut, impl="ref")   -> dict   the unmodified reference (_ref/libref_harness.so)
+    dispatch(src, cut, flags)         -> dict   full reference mcDispatch (CC counts)
+
+Only tests, the package's smoke check and the CPU-baseline leg of bench.py
+import this module. The product path never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_harness.so")
+
+FE_OK, FE_GP_VIOLATION, FE_DEGENERATE_SRC_FACE, FE_DEGENERATE_CUT_FACE, FE_INVALID_INPUT = range(5)
+MC_DISPATCH_VERTEX_ARRAY_FLOAT = 1 << 0
+MC_DISPATCH_VERTEX_ARRAY_DOUBLE = 1 << 1
+MC_DISPATCH_ENFORCE_GENERAL_POSITION = 1 << 15
+
+
+class FeResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("bad_face", C.c_int32), ("cut_eps", C.c_double),
+        ("n_pairs", C.c_int64), ("pairs", C.POINTER(C.c_uint32)),
+        ("n_tests", C.c_int64), ("tests", C.POINTER(C.c_uint32)), ("test_info", C.POINTER(C.c_int8)),
+        ("n_records", C.c_int64), ("rec_ids", C.POINTER(C.c_uint32)), ("rec_pts", C.POINTER(C.c_double)),
+        ("face_boxes", C.POINTER(C.c_double)), ("src_xyz", C.POINTER(C.c_double)),
+        ("cut_xyz", C.POINTER(C.c_double)),
+    ]
+
+
+_libs = {}
+
+
+def build(ref: bool = False, ref_root: str | None = None) -> None:
+    """Compile liboracle.so (and, with ref=True, the reference harness) via the Makefile."""
+    cmd = ["make", "-s", "-C", HERE] + (["ref"] if ref else ["liboracle.so"])
+    if ref_root:
+        cmd.append(f"REF_ROOT={ref_root}")
+    subprocess.run(cmd, check=True)
+
+
+def _lib(impl: str):
+    if impl in _libs:
+        return _libs[impl]
+    path = PORT_LIB if impl == "port" else REF_LIB
+    if not os.path.exists(path):
+        build(ref=(impl == "ref"))
+    lib = C.CDLL(path)
+    fn = lib.oracle_front_end if impl == "port" else lib.ref_front_end
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                   C.c_int, C.c_int, C.POINTER(FeResult)]
+    fr = lib.oracle_free if impl == "port" else lib.ref_free
+    fr.argtypes = [C.POINTER(FeResult)]
+    if impl == "ref":
+        for nm, k in (("ref_orient3d", 4), ("ref_orient2d", 3)):
+            getattr(lib, nm).restype = C.c_double
+            getattr(lib, nm).argtypes = [C.c_void_p] * k
+        lib.ref_dispatch.restype = C.c_int
+        lib.ref_dispatch.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                     C.c_uint32, C.c_int, C.c_char_p, C.c_void_p, C.c_int,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_long)]
+    _libs[impl] = (lib, fn, fr)
+    return _libs[impl]
+
+
+def _mesh_args(m, float_input=False):
+    v = np.ascontiguousarray(m["v"], dtype=np.float32 if float_input else np.float64)
+    f = np.ascontiguousarray(m["f"], dtype=np.uint32)
+    fs = None if m.get("fs") is None else np.ascontiguousarray(m["fs"], dtype=np.uint32)
+    nf = int(fs.shape[0]) if fs is not None else int(f.shape[0] // 3)
+    keep = (v, f, fs)
+    return keep, [v.ctypes.data, f.ctypes.data, None if fs is None else fs.ctypes.data, v.shape[0], nf]
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def front_end(src, cut, impl: str = "port", threads: int = 0, float_input: bool = False):
+    """Run one front-end dispatch; canonical-ordered numpy outputs."""
+    lib, fn, fr = _lib(impl)
+    ks, sa = _mesh_args(src, float_input)
+    kc, ca = _mesh_args(cut, float_input)
+    res = FeResult()
+    rc = fn(*sa, *ca, int(bool(float_input)), int(threads), C.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"oracle front_end failed rc={rc}")
+    nsf, ncf = sa[4], ca[4]
+    out = dict(
+        status=int(res.status), bad_face=int(res.bad_face), cut_eps=float(res.cut_eps),
+        pairs=_arr(res.pairs, 2 * res.n_pairs, np.uint32).reshape(-1, 2),
+        tests=_arr(res.tests, 3 * res.n_tests, np.uint32).reshape(-1, 3),
+        test_info=_arr(res.test_info, 4 * res.n_tests, np.int8).reshape(-1, 4),
+        rec_ids=_arr(res.rec_ids, 3 * res.n_records, np.uint32).reshape(-1, 3),
+        rec_pts=_arr(res.rec_pts, 3 * res.n_records, np.float64).reshape(-1, 3),
+        face_boxes=_arr(res.face_boxes, 6 * (nsf + ncf), np.float64).reshape(-1, 6),
+        src_xyz=_arr(res.src_xyz, 3 * sa[3], np.float64).reshape(-1, 3),
+        cut_xyz=_arr(res.cut_xyz, 3 * ca[3], np.float64).reshape(-1, 3),
+    )
+    fr(C.byref(res))
+    del ks, kc
+    return out
+
+
+def _pts(*ps):
+    return [np.ascontiguousarray(p, dtype=np.float64) for p in ps]
+
+
+def ref_orient3d(a, b, c, d) -> float:
+    lib, _, _ = _lib("ref")
+    k = _pts(a, b, c, d)
+    return lib.ref_orient3d(*[x.ctypes.data for x in k])
+
+
+def ref_orient2d(a, b, c) -> float:
+    lib, _, _ = _lib("ref")
+    k = _pts(a, b, c)
+    return lib.ref_orient2d(*[x.ctypes.data for x in k])
+
+
+def port_orient3d_sign(a, b, c, d) -> int:
+    lib, _, _ = _lib("port")
+    lib.oracle_orient3d_sign.argtypes = [C.c_void_p] * 4
+    k = _pts(a, b, c, d)
+    return lib.oracle_orient3d_sign(*[x.ctypes.data for x in k])
+
+
+def port_orient2d(a, b, c) -> float:
+    lib, _, _ = _lib("port")
+    lib.oracle_orient2d.restype = C.c_double
+    lib.oracle_orient2d.argtypes = [C.c_void_p] * 3
+    k = _pts(a, b, c)
+    return lib.oracle_orient2d(*[x.ctypes.data for x in k])
+
+
+def dispatch(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: int = 0, max_cc: int = 4096):
+    """Full reference mcDispatch. Returns status, CCs as (type, nverts, nfaces), and
+    the intersection-point count of the last kernel invocation."""
+    lib, _, _ = _lib("ref")
+    fin = bool(flags & MC_DISPATCH_VERTEX_ARRAY_FLOAT)
+    ks, sa = _mesh_args(src, fin)
+    kc, ca = _mesh_args(cut, fin)
+    info = np.zeros((max_cc, 3), dtype=np.int32)
+    ncc = C.c_int(0)
+    niv = C.c_long(-1)
+    with tempfile.TemporaryDirectory() as td:
+        rc = lib.ref_dispatch(*sa, *ca, int(flags), int(helpers), td.encode(), info.ctypes.data, max_cc,
+                              C.byref(ncc), C.byref(niv))
+    del ks, kc
+    return dict(result=rc, ccs=info[:ncc.value].copy(), n_ivtx=int(niv.value))

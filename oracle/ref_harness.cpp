@@ -1,0 +1,395 @@
+// Harness around the UNMODIFIED reference (MCUT 1.2.0) compiled into
+// _ref/libmcut_ref.so from its own sources. Test infrastructure only: it is
+// built where the reference checkout exists, pins the plain-C oracle and
+// generates golden fixtures; nothing in the product links it.
+//
+// What it exposes (extern "C", consumed through ctypes by tests/golden/make_golden.py):
+//   ref_front_end : the front end of one dispatch, step for step as
+//                   preproc.cpp:2292-2926 and kernel.cpp:1593-2878 run it,
+//                   calling the reference's own build_oibvh, intersectOIBVHs,
+//                   compute_polygon_plane_coefficients,
+//                   compute_segment_plane_intersection_type,
+//                   compute_segment_plane_intersection,
+//                   compute_point_in_polygon_test and ::orient3d.
+//                   The only restated parts are the container plumbing of
+//                   kernel.cpp (edge->faces map, culling loop), which the
+//                   reference keeps inside dispatch().
+//   ref_dispatch  : the full public API (mcCreateContext / mcDispatch /
+//                   mcGetConnectedComponents / mcGetConnectedComponentData)
+//                   returning status and per-CC type / vertex / face counts,
+//                   plus the intersection-point count read back from the
+//                   reference's own verbose dumps (kernel.cpp:1736-1738,3260-3266).
+#include <mcut/mcut.h>
+#include <mcut/internal/bvh.h>
+#include <mcut/internal/hmesh.h>
+#include <mcut/internal/math.h>
+#include <mcut/internal/tpool.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <tuple>
+#include <unistd.h>
+#include <vector>
+
+#include "mcut_oracle.h"
+
+bool calculate_vertex_parameters(double& quantization_multiplier, vec3_<double>& pre_quantization_translation,
+    vec3_<double>& srcmesh_cutmesh_com, vec3_<double>& srcmesh_bboxmin, vec3_<double>& srcmesh_bboxmax,
+    vec3_<double>& cutmesh_bboxmin, vec3_<double>& cutmesh_bboxmax, McFlags dispatchFlags,
+    const void* pSrcMeshVertices, McUint32 numSrcMeshVertices, const void* pCutMeshVertices,
+    McUint32 numCutMeshVertices);
+bool determine_three_noncollinear_vertices(int& i, int& j, int& k, const std::vector<vec3>& polygon_vertices,
+    const vec3& polygon_normal, const int polygon_normal_largest_component, const double multiplier);
+
+namespace {
+
+struct Mesh {
+    const void* v; // double[3*nv], or float[3*nv] for float input
+    const uint32_t* f;
+    const uint32_t* fs; // nullable -> triangles
+    uint32_t nv, nf;
+};
+
+// Recentring exactly as client_input_arrays_to_hmesh does it (preproc.cpp:100-181):
+// float input is recentred in float arithmetic, then widened.
+void recentre(const Mesh& m, bool fin, const vec3_<double>& com, const vec3_<double>& t, std::vector<double>& out)
+{
+    out.resize((size_t)m.nv * 3);
+    for (uint32_t i = 0; i < m.nv; ++i)
+        for (int j = 0; j < 3; ++j) {
+            if (fin) {
+                const float x = (((const float*)m.v)[i * 3 + j] - (float)com[j]) + (float)t[j];
+                out[i * 3 + j] = double(x);
+            } else {
+                out[i * 3 + j] = (((const double*)m.v)[i * 3 + j] - com[j]) + t[j];
+            }
+        }
+}
+
+void add_faces(hmesh_t& h, const Mesh& m, uint32_t voff)
+{
+    size_t o = 0;
+    std::vector<vd_t> fv;
+    for (uint32_t f = 0; f < m.nf; ++f) {
+        const uint32_t n = m.fs ? m.fs[f] : 3;
+        fv.clear();
+        for (uint32_t j = 0; j < n; ++j)
+            fv.push_back(vd_t(m.f[o + j] + voff));
+        o += n;
+        h.add_face(fv);
+    }
+}
+
+template <class T>
+T* dup(const std::vector<T>& v)
+{
+    T* p = (T*)malloc(std::max<size_t>(1, v.size() * sizeof(T)));
+    if (!v.empty())
+        memcpy(p, v.data(), v.size() * sizeof(T));
+    return p;
+}
+
+int sgn(double x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
+
+} // namespace
+
+extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
+    const void* cv, const uint32_t* cf, const uint32_t* cfs, uint32_t ncv, uint32_t ncf,
+    int float_input, int n_helpers, fe_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    out->bad_face = -1;
+    Mesh S { sv, sf, sfs, nsv, nsf }, C { cv, cf, cfs, ncv, ncf };
+
+    double multiplier = 1;
+    vec3_<double> smin, smax, cmin, cmax, com, trans;
+    calculate_vertex_parameters(multiplier, trans, com, smin, smax, cmin, cmax,
+        float_input ? MC_DISPATCH_VERTEX_ARRAY_FLOAT : MC_DISPATCH_VERTEX_ARRAY_DOUBLE, sv, nsv, cv, ncv);
+    std::vector<double> sx, cx;
+    recentre(S, float_input != 0, com, trans, sx);
+    recentre(C, float_input != 0, com, trans, cx);
+    out->src_xyz = dup(sx);
+    out->cut_xyz = dup(cx);
+
+    // cut-mesh enlargement: diag length of the (translated) cut box times the
+    // default general-position constant (preproc.cpp:2518, 2667-2676; frontend.h:596)
+    const double cut_diag = length(cmax - cmin, 1);
+    const double eps = cut_diag * 1e-4;
+    out->cut_eps = eps;
+
+    hmesh_t sm, cm, ps;
+    for (uint32_t i = 0; i < nsv; ++i) {
+        sm.add_vertex(sx[i * 3], sx[i * 3 + 1], sx[i * 3 + 2]);
+        ps.add_vertex(sx[i * 3], sx[i * 3 + 1], sx[i * 3 + 2]);
+    }
+    for (uint32_t i = 0; i < ncv; ++i) {
+        cm.add_vertex(cx[i * 3], cx[i * 3 + 1], cx[i * 3 + 2]);
+        ps.add_vertex(cx[i * 3], cx[i * 3 + 1], cx[i * 3 + 2]);
+    }
+    add_faces(sm, S, 0);
+    add_faces(cm, C, 0);
+    add_faces(ps, S, 0);
+    add_faces(ps, C, nsv);
+
+    thread_pool pool((uint32_t)n_helpers, 0);
+    std::vector<bounding_box_t<vec3_<double>>> sAABB, cAABB, sFB, cFB;
+    std::vector<fd_t> sLeaf, cLeaf;
+    build_oibvh(pool, sm, sAABB, sLeaf, sFB, 0.0, multiplier);
+    build_oibvh(pool, cm, cAABB, cLeaf, cFB, eps, multiplier);
+
+    std::vector<double> boxes;
+    for (auto& b : sFB)
+        for (int k = 0; k < 2; ++k)
+            for (int j = 0; j < 3; ++j)
+                boxes.push_back(k ? b.maximum()[j] : b.minimum()[j]);
+    for (auto& b : cFB)
+        for (int k = 0; k < 2; ++k)
+            for (int j = 0; j < 3; ++j)
+                boxes.push_back(k ? b.maximum()[j] : b.minimum()[j]);
+    out->face_boxes = dup(boxes);
+
+    std::map<fd_t, std::vector<fd_t>> cand;
+    intersectOIBVHs(cand, sAABB, sLeaf, cAABB, cLeaf);
+
+    std::vector<uint32_t> pairs;
+    for (auto& kv : cand)
+        if ((uint32_t)kv.first < nsf)
+            for (fd_t g : kv.second) {
+                pairs.push_back((uint32_t)kv.first);
+                pairs.push_back((uint32_t)g - nsf);
+            }
+    {
+        std::vector<std::pair<uint32_t, uint32_t>> pp;
+        for (size_t i = 0; i < pairs.size(); i += 2)
+            pp.emplace_back(pairs[i], pairs[i + 1]);
+        std::sort(pp.begin(), pp.end());
+        pairs.clear();
+        for (auto& p : pp) {
+            pairs.push_back(p.first);
+            pairs.push_back(p.second);
+        }
+    }
+    out->n_pairs = (int64_t)pairs.size() / 2;
+    out->pairs = dup(pairs);
+    if (cand.empty()) {
+        out->tests = dup(std::vector<uint32_t>());
+        out->test_info = dup(std::vector<int8_t>());
+        out->rec_ids = dup(std::vector<uint32_t>());
+        out->rec_pts = dup(std::vector<double>());
+        return 0;
+    }
+
+    // edge -> sorted union of partner faces (kernel.cpp:1781-1983)
+    std::map<uint32_t, std::set<uint32_t>> e2f;
+    for (auto& kv : cand) {
+        for (hd_t h : ps.get_halfedges_around_face(kv.first)) {
+            auto& s = e2f[(uint32_t)ps.edge(h)];
+            for (fd_t g : kv.second)
+                s.insert((uint32_t)g);
+        }
+    }
+
+    // face properties for every candidate face, degenerate check (kernel.cpp:2184-2356)
+    std::map<uint32_t, std::tuple<vec3, double, int, std::vector<vec3>>> props;
+    for (auto& kv : cand) {
+        std::vector<vec3> fverts;
+        for (vd_t v : ps.get_vertices_around_face(kv.first))
+            fverts.push_back(ps.vertex(v));
+        vec3 n(0.0);
+        double d = 0;
+        int mc = compute_polygon_plane_coefficients(n, d, fverts.data(), (int)fverts.size(), multiplier);
+        if (squared_length(n) == 0 || std::isnan(n.x()) || std::isnan(n.y()) || std::isnan(n.z())) {
+            if (out->bad_face < 0 || (int)kv.first < out->bad_face)
+                out->bad_face = (int)kv.first;
+        }
+        props[(uint32_t)kv.first] = std::make_tuple(n, d, mc, fverts);
+    }
+    if (out->bad_face >= 0)
+        out->status = (uint32_t)out->bad_face >= nsf ? FE_DEGENERATE_CUT_FACE : FE_DEGENERATE_SRC_FACE;
+
+    // culling + narrow phase (kernel.cpp:2074-2177, 2456-2658)
+    std::vector<std::tuple<uint32_t, uint32_t, uint32_t, int8_t, int8_t, int8_t, int8_t>> tests;
+    std::vector<std::tuple<uint32_t, uint32_t, uint32_t, double, double, double>> recs;
+    bool gp = false;
+    for (auto& ef : e2f) {
+        const ed_t e((uint32_t)ef.first);
+        const hd_t h0 = ps.halfedge(e, 0);
+        const vd_t qd = ps.source(h0), rd = ps.target(h0);
+        const vec3 q = ps.vertex(qd), r = ps.vertex(rd);
+        bounding_box_t<vec3_<double>> eb;
+        eb.expand(ps.vertex(ps.vertex(e, 0)));
+        eb.expand(ps.vertex(ps.vertex(e, 1)));
+        for (uint32_t g : ef.second) {
+            const bounding_box_t<vec3_<double>>& fb = g < nsf ? sFB[g] : cFB[g - nsf];
+            if (!intersect_bounding_boxes(eb, fb))
+                continue;
+            if (out->status != FE_OK && out->status != FE_GP_VIOLATION)
+                continue; // the reference stops before the narrow phase on a degenerate face
+            auto& pr = props[g];
+            const vec3& n = std::get<0>(pr);
+            const double d = std::get<1>(pr);
+            const int mc = std::get<2>(pr);
+            const std::vector<vec3>& fv = std::get<3>(pr);
+            int i = 0, j = 1, k = 2;
+            if (fv.size() > 3)
+                determine_three_noncollinear_vertices(i, j, k, fv, n, mc, multiplier);
+            const int8_t sq = (int8_t)sgn(orient3d(fv[i], fv[j], fv[k], q));
+            const int8_t sr = (int8_t)sgn(orient3d(fv[i], fv[j], fv[k], r));
+            const char type = compute_segment_plane_intersection_type(q, r, fv, n, mc, multiplier);
+            char pip = 0;
+            if (type == 'q' || type == 'r') {
+                pip = compute_point_in_polygon_test(type == 'q' ? q : r, fv, n, mc, multiplier);
+            } else if (type == 'p') {
+                pip = compute_point_in_polygon_test(q, fv, n, mc, multiplier);
+                if (!(pip == 'i' || pip == 'v' || pip == 'e'))
+                    pip = compute_point_in_polygon_test(r, fv, n, mc, multiplier);
+            } else if (type == '1') {
+                vec3 p(0., 0., 0.);
+                compute_segment_plane_intersection(p, n, d, q, r);
+                pip = compute_point_in_polygon_test(p, fv, n, mc, multiplier);
+                if (pip == 'i')
+                    recs.emplace_back((uint32_t)qd, (uint32_t)rd, g, p.x(), p.y(), p.z());
+            }
+            if ((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
+                gp = true;
+            if (type == '1' && (pip == 'v' || pip == 'e'))
+                gp = true;
+            tests.emplace_back((uint32_t)qd, (uint32_t)rd, g, sq, sr, (int8_t)type, (int8_t)pip);
+        }
+    }
+    if (out->status == FE_OK && gp)
+        out->status = FE_GP_VIOLATION;
+    std::sort(tests.begin(), tests.end());
+    std::sort(recs.begin(), recs.end(), [](const auto& a, const auto& b) {
+        return std::make_tuple(std::get<0>(a), std::get<1>(a), std::get<2>(a))
+            < std::make_tuple(std::get<0>(b), std::get<1>(b), std::get<2>(b));
+    });
+    std::vector<uint32_t> tid, rid;
+    std::vector<int8_t> tinfo;
+    std::vector<double> rpt;
+    for (auto& t : tests) {
+        tid.push_back(std::get<0>(t));
+        tid.push_back(std::get<1>(t));
+        tid.push_back(std::get<2>(t));
+        tinfo.push_back(std::get<3>(t));
+        tinfo.push_back(std::get<4>(t));
+        tinfo.push_back(std::get<5>(t));
+        tinfo.push_back(std::get<6>(t));
+    }
+    for (auto& r : recs) {
+        rid.push_back(std::get<0>(r));
+        rid.push_back(std::get<1>(r));
+        rid.push_back(std::get<2>(r));
+        rpt.push_back(std::get<3>(r));
+        rpt.push_back(std::get<4>(r));
+        rpt.push_back(std::get<5>(r));
+    }
+    out->n_tests = (int64_t)tests.size();
+    out->tests = dup(tid);
+    out->test_info = dup(tinfo);
+    out->n_records = (int64_t)recs.size();
+    out->rec_ids = dup(rid);
+    out->rec_pts = dup(rpt);
+    return 0;
+}
+
+extern "C" double ref_orient3d(const double* pa, const double* pb, const double* pc, const double* pd)
+{
+    return ::orient3d((double*)pa, (double*)pb, (double*)pc, (double*)pd);
+}
+extern "C" double ref_orient2d(const double* pa, const double* pb, const double* pc)
+{
+    return ::orient2d((double*)pa, (double*)pb, (double*)pc);
+}
+
+extern "C" void ref_free(fe_result* r)
+{
+    free(r->pairs);
+    free(r->tests);
+    free(r->test_info);
+    free(r->rec_ids);
+    free(r->rec_pts);
+    free(r->face_boxes);
+    free(r->src_xyz);
+    free(r->cut_xyz);
+    memset(r, 0, sizeof(*r));
+}
+
+static long off_vertex_count(const char* path)
+{
+    FILE* f = fopen(path, "r");
+    if (!f)
+        return -1;
+    char line[256];
+    long nv = -1;
+    while (fgets(line, sizeof line, f)) {
+        if (line[0] == '#' || line[0] == '\n' || strncmp(line, "OFF", 3) == 0)
+            continue;
+        nv = strtol(line, nullptr, 10);
+        break;
+    }
+    fclose(f);
+    return nv;
+}
+
+// Full public-API dispatch. cc_info receives, per connected component,
+// (type, vertex count, face count), capacity max_cc. workdir receives the
+// reference's verbose dumps. Returns the McResult of mcDispatch; *n_cc and
+// *n_ivtx (intersection points of the last kernel invocation) are filled on
+// success.
+extern "C" int ref_dispatch(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
+    const void* cv, const uint32_t* cf, const uint32_t* cfs, uint32_t ncv, uint32_t ncf, uint32_t flags,
+    int n_helpers, const char* workdir, int32_t* cc_info, int max_cc, int* n_cc, long* n_ivtx)
+{
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd))
+        return -1000;
+    if (workdir && chdir(workdir) != 0)
+        return -1001;
+    McContext ctx = MC_NULL_HANDLE;
+    McResult err = n_helpers > 0 ? mcCreateContextWithHelpers(&ctx, MC_NULL_HANDLE, (McUint32)n_helpers)
+                                 : mcCreateContext(&ctx, MC_NULL_HANDLE);
+    if (err == MC_NO_ERROR) {
+        err = mcDispatch(ctx, flags, sv, sf, sfs, nsv, nsf, cv, cf, cfs, ncv, ncf);
+    }
+    *n_cc = 0;
+    *n_ivtx = -1;
+    if (err == MC_NO_ERROR) {
+        McUint32 n = 0;
+        mcGetConnectedComponents(ctx, MC_CONNECTED_COMPONENT_TYPE_ALL, 0, NULL, &n);
+        std::vector<McConnectedComponent> ccs(n);
+        if (n)
+            mcGetConnectedComponents(ctx, MC_CONNECTED_COMPONENT_TYPE_ALL, n, ccs.data(), NULL);
+        for (McUint32 i = 0; i < n && (int)i < max_cc; ++i) {
+            McSize nb = 0;
+            McConnectedComponentType t;
+            mcGetConnectedComponentData(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_TYPE, sizeof(t), &t, NULL);
+            mcGetConnectedComponentData(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_VERTEX_DOUBLE, 0, NULL, &nb);
+            const long nvtx = (long)(nb / (3 * sizeof(double)));
+            mcGetConnectedComponentData(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_FACE_SIZE, 0, NULL, &nb);
+            const long nfc = (long)(nb / sizeof(McUint32));
+            cc_info[i * 3 + 0] = (int32_t)t;
+            cc_info[i * 3 + 1] = (int32_t)nvtx;
+            cc_info[i * 3 + 2] = (int32_t)nfc;
+        }
+        *n_cc = (int)n;
+        if (n)
+            mcReleaseConnectedComponents(ctx, 0, NULL);
+        const long m0v = off_vertex_count("m0.v.off");
+        const long psv = off_vertex_count("polygon-soup.off");
+        if (m0v >= 0 && psv >= 0)
+            *n_ivtx = m0v - psv;
+    }
+    if (ctx != MC_NULL_HANDLE)
+        mcReleaseContext(ctx);
+    if (workdir && chdir(cwd) != 0)
+        return -1002;
+    return (int)err;
+}
