@@ -1,0 +1,159 @@
+/*
+ * mcut_gb300 — GB300-native intersection front end for MCUT, C ABI.
+ *
+ * This library replaces the data-parallel front end of one MCUT dispatch:
+ *
+ *   reference seam                                   replaced by
+ *   -----------------------------------------------  ---------------------------
+ *   build_oibvh(src) / build_oibvh(cut, eps)          mcgpu_dispatch (stage 1: face
+ *     source/preproc.cpp:2456, 2685                     boxes, Morton codes, radix
+ *     source/bvh.cpp:219-636                            sort, LBVH + refit)
+ *   intersectOIBVHs(...)                              mcgpu_dispatch (stage 2:
+ *     source/preproc.cpp:2839, bvh.cpp:638-783          tree traversal -> face pairs)
+ *   dispatch() front section                          mcgpu_dispatch (stage 3: edge /
+ *     source/kernel.cpp:1781-3206                       face expansion, culling,
+ *                                                       planes, orient3d narrow
+ *                                                       phase, records + points)
+ *
+ * Everything downstream of the records (cut-path tracing, polygon clipping,
+ * connected components; kernel.cpp:3332 onwards) stays in the host C++ that
+ * calls this library. Plain pointers and sizes only; no C++ or torch types.
+ *
+ * Identifiers are the reference's polygon-soup ("ps") ids of one dispatch
+ * (kernel.cpp:1593-1732): vertices [0,Vs) source then [Vs,Vs+Vc) cut mesh,
+ * faces [0,Fs) source then [Fs,Fs+Fc) cut mesh. An edge is reported as
+ * (q, r): source and target of its primary halfedge, i.e. its direction in
+ * the lowest-numbered face containing it (hmesh.cpp:405-651), with f0 that
+ * face and f1 the other face or 0xFFFFFFFF on a border.
+ *
+ * Threading: a context owns one CUDA stream and its device memory; calls on
+ * one context must be serialised by the caller (MCUT runs one API thread per
+ * context, frontend.h:548-580). Different contexts may run concurrently.
+ * Errors never abort the process: every entry point returns an mcgpu_status.
+ */
+#ifndef MCUT_GB300_H
+#define MCUT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mcgpu_context_t* mcgpu_context;
+
+/* Results of a front-end dispatch. GP_VIOLATION / DEGENERATE_* are valid
+ * outcomes of the algorithm (the reference reports them as status_t values,
+ * kernel.h:52-92, and mcDispatch turns them into MC_INVALID_OPERATION);
+ * the others are failures of the call. */
+typedef enum mcgpu_status {
+    MCGPU_OK = 0,
+    MCGPU_GP_VIOLATION = 1,        /* touching / on-edge / on-vertex configuration */
+    MCGPU_DEGENERATE_SRC_FACE = 2, /* a candidate source face has |Newell n|^2 < 1e-9 */
+    MCGPU_DEGENERATE_CUT_FACE = 3,
+    MCGPU_INVALID_INPUT = 4,       /* face size < 3, index out of range, non-manifold edge */
+    MCGPU_CUDA_ERROR = 5,
+    MCGPU_OUT_OF_MEMORY = 6,
+    MCGPU_INVALID_VALUE = 7,       /* bad argument (null pointer, unknown query, ...) */
+    MCGPU_TOO_LARGE = 8            /* exceeds a fixed capacity of the entry point */
+} mcgpu_status;
+
+/* dispatch flags */
+#define MCGPU_VERTEX_ARRAY_FLOAT (1u << 0) /* vertices are float[3*V] (MC_DISPATCH_VERTEX_ARRAY_FLOAT) */
+#define MCGPU_RECENTRE (1u << 1)           /* vertices are user coordinates: apply preproc's
+                                              recentring (preproc.cpp:2124-2290, 147-181) and
+                                              derive cut_eps = |cut box diagonal| * 1e-4 */
+#define MCGPU_KEEP_TESTS (1u << 2)         /* keep every culled edge-face test and its predicates */
+#define MCGPU_KEEP_PAIRS (1u << 3)         /* keep the candidate face pairs */
+#define MCGPU_PROFILE (1u << 4)            /* time the stages with CUDA events */
+#define MCGPU_DEVICE_POINTERS (1u << 5)    /* mesh arrays are device pointers (recentred, double) */
+
+typedef struct mcgpu_mesh {
+    const void* vertices;         /* double[3*num_vertices], float with MCGPU_VERTEX_ARRAY_FLOAT */
+    const uint32_t* face_indices; /* concatenated face-vertex indices */
+    const uint32_t* face_sizes;   /* NULL: all faces are triangles (preproc.cpp:206) */
+    uint32_t num_vertices;
+    uint32_t num_faces;
+} mcgpu_mesh;
+
+/* stage_ms[] slots filled with MCGPU_PROFILE */
+enum {
+    MCGPU_STAGE_UPLOAD = 0,   /* host->device copies */
+    MCGPU_STAGE_BOUNDS = 1,   /* face boxes, mesh boxes, Morton codes */
+    MCGPU_STAGE_SORT = 2,     /* radix sorts */
+    MCGPU_STAGE_HIERARCHY = 3,/* LBVH hierarchy + refit */
+    MCGPU_STAGE_TRAVERSE = 4, /* tree traversal -> candidate pairs */
+    MCGPU_STAGE_ADJACENCY = 5,/* vertex->face incidence + face planes */
+    MCGPU_STAGE_NARROW = 6,   /* edge-face expansion, culling, narrow phase, records */
+    MCGPU_STAGE_DOWNLOAD = 7  /* device->host copies */
+};
+
+typedef struct mcgpu_summary {
+    int32_t status;           /* mcgpu_status of the front end */
+    int32_t bad_face;         /* lowest degenerate candidate ps face, or -1 */
+    double cut_eps;           /* cut-mesh face-box enlargement used */
+    uint64_t num_pairs;       /* candidate (source face, cut face) pairs */
+    uint64_t num_tests;       /* culled edge-face tests */
+    uint64_t num_records;     /* intersection records (type '1', point inside) */
+    uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, exact stage */
+    float stage_ms[8];        /* per-stage device time (MCGPU_PROFILE) */
+} mcgpu_summary;
+
+/* mcgpu_get_data queries */
+typedef enum mcgpu_data {
+    MCGPU_DATA_RECORD_IDS = 1,    /* uint32[5*R]: q, r, tested face, f0, f1 (edge creation order, then face) */
+    MCGPU_DATA_RECORD_POINTS = 2, /* double[3*R]: intersection points (recentred coordinates) */
+    MCGPU_DATA_PAIRS = 3,         /* uint32[2*P]: (source face, cut face); MCGPU_KEEP_PAIRS */
+    MCGPU_DATA_TESTS = 4,         /* uint32[3*T]: q, r, face; MCGPU_KEEP_TESTS */
+    MCGPU_DATA_TEST_INFO = 5,     /* int8[4*T]: sign(orient3d q), sign(orient3d r), type char, pip char */
+    MCGPU_DATA_VERTICES = 6,      /* double[3*(Vs+Vc)]: the ps coordinates used */
+    MCGPU_DATA_FACE_BOXES = 7     /* double[6*(Fs+Fc)]: min xyz, max xyz (cut boxes enlarged) */
+} mcgpu_data;
+
+/* Context with its own stream and device memory pool on `device`.
+ * Replaces: nothing in the reference (mcCreateContext, mcut.cpp:62-86, makes
+ * the host context; the caller creates one of these beside it). */
+int mcgpu_context_create(mcgpu_context* ctx, int device);
+int mcgpu_context_release(mcgpu_context ctx);
+
+/* One front-end dispatch: source mesh `src` against cut mesh `cut`.
+ * Replaces build_oibvh x2 + intersectOIBVHs (preproc.cpp:2456, 2685, 2839;
+ * bvh.cpp:219-783) and kernel.cpp:1781-3206 of dispatch().
+ * Vertices are the reference's internal (recentred) coordinates unless
+ * MCGPU_RECENTRE is given; cut_eps is the cut-mesh box enlargement
+ * (preproc.cpp:2667-2693), ignored with MCGPU_RECENTRE. Host arrays are read
+ * before the call returns. Results stay in the context until the next
+ * dispatch on it. Returns MCGPU_OK when the call ran; the front end's own
+ * outcome is out->status. */
+int mcgpu_dispatch(mcgpu_context ctx, uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
+    mcgpu_summary* out);
+
+/* Copy a result array of the last dispatch. Two-call pattern as
+ * mcGetConnectedComponentData (mcut.cpp:806): mem == NULL && bytes == 0
+ * returns the size in *bytes_out. */
+int mcgpu_get_data(mcgpu_context ctx, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out);
+
+/* Many independent pairs in one pass (one launch per stage over all pairs).
+ * Replaces n_pairs sequential mcDispatch front ends. Per-pair results are
+ * summaries[i] and mcgpu_get_batch_data(ctx, i, ...). cut_eps may be NULL
+ * with MCGPU_RECENTRE. */
+int mcgpu_dispatch_batch(mcgpu_context ctx, uint32_t flags, uint32_t n_pairs, const mcgpu_mesh* srcs,
+    const mcgpu_mesh* cuts, const double* cut_eps, mcgpu_summary* summaries);
+int mcgpu_get_batch_data(mcgpu_context ctx, uint32_t pair, uint32_t query, uint64_t bytes, void* mem,
+    uint64_t* bytes_out);
+
+/* The reference's recentring on the host (calculate_vertex_parameters +
+ * client_input_arrays_to_hmesh, preproc.cpp:2124-2290, 147-181): writes the
+ * internal coordinates of both meshes and the default cut-box enlargement
+ * (|translated cut box diagonal| * 1e-4, preproc.cpp:2518, 2667-2676). */
+int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut, double* src_out, double* cut_out,
+    double* cut_eps_out);
+
+/* Human-readable description of the last failure on this thread. */
+const char* mcgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCUT_GB300_H */

@@ -1,0 +1,92 @@
+"""ctypes binding of libmcut_gb300.so (the C ABI declared in include/mcut_gb300.h).
+
+The library is the product: there is no CPU fallback. Loading fails loudly
+when it has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmcut_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "mcut_gb300.h")
+
+OK, GP_VIOLATION, DEGENERATE_SRC_FACE, DEGENERATE_CUT_FACE, INVALID_INPUT, CUDA_ERROR, OUT_OF_MEMORY, \
+    INVALID_VALUE, TOO_LARGE = range(9)
+STATUS_NAMES = ["OK", "GP_VIOLATION", "DEGENERATE_SRC_FACE", "DEGENERATE_CUT_FACE", "INVALID_INPUT",
+                "CUDA_ERROR", "OUT_OF_MEMORY", "INVALID_VALUE", "TOO_LARGE"]
+
+VERTEX_ARRAY_FLOAT = 1 << 0
+RECENTRE = 1 << 1
+KEEP_TESTS = 1 << 2
+KEEP_PAIRS = 1 << 3
+PROFILE = 1 << 4
+DEVICE_POINTERS = 1 << 5
+
+DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DATA_VERTICES, DATA_FACE_BOXES = \
+    range(1, 8)
+
+STAGES = ["upload", "bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow", "download"]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("face_indices", C.c_void_p), ("face_sizes", C.c_void_p),
+                ("num_vertices", C.c_uint32), ("num_faces", C.c_uint32)]
+
+
+class Summary(C.Structure):
+    _fields_ = [("status", C.c_int32), ("bad_face", C.c_int32), ("cut_eps", C.c_double),
+                ("num_pairs", C.c_uint64), ("num_tests", C.c_uint64), ("num_records", C.c_uint64),
+                ("escalations", C.c_uint64 * 3), ("stage_ms", C.c_float * 8)]
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def exported_names_in_header(path: str = HEADER):
+    """Every function the C header declares."""
+    txt = open(path).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(mcgpu_\w+)\s*\(", txt, re.M)))
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise LibraryNotBuilt(f"{LIB_PATH} is missing: run `python -m mcut_gb300.build` (needs nvcc)")
+    lib = C.CDLL(LIB_PATH)
+    ctx = C.c_void_p
+    lib.mcgpu_context_create.argtypes = [C.POINTER(ctx), C.c_int]
+    lib.mcgpu_context_release.argtypes = [ctx]
+    lib.mcgpu_dispatch.argtypes = [ctx, C.c_uint32, C.POINTER(Mesh), C.POINTER(Mesh), C.c_double,
+                                   C.POINTER(Summary)]
+    lib.mcgpu_dispatch_batch.argtypes = [ctx, C.c_uint32, C.c_uint32, C.POINTER(Mesh), C.POINTER(Mesh),
+                                         C.POINTER(C.c_double), C.POINTER(Summary)]
+    lib.mcgpu_get_data.argtypes = [ctx, C.c_uint32, C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.mcgpu_get_batch_data.argtypes = [ctx, C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p,
+                                         C.POINTER(C.c_uint64)]
+    lib.mcgpu_recentre.argtypes = [C.c_uint32, C.POINTER(Mesh), C.POINTER(Mesh), C.c_void_p, C.c_void_p,
+                                   C.POINTER(C.c_double)]
+    lib.mcgpu_last_error.restype = C.c_char_p
+    for name in exported_names_in_header():
+        if name not in ("mcgpu_last_error",):
+            getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().mcgpu_last_error().decode()
+
+
+def check(rc: int, what: str):
+    if rc != OK:
+        raise RuntimeError(f"{what} failed: {STATUS_NAMES[rc] if 0 <= rc < len(STATUS_NAMES) else rc}: "
+                           f"{last_error()}")

@@ -1,0 +1,746 @@
+// C ABI of the GB300 intersection front end: contexts, device memory,
+// stage orchestration, result retrieval.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fe_common.cuh"
+#include "fe_kernels.cuh"
+#include "fe_sort.cuh"
+#include "mcut_gb300.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+struct CudaError {
+    cudaError_t e;
+    std::string where;
+};
+
+inline void ck(cudaError_t e, const char* where)
+{
+    if (e != cudaSuccess) throw CudaError { e, where };
+}
+
+// grow-only device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <typename T>
+    T* get(size_t count)
+    {
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+        if (bytes > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            cap = 0;
+            size_t want = bytes + bytes / 4;
+            ck(cudaMalloc(&p, want), "cudaMalloc");
+            cap = want;
+        }
+        return reinterpret_cast<T*>(p);
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct PinBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <typename T>
+    T* get(size_t count)
+    {
+        const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+        if (bytes > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            size_t want = bytes + bytes / 4;
+            ck(cudaMallocHost(&p, want), "cudaMallocHost");
+            cap = want;
+        }
+        return reinterpret_cast<T*>(p);
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+enum BufId {
+    B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
+    B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
+    B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_COUNT
+};
+
+// host per-pair tables and results of the last dispatch
+struct Layout {
+    uint32_t n_pairs = 0;
+    std::vector<uint32_t> vbase, vs, fbase, fs, sbase, cbase, ibase, is; // ibase: index base, is: src index count
+    std::vector<double> eps;
+    uint64_t nv = 0, nf = 0, ns = 0, nc = 0, nidx = 0;
+    bool all_tri = true;
+    uint64_t tri_stride = 0, n_poly = 0;
+    uint32_t max_face = 3;
+};
+
+} // namespace
+
+struct mcgpu_context_t {
+    int device = 0;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[9] = {};
+    DevBuf buf[B_COUNT];
+    PinBuf pin_counters, pin_tab, pin_stage;
+    Layout L;
+    mcgpu::Problem P {};
+    mcgpu::Work W {};
+    std::vector<mcgpu_summary> sums;
+    std::vector<uint64_t> rec_begin;  // per pair, +1
+    uint64_t n_pairs_found = 0, n_tests = 0, n_records = 0;
+    uint32_t flags = 0;
+    int rec_buf = 0;
+};
+
+namespace {
+
+using namespace mcgpu;
+
+// ---------------------------------------------------------------------------
+// host recentring (calculate_vertex_parameters + client_input_arrays_to_hmesh,
+// preproc.cpp:2124-2290, 147-181)
+// ---------------------------------------------------------------------------
+double dmaxr(double a, double b) { return (a < b) ? b : a; }
+double dminr(double a, double b) { return (b < a) ? b : a; }
+float fmaxr(float a, float b) { return (a < b) ? b : a; }
+float fminr(float a, float b) { return (b < a) ? b : a; }
+
+void vertex_bounds(const void* v, bool fin, uint32_t n, double* mn, double* mx, double* com)
+{
+    for (int j = 0; j < 3; ++j) {
+        mn[j] = 1.7976931348623157e308;
+        mx[j] = -1.7976931348623157e308;
+        com[j] = 0.0;
+    }
+    if (fin) {
+        const float* p = (const float*)v;
+        for (uint32_t i = 0; i < n; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const float x = p[(size_t)i * 3 + j];
+                mx[j] = (double)fmaxr((float)mx[j], x);
+                mn[j] = (double)fminr((float)mn[j], x);
+                com[j] += (double)x;
+            }
+    } else {
+        const double* p = (const double*)v;
+        for (uint32_t i = 0; i < n; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const double x = p[(size_t)i * 3 + j];
+                mx[j] = dmaxr(mx[j], x);
+                mn[j] = dminr(mn[j], x);
+                com[j] += x;
+            }
+    }
+    for (int j = 0; j < 3; ++j) com[j] = com[j] / (double)n;
+}
+
+double hdot(const double* a, const double* b)
+{
+    double o = 0.0;
+    o = o + a[0] * b[0];
+    o = o + a[1] * b[1];
+    o = o + a[2] * b[2];
+    return o;
+}
+
+void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out)
+{
+    double smn[3], smx[3], scom[3], cmn[3], cmx[3], ccom[3], com[3], gmn[3], tp[3], t[3];
+    vertex_bounds(S.vertices, fin, S.num_vertices, smn, smx, scom);
+    vertex_bounds(Cm.vertices, fin, Cm.num_vertices, cmn, cmx, ccom);
+    for (int j = 0; j < 3; ++j) {
+        com[j] = (scom[j] + ccom[j]) / 2.0;
+        gmn[j] = dminr(smn[j], cmn[j]);
+        tp[j] = com[j] - gmn[j];
+    }
+    const double len = std::sqrt(hdot(tp, tp));
+    for (int j = 0; j < 3; ++j) t[j] = tp[j] + tp[j] / len;
+    auto conv = [&](const mcgpu_mesh& m, double* out) {
+        if (fin) {
+            const float* p = (const float*)m.vertices;
+            for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
+                const int j = (int)(k % 3);
+                const float x = (p[k] - (float)com[j]) + (float)t[j];
+                out[k] = (double)x;
+            }
+        } else {
+            const double* p = (const double*)m.vertices;
+            for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
+                const int j = (int)(k % 3);
+                out[k] = (p[k] - com[j]) + t[j];
+            }
+        }
+    };
+    conv(S, sx);
+    conv(Cm, cx);
+    double d[3];
+    for (int j = 0; j < 3; ++j) d[j] = (cmx[j] + t[j]) - (cmn[j] + t[j]);
+    *eps_out = std::sqrt(hdot(d, d)) * 1e-4;
+}
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint32_t* __restrict__ fidx, uint64_t nidx,
+    uint32_t* __restrict__ face_pair, uint64_t nf)
+{
+    // tab rows (n_pairs+1 each): ibase, is, vbase, vs, fbase, fs
+    const uint32_t* ibase = tab;
+    const uint32_t* is = tab + (n_pairs + 1);
+    const uint32_t* vbase = tab + 2 * (n_pairs + 1);
+    const uint32_t* vs = tab + 3 * (n_pairs + 1);
+    const uint32_t* fbase = tab + 4 * (n_pairs + 1);
+    const uint32_t* fs = tab + 5 * (n_pairs + 1);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nidx; i += stride) {
+        uint32_t lo = 0, hi = n_pairs; // last pair with ibase <= i
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (ibase[mid] <= i) lo = mid; else hi = mid;
+        }
+        const uint32_t p = lo;
+        const bool cut = (i - ibase[p]) >= is[p];
+        fidx[i] = fidx[i] + vbase[p] + (cut ? vs[p] : 0u);
+    }
+    for (uint64_t f = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; f < nf; f += stride) {
+        uint32_t lo = 0, hi = n_pairs;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (fbase[mid] <= f) lo = mid; else hi = mid;
+        }
+        const uint32_t p = lo;
+        face_pair[f] = p | (((f - fbase[p]) >= fs[p]) ? kCutBit : 0u);
+    }
+}
+
+__global__ void k_init_meshbox(unsigned long long* mb, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        mb[i] = (i % 6) < 3 ? ~0ull : 0ull;
+}
+
+int grid1(uint64_t n)
+{
+    const uint64_t g = (n + 255) / 256;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, 152 * 16));
+}
+
+uint32_t face_size(const mcgpu_mesh& m, uint32_t f) { return m.face_sizes ? m.face_sizes[f] : 3u; }
+
+int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts,
+    const double* eps)
+{
+    Layout& L = c->L;
+    L = Layout();
+    L.n_pairs = n;
+    L.vbase.resize(n + 1); L.vs.resize(n + 1); L.fbase.resize(n + 1); L.fs.resize(n + 1);
+    L.sbase.resize(n + 1); L.cbase.resize(n + 1); L.ibase.resize(n + 1); L.is.resize(n + 1);
+    L.eps.assign(n, 0.0);
+    uint64_t v = 0, f = 0, sf = 0, cf = 0, ix = 0;
+    for (uint32_t p = 0; p < n; ++p) {
+        const mcgpu_mesh &S = srcs[p], &C = cuts[p];
+        if (!S.vertices || !S.face_indices || !C.vertices || !C.face_indices)
+            return fail(MCGPU_INVALID_VALUE, "null mesh array");
+        if (S.num_vertices < 3 || C.num_vertices < 3 || S.num_faces < 1 || C.num_faces < 1)
+            return fail(MCGPU_INVALID_INPUT, "mesh needs >= 3 vertices and >= 1 face");
+        L.vbase[p] = (uint32_t)v; L.vs[p] = S.num_vertices;
+        L.fbase[p] = (uint32_t)f; L.fs[p] = S.num_faces;
+        L.sbase[p] = (uint32_t)sf; L.cbase[p] = (uint32_t)cf; L.ibase[p] = (uint32_t)ix;
+        uint64_t is = 0, ic = 0;
+        for (int side = 0; side < 2; ++side) {
+            const mcgpu_mesh& m = side ? C : S;
+            if (m.face_sizes) {
+                L.all_tri = false;
+                for (uint32_t k = 0; k < m.num_faces; ++k) {
+                    const uint32_t sz = m.face_sizes[k];
+                    if (sz < 3) return fail(MCGPU_INVALID_INPUT, "face with fewer than 3 vertices");
+                    (side ? ic : is) += sz;
+                    L.max_face = std::max(L.max_face, sz);
+                    if (sz > 3) {
+                        L.n_poly++;
+                        L.tri_stride = std::max<uint64_t>(L.tri_stride, (uint64_t)sz * (sz - 1) * (sz - 2) / 6);
+                    }
+                }
+            } else {
+                (side ? ic : is) += 3ull * m.num_faces;
+            }
+        }
+        L.is[p] = (uint32_t)is;
+        v += (uint64_t)S.num_vertices + C.num_vertices;
+        f += (uint64_t)S.num_faces + C.num_faces;
+        sf += S.num_faces;
+        cf += C.num_faces;
+        ix += is + ic;
+        if (eps && !(flags & MCGPU_RECENTRE)) L.eps[p] = eps[p];
+    }
+    if (v >= 0x7FFFFFFFull || f >= 0x7FFFFFFFull || ix >= 0xFFFFFFFFull)
+        return fail(MCGPU_TOO_LARGE, "more than 2^31 vertices / faces in one dispatch");
+    if (n > 65535) return fail(MCGPU_TOO_LARGE, "more than 65535 pairs in one batch");
+    L.vbase[n] = (uint32_t)v; L.fbase[n] = (uint32_t)f; L.sbase[n] = (uint32_t)sf; L.cbase[n] = (uint32_t)cf;
+    L.ibase[n] = (uint32_t)ix;
+    L.nv = v; L.nf = f; L.ns = sf; L.nc = cf; L.nidx = ix;
+    return MCGPU_OK;
+}
+
+// upload ps arrays: coordinates (recentred on the host when asked), indices, offsets
+void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts)
+{
+    Layout& L = c->L;
+    const uint32_t n = L.n_pairs;
+    cudaStream_t s = c->s;
+    double* X = c->buf[B_X].get<double>(L.nv * 3);
+    uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
+    const bool fin = (flags & MCGPU_VERTEX_ARRAY_FLOAT) != 0;
+    const bool dev = (flags & MCGPU_DEVICE_POINTERS) != 0;
+    if (flags & MCGPU_RECENTRE) {
+        double* st = c->pin_stage.get<double>(L.nv * 3);
+        for (uint32_t p = 0; p < n; ++p)
+            recentre_pair(fin, srcs[p], cuts[p], st + (size_t)L.vbase[p] * 3,
+                st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
+        ck(cudaMemcpyAsync(X, st, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s), "H2D X");
+    } else {
+        const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        for (uint32_t p = 0; p < n; ++p) {
+            ck(cudaMemcpyAsync(X + (size_t)L.vbase[p] * 3, srcs[p].vertices, (size_t)L.vs[p] * 3 * sizeof(double),
+                   kind, s), "H2D Xs");
+            ck(cudaMemcpyAsync(X + ((size_t)L.vbase[p] + L.vs[p]) * 3, cuts[p].vertices,
+                   (size_t)cuts[p].num_vertices * 3 * sizeof(double), kind, s), "H2D Xc");
+        }
+    }
+    const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    for (uint32_t p = 0; p < n; ++p) {
+        const uint64_t ic = (uint64_t)(p + 1 < n + 1 ? L.ibase[p + 1] : L.nidx) - L.ibase[p] - L.is[p];
+        ck(cudaMemcpyAsync(fidx + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, ikind, s), "H2D Is");
+        ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, ikind, s), "H2D Ic");
+    }
+    // per pair tables: ibase, is, vbase, vs, fbase, fs, sbase, cbase (n+1 each), eps
+    uint32_t* tab = c->pin_tab.get<uint32_t>((size_t)8 * (n + 1) + 2 * (size_t)(n + 1));
+    const std::vector<uint32_t>* rows[8] = { &L.ibase, &L.is, &L.vbase, &L.vs, &L.fbase, &L.fs, &L.sbase, &L.cbase };
+    for (int r = 0; r < 8; ++r) memcpy(tab + (size_t)r * (n + 1), rows[r]->data(), sizeof(uint32_t) * (n + 1));
+    double* teps = reinterpret_cast<double*>(tab + (size_t)8 * (n + 1) + ((8 * (n + 1)) & 1));
+    memcpy(teps, L.eps.data(), sizeof(double) * n);
+    uint32_t* dtab = c->buf[B_PTAB].get<uint32_t>((size_t)8 * (n + 1));
+    double* deps = c->buf[B_EPS].get<double>(n);
+    ck(cudaMemcpyAsync(dtab, tab, sizeof(uint32_t) * 8 * (n + 1), cudaMemcpyHostToDevice, s), "H2D tab");
+    ck(cudaMemcpyAsync(deps, teps, sizeof(double) * n, cudaMemcpyHostToDevice, s), "H2D eps");
+    uint32_t* foff = nullptr;
+    if (!L.all_tri) {
+        std::vector<uint32_t> off(L.nf + 1);
+        uint64_t o = 0, f = 0;
+        for (uint32_t p = 0; p < n; ++p)
+            for (int side = 0; side < 2; ++side) {
+                const mcgpu_mesh& m = side ? cuts[p] : srcs[p];
+                for (uint32_t k = 0; k < m.num_faces; ++k) {
+                    off[f++] = (uint32_t)o;
+                    o += face_size(m, k);
+                }
+            }
+        off[f] = (uint32_t)o;
+        foff = c->buf[B_FOFF].get<uint32_t>(L.nf + 1);
+        ck(cudaMemcpyAsync(foff, off.data(), sizeof(uint32_t) * (L.nf + 1), cudaMemcpyHostToDevice, s), "H2D foff");
+        ck(cudaStreamSynchronize(s), "sync foff"); // `off` is a pageable temporary
+    }
+    uint32_t* face_pair = c->buf[B_FPAIR].get<uint32_t>(L.nf);
+    k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf);
+
+    Problem& P = c->P;
+    P.n_pairs = n;
+    P.nv = (uint32_t)L.nv;
+    P.nf = (uint32_t)L.nf;
+    P.ns = (uint32_t)L.ns;
+    P.nc = (uint32_t)L.nc;
+    P.X = X;
+    P.foff = foff;
+    P.fidx = fidx;
+    P.face_pair = face_pair;
+    P.pair_fbase = dtab + 4 * (n + 1);
+    P.pair_fs = dtab + 5 * (n + 1);
+    P.pair_vbase = dtab + 2 * (n + 1);
+    P.pair_vs = dtab + 3 * (n + 1);
+    P.pair_sbase = dtab + 6 * (n + 1);
+    P.pair_cbase = dtab + 7 * (n + 1);
+    P.pair_eps = deps;
+    P.all_triangles = L.all_tri ? 1 : 0;
+}
+
+inline void rec(mcgpu_context_t* c, int i)
+{
+    if (c->flags & MCGPU_PROFILE) ck(cudaEventRecord(c->ev[i], c->s), "event");
+}
+
+int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts,
+    const double* eps, mcgpu_summary* out)
+{
+    if (!c || !srcs || !cuts || n == 0) return fail(MCGPU_INVALID_VALUE, "null argument");
+    if (flags & MCGPU_DEVICE_POINTERS && flags & (MCGPU_RECENTRE | MCGPU_VERTEX_ARRAY_FLOAT))
+        return fail(MCGPU_INVALID_VALUE, "device pointers must hold recentred double coordinates");
+    if (!(flags & MCGPU_RECENTRE) && !eps) return fail(MCGPU_INVALID_VALUE, "cut_eps required without RECENTRE");
+    if ((flags & MCGPU_VERTEX_ARRAY_FLOAT) && !(flags & MCGPU_RECENTRE))
+        return fail(MCGPU_INVALID_VALUE, "float vertices need MCGPU_RECENTRE");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    c->flags = flags;
+    int rc = build_layout(c, flags, n, srcs, cuts, eps);
+    if (rc != MCGPU_OK) return rc;
+    Layout& L = c->L;
+    cudaStream_t s = c->s;
+    rec(c, 0);
+    upload(c, flags, srcs, cuts);
+    rec(c, 1);
+
+    Problem& P = c->P;
+    Work& W = c->W;
+    const bool wide = n > 1;
+    const int pbits = n > 1 ? 32 - __builtin_clz(n - 1) : 0;
+    const int key_bits = kMortonBits + pbits;
+    // stage-1 buffers
+    W.fbox = c->buf[B_FBOX].get<double>(L.nf * 6);
+    W.mesh_box = c->buf[B_MESHBOX].get<unsigned long long>((size_t)n * 12);
+    const size_t ksz = wide ? 8 : 4;
+    W.skeys[0] = c->buf[B_SK0].get<uint8_t>(L.ns * ksz);
+    W.skeys[1] = c->buf[B_SK1].get<uint8_t>(L.ns * ksz);
+    W.svals[0] = c->buf[B_SV0].get<uint32_t>(L.ns);
+    W.svals[1] = c->buf[B_SV1].get<uint32_t>(L.ns);
+    W.ckeys[0] = c->buf[B_CK0].get<uint8_t>(L.nc * ksz);
+    W.ckeys[1] = c->buf[B_CK1].get<uint8_t>(L.nc * ksz);
+    W.cvals[0] = c->buf[B_CV0].get<uint32_t>(L.nc);
+    W.cvals[1] = c->buf[B_CV1].get<uint32_t>(L.nc);
+    W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.nc, 2) - 1);
+    W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.nc, 1));
+    W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.nc, 2));
+    W.counters = c->buf[B_COUNTERS].get<uint32_t>(16);
+    W.cand = c->buf[B_CAND].get<uint8_t>(L.nf);
+    W.pair_status = c->buf[B_PSTAT].get<uint32_t>(n);
+    W.pair_bad = c->buf[B_PBAD].get<int32_t>(n);
+    W.pair_nrec = c->buf[B_PNREC].get<uint32_t>(n);
+    W.scan_temp = c->buf[B_SCANTMP].get<uint32_t>(scan_temp_bytes((uint32_t)L.nv + 1) / 4 + 64);
+    if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
+    W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
+
+    // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
+    k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
+    ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
+    ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
+    ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+    ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
+    ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)n, s), "memset");
+
+    launch_bounds_morton(P, W, wide, s);
+    rec(c, 2);
+    W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(radix_sort_temp_bytes((uint32_t)std::max(L.ns, L.nc)) / 4 + 64);
+    int cut_buf = 0;
+    const int src_buf = launch_sort(P, W, wide, key_bits, s, cut_buf);
+    rec(c, 3);
+    launch_hierarchy(P, W, wide, cut_buf, s);
+    rec(c, 4);
+    launch_traverse(P, W, src_buf, cut_buf, false, s);
+
+    // readback 1: pair count and traversal flags
+    uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
+    ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+    ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+    ck(cudaStreamSynchronize(s), "sync traverse");
+    bool deep = false;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        bool stack = false;
+        for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
+        const uint64_t np = hc[0];
+        if (!stack && np <= W.pair_cap) break;
+        if (np > W.pair_cap) {
+            W.pair_cap = np + np / 8 + 1024;
+            W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
+        }
+        deep = deep || stack;
+        ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
+        ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
+        ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+        launch_traverse(P, W, src_buf, cut_buf, deep, s);
+        ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+        ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+        ck(cudaStreamSynchronize(s), "sync traverse");
+    }
+    rec(c, 5);
+    const uint64_t npairs = hc[0];
+    c->n_pairs_found = npairs;
+
+    // stage-3 buffers sized from the pair count
+    W.plane_cap = std::min<uint64_t>(L.nf, 2 * npairs + 1);
+    W.plane_slot = c->buf[B_PSLOT].get<uint32_t>(L.nf);
+    W.planes = c->buf[B_PLANES].get<FacePlane>(W.plane_cap);
+    W.poly_list = c->buf[B_POLY].get<uint32_t>(L.all_tri ? 1 : L.nf);
+    W.tri_stride = L.all_tri ? 0 : L.tri_stride;
+    W.tri_scratch_cap = W.tri_stride * std::max<uint64_t>(L.n_poly, 1);
+    W.tri_scratch = c->buf[B_TRI].get<double>(W.tri_scratch_cap * 3 + 1);
+    W.vneed = c->buf[B_VNEED].get<uint8_t>(L.nv);
+    W.voff = c->buf[B_VOFF].get<uint32_t>(L.nv + 1);
+    W.vcur = c->buf[B_VCUR].get<uint32_t>(L.nv);
+    W.inc_cap = L.nidx;
+    W.vface = c->buf[B_VFACE].get<uint32_t>(L.nidx);
+    W.test_cap = std::max<uint64_t>(1, 2ull * L.max_face * npairs);
+    if (W.test_cap > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "edge-face tests exceed 2^32");
+    W.tests = c->buf[B_TESTS].get<Test>(W.test_cap);
+    W.test_info = c->buf[B_TINFO].get<int8_t>((flags & MCGPU_KEEP_TESTS) ? W.test_cap * 4 : 4);
+    W.rec_key[0] = c->buf[B_RK0].get<unsigned long long>(W.test_cap);
+    W.rec_key[1] = c->buf[B_RK1].get<unsigned long long>(W.test_cap);
+    W.rec_val[0] = c->buf[B_RV0].get<uint32_t>(W.test_cap);
+    W.rec_val[1] = c->buf[B_RV1].get<uint32_t>(W.test_cap);
+    W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
+    W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
+        radix_sort_temp_bytes((uint32_t)std::max<uint64_t>({ L.ns, L.nc, W.test_cap })) / 4 + 64);
+    ck(cudaMemsetAsync(W.vneed, 0, L.nv, s), "memset");
+
+    launch_adjacency_planes(P, W, s);
+    rec(c, 6);
+    launch_tests(P, W, s);
+    launch_narrow(P, W, (flags & MCGPU_KEEP_TESTS) != 0, s);
+
+    // readback 2: counters, per-pair status / degenerate face / record count
+    ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+    ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+    ck(cudaMemcpyAsync(hc + 16 + n, W.pair_bad, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H bad");
+    ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H nrec");
+    ck(cudaStreamSynchronize(s), "sync narrow");
+    c->n_tests = hc[1];
+    c->n_records = hc[2];
+    W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
+    W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
+    c->rec_buf = launch_records(P, W, (uint32_t)c->n_records, s);
+    rec(c, 7);
+    ck(cudaStreamSynchronize(s), "sync records");
+    ck(cudaGetLastError(), "kernel launch");
+
+    c->sums.assign(n, mcgpu_summary());
+    c->rec_begin.assign(n + 1, 0);
+    for (uint32_t p = 0; p < n; ++p) {
+        mcgpu_summary& m = c->sums[p];
+        memset(&m, 0, sizeof m);
+        const uint32_t st = hc[16 + p];
+        const int32_t bad = (int32_t)hc[16 + n + p];
+        m.bad_face = -1;
+        if (st & ST_INVALID) m.status = MCGPU_INVALID_INPUT;
+        else if (bad != kNoBad) {
+            m.bad_face = bad;
+            m.status = (uint32_t)bad >= L.fs[p] ? MCGPU_DEGENERATE_CUT_FACE : MCGPU_DEGENERATE_SRC_FACE;
+        } else if (st & ST_GP) m.status = MCGPU_GP_VIOLATION;
+        else m.status = MCGPU_OK;
+        m.cut_eps = L.eps[p];
+        m.num_records = hc[16 + 2 * n + p];
+        c->rec_begin[p + 1] = c->rec_begin[p] + m.num_records;
+    }
+    if (n == 1) {
+        c->sums[0].num_pairs = npairs;
+        c->sums[0].num_tests = c->n_tests;
+        c->sums[0].escalations[0] = hc[5];
+        c->sums[0].escalations[1] = hc[6];
+        c->sums[0].escalations[2] = hc[7];
+        if (flags & MCGPU_PROFILE) {
+            for (int k = 0; k < 7; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+                c->sums[0].stage_ms[k] = ms;
+            }
+        }
+    }
+    if (out) {
+        if (n == 1) *out = c->sums[0];
+        else memcpy(out, c->sums.data(), sizeof(mcgpu_summary) * n);
+    }
+    return MCGPU_OK;
+}
+
+int copy_out(mcgpu_context_t* c, const void* dptr, uint64_t need, uint64_t bytes, void* mem, uint64_t* bytes_out)
+{
+    if (bytes_out) *bytes_out = need;
+    if (!mem && bytes == 0) return MCGPU_OK;
+    if (!mem || bytes < need) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+    if (need) {
+        ck(cudaMemcpyAsync(mem, dptr, need, cudaMemcpyDeviceToHost, c->s), "D2H data");
+        ck(cudaStreamSynchronize(c->s), "sync data");
+    }
+    return MCGPU_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int mcgpu_context_create(mcgpu_context* out, int device)
+{
+    if (!out) return fail(MCGPU_INVALID_VALUE, "null context pointer");
+    *out = nullptr;
+    try {
+        int n = 0;
+        ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        if (device < 0 || device >= n) return fail(MCGPU_INVALID_VALUE, "no such CUDA device");
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        mcgpu_context_t* c = new (std::nothrow) mcgpu_context_t();
+        if (!c) return fail(MCGPU_OUT_OF_MEMORY, "host allocation");
+        c->device = device;
+        ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
+        for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
+        *out = c;
+        return MCGPU_OK;
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_context_release(mcgpu_context c)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    cudaSetDevice(c->device);
+    if (c->s) cudaStreamSynchronize(c->s);
+    for (auto& b : c->buf) b.release();
+    c->pin_counters.release();
+    c->pin_tab.release();
+    c->pin_stage.release();
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->s) cudaStreamDestroy(c->s);
+    delete c;
+    return MCGPU_OK;
+}
+
+int mcgpu_dispatch(mcgpu_context c, uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
+    mcgpu_summary* out)
+{
+    try {
+        return run(c, flags, 1, src, cut, &cut_eps, out);
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_dispatch_batch(mcgpu_context c, uint32_t flags, uint32_t n_pairs, const mcgpu_mesh* srcs,
+    const mcgpu_mesh* cuts, const double* cut_eps, mcgpu_summary* summaries)
+{
+    try {
+        return run(c, flags, n_pairs, srcs, cuts, cut_eps, summaries);
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    try {
+        const Work& W = c->W;
+        switch (query) {
+        case MCGPU_DATA_RECORD_IDS:
+            return copy_out(c, W.rec_ids, c->n_records * 5 * 4, bytes, mem, bytes_out);
+        case MCGPU_DATA_RECORD_POINTS:
+            return copy_out(c, W.rec_pts, c->n_records * 3 * 8, bytes, mem, bytes_out);
+        case MCGPU_DATA_PAIRS: {
+            // (source face, cut face) in per-pair local ids of a single dispatch
+            const uint64_t need = c->n_pairs_found * 8;
+            if (bytes_out) *bytes_out = need;
+            if (!mem && bytes == 0) return MCGPU_OK;
+            if (!mem || bytes < need) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+            std::vector<unsigned long long> raw(c->n_pairs_found);
+            ck(cudaMemcpyAsync(raw.data(), W.pairs, need, cudaMemcpyDeviceToHost, c->s), "D2H pairs");
+            ck(cudaStreamSynchronize(c->s), "sync");
+            uint32_t* o = (uint32_t*)mem;
+            for (uint64_t i = 0; i < c->n_pairs_found; ++i) {
+                const uint32_t sface = (uint32_t)(raw[i] >> 32), cface = (uint32_t)raw[i];
+                // single dispatch: pair 0, cut faces follow the Fs source faces
+                o[2 * i] = sface;
+                o[2 * i + 1] = cface - c->L.fs[0];
+            }
+            return MCGPU_OK;
+        }
+        case MCGPU_DATA_TESTS: {
+            if (!(c->flags & MCGPU_KEEP_TESTS)) return fail(MCGPU_INVALID_VALUE, "dispatch without MCGPU_KEEP_TESTS");
+            const uint64_t need = c->n_tests * 12;
+            if (bytes_out) *bytes_out = need;
+            if (!mem && bytes == 0) return MCGPU_OK;
+            if (!mem || bytes < need) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+            std::vector<Test> raw(c->n_tests);
+            ck(cudaMemcpyAsync(raw.data(), W.tests, c->n_tests * sizeof(Test), cudaMemcpyDeviceToHost, c->s), "D2H");
+            ck(cudaStreamSynchronize(c->s), "sync");
+            uint32_t* o = (uint32_t*)mem;
+            for (uint64_t i = 0; i < c->n_tests; ++i) {
+                o[3 * i] = raw[i].q;
+                o[3 * i + 1] = raw[i].r;
+                o[3 * i + 2] = raw[i].g;
+            }
+            return MCGPU_OK;
+        }
+        case MCGPU_DATA_TEST_INFO:
+            if (!(c->flags & MCGPU_KEEP_TESTS)) return fail(MCGPU_INVALID_VALUE, "dispatch without MCGPU_KEEP_TESTS");
+            return copy_out(c, W.test_info, c->n_tests * 4, bytes, mem, bytes_out);
+        case MCGPU_DATA_VERTICES:
+            return copy_out(c, c->P.X, c->L.nv * 24, bytes, mem, bytes_out);
+        case MCGPU_DATA_FACE_BOXES:
+            return copy_out(c, W.fbox, c->L.nf * 48, bytes, mem, bytes_out);
+        default:
+            return fail(MCGPU_INVALID_VALUE, "unknown query");
+        }
+    } catch (const CudaError& e) {
+        return fail(MCGPU_CUDA_ERROR, e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_get_batch_data(mcgpu_context c, uint32_t pair, uint32_t query, uint64_t bytes, void* mem,
+    uint64_t* bytes_out)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    if (pair >= c->L.n_pairs) return fail(MCGPU_INVALID_VALUE, "pair index out of range");
+    try {
+        const uint64_t b = c->rec_begin[pair], n = c->rec_begin[pair + 1] - b;
+        switch (query) {
+        case MCGPU_DATA_RECORD_IDS:
+            return copy_out(c, c->W.rec_ids + b * 5, n * 20, bytes, mem, bytes_out);
+        case MCGPU_DATA_RECORD_POINTS:
+            return copy_out(c, c->W.rec_pts + b * 3, n * 24, bytes, mem, bytes_out);
+        default:
+            return fail(MCGPU_INVALID_VALUE, "batch queries: record ids and points");
+        }
+    } catch (const CudaError& e) {
+        return fail(MCGPU_CUDA_ERROR, e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut, double* src_out, double* cut_out,
+    double* cut_eps_out)
+{
+    if (!src || !cut || !src_out || !cut_out || !cut_eps_out) return fail(MCGPU_INVALID_VALUE, "null argument");
+    if (src->num_vertices < 1 || cut->num_vertices < 1) return fail(MCGPU_INVALID_INPUT, "empty mesh");
+    recentre_pair((flags & MCGPU_VERTEX_ARRAY_FLOAT) != 0, *src, *cut, src_out, cut_out, cut_eps_out);
+    return MCGPU_OK;
+}
+
+const char* mcgpu_last_error(void) { return g_last_error.c_str(); }
+
+} // extern "C"

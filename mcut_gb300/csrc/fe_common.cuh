@@ -1,0 +1,391 @@
+// Shared device code of the GB300 intersection front end.
+//
+// Everything here is compiled with --fmad=false: each a*b+c is two IEEE
+// roundings, as in the reference's x86 build. That is what keeps face planes,
+// intersection points and the point-in-polygon arithmetic bit-identical to
+// math.cpp, and what the error-free transforms of the exact predicates need.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mcut_gb300.h"
+
+namespace mcgpu {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+// status word bits (device-side, one uint32 per dispatch)
+enum : uint32_t {
+    ST_GP = 1u,               // a test violated general position
+    ST_OVERFLOW_PAIRS = 2u,   // candidate-pair buffer too small
+    ST_OVERFLOW_TESTS = 4u,   // edge-face test buffer too small
+    ST_STACK = 8u,            // traversal stack overflow (re-run deep)
+    ST_INVALID = 16u,         // invalid input (index out of range, non-manifold)
+};
+
+// ---------------------------------------------------------------------------
+// fp64 boxes: bounding_box_t / intersect_bounding_boxes (math.h:866-943)
+// ---------------------------------------------------------------------------
+struct Box {
+    double mn[3], mx[3];
+};
+
+__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }  // std::max
+__device__ __forceinline__ double dmin_ref(double a, double b) { return (b < a) ? b : a; }  // std::min
+
+__device__ __forceinline__ bool box_overlap(const Box& a, const Box& b)
+{
+    return (a.mn[0] <= b.mx[0] && a.mx[0] >= b.mn[0]) && (a.mn[1] <= b.mx[1] && a.mx[1] >= b.mn[1])
+        && (a.mn[2] <= b.mx[2] && a.mx[2] >= b.mn[2]);
+}
+
+__device__ __forceinline__ Box load_box(const double* __restrict__ boxes, uint32_t f)
+{
+    const double2* p = reinterpret_cast<const double2*>(boxes + (size_t)f * 6);
+    double2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    Box r;
+    r.mn[0] = a.x; r.mn[1] = a.y; r.mn[2] = b.x;
+    r.mx[0] = b.y; r.mx[1] = c.x; r.mx[2] = c.y;
+    return r;
+}
+
+__device__ __forceinline__ void load_xyz(const double* __restrict__ X, uint32_t v, double* p)
+{
+    const double* s = X + (size_t)v * 3;
+    p[0] = __ldg(s);
+    p[1] = __ldg(s + 1);
+    p[2] = __ldg(s + 2);
+}
+
+// dot_product: out = 0; out += a[i]*b[i]  (math.h:635-643)
+__device__ __forceinline__ double dot3(const double* a, const double* b)
+{
+    double o = 0.0;
+    o = o + a[0] * b[0];
+    o = o + a[1] * b[1];
+    o = o + a[2] * b[2];
+    return o;
+}
+
+// order-preserving map of a double onto uint64 (for atomic min / max)
+__device__ __forceinline__ unsigned long long ord_of(double x)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__host__ __device__ inline double of_ord(unsigned long long u)
+{
+    u = (u & 0x8000000000000000ull) ? (u & 0x7FFFFFFFFFFFFFFFull) : ~u;
+    union { unsigned long long i; double d; } c;
+    c.i = u;
+    return c.d;
+}
+
+// ---------------------------------------------------------------------------
+// Expansion arithmetic (Shewchuk, DCG 18:305-363, 1997, section 2)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(double a, double b, double& x, double& y)
+{
+    double s = a + b, bv = s - a, av = s - bv;
+    x = s;
+    y = (a - av) + (b - bv);
+}
+__device__ __forceinline__ void fast_two_sum(double a, double b, double& x, double& y)
+{
+    double s = a + b;
+    x = s;
+    y = b - (s - a);
+}
+__device__ __forceinline__ void two_diff(double a, double b, double& x, double& y)
+{
+    double s = a - b, bv = a - s, av = s + bv;
+    x = s;
+    y = (a - av) + (bv - b);
+}
+__device__ __forceinline__ double two_diff_tail(double a, double b, double x)
+{
+    double bv = a - x, av = x + bv;
+    return (a - av) + (bv - b);
+}
+__device__ __forceinline__ void split(double a, double& hi, double& lo)
+{
+    double c = 134217729.0 * a, big = c - a;
+    hi = c - big;
+    lo = a - hi;
+}
+__device__ __forceinline__ void two_product(double a, double b, double& x, double& y)
+{
+    double p = a * b, ah, al, bh, bl;
+    split(a, ah, al);
+    split(b, bh, bl);
+    double e1 = p - ah * bh, e2 = e1 - al * bh, e3 = e2 - ah * bl;
+    x = p;
+    y = al * bl - e3;
+}
+__device__ __forceinline__ void two_two_diff(double a1, double a0, double b1, double b0, double* x)
+{
+    double i, j, k0;
+    two_diff(a0, b0, i, x[0]);
+    two_sum(a1, i, j, k0);
+    two_diff(k0, b1, i, x[1]);
+    two_sum(j, i, x[3], x[2]);
+}
+__device__ inline int fast_expansion_sum_zeroelim(int elen, const double* e, int flen, const double* f, double* h)
+{
+    int ei = 0, fi = 0, hi = 0;
+    double q, qn, hh, en = e[0], fn = f[0];
+    if ((fn > en) == (fn > -en)) { q = en; ++ei; en = ei < elen ? e[ei] : 0.0; }
+    else { q = fn; ++fi; fn = fi < flen ? f[fi] : 0.0; }
+    if (ei < elen && fi < flen) {
+        if ((fn > en) == (fn > -en)) { fast_two_sum(en, q, qn, hh); ++ei; en = ei < elen ? e[ei] : 0.0; }
+        else { fast_two_sum(fn, q, qn, hh); ++fi; fn = fi < flen ? f[fi] : 0.0; }
+        q = qn;
+        if (hh != 0.0) h[hi++] = hh;
+        while (ei < elen && fi < flen) {
+            if ((fn > en) == (fn > -en)) { two_sum(q, en, qn, hh); ++ei; en = ei < elen ? e[ei] : 0.0; }
+            else { two_sum(q, fn, qn, hh); ++fi; fn = fi < flen ? f[fi] : 0.0; }
+            q = qn;
+            if (hh != 0.0) h[hi++] = hh;
+        }
+    }
+    while (ei < elen) {
+        two_sum(q, en, qn, hh); ++ei; en = ei < elen ? e[ei] : 0.0;
+        q = qn;
+        if (hh != 0.0) h[hi++] = hh;
+    }
+    while (fi < flen) {
+        two_sum(q, fn, qn, hh); ++fi; fn = fi < flen ? f[fi] : 0.0;
+        q = qn;
+        if (hh != 0.0) h[hi++] = hh;
+    }
+    if (q != 0.0 || hi == 0) h[hi++] = q;
+    return hi;
+}
+__device__ inline int scale_expansion_zeroelim(int elen, const double* e, double b, double* h)
+{
+    double q, sum, hh, bh, bl, ah, al;
+    int hi = 0;
+    split(b, bh, bl);
+    {
+        double p = e[0] * b;
+        split(e[0], ah, al);
+        double e1 = p - ah * bh, e2 = e1 - al * bh, e3 = e2 - ah * bl;
+        q = p;
+        hh = al * bl - e3;
+    }
+    if (hh != 0.0) h[hi++] = hh;
+    for (int i = 1; i < elen; ++i) {
+        double p = e[i] * b;
+        split(e[i], ah, al);
+        double e1 = p - ah * bh, e2 = e1 - al * bh, e3 = e2 - ah * bl;
+        double p0 = al * bl - e3;
+        two_sum(q, p0, sum, hh);
+        if (hh != 0.0) h[hi++] = hh;
+        fast_two_sum(p, sum, q, hh);
+        if (hh != 0.0) h[hi++] = hh;
+    }
+    if (q != 0.0 || hi == 0) h[hi++] = q;
+    return hi;
+}
+
+// ---------------------------------------------------------------------------
+// orient3d sign: FP32 filter -> FP64 filter -> exact (the reference returns
+// Shewchuk's adaptive value, shewchuk.c:2367-2407, of which only the sign is
+// read, math.cpp:391-427)
+// ---------------------------------------------------------------------------
+static __device__ __noinline__ int orient3d_exact_sign(const double* pa, const double* pb, const double* pc, const double* pd)
+{
+    double ab[4], bc[4], cd[4], da[4], ac[4], bd[4], t8[8], abc[12], bcd[12], cda[12], dab[12];
+    double adet[24], bdet[24], cdet[24], ddet[24], abd[48], cdd[48], det[96];
+    auto cross2 = [](const double* p, const double* q, double* o) {
+        double a1, a0, b1, b0;
+        two_product(p[0], q[1], a1, a0);
+        two_product(q[0], p[1], b1, b0);
+        two_two_diff(a1, a0, b1, b0, o);
+    };
+    cross2(pa, pb, ab); cross2(pb, pc, bc); cross2(pc, pd, cd);
+    cross2(pd, pa, da); cross2(pa, pc, ac); cross2(pb, pd, bd);
+    int tl = fast_expansion_sum_zeroelim(4, cd, 4, da, t8);
+    int cdal = fast_expansion_sum_zeroelim(tl, t8, 4, ac, cda);
+    tl = fast_expansion_sum_zeroelim(4, da, 4, ab, t8);
+    int dabl = fast_expansion_sum_zeroelim(tl, t8, 4, bd, dab);
+    for (int i = 0; i < 4; ++i) { bd[i] = -bd[i]; ac[i] = -ac[i]; }
+    tl = fast_expansion_sum_zeroelim(4, ab, 4, bc, t8);
+    int abcl = fast_expansion_sum_zeroelim(tl, t8, 4, ac, abc);
+    tl = fast_expansion_sum_zeroelim(4, bc, 4, cd, t8);
+    int bcdl = fast_expansion_sum_zeroelim(tl, t8, 4, bd, bcd);
+    int al = scale_expansion_zeroelim(bcdl, bcd, pa[2], adet);
+    int bl = scale_expansion_zeroelim(cdal, cda, -pb[2], bdet);
+    int cl = scale_expansion_zeroelim(dabl, dab, pc[2], cdet);
+    int dl = scale_expansion_zeroelim(abcl, abc, -pd[2], ddet);
+    int abl = fast_expansion_sum_zeroelim(al, adet, bl, bdet, abd);
+    int cdl = fast_expansion_sum_zeroelim(cl, cdet, dl, ddet, cdd);
+    int n = fast_expansion_sum_zeroelim(abl, abd, cdl, cdd, det);
+    double top = det[n - 1];
+    return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
+}
+
+// Which stage decided a sign (escalation counters).
+enum { ESC_F32 = 0, ESC_F64 = 1, ESC_EXACT = 2 };
+
+// FP32 filter. The nine differences are formed in fp64 and rounded once to
+// fp32, so each carries a relative error of at most u(1+2^-28) (u = 2^-24).
+// Shewchuk's stage-A analysis with that per-input error and u per fp32
+// operation gives |det - det_exact| <= (7u + 56u^2) * permanent; 8u covers
+// the slightly larger input error. The filter only runs when every nonzero
+// difference lies in [1e-12, 1e12]: then no fp32 product or sum can
+// underflow or overflow and the relative-error model holds for every
+// operation. Otherwise, or when the bound is not met, it escalates.
+__device__ __forceinline__ bool f32_ok(double d, float f)
+{
+    const bool zero = ((unsigned long long)__double_as_longlong(d) << 1) == 0ull;
+    const float a = fabsf(f);
+    return (zero || a >= 1e-12f) && a <= 1e12f;
+}
+__device__ __forceinline__ int orient3d_sign_filtered(const double* pa, const double* pb, const double* pc,
+    const double* pd, int& stage)
+{
+    const double adx = pa[0] - pd[0], bdx = pb[0] - pd[0], cdx = pc[0] - pd[0];
+    const double ady = pa[1] - pd[1], bdy = pb[1] - pd[1], cdy = pc[1] - pd[1];
+    const double adz = pa[2] - pd[2], bdz = pb[2] - pd[2], cdz = pc[2] - pd[2];
+    {
+        const float ax = (float)adx, bx = (float)bdx, cx = (float)cdx;
+        const float ay = (float)ady, by = (float)bdy, cy = (float)cdy;
+        const float az = (float)adz, bz = (float)bdz, cz = (float)cdz;
+        const bool ok = f32_ok(adx, ax) && f32_ok(bdx, bx) && f32_ok(cdx, cx) && f32_ok(ady, ay) && f32_ok(bdy, by)
+            && f32_ok(cdy, cy) && f32_ok(adz, az) && f32_ok(bdz, bz) && f32_ok(cdz, cz);
+        if (ok) {
+            const float bxcy = bx * cy, cxby = cx * by, cxay = cx * ay, axcy = ax * cy, axby = ax * by, bxay = bx * ay;
+            const float det = az * (bxcy - cxby) + bz * (cxay - axcy) + cz * (axby - bxay);
+            const float perm = (fabsf(bxcy) + fabsf(cxby)) * fabsf(az) + (fabsf(cxay) + fabsf(axcy)) * fabsf(bz)
+                + (fabsf(axby) + fabsf(bxay)) * fabsf(cz);
+            const float eb = 4.76837158203125e-07f * perm; // 8 * 2^-24
+            if (det > eb) { stage = ESC_F32; return 1; }
+            if (-det > eb) { stage = ESC_F32; return -1; }
+        }
+    }
+    const double bdxcdy = bdx * cdy, cdxbdy = cdx * bdy, cdxady = cdx * ady, adxcdy = adx * cdy;
+    const double adxbdy = adx * bdy, bdxady = bdx * ady;
+    const double det = adz * (bdxcdy - cdxbdy) + bdz * (cdxady - adxcdy) + cdz * (adxbdy - bdxady);
+    const double perm = (fabs(bdxcdy) + fabs(cdxbdy)) * fabs(adz) + (fabs(cdxady) + fabs(adxcdy)) * fabs(bdz)
+        + (fabs(adxbdy) + fabs(bdxady)) * fabs(cdz);
+    const double eb = 7.7715611723761027e-16 * perm; // o3derrboundA
+    if (det > eb) { stage = ESC_F64; return 1; }
+    if (-det > eb) { stage = ESC_F64; return -1; }
+    stage = ESC_EXACT;
+    return orient3d_exact_sign(pa, pb, pc, pd);
+}
+
+// ---------------------------------------------------------------------------
+// orient2d with the paper's adaptive stage outputs (value, not just sign):
+// its magnitude ranks vertex triplets of polygons (math.cpp:289-389)
+// ---------------------------------------------------------------------------
+static __device__ __noinline__ double orient2d_adapt(const double* pa, const double* pb, const double* pc, double detsum)
+{
+    const double EPS = 1.1102230246251565e-16;
+    const double CCW_B = (2.0 + 12.0 * EPS) * EPS, CCW_C = (9.0 + 64.0 * EPS) * EPS * EPS,
+                 RES = (3.0 + 8.0 * EPS) * EPS;
+    double acx = pa[0] - pc[0], bcx = pb[0] - pc[0], acy = pa[1] - pc[1], bcy = pb[1] - pc[1];
+    double dl, dlt, dr, drt, B[4], C1[8], C2[12], D[16], u[4], s1, s0, t1, t0;
+    two_product(acx, bcy, dl, dlt);
+    two_product(acy, bcx, dr, drt);
+    two_two_diff(dl, dlt, dr, drt, B);
+    double det = B[0];
+    for (int i = 1; i < 4; ++i) det += B[i];
+    double eb = CCW_B * detsum;
+    if (det >= eb || -det >= eb) return det;
+    double acxt = two_diff_tail(pa[0], pc[0], acx), bcxt = two_diff_tail(pb[0], pc[0], bcx);
+    double acyt = two_diff_tail(pa[1], pc[1], acy), bcyt = two_diff_tail(pb[1], pc[1], bcy);
+    if (acxt == 0.0 && acyt == 0.0 && bcxt == 0.0 && bcyt == 0.0) return det;
+    eb = CCW_C * detsum + RES * fabs(det);
+    det += (acx * bcyt + bcy * acxt) - (acy * bcxt + bcx * acyt);
+    if (det >= eb || -det >= eb) return det;
+    two_product(acxt, bcy, s1, s0);
+    two_product(acyt, bcx, t1, t0);
+    two_two_diff(s1, s0, t1, t0, u);
+    int c1 = fast_expansion_sum_zeroelim(4, B, 4, u, C1);
+    two_product(acx, bcyt, s1, s0);
+    two_product(acy, bcxt, t1, t0);
+    two_two_diff(s1, s0, t1, t0, u);
+    int c2 = fast_expansion_sum_zeroelim(c1, C1, 4, u, C2);
+    two_product(acxt, bcyt, s1, s0);
+    two_product(acyt, bcxt, t1, t0);
+    two_two_diff(s1, s0, t1, t0, u);
+    int dn = fast_expansion_sum_zeroelim(c2, C2, 4, u, D);
+    return D[dn - 1];
+}
+__device__ inline double orient2d(const double* pa, const double* pb, const double* pc)
+{
+    const double CCW_A = 3.3306690738754716e-16;
+    double dl = (pa[0] - pc[0]) * (pb[1] - pc[1]);
+    double dr = (pa[1] - pc[1]) * (pb[0] - pc[0]);
+    double det = dl - dr, ds;
+    if (dl > 0.0) {
+        if (dr <= 0.0) return det;
+        ds = dl + dr;
+    } else if (dl < 0.0) {
+        if (dr >= 0.0) return det;
+        ds = -dl - dr;
+    } else {
+        return det;
+    }
+    double eb = CCW_A * ds;
+    if (det >= eb || -det >= eb) return det;
+    return orient2d_adapt(pa, pb, pc, ds);
+}
+
+// ---------------------------------------------------------------------------
+// Per-face plane record (compute_polygon_plane_coefficients, math.cpp:130-239;
+// calculate_projection_matrix, math.cpp:710-793)
+// ---------------------------------------------------------------------------
+struct FacePlane {
+    double n[3];
+    double d;
+    double P[6];      // 2x3 projection, row major
+    int32_t mc;       // largest |n| component
+    int32_t tri[3];   // plane-defining vertex positions in the face's vertex list (-1: none)
+};
+
+// projection matrix P = K * R with the reference's operation order
+__device__ inline void projection_matrix(const double* nrm, int mc, double* P)
+{
+    const double len = sqrt(dot3(nrm, nrm));
+    const double a[3] = { nrm[0] / len, nrm[1] / len, nrm[2] / len };
+    double b[3] = { 0.0, 0.0, 0.0 };
+    const int s = (0.0 < nrm[mc]) - (nrm[mc] < 0.0);
+    b[mc] = 1.0 * (double)s;
+    double R[3][3] = { { 1.0, 0.0, 0.0 }, { 0.0, -1.0, 0.0 }, { 0.0, 0.0, 1.0 } };
+    if (a[0] != b[0] || a[1] != b[1] || a[2] != b[2]) {
+        const double apb[3] = { a[0] + b[0], a[1] + b[1], a[2] + b[2] };
+        const double adb = dot3(a, b);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const double I = (i == j) ? (i == 1 ? -1.0 : 1.0) : 0.0;
+                R[i][j] = (((apb[i] * apb[j]) / adb) * 2.0) - I;
+            }
+    }
+    double K[2][3] = { { 0.0, 0.0, 0.0 }, { 0.0, 0.0, 0.0 } };
+    if (mc == 0) { K[0][1] = 1.0; K[1][2] = 1.0; }
+    else if (mc == 1) { K[0][0] = 1.0; K[1][2] = 1.0; }
+    else { K[0][0] = 1.0; K[1][1] = 1.0; }
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = acc + K[i][k] * R[k][j];
+            P[i * 3 + j] = acc;
+        }
+}
+
+// matrix_t * vec3 (math.h:508-520)
+__device__ __forceinline__ void project2(const double* P, const double* v, double* o)
+{
+    double r0 = 0.0, r1 = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        r0 = r0 + P[c] * v[c];
+        r1 = r1 + P[3 + c] * v[c];
+    }
+    o[0] = r0;
+    o[1] = r1;
+}
+
+} // namespace mcgpu

@@ -1,0 +1,912 @@
+// Kernels of the GB300 intersection front end.
+//
+// Stage map (reference function -> kernel):
+//   bvh.cpp:242-433  face boxes, mesh box, Morton codes   -> k_face_bounds, k_morton
+//   bvh.cpp:437-442  std::sort by Morton code             -> radix_sort_pairs (fe_sort.cu)
+//   bvh.cpp:444-635  implicit-tree build + refit          -> k_karras, k_refit (LBVH)
+//   bvh.cpp:638-783  intersectOIBVHs                       -> k_traverse
+//   kernel.cpp:1781-2177 edge->faces, edge boxes, culling -> k_pair_tests
+//   kernel.cpp:2184-2356 tested-face planes               -> k_planes, k_triplets
+//   kernel.cpp:2456-2658 narrow phase + records           -> k_narrow, k_gather_records
+//
+// The candidate-pair set does not depend on the tree's shape: internal boxes
+// only prune, and every leaf-leaf test is the reference's exact closed fp64
+// test. So the tree is a Karras LBVH with fp32 node boxes rounded outward,
+// not the reference's implicit complete tree.
+
+#include "fe_common.cuh"
+#include "fe_kernels.cuh"
+#include "fe_sort.cuh"
+
+namespace mcgpu {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ uint32_t face_n(const Problem& P, uint32_t f)
+{
+    return P.all_triangles ? 3u : (P.foff[f + 1] - P.foff[f]);
+}
+__device__ __forceinline__ uint32_t face_o(const Problem& P, uint32_t f)
+{
+    return P.all_triangles ? 3u * f : P.foff[f];
+}
+
+// warp-aggregated append: returns the slot for this thread's item
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
+{
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, want);
+    if (!want) return 0;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// face boxes + per-mesh boxes (bvh.cpp:242-368)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
+    unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const uint32_t fp = P.face_pair[f];
+        const uint32_t p = fp & ~kCutBit;
+        const bool is_cut = (fp & kCutBit) != 0;
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
+        Box b;
+        for (int j = 0; j < 3; ++j) { b.mn[j] = 1.7976931348623157e308; b.mx[j] = -1.7976931348623157e308; }
+        bool bad = false;
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = P.fidx[o + k];
+            if (v < vlo || v >= vhi) { bad = true; continue; }
+            double x[3];
+            load_xyz(P.X, v, x);
+            for (int j = 0; j < 3; ++j) { b.mx[j] = dmax_ref(b.mx[j], x[j]); b.mn[j] = dmin_ref(b.mn[j], x[j]); }
+        }
+        if (bad) atomicOr(&pair_status[p], ST_INVALID);
+        if (is_cut) {
+            const double eps = P.pair_eps[p];
+            if (eps > 0.0)
+                for (int j = 0; j < 3; ++j) { b.mx[j] = b.mx[j] + eps; b.mn[j] = b.mn[j] - eps; }
+        }
+        double2* d = reinterpret_cast<double2*>(fbox + (size_t)f * 6);
+        d[0] = make_double2(b.mn[0], b.mn[1]);
+        d[1] = make_double2(b.mn[2], b.mx[0]);
+        d[2] = make_double2(b.mx[1], b.mx[2]);
+        // mesh box (only steers Morton codes: any order of min/max is exact)
+        unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
+        for (int j = 0; j < 3; ++j) {
+            atomicMin(&mb[j], ord_of(b.mn[j]));
+            atomicMax(&mb[3 + j], ord_of(b.mx[j]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// Morton code of the box centre in its mesh's box (morton3D, bvh.cpp:196-217),
+// written to the source-face or cut-face key list.
+template <typename K>
+__global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __restrict__ fbox,
+    const unsigned long long* __restrict__ mesh_box, K* __restrict__ skey, uint32_t* __restrict__ sval,
+    K* __restrict__ ckey, uint32_t* __restrict__ cval)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const uint32_t fp = P.face_pair[f];
+        const uint32_t p = fp & ~kCutBit;
+        const bool is_cut = (fp & kCutBit) != 0;
+        const Box b = load_box(fbox, f);
+        const unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
+        uint32_t c[3];
+        for (int j = 0; j < 3; ++j) {
+            const double lo = of_ord(mb[j]), hi = of_ord(mb[3 + j]);
+            const double mid = (b.mn[j] + b.mx[j]) / 2.0;
+            float t = (float)((mid - lo) / (hi - lo));
+            t = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+            c[j] = expand_bits((uint32_t)t);
+        }
+        const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]);
+        const uint32_t local = f - P.pair_fbase[p];
+        if (is_cut) {
+            const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);
+            ckey[pos] = key;
+            cval[pos] = f;
+        } else {
+            const uint32_t pos = P.pair_sbase[p] + local;
+            skey[pos] = key;
+            sval[pos] = f;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Karras (HPG 2012) hierarchy over the sorted cut-face keys; duplicate keys
+// are ordered by position.
+// ---------------------------------------------------------------------------
+template <typename K>
+__device__ __forceinline__ int delta(const K* __restrict__ key, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    const K a = key[i], b = key[j];
+    if (a == b) return 8 * (int)sizeof(K) + __clz((unsigned)(i ^ j));
+    if (sizeof(K) == 8) return __clzll((long long)((unsigned long long)a ^ (unsigned long long)b));
+    return __clz((unsigned)((uint32_t)a ^ (uint32_t)b));
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, int n, Node* __restrict__ nodes,
+    int32_t* __restrict__ parent)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int d = (delta(key, n, i, i + 1) - delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(key, n, i, i - d);
+        int lmax = 2;
+        while (delta(key, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(key, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = delta(key, n, i, j);
+        int s = 0;
+        for (int t = (l + 1) >> 1;; t = (t + 1) >> 1) {
+            if (delta(key, n, i, i + (s + t) * d) > dnode) s += t;
+            if (t == 1) break;
+        }
+        const int gamma = i + s * d + min(d, 0);
+        const int lo = min(i, j), hi = max(i, j);
+        const int left = (lo == gamma) ? ~gamma : gamma;
+        const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+        nodes[i].child[0] = left;
+        nodes[i].child[1] = right;
+        parent[left >= 0 ? left : (n - 1) + ~left] = i;
+        parent[right >= 0 ? right : (n - 1) + ~right] = i;
+    }
+}
+
+struct FBox { float lo[3], hi[3]; uint32_t plo, phi; };
+
+__device__ __forceinline__ void put_child(Node* nd, int slot, const FBox& b)
+{
+    float* f0 = reinterpret_cast<float*>(&nd->b0);
+    // 12 floats: left lo3 hi3, right lo3 hi3
+    float* o = f0 + slot * 6;
+    o[0] = b.lo[0]; o[1] = b.lo[1]; o[2] = b.lo[2];
+    o[3] = b.hi[0]; o[4] = b.hi[1]; o[5] = b.hi[2];
+    nd->prange[slot] = b.plo | (b.phi << 16);
+}
+__device__ __forceinline__ FBox get_child(const Node* nd, int slot)
+{
+    const float* o = reinterpret_cast<const float*>(&nd->b0) + slot * 6;
+    FBox b;
+    b.lo[0] = __ldcg(o); b.lo[1] = __ldcg(o + 1); b.lo[2] = __ldcg(o + 2);
+    b.hi[0] = __ldcg(o + 3); b.hi[1] = __ldcg(o + 4); b.hi[2] = __ldcg(o + 5);
+    const uint32_t pr = __ldcg(&nd->prange[slot]);
+    b.plo = pr & 0xFFFFu;
+    b.phi = pr >> 16;
+    return b;
+}
+
+// bottom-up refit: the second child to arrive at a node merges both boxes
+__global__ void __launch_bounds__(kBlock) k_refit(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ leaf_face, int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent,
+    uint32_t* __restrict__ flag)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t f = leaf_face[i];
+        const Box b = load_box(fbox, f);
+        FBox fb;
+        for (int j = 0; j < 3; ++j) {
+            fb.lo[j] = __double2float_rd(b.mn[j]);
+            fb.hi[j] = __double2float_ru(b.mx[j]);
+        }
+        fb.plo = fb.phi = P.face_pair[f] & ~kCutBit;
+        int child = ~i;
+        int node = parent[(n - 1) + i];
+        while (node >= 0) {
+            Node* nd = &nodes[node];
+            const int slot = (nd->child[0] == child) ? 0 : 1;
+            put_child(nd, slot, fb);
+            __threadfence();
+            if (atomicAdd(&flag[node], 1u) == 0) break; // the sibling finishes this node
+            __threadfence();
+            const FBox o = get_child(nd, slot ^ 1);
+            for (int j = 0; j < 3; ++j) {
+                fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
+                fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
+            }
+            fb.plo = min(fb.plo, o.plo);
+            fb.phi = max(fb.phi, o.phi);
+            child = node;
+            node = node == 0 ? -1 : parent[node];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// traversal: every source face queries the cut-face LBVH (intersectOIBVHs,
+// bvh.cpp:638-783). Queries run in Morton order so neighbouring threads walk
+// similar paths. Leaf tests are the reference's exact closed fp64 test.
+// ---------------------------------------------------------------------------
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ qface, const uint32_t* __restrict__ leaf_face, int nleaf,
+    const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
+    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < P.ns; t += gridDim.x * blockDim.x) {
+        const uint32_t s = qface[t];
+        const uint32_t p = P.face_pair[s] & ~kCutBit;
+        const Box qb = load_box(fbox, s);
+        float ql[3], qh[3];
+        for (int j = 0; j < 3; ++j) {
+            ql[j] = __double2float_rd(qb.mn[j]);
+            qh[j] = __double2float_ru(qb.mx[j]);
+        }
+        unsigned long long buf[8];
+        int nb = 0;
+        bool any = false;
+        auto flush = [&]() {
+            if (nb == 0) return;
+            const uint32_t pos = atomicAdd(&counters[0], (uint32_t)nb);
+            for (int k = 0; k < nb; ++k)
+                if ((uint64_t)pos + k < cap) pairs[pos + k] = buf[k];
+            nb = 0;
+        };
+        auto leaf = [&](int li) {
+            const uint32_t c = leaf_face[li];
+            if ((P.face_pair[c] & ~kCutBit) != p) return;
+            const Box cb = load_box(fbox, c);
+            if (box_overlap(qb, cb)) {
+                buf[nb++] = ((unsigned long long)s << 32) | c;
+                cand[c] = 1;
+                any = true;
+                if (nb == 8) flush();
+            }
+        };
+        if (nleaf == 1) {
+            leaf(0);
+        } else {
+            int stack[STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            bool overflow = false;
+            while (sp > 0) {
+                const int nd = stack[--sp];
+                const float4 a = __ldg(&nodes[nd].b0), b = __ldg(&nodes[nd].b1), c = __ldg(&nodes[nd].b2);
+                const int2 ch = __ldg(reinterpret_cast<const int2*>(&nodes[nd].child[0]));
+                const uint2 pr = __ldg(reinterpret_cast<const uint2*>(&nodes[nd].prange[0]));
+                const bool hit0 = (pr.x & 0xFFFFu) <= p && p <= (pr.x >> 16) && ql[0] <= a.w && qh[0] >= a.x
+                    && ql[1] <= b.x && qh[1] >= a.y && ql[2] <= b.y && qh[2] >= a.z;
+                const bool hit1 = (pr.y & 0xFFFFu) <= p && p <= (pr.y >> 16) && ql[0] <= c.y && qh[0] >= b.z
+                    && ql[1] <= c.z && qh[1] >= b.w && ql[2] <= c.w && qh[2] >= c.x;
+                if (hit0) {
+                    if (ch.x < 0) leaf(~ch.x);
+                    else if (sp < STACK) stack[sp++] = ch.x;
+                    else overflow = true;
+                }
+                if (hit1) {
+                    if (ch.y < 0) leaf(~ch.y);
+                    else if (sp < STACK) stack[sp++] = ch.y;
+                    else overflow = true;
+                }
+            }
+            if (overflow) atomicOr(&pair_status[p], ST_STACK);
+        }
+        flush();
+        if (any) cand[s] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// candidate-face properties: vertex needs, face planes, degenerate check
+// (kernel.cpp:2184-2356, math.cpp:130-239)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_mark_vertices(Problem P, const uint8_t* __restrict__ cand,
+    uint8_t* __restrict__ vneed)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        if (!cand[f]) continue;
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        for (uint32_t k = 0; k < n; ++k) vneed[P.fidx[o + k]] = 1;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_vf_count(Problem P, const uint8_t* __restrict__ vneed,
+    uint32_t* __restrict__ vdeg)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = P.fidx[o + k];
+            if (vneed[v]) atomicAdd(&vdeg[v], 1u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_vf_fill(Problem P, const uint8_t* __restrict__ vneed,
+    const uint32_t* __restrict__ voff, uint32_t* __restrict__ vcur, uint32_t* __restrict__ vface, uint64_t cap)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = P.fidx[o + k];
+            if (vneed[v]) {
+                const uint32_t pos = voff[v] + atomicAdd(&vcur[v], 1u);
+                if (pos < cap) vface[pos] = f;
+            }
+        }
+    }
+}
+
+// vertex k of the face's list as the reference sees it: hmesh_t's
+// get_vertices_around_face returns the TARGETS of the face's halfedges, i.e.
+// the input order rotated by one (hmesh.cpp:722-733)
+__device__ __forceinline__ uint32_t face_vertex(const Problem& P, uint32_t o, uint32_t n, uint32_t k)
+{
+    const uint32_t j = k + 1;
+    return P.fidx[o + (j == n ? 0 : j)];
+}
+
+__global__ void __launch_bounds__(kBlock) k_planes(Problem P, const uint8_t* __restrict__ cand,
+    uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, uint64_t plane_cap,
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const bool c = cand[f] != 0;
+        const uint32_t slot = warp_append(&counters[3], c);
+        if (!c) continue;
+        plane_slot[f] = slot;
+        if (slot >= plane_cap) continue;
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        // Newell's normal over the rotated vertex list
+        double nx = 0.0, ny = 0.0, nz = 0.0;
+        double cur[3], nxt[3], first[3];
+        load_xyz(P.X, face_vertex(P, o, n, 0), first);
+        cur[0] = first[0]; cur[1] = first[1]; cur[2] = first[2];
+        for (uint32_t k = 0; k < n; ++k) {
+            if (k + 1 < n) load_xyz(P.X, face_vertex(P, o, n, k + 1), nxt);
+            else { nxt[0] = first[0]; nxt[1] = first[1]; nxt[2] = first[2]; }
+            nx = nx + (cur[1] - nxt[1]) * (cur[2] + nxt[2]);
+            ny = ny + (cur[2] - nxt[2]) * (cur[0] + nxt[0]);
+            nz = nz + (cur[0] - nxt[0]) * (cur[1] + nxt[1]);
+            cur[0] = nxt[0]; cur[1] = nxt[1]; cur[2] = nxt[2];
+        }
+        FacePlane pl;
+        const double nn[3] = { nx, ny, nz };
+        const double sq = dot3(nn, nn);
+        const uint32_t p = P.face_pair[f] & ~kCutBit;
+        if (isnan(nx) || isnan(ny) || isnan(nz) || sq < 1e-9 || sq == 0.0) {
+            atomicMin(&pair_bad[p], (int32_t)(f - P.pair_fbase[p]));
+            pl.tri[0] = -1;
+            planes[slot] = pl;
+            continue;
+        }
+        const double len = sqrt(sq);
+        pl.n[0] = nx / len; pl.n[1] = ny / len; pl.n[2] = nz / len;
+        pl.d = dot3(first, pl.n);
+        double big = 0.0;
+        pl.mc = 0;
+        for (int i = 0; i < 3; ++i) {
+            const double t = fabs(pl.n[i]);
+            if (t > big) { big = t; pl.mc = i; }
+        }
+        projection_matrix(pl.n, pl.mc, pl.P);
+        pl.tri[0] = 0; pl.tri[1] = 1; pl.tri[2] = 2;
+        planes[slot] = pl;
+        if (n > 3) {
+            const uint32_t k = atomicAdd(&counters[4], 1u);
+            poly_list[k] = f;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// plane-defining triplet of polygons with > 3 vertices
+// (determine_three_noncollinear_vertices, math.cpp:289-389): every triplet's
+// orient2d value in the projected frame, the first after libstdc++'s
+// std::sort by |value| descending (its introsort + insertion-sort schedule
+// decides ties, so it is replayed), entries in global scratch.
+// ---------------------------------------------------------------------------
+struct Trip { double v; int i, j, k, pad; };
+__device__ __forceinline__ bool tless(const Trip& a, const Trip& b) { return fabs(a.v) > fabs(b.v); }
+__device__ void t_swap(Trip* a, Trip* b) { Trip t = *a; *a = *b; *b = t; }
+__device__ void t_ins_sort(Trip* f, long n)
+{
+    for (long i = 1; i < n; ++i) {
+        Trip v = f[i];
+        if (tless(v, f[0])) {
+            for (long j = i; j > 0; --j) f[j] = f[j - 1];
+            f[0] = v;
+        } else {
+            long j = i;
+            while (tless(v, f[j - 1])) { f[j] = f[j - 1]; --j; }
+            f[j] = v;
+        }
+    }
+}
+__device__ void t_unguarded_ins(Trip* f, long from, long n)
+{
+    for (long i = from; i < n; ++i) {
+        Trip v = f[i];
+        long j = i;
+        while (tless(v, f[j - 1])) { f[j] = f[j - 1]; --j; }
+        f[j] = v;
+    }
+}
+__device__ void t_median(Trip* r, Trip* a, Trip* b, Trip* c)
+{
+    if (tless(*a, *b)) {
+        if (tless(*b, *c)) t_swap(r, b);
+        else if (tless(*a, *c)) t_swap(r, c);
+        else t_swap(r, a);
+    } else if (tless(*a, *c)) t_swap(r, a);
+    else if (tless(*b, *c)) t_swap(r, c);
+    else t_swap(r, b);
+}
+__device__ void t_sift(Trip* f, long hole, long len, Trip v)
+{
+    const long top = hole;
+    long child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (tless(f[child], f[child - 1])) child--;
+        f[hole] = f[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        f[hole] = f[child - 1];
+        hole = child - 1;
+    }
+    long par = (hole - 1) / 2;
+    while (hole > top && tless(f[par], v)) {
+        f[hole] = f[par];
+        hole = par;
+        par = (hole - 1) / 2;
+    }
+    f[hole] = v;
+}
+__device__ void t_heap_sort(Trip* f, long n)
+{
+    if (n < 2) return;
+    for (long par = (n - 2) / 2;; --par) {
+        t_sift(f, par, n, f[par]);
+        if (par == 0) break;
+    }
+    for (long last = n - 1; last > 0; --last) {
+        Trip v = f[last];
+        f[last] = f[0];
+        t_sift(f, 0, last, v);
+    }
+}
+__device__ void t_std_sort(Trip* f, long n)
+{
+    if (n < 2) return;
+    // introsort loop, iterative on the left part, explicit stack for the right parts
+    struct Seg { long off, n; int depth; };
+    Seg st[64];
+    int sp = 0;
+    int depth0 = 2 * (63 - __clzll((long long)n));
+    long off = 0, len = n;
+    int depth = depth0;
+    for (;;) {
+        while (len > 16) {
+            if (depth == 0) { t_heap_sort(f + off, len); len = 0; break; }
+            --depth;
+            Trip* g = f + off;
+            const long mid = len / 2;
+            t_median(&g[0], &g[1], &g[mid], &g[len - 1]);
+            long lo = 1, hi = len;
+            for (;;) {
+                while (tless(g[lo], g[0])) ++lo;
+                --hi;
+                while (tless(g[0], g[hi])) --hi;
+                if (!(lo < hi)) break;
+                t_swap(&g[lo], &g[hi]);
+                ++lo;
+            }
+            // the reference recurses into [lo, len) first, then loops on [0, lo)
+            if (sp < 64) st[sp++] = Seg { off + lo, len - lo, depth };
+            len = lo;
+        }
+        // left part done (len <= 16 is left for the final insertion sort);
+        // continue with the most recently deferred right part -- the
+        // recursion order does not change the result, each segment is
+        // partitioned independently
+        if (sp == 0) break;
+        --sp;
+        off = st[sp].off;
+        len = st[sp].n;
+        depth = st[sp].depth;
+    }
+    if (n > 16) {
+        t_ins_sort(f, 16);
+        t_unguarded_ins(f, 16, n);
+    } else {
+        t_ins_sort(f, n);
+    }
+}
+
+__global__ void k_triplets(Problem P, const uint32_t* __restrict__ poly_list, const uint32_t* __restrict__ counters,
+    const uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, Trip* __restrict__ scratch,
+    uint64_t scratch_cap, uint64_t stride, uint32_t* __restrict__ pair_status)
+{
+    const uint32_t npoly = counters[4];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < npoly; t += gridDim.x * blockDim.x) {
+        const uint32_t f = poly_list[t];
+        FacePlane& pl = planes[plane_slot[f]];
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        // scratch: one region of `stride` triplets (the largest polygon's count) per polygon
+        const uint64_t per = (uint64_t)n * (n - 1) * (n - 2) / 6;
+        const uint64_t base = (uint64_t)t * stride;
+        if (base + per > scratch_cap || per == 0) {
+            atomicOr(&pair_status[P.face_pair[f] & ~kCutBit], ST_INVALID);
+            pl.tri[0] = -1;
+            continue;
+        }
+        Trip* tr = scratch + base;
+        long m = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            double vi[3], xi[2];
+            load_xyz(P.X, face_vertex(P, o, n, i), vi);
+            project2(pl.P, vi, xi);
+            for (uint32_t j = i + 1; j < n; ++j) {
+                double vj[3], xj[2];
+                load_xyz(P.X, face_vertex(P, o, n, j), vj);
+                project2(pl.P, vj, xj);
+                for (uint32_t k = j + 1; k < n; ++k) {
+                    double vk[3], xk[2];
+                    load_xyz(P.X, face_vertex(P, o, n, k), vk);
+                    project2(pl.P, vk, xk);
+                    const double r = orient2d(xi, xj, xk);
+                    if (!(r == 0.0)) tr[m++] = Trip { r, (int)i, (int)j, (int)k, 0 };
+                }
+            }
+        }
+        if (m == 0) { pl.tri[0] = -1; continue; }
+        t_std_sort(tr, m);
+        pl.tri[0] = tr[0].i; pl.tri[1] = tr[0].j; pl.tri[2] = tr[0].k;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// candidate pair -> culled edge-face tests (kernel.cpp:1781-2177)
+//
+// The reference tests each edge of a candidate face against the union of the
+// partners of the (up to two) candidate faces containing it. Here every pair
+// (s, c) proposes (edge of s, c) and (edge of c, s); the proposal is dropped
+// when the edge's other face F' is lower-numbered and also a partner of the
+// tested face -- and "partner" is exactly "face boxes overlap" (the pair set
+// is all overlapping face-box pairs), so no pair lookup is needed. Edge boxes
+// cull as kernel.cpp:2074-2177 does.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t other_face(const Problem& P, const uint32_t* __restrict__ voff,
+    const uint32_t* __restrict__ vface, uint32_t F, uint32_t a, uint32_t b, uint32_t& slot_out)
+{
+    // faces incident to a that hold the halfedge b -> a
+    const uint32_t lo = voff[a], hi = voff[a + 1];
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t G = vface[i];
+        if (G == F) continue;
+        const uint32_t o = face_o(P, G), n = face_n(P, G);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t x = P.fidx[o + k];
+            const uint32_t y = P.fidx[o + (k + 1 == n ? 0 : k + 1)];
+            if (x == b && y == a) { slot_out = o + k; return G; }
+        }
+    }
+    return kNone;
+}
+
+__global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* __restrict__ fbox,
+    const unsigned long long* __restrict__ pairs, const uint32_t* __restrict__ counters_ro, uint64_t pair_cap,
+    const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vface, Test* __restrict__ tests, uint64_t test_cap,
+    uint32_t* __restrict__ counters, const int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_status)
+{
+    const uint64_t np = min((uint64_t)counters_ro[0], pair_cap);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < np; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long pr = pairs[i];
+        const uint32_t sface = (uint32_t)(pr >> 32), cface = (uint32_t)pr;
+        const uint32_t p = P.face_pair[sface] & ~kCutBit;
+        if (pair_bad[p] != kNoBad) continue; // the reference stops before the narrow phase
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t F = side == 0 ? sface : cface;
+            const uint32_t g = side == 0 ? cface : sface;
+            const Box gb = load_box(fbox, g);
+            const uint32_t o = face_o(P, F), n = face_n(P, F);
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t a = P.fidx[o + k], b = P.fidx[o + (k + 1 == n ? 0 : k + 1)];
+                uint32_t oslot = kNone;
+                const uint32_t G = other_face(P, voff, vface, F, a, b, oslot);
+                bool emit = true;
+                if (G != kNone && G < F && box_overlap(load_box(fbox, G), gb)) emit = false;
+                if (emit) {
+                    double xa[3], xb[3];
+                    load_xyz(P.X, a, xa);
+                    load_xyz(P.X, b, xb);
+                    Box eb;
+                    for (int j = 0; j < 3; ++j) {
+                        eb.mx[j] = dmax_ref(dmax_ref(-1.7976931348623157e308, xa[j]), xb[j]);
+                        eb.mn[j] = dmin_ref(dmin_ref(1.7976931348623157e308, xa[j]), xb[j]);
+                    }
+                    emit = box_overlap(eb, gb);
+                }
+                const uint32_t pos = warp_append(&counters[1], emit);
+                if (!emit) continue;
+                if (pos >= test_cap) { atomicOr(&pair_status[p], ST_OVERFLOW_TESTS); continue; }
+                Test t;
+                t.g = g;
+                if (G != kNone && G < F) {
+                    t.q = b; t.r = a; t.f0 = G; t.f1 = F; t.slot = oslot;
+                } else {
+                    t.q = a; t.r = b; t.f0 = F; t.f1 = G; t.slot = o + k;
+                }
+                tests[pos] = t;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// narrow phase (kernel.cpp:2456-2658; math.cpp:249-287, 391-427, 643-703, 851-902)
+// ---------------------------------------------------------------------------
+__device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint32_t n, const double* pt)
+{
+    double q[2];
+    project2(pl.P, pt, q);
+    int rc = 0, lc = 0;
+    double prv[2], first[2];
+    {
+        double v[3];
+        load_xyz(P.X, face_vertex(P, o, n, n - 1), v);
+        project2(pl.P, v, prv);
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        double v[3], c[2];
+        load_xyz(P.X, face_vertex(P, o, n, i), v);
+        project2(pl.P, v, c);
+        if (i == 0) { first[0] = c[0]; first[1] = c[1]; }
+        const double xi = c[0] - q[0], yi = c[1] - q[1];
+        if (xi == 0.0 && yi == 0.0) return 'v';
+        const double xl = prv[0] - q[0], yl = prv[1] - q[1];
+        const bool rs = (yi > 0.0) != (yl > 0.0);
+        const bool ls = (yi < 0.0) != (yl < 0.0);
+        if (rs || ls) {
+            const double x = (xi * yl - xl * yi) / (yl - yi);
+            if (rs && x > 0.0) rc++;
+            if (ls && x < 0.0) lc++;
+        }
+        prv[0] = c[0]; prv[1] = c[1];
+    }
+    (void)first;
+    if ((rc & 1) != (lc & 1)) return 'e';
+    return (rc & 1) ? 'i' : 'o';
+}
+
+__global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __restrict__ tests,
+    const uint32_t* __restrict__ counters_ro, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
+    const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
+    unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status, uint32_t* __restrict__ pair_nrec)
+{
+    const uint64_t nt = min((uint64_t)counters_ro[1], test_cap);
+    uint32_t esc[3] = { 0, 0, 0 };
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nt; i += (uint64_t)gridDim.x * blockDim.x) {
+        const Test t = tests[i];
+        const FacePlane pl = planes[plane_slot[t.g]];
+        const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
+        double q[3], r[3];
+        load_xyz(P.X, t.q, q);
+        load_xyz(P.X, t.r, r);
+        int8_t sq = 0, sr = 0;
+        char type = '0', pip = 0;
+        if (pl.tri[0] >= 0) {
+            double a[3], b[3], c[3];
+            load_xyz(P.X, face_vertex(P, o, n, pl.tri[0]), a);
+            load_xyz(P.X, face_vertex(P, o, n, pl.tri[1]), b);
+            load_xyz(P.X, face_vertex(P, o, n, pl.tri[2]), c);
+            int st0, st1;
+            sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
+            sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
+            esc[st0]++;
+            esc[st1]++;
+            if (sq == 0 && sr == 0) type = 'p';
+            else if (sq == 0) type = 'q';
+            else if (sr == 0) type = 'r';
+            else if ((sr < 0 && sq < 0) || (sr > 0 && sq > 0)) type = '0';
+            else type = '1';
+        }
+        bool rec = false;
+        double pt[3] = { 0.0, 0.0, 0.0 };
+        if (type == 'q' || type == 'r') {
+            pip = pip_face(P, pl, o, n, type == 'q' ? q : r);
+        } else if (type == 'p') {
+            pip = pip_face(P, pl, o, n, q);
+            if (!(pip == 'i' || pip == 'v' || pip == 'e')) pip = pip_face(P, pl, o, n, r);
+        } else if (type == '1') {
+            const double num = pl.d - dot3(q, pl.n);
+            const double rq[3] = { r[0] - q[0], r[1] - q[1], r[2] - q[2] };
+            const double den = dot3(rq, pl.n);
+            if (!(den == 0.0)) {
+                const double tt = num / den;
+                for (int k = 0; k < 3; ++k) pt[k] = q[k] + tt * (r[k] - q[k]);
+            }
+            pip = pip_face(P, pl, o, n, pt);
+            rec = pip == 'i';
+        }
+        const uint32_t p = P.face_pair[t.g] & ~kCutBit;
+        if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
+            || (type == '1' && (pip == 'v' || pip == 'e')))
+            atomicOr(&pair_status[p], ST_GP);
+        if (keep_tests) {
+            char4 info = make_char4(sq, sr, type, pip);
+            reinterpret_cast<char4*>(test_info)[i] = info;
+        }
+        const uint32_t pos = warp_append(&counters[2], rec);
+        if (rec) {
+            rec_key[pos] = ((unsigned long long)t.slot << 32) | t.g;
+            rec_val[pos] = (uint32_t)i;
+            rec_pt[(size_t)i * 3 + 0] = pt[0];
+            rec_pt[(size_t)i * 3 + 1] = pt[1];
+            rec_pt[(size_t)i * 3 + 2] = pt[2];
+            atomicAdd(&pair_nrec[p], 1u);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        uint32_t v = esc[k];
+        for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&counters[5 + k], v);
+    }
+}
+
+// sorted record order -> output arrays with per-pair local ids
+__global__ void __launch_bounds__(kBlock) k_gather_records(Problem P, const uint32_t* __restrict__ order,
+    uint32_t nrec, const Test* __restrict__ tests, const double* __restrict__ rec_pt, uint32_t* __restrict__ rec_ids,
+    double* __restrict__ rec_pts)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += gridDim.x * blockDim.x) {
+        const uint32_t ti = order[i];
+        const Test t = tests[ti];
+        const uint32_t p = P.face_pair[t.g] & ~kCutBit;
+        const uint32_t vb = P.pair_vbase[p], fb = P.pair_fbase[p];
+        rec_ids[(size_t)i * 5 + 0] = t.q - vb;
+        rec_ids[(size_t)i * 5 + 1] = t.r - vb;
+        rec_ids[(size_t)i * 5 + 2] = t.g - fb;
+        rec_ids[(size_t)i * 5 + 3] = t.f0 - fb;
+        rec_ids[(size_t)i * 5 + 4] = t.f1 == kNone ? kNone : t.f1 - fb;
+        rec_pts[(size_t)i * 3 + 0] = rec_pt[(size_t)ti * 3 + 0];
+        rec_pts[(size_t)i * 3 + 1] = rec_pt[(size_t)ti * 3 + 1];
+        rec_pts[(size_t)i * 3 + 2] = rec_pt[(size_t)ti * 3 + 2];
+    }
+}
+
+int grid_for(uint64_t n)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 148;
+    }
+    const uint64_t want = (n + kBlock - 1) / kBlock;
+    const uint64_t cap = (uint64_t)sms * 8;
+    return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_bounds_morton(const Problem& P, Work& W, bool wide, cudaStream_t s)
+{
+    const int g = grid_for(P.nf);
+    k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, W.pair_status);
+    if (wide)
+        k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box,
+            (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0]);
+    else
+        k_morton<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, (uint32_t*)W.skeys[0], W.svals[0],
+            (uint32_t*)W.ckeys[0], W.cvals[0]);
+}
+
+int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)
+{
+    int src_buf;
+    if (wide) {
+        src_buf = radix_sort_pairs<unsigned long long>((unsigned long long*)W.skeys[0], W.svals[0],
+            (unsigned long long*)W.skeys[1], W.svals[1], P.ns, 0, key_bits, W.sort_temp, s);
+        cut_buf = radix_sort_pairs<unsigned long long>((unsigned long long*)W.ckeys[0], W.cvals[0],
+            (unsigned long long*)W.ckeys[1], W.cvals[1], P.nc, 0, key_bits, W.sort_temp, s);
+    } else {
+        src_buf = radix_sort_pairs<uint32_t>((uint32_t*)W.skeys[0], W.svals[0], (uint32_t*)W.skeys[1], W.svals[1],
+            P.ns, 0, key_bits, W.sort_temp, s);
+        cut_buf = radix_sort_pairs<uint32_t>((uint32_t*)W.ckeys[0], W.cvals[0], (uint32_t*)W.ckeys[1], W.cvals[1],
+            P.nc, 0, key_bits, W.sort_temp, s);
+    }
+    return src_buf;
+}
+
+void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStream_t s)
+{
+    const int n = (int)P.nc;
+    if (n < 2) return;
+    const int g = grid_for(n);
+    if (wide)
+        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.ckeys[cut_buf], n, W.nodes,
+            W.parent);
+    else
+        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.ckeys[cut_buf], n, W.nodes, W.parent);
+    cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
+    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], n, W.nodes, W.parent, W.refit_flag);
+}
+
+void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
+{
+    const int g = grid_for(P.ns);
+    if (deep)
+        k_traverse<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], (int)P.nc, W.nodes,
+            W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+    else
+        k_traverse<64><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], (int)P.nc, W.nodes,
+            W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+}
+
+void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
+{
+    const int g = grid_for(P.nf);
+    k_planes<<<g, kBlock, 0, s>>>(P, W.cand, W.plane_slot, (FacePlane*)W.planes, W.plane_cap, W.counters,
+        W.poly_list, W.pair_bad);
+    if (W.tri_stride)
+        k_triplets<<<grid_for(1024), kBlock, 0, s>>>(P, W.poly_list, W.counters, W.plane_slot, (FacePlane*)W.planes,
+            (Trip*)W.tri_scratch, W.tri_scratch_cap, W.tri_stride, W.pair_status);
+    k_mark_vertices<<<g, kBlock, 0, s>>>(P, W.cand, W.vneed);
+    cudaMemsetAsync(W.voff, 0, sizeof(uint32_t) * ((size_t)P.nv + 1), s);
+    k_vf_count<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff);
+    exclusive_scan(W.voff, P.nv + 1, nullptr, W.scan_temp, s);
+    cudaMemsetAsync(W.vcur, 0, sizeof(uint32_t) * (size_t)P.nv, s);
+    k_vf_fill<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff, W.vcur, W.vface, W.inc_cap);
+}
+
+void launch_tests(const Problem& P, Work& W, cudaStream_t s)
+{
+    const int g = grid_for(W.pair_cap);
+    k_pair_tests<<<g, kBlock, 0, s>>>(P, W.fbox, W.pairs, W.counters, W.pair_cap, W.voff, W.vface, W.tests,
+        W.test_cap, W.counters, W.pair_bad, W.pair_status);
+}
+
+void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
+{
+    const int g = grid_for(W.test_cap);
+    k_narrow<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
+        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
+        W.pair_nrec);
+}
+
+int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
+{
+    if (nrec == 0) return 0;
+    // key = halfedge slot (edge creation order) << 32 | face: both global and
+    // monotone in the pair index, so records come out grouped by pair
+    const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1],
+        nrec, 0, 64, W.sort_temp, s);
+    k_gather_records<<<grid_for(nrec), kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids,
+        W.rec_pts);
+    return buf;
+}
+
+} // namespace mcgpu

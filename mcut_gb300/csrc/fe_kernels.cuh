@@ -1,0 +1,109 @@
+// Kernel interface of the GB300 intersection front end (host-callable launchers).
+//
+// Layout in HBM (one dispatch or one batch of independent pairs; a single
+// dispatch is a batch of one):
+//   X          double[nv][3]      ps vertex coordinates, pair after pair; within a
+//                                 pair the source vertices then the cut vertices
+//   foff       uint32[nf+1]       CSR offsets of ps faces into fidx
+//   fidx       uint32[foff[nf]]   global vertex ids (cut-mesh ids already offset)
+//   face_pair  uint32[nf]         pair id | kCutBit for cut-mesh faces
+//   fbox       double[nf][6]      exact fp64 face boxes (cut boxes enlarged by eps)
+//   tree       Node[Nc-1]         LBVH over all cut faces, key = pair << 30 | Morton
+//   pairs      uint64[P]          (source face << 32 | cut face), global ids
+//   tests      Test[T]            culled edge-face tests
+//   records    Record[R]          intersection records, sorted by (edge, face)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcgpu {
+
+constexpr uint32_t kCutBit = 0x80000000u;
+constexpr int32_t kNoBad = 0x7F7F7F7F; // pair_bad when no face is degenerate (memset 0x7F)
+constexpr int kMortonBits = 30;
+
+struct __align__(16) Node {
+    float4 b0;            // left  lo.x lo.y lo.z hi.x
+    float4 b1;            // left  hi.y hi.z | right lo.x lo.y
+    float4 b2;            // right lo.z hi.x hi.y hi.z
+    int32_t child[2];     // >= 0: internal node; < 0: ~(sorted leaf position)
+    uint32_t prange[2];   // pair-id range of each child: lo | hi << 16
+};
+
+struct Test {
+    uint32_t q, r;    // oriented edge (global vertex ids)
+    uint32_t g;       // tested face (global)
+    uint32_t f0, f1;  // faces of the edge (f0: lowest, owns the orientation), f1 may be kNone
+    uint32_t slot;    // halfedge slot of q->r in f0 (edge creation order)
+};
+
+struct Problem {
+    uint32_t n_pairs;
+    uint32_t nv, nf;
+    uint32_t ns, nc;            // total source / cut faces
+    const double* X;
+    const uint32_t* foff;
+    const uint32_t* fidx;
+    const uint32_t* face_pair;
+    // per pair tables [n_pairs (+1)]
+    const uint32_t* pair_fbase; // first ps face of the pair
+    const uint32_t* pair_fs;    // source faces of the pair
+    const uint32_t* pair_vbase; // first ps vertex of the pair
+    const uint32_t* pair_vs;    // source vertices of the pair
+    const uint32_t* pair_sbase; // first position of the pair in the source-face list
+    const uint32_t* pair_cbase; // first position of the pair in the cut-face list
+    const double* pair_eps;     // cut-box enlargement
+    int all_triangles;          // foff[f] == 3f
+};
+
+struct Work {
+    double* fbox;                     // [nf*6]
+    unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
+    // sort buffers (keys u32 for one pair, u64 for batches)
+    void* skeys[2];                   // source-face keys
+    uint32_t* svals[2];
+    void* ckeys[2];                   // cut-face keys
+    uint32_t* cvals[2];
+    uint32_t* sort_temp;
+    Node* nodes;                      // [nc-1]
+    int32_t* parent;                  // [2nc-1]
+    uint32_t* refit_flag;             // [nc-1]
+    unsigned long long* pairs;        // [pair_cap]
+    uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
+                                      //        5..7 escalations
+    uint8_t* cand;                    // [nf]
+    uint32_t* plane_slot;             // [nf]
+    void* planes;                     // FacePlane[cap]
+    uint32_t* poly_list;              // [nf] faces with > 3 vertices among candidates
+    uint8_t* vneed;                   // [nv]
+    uint32_t* voff;                   // [nv+1]
+    uint32_t* vcur;                   // [nv]
+    uint32_t* vface;                  // [incidence cap]
+    uint32_t* scan_temp;
+    Test* tests;                      // [test_cap]
+    int8_t* test_info;                // [test_cap*4]
+    unsigned long long* rec_key[2];   // [test_cap]
+    uint32_t* rec_val[2];
+    double* rec_pt_raw;               // [test_cap*3]
+    uint32_t* rec_ids;                // [test_cap*5] final, sorted
+    double* rec_pts;                  // [test_cap*3] final, sorted
+    uint32_t* pair_status;            // [n_pairs] ST_* bits
+    int32_t* pair_bad;                // [n_pairs] lowest degenerate ps face (local), INT_MAX if none
+    uint32_t* pair_nrec;              // [n_pairs]
+    double* tri_scratch;              // polygon triplet scratch (24-byte entries)
+    uint64_t tri_scratch_cap;         // entries
+    uint64_t tri_stride;              // entries per polygon (largest C(n,3)); 0: no polygons
+    uint64_t pair_cap, test_cap, inc_cap, plane_cap;
+};
+
+// stage launchers (all asynchronous on `s`)
+void launch_bounds_morton(const Problem& P, Work& W, bool wide_keys, cudaStream_t s);
+int launch_sort(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s, int& cut_buf);
+void launch_hierarchy(const Problem& P, Work& W, bool wide_keys, int cut_buf, cudaStream_t s);
+void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s);
+void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s);
+void launch_tests(const Problem& P, Work& W, cudaStream_t s);
+void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s);
+int launch_records(const Problem& P, Work& W, uint32_t n_records, cudaStream_t s);
+
+} // namespace mcgpu

@@ -1,0 +1,223 @@
+// LSD radix sort of (key, uint32 value) pairs, 8-bit digits, stable.
+//
+// One pass = three launches:
+//   upsweep  : per-tile digit histogram (shared-memory atomics)
+//   scan     : exclusive scan of the digit-major [256 x tiles] table (one CTA)
+//   downsweep: each warp ranks its keys with __match_any_sync in input order,
+//              warps are combined per digit in shared memory, keys scatter to
+//              their global rank.
+// A tile is 256 threads x 16 keys. Keys and values stream through HBM once
+// per launch; the histogram table stays in L2.
+#include "fe_sort.cuh"
+
+namespace mcgpu {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;
+constexpr int kWarps = kThreads / 32;
+constexpr int kDigits = 256;
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_upsweep(const K* __restrict__ keys, uint32_t n, int shift,
+    uint32_t* __restrict__ hist, uint32_t tiles)
+{
+    __shared__ uint32_t h[kDigits];
+    for (int i = threadIdx.x; i < kDigits; i += kThreads) h[i] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kTile;
+    for (int i = 0; i < kItems; ++i) {
+        const size_t k = base + (size_t)i * kThreads + threadIdx.x;
+        if (k < n) atomicAdd(&h[(uint32_t)(keys[k] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDigits; i += kThreads) hist[(size_t)i * tiles + blockIdx.x] = h[i];
+}
+
+// exclusive scan of m entries by one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ a, uint32_t m)
+{
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (m + 1023) / 1024;
+    const uint32_t lo = threadIdx.x * per, hi = min(m, lo + per);
+    uint32_t s = 0;
+    for (uint32_t i = lo; i < hi; ++i) s += a[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
+    K* __restrict__ okeys, uint32_t* __restrict__ ovals, uint32_t n, int shift, const uint32_t* __restrict__ hist,
+    uint32_t tiles)
+{
+    __shared__ uint32_t wh[kWarps][kDigits];
+    __shared__ uint32_t goff[kDigits];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kWarps * kDigits; i += kThreads) (&wh[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < kDigits; i += kThreads) goff[i] = hist[(size_t)i * tiles + blockIdx.x];
+    __syncthreads();
+
+    const size_t wbase = (size_t)blockIdx.x * kTile + (size_t)warp * 32 * kItems;
+    K k[kItems];
+    uint32_t v[kItems], rank[kItems];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const size_t idx = wbase + (size_t)i * 32 + lane;
+        const bool ok = idx < n;
+        k[i] = ok ? keys[idx] : (K)0;
+        v[i] = ok ? vals[idx] : 0u;
+        const uint32_t d = ok ? ((uint32_t)(k[i] >> shift) & 0xFFu) : 0x100u; // 0x100: padding, no digit
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t prev = 0;
+        if (ok) prev = wh[warp][d];
+        __syncwarp();
+        if (ok && (peers & lt) == 0) wh[warp][d] = prev + __popc(peers);
+        __syncwarp();
+        rank[i] = prev + __popc(peers & lt);
+    }
+    __syncthreads();
+    // per digit: exclusive prefix across warps, plus the tile's global offset
+    for (int d = threadIdx.x; d < kDigits; d += kThreads) {
+        uint32_t run = goff[d];
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wh[w][d];
+            wh[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const size_t idx = wbase + (size_t)i * 32 + lane;
+        if (idx < n) {
+            const uint32_t d = (uint32_t)(k[i] >> shift) & 0xFFu;
+            const uint32_t dst = wh[warp][d] + rank[i];
+            okeys[dst] = k[i];
+            ovals[dst] = v[i];
+        }
+    }
+}
+} // namespace
+
+namespace {
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_block_reduce(const uint32_t* __restrict__ a, uint32_t n,
+    uint32_t* __restrict__ bsum)
+{
+    __shared__ uint32_t ws[32];
+    const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t s = 0;
+    for (int i = 0; i < kScanItems; ++i)
+        if (base + i < n) s += a[base + i];
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = ws[threadIdx.x];
+        for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_block_scan(uint32_t* __restrict__ a, uint32_t n,
+    const uint32_t* __restrict__ boff, uint32_t* __restrict__ total_out)
+{
+    __shared__ uint32_t ws[32];
+    const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], s = 0;
+    for (int i = 0; i < kScanItems; ++i) {
+        v[i] = base + i < n ? a[base + i] : 0u;
+        s += v[i];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = ws[lane], y = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, y, o);
+            if (lane >= o) y += t;
+        }
+        ws[lane] = y - x;
+    }
+    __syncthreads();
+    uint32_t run = boff[blockIdx.x] + ws[w] + inc - s;
+    for (int i = 0; i < kScanItems; ++i) {
+        if (base + i < n) a[base + i] = run;
+        run += v[i];
+    }
+    if (total_out && blockIdx.x == gridDim.x - 1 && threadIdx.x == kScanThreads - 1) *total_out = run;
+}
+} // namespace
+
+size_t scan_temp_bytes(uint32_t n)
+{
+    const uint32_t nb = (n + kScanTile - 1) / kScanTile;
+    return (size_t)(nb ? nb : 1) * sizeof(uint32_t);
+}
+
+void exclusive_scan(uint32_t* a, uint32_t n, uint32_t* total_out, uint32_t* temp, cudaStream_t s)
+{
+    if (n == 0) {
+        if (total_out) cudaMemsetAsync(total_out, 0, sizeof(uint32_t), s);
+        return;
+    }
+    const uint32_t nb = (n + kScanTile - 1) / kScanTile;
+    k_block_reduce<<<nb, kScanThreads, 0, s>>>(a, n, temp);
+    k_scan<<<1, 1024, 0, s>>>(temp, nb);
+    k_block_scan<<<nb, kScanThreads, 0, s>>>(a, n, temp, total_out);
+}
+
+size_t radix_sort_temp_bytes(uint32_t n)
+{
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    return (size_t)kDigits * (tiles ? tiles : 1) * sizeof(uint32_t);
+}
+
+template <typename K>
+int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
+    uint32_t* temp, cudaStream_t s)
+{
+    if (n == 0) return 0;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    int cur = 0;
+    K* kb[2] = { keys, keys_alt };
+    uint32_t* vb[2] = { vals, vals_alt };
+    for (int shift = begin_bit; shift < end_bit; shift += 8) {
+        k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);
+        k_scan<<<1, 1024, 0, s>>>(temp, kDigits * tiles);
+        k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles);
+        cur ^= 1;
+    }
+    return cur;
+}
+
+template int radix_sort_pairs<uint32_t>(uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t, int, int, uint32_t*,
+    cudaStream_t);
+template int radix_sort_pairs<unsigned long long>(unsigned long long*, uint32_t*, unsigned long long*, uint32_t*,
+    uint32_t, int, int, uint32_t*, cudaStream_t);
+
+} // namespace mcgpu

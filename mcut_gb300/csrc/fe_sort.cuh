@@ -1,0 +1,23 @@
+// Device radix sort and scan used by the front-end kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mcgpu {
+
+// Scratch (bytes) the sort needs for n keys.
+size_t radix_sort_temp_bytes(uint32_t n);
+
+// Sorts (keys, vals) by bits [begin_bit, end_bit) of the key, stably.
+// Ping-pongs between (keys, vals) and (keys_alt, vals_alt); returns 0 if the
+// result is in (keys, vals), 1 if in the alternates.
+template <typename K>
+int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
+    uint32_t* temp, cudaStream_t s);
+
+// In-place exclusive scan of n uint32 (n+1-th element receives the total if
+// total_out != nullptr). temp: scan_temp_bytes(n).
+size_t scan_temp_bytes(uint32_t n);
+void exclusive_scan(uint32_t* a, uint32_t n, uint32_t* total_out, uint32_t* temp, cudaStream_t s);
+
+} // namespace mcgpu

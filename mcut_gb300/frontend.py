@@ -1,0 +1,161 @@
+"""Host-side mirror of the reference's front-end seam, over the C ABI.
+
+    ctx = Context()
+    r = ctx.dispatch(src, cut)               # build_oibvh x2 + intersectOIBVHs +
+                                             # kernel.cpp:1781-3206, on the GPU
+    r.status, r.records, r.points
+
+A mesh is a dict(v=[V,3] float64, f=flat uint32 indices, fs=uint32 sizes or
+None for triangles), as mcut_gb300.meshgen makes them. Identifiers follow the
+reference's polygon soup (see include/mcut_gb300.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _as_mesh(m, float_input=False):
+    v = np.ascontiguousarray(m["v"], dtype=np.float32 if float_input else np.float64)
+    f = np.ascontiguousarray(m["f"], dtype=np.uint32)
+    fs = None if m.get("fs") is None else np.ascontiguousarray(m["fs"], dtype=np.uint32)
+    nf = int(fs.shape[0]) if fs is not None else int(f.shape[0] // 3)
+    cm = L.Mesh(v.ctypes.data, f.ctypes.data, None if fs is None else fs.ctypes.data, v.shape[0], nf)
+    return cm, (v, f, fs)
+
+
+@dataclass
+class FrontEndResult:
+    status: int
+    status_name: str
+    bad_face: int
+    cut_eps: float
+    num_pairs: int
+    num_tests: int
+    num_records: int
+    escalations: tuple
+    stage_ms: dict
+    record_ids: np.ndarray = field(default=None)     # [R,5] q, r, face, f0, f1
+    record_points: np.ndarray = field(default=None)  # [R,3]
+    pairs: np.ndarray = field(default=None)          # [P,2]
+    tests: np.ndarray = field(default=None)          # [T,3]
+    test_info: np.ndarray = field(default=None)      # [T,4] int8
+
+
+class Context:
+    """One GPU context (stream + device memory pool), like an MCUT context."""
+
+    def __init__(self, device: int = 0):
+        self._lib = L.load()
+        self._h = C.c_void_p()
+        L.check(self._lib.mcgpu_context_create(C.byref(self._h), int(device)), "mcgpu_context_create")
+
+    def close(self):
+        if self._h:
+            self._lib.mcgpu_context_release(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _get(self, query, dtype, cols):
+        n = C.c_uint64(0)
+        L.check(self._lib.mcgpu_get_data(self._h, query, 0, None, C.byref(n)), "mcgpu_get_data(size)")
+        out = np.empty(n.value // np.dtype(dtype).itemsize, dtype=dtype)
+        if n.value:
+            L.check(self._lib.mcgpu_get_data(self._h, query, n.value, out.ctypes.data, C.byref(n)),
+                    "mcgpu_get_data")
+        return out.reshape(-1, cols)
+
+    def dispatch(self, src, cut, cut_eps: float | None = None, recentre: bool = True, float_input: bool = False,
+                 keep_tests: bool = False, keep_pairs: bool = False, profile: bool = False,
+                 fetch: bool = True) -> FrontEndResult:
+        flags = (L.RECENTRE if recentre else 0) | (L.VERTEX_ARRAY_FLOAT if float_input else 0) \
+            | (L.KEEP_TESTS if keep_tests else 0) | (L.KEEP_PAIRS if keep_pairs else 0) \
+            | (L.PROFILE if profile else 0)
+        ms, ks = _as_mesh(src, float_input)
+        mc, kc = _as_mesh(cut, float_input)
+        sm = L.Summary()
+        rc = self._lib.mcgpu_dispatch(self._h, flags, C.byref(ms), C.byref(mc),
+                                      float(cut_eps if cut_eps is not None else 0.0), C.byref(sm))
+        L.check(rc, "mcgpu_dispatch")
+        del ks, kc
+        r = FrontEndResult(
+            status=sm.status, status_name=L.STATUS_NAMES[sm.status], bad_face=sm.bad_face, cut_eps=sm.cut_eps,
+            num_pairs=sm.num_pairs, num_tests=sm.num_tests, num_records=sm.num_records,
+            escalations=tuple(sm.escalations), stage_ms=dict(zip(L.STAGES, list(sm.stage_ms))))
+        if fetch:
+            r.record_ids = self._get(L.DATA_RECORD_IDS, np.uint32, 5)
+            r.record_points = self._get(L.DATA_RECORD_POINTS, np.float64, 3)
+            if keep_pairs:
+                r.pairs = self._get(L.DATA_PAIRS, np.uint32, 2)
+            if keep_tests:
+                r.tests = self._get(L.DATA_TESTS, np.uint32, 3)
+                r.test_info = self._get(L.DATA_TEST_INFO, np.int8, 4)
+        return r
+
+    def vertices(self):
+        return self._get(L.DATA_VERTICES, np.float64, 3)
+
+    def face_boxes(self):
+        return self._get(L.DATA_FACE_BOXES, np.float64, 6)
+
+    def dispatch_batch(self, pairs, recentre: bool = True, cut_eps=None, fetch: bool = True):
+        """Many independent (src, cut) pairs in one pass. Returns per-pair
+        (summary dict, record ids, record points)."""
+        n = len(pairs)
+        ms = (L.Mesh * n)()
+        mc = (L.Mesh * n)()
+        keep = []
+        for i, (s, c) in enumerate(pairs):
+            a, ka = _as_mesh(s)
+            b, kb = _as_mesh(c)
+            ms[i], mc[i] = a, b
+            keep += [ka, kb]
+        sums = (L.Summary * n)()
+        eps = None
+        if cut_eps is not None:
+            eps = (C.c_double * n)(*[float(e) for e in cut_eps])
+        flags = L.RECENTRE if recentre else 0
+        L.check(self._lib.mcgpu_dispatch_batch(self._h, flags, n, ms, mc, eps, sums), "mcgpu_dispatch_batch")
+        del keep
+        out = []
+        for i in range(n):
+            s = sums[i]
+            ids = pts = None
+            if fetch:
+                ids = self._batch_get(i, L.DATA_RECORD_IDS, np.uint32, 5)
+                pts = self._batch_get(i, L.DATA_RECORD_POINTS, np.float64, 3)
+            out.append((dict(status=s.status, bad_face=s.bad_face, cut_eps=s.cut_eps, num_records=s.num_records),
+                        ids, pts))
+        return out
+
+    def _batch_get(self, pair, query, dtype, cols):
+        n = C.c_uint64(0)
+        L.check(self._lib.mcgpu_get_batch_data(self._h, pair, query, 0, None, C.byref(n)), "get_batch_data")
+        out = np.empty(n.value // np.dtype(dtype).itemsize, dtype=dtype)
+        if n.value:
+            L.check(self._lib.mcgpu_get_batch_data(self._h, pair, query, n.value, out.ctypes.data, C.byref(n)),
+                    "get_batch_data")
+        return out.reshape(-1, cols)
+
+
+def recentre(src, cut, float_input: bool = False):
+    """The reference's recentring (host): -> (src_xyz, cut_xyz, cut_eps)."""
+    lib = L.load()
+    ms, ks = _as_mesh(src, float_input)
+    mc, kc = _as_mesh(cut, float_input)
+    so = np.empty((ms.num_vertices, 3), np.float64)
+    co = np.empty((mc.num_vertices, 3), np.float64)
+    eps = C.c_double(0)
+    L.check(lib.mcgpu_recentre(L.VERTEX_ARRAY_FLOAT if float_input else 0, C.byref(ms), C.byref(mc),
+                               so.ctypes.data, co.ctypes.data, C.byref(eps)), "mcgpu_recentre")
+    del ks, kc
+    return so, co, eps.value
