@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Throughput of the MCUT intersection front end on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one step = one front-end dispatch of one mesh pair): the single
+large pair, x16-scaled so the reference accepts its faces -- a level-7
+icosphere with radial noise N(0, 0.01) (327,680 triangles) against a
+1024 x 1024 height field of 8 random sinusoids (2,093,058 triangles),
+all coordinates multiplied by 16 (exact in fp64). Synthetic, seeded.
+
+Metric: cut pairs/s (completed front-end dispatches per second: trees
+built, traversal, narrow phase, records + status delivered).
+  value : inputs resident in HBM (the reference's internal, recentred
+          coordinates and face indices), L2 flushed before every step,
+          each step timed with CUDA events.
+  e2e   : the same dispatch through the C ABI with host buffers: the
+          host->device upload of coordinates + indices and the
+          device->host read of the records inside the timed region.
+The reference arm (--impl reference) times the CPU restatement of the
+reference's front end (oracle/, the same algorithm: OIBVH build, serial
+breadth-first traversal, edge-face narrow phase) on the host cores.
+
+With torchrun (N > 1) every rank runs its own replica of the workload on
+its GPU (the front end has no cross-GPU exchange): value is the sum of the
+ranks' throughputs over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("sphere_heightfield_x16: level-7 noisy icosphere (327,680 tris) vs 1024x1024 height field "
+            "(2,093,058 tris), coordinates x16")
+METRIC = "cut pairs/s"
+UNIT = "pairs/s"
+
+# algorithmic bytes per unit of work, per stage
+BYTES = {
+    "bounds": ("face", 80),        # read idx 12 + positions ~12, write box 48 + key 4 + id 4
+    "sort": ("face", 68),          # 4 passes x (8 read + 8 write) + histogram
+    "hierarchy": ("node", 160),    # children/parent 12, 2 child boxes read, box write, flag
+    "traverse": ("pair-of-trees", None),
+    "adjacency": ("face", 40),     # incidence count + fill over indices, planes of candidates
+    "narrow": ("test", 152),       # edge 2x24 + face 3x24 + plane 32 (+40 per record)
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh,
+                                      stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.p:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for k, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(k)
+        except Exception:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload():
+    from mcut_gb300 import meshgen
+    return meshgen.sphere_heightfield(16.0)
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_port_run(src, cut, steps, warmup, threads):
+    """The oracle (CPU restatement of the reference front end), timed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    for _ in range(warmup):
+        oracle.front_end(src, cut, impl="port", threads=threads)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        oracle.front_end(src, cut, impl="port", threads=threads)
+        ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    src, cut = make_workload()
+    threads = os.cpu_count() or 1
+    steps = max(1, args.steps)
+    ts = cpu_port_run(src, cut, steps, min(args.warmup, 1), threads)
+    v = steps / sum(ts)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sum(ts) / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "path": "CPU restatement of the reference front end (oracle/)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} full front-end dispatches of the workload"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    import ctypes as C
+    from mcut_gb300 import Context, recentre
+    from mcut_gb300 import _lib as L
+    from mcut_gb300.frontend import _as_mesh
+
+    torch.cuda.set_device(local)
+    src, cut = make_workload()
+    sx, cx, eps = recentre(src, cut)
+    fs_, fc_ = src["f"], cut["f"]
+    ctx = Context(local)
+    lib = L.load()
+
+    # device-resident inputs: the reference's internal coordinates + indices
+    d_sx = torch.from_numpy(sx).cuda()
+    d_cx = torch.from_numpy(cx).cuda()
+    d_fs = torch.from_numpy(fs_.astype(np.int32)).cuda()
+    d_fc = torch.from_numpy(fc_.astype(np.int32)).cuda()
+    ms = L.Mesh(d_sx.data_ptr(), d_fs.data_ptr(), None, sx.shape[0], fs_.shape[0] // 3)
+    mc = L.Mesh(d_cx.data_ptr(), d_fc.data_ptr(), None, cx.shape[0], fc_.shape[0] // 3)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    sm = L.Summary()
+    flags = L.DEVICE_POINTERS | L.PROFILE
+
+    def step_dev():
+        L.check(lib.mcgpu_dispatch(ctx._h, flags, C.byref(ms), C.byref(mc), eps, C.byref(sm)), "dispatch")
+
+    for _ in range(max(args.warmup, 3)):
+        step_dev()
+    torch.cuda.synchronize()
+    barrier(world)
+    times, stage_acc, launches = [], {k: 0.0 for k in L.STAGES}, 0
+    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st.record()
+            step_dev()
+            en.record()
+            torch.cuda.synchronize()
+            times.append(st.elapsed_time(en))
+            for k, v in zip(L.STAGES, sm.stage_ms):
+                stage_acc[k] += v
+            launches += sm.kernel_launches
+    barrier(world)
+    tot_ms = reduce_max(sum(times), world)
+    value = world * args.steps / (tot_ms / 1e3)
+    summ = {"status": L.STATUS_NAMES[sm.status], "pairs": int(sm.num_pairs), "tests": int(sm.num_tests),
+            "records": int(sm.num_records), "escalations": list(map(int, sm.escalations))}
+
+    # end to end through the C ABI with host buffers (internal coordinates as
+    # the reference's hmesh holds them)
+    hs, _k1 = _as_mesh(dict(v=sx, f=fs_, fs=None))
+    hc, _k2 = _as_mesh(dict(v=cx, f=fc_, fs=None))
+    rid = np.empty(max(1, sm.num_records) * 5, np.uint32)
+    rpt = np.empty(max(1, sm.num_records) * 3, np.float64)
+    nb = C.c_uint64(0)
+
+    def step_e2e():
+        L.check(lib.mcgpu_dispatch(ctx._h, 0, C.byref(hs), C.byref(hc), eps, C.byref(sm)), "dispatch")
+        L.check(lib.mcgpu_get_data(ctx._h, L.DATA_RECORD_IDS, rid.nbytes, rid.ctypes.data, C.byref(nb)), "ids")
+        L.check(lib.mcgpu_get_data(ctx._h, L.DATA_RECORD_POINTS, rpt.nbytes, rpt.ctypes.data, C.byref(nb)), "pts")
+
+    for _ in range(2):
+        step_e2e()
+    barrier(world)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_tot = reduce_max(sum(e2e_t), world)
+    e2e_value = world * args.steps / e2e_tot
+    h2d = sx.nbytes + cx.nbytes + fs_.nbytes + fc_.nbytes
+    d2h = int(sm.num_records) * (20 + 24)
+
+    if rank != 0:
+        return
+    # roofline of the dominant stage
+    hbm, src_peak = peaks()
+    per = {k: v / args.steps for k, v in stage_acc.items()}
+    comp = {k: per[k] for k in ("bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow")}
+    dom = max(comp, key=comp.get)
+    Fs, Fc = fs_.shape[0] // 3, fc_.shape[0] // 3
+    if dom == "traverse":
+        algo = 48 * (2 * Fs + 2 * Fc) + 8 * summ["pairs"]
+        units = f"48 B x (2Fs + 2Fc) + 8 B x {summ['pairs']} pairs"
+    elif dom == "narrow":
+        algo = 152 * summ["tests"] + 40 * summ["records"]
+        units = f"152 B x {summ['tests']} tests + 40 B x {summ['records']} records"
+    elif dom == "hierarchy":
+        algo = 160 * (Fc - 1)
+        units = f"160 B x {Fc - 1} nodes"
+    else:
+        algo = BYTES[dom][1] * (Fs + Fc)
+        units = f"{BYTES[dom][1]} B x {Fs + Fc} faces"
+    achieved = algo / (per[dom] / 1e3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get(dom)
+        except Exception:
+            traffic = None
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        ts = cpu_port_run(src, cut, 1, 0, threads)
+        cpu = {"value": 1.0 / ts[0], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "1 full front-end dispatch of the workload (oracle/, CPU restatement)"}
+    ms_step = tot_ms / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed (256 MB write) before every step",
+                   "parallelism": f"replicas x{world}", "path": "plain GPU per-dispatch path"},
+        "latency_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "algorithmic_bytes": algo,
+                     "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)"},
+        "stage_ms": {k: round(v, 4) for k, v in per.items()},
+        "front_end": summ,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * e2e_tot / args.steps},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -39,7 +39,8 @@ class Mesh(C.Structure):
 class Summary(C.Structure):
     _fields_ = [("status", C.c_int32), ("bad_face", C.c_int32), ("cut_eps", C.c_double),
                 ("num_pairs", C.c_uint64), ("num_tests", C.c_uint64), ("num_records", C.c_uint64),
-                ("escalations", C.c_uint64 * 3), ("stage_ms", C.c_float * 8)]
+                ("escalations", C.c_uint64 * 3), ("stage_ms", C.c_float * 8),
+                ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class LibraryNotBuilt(RuntimeError):

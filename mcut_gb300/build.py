@@ -20,8 +20,11 @@ OUT = os.path.join(HERE, "libmcut_gb300.so")
 OBJ = os.path.join(HERE, "_build")
 SOURCES = ["fe_sort.cu", "fe_kernels.cu", "fe_api.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
+# --fmad=false keeps device a*b+c as two roundings; -ffp-contract=off does the
+# same for the host code (aarch64 g++ would otherwise fuse them, which changes
+# the recentred coordinates the reference computes).
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "--fmad=false", "-std=c++17",
-         "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+         "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 
 def _compile(src: str) -> str:

@@ -370,6 +370,7 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         ck(cudaStreamSynchronize(s), "sync foff"); // `off` is a pageable temporary
     }
     uint32_t* face_pair = c->buf[B_FPAIR].get<uint32_t>(L.nf);
+    g_launches++;
     k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf);
 
     Problem& P = c->P;
@@ -408,6 +409,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         return fail(MCGPU_INVALID_VALUE, "float vertices need MCGPU_RECENTRE");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     c->flags = flags;
+    const unsigned long long launches0 = g_launches;
     int rc = build_layout(c, flags, n, srcs, cuts, eps);
     if (rc != MCGPU_OK) return rc;
     Layout& L = c->L;
@@ -446,6 +448,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
 
     // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
+    g_launches++;
     k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
     ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
     ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
@@ -569,6 +572,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
             }
         }
     }
+    for (auto& m : c->sums) m.kernel_launches = (uint32_t)(g_launches - launches0);
     if (out) {
         if (n == 1) *out = c->sums[0];
         else memcpy(out, c->sums.data(), sizeof(mcgpu_summary) * n);

@@ -815,7 +815,9 @@ int grid_for(uint64_t n)
 void launch_bounds_morton(const Problem& P, Work& W, bool wide, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
+    g_launches++;
     k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, W.pair_status);
+    g_launches++;
     if (wide)
         k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box,
             (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0]);
@@ -846,18 +848,21 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
     const int n = (int)P.nc;
     if (n < 2) return;
     const int g = grid_for(n);
+    g_launches++;
     if (wide)
         k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.ckeys[cut_buf], n, W.nodes,
             W.parent);
     else
         k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.ckeys[cut_buf], n, W.nodes, W.parent);
     cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
+    g_launches++;
     k_refit<<<g, kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], n, W.nodes, W.parent, W.refit_flag);
 }
 
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
 {
     const int g = grid_for(P.ns);
+    g_launches++;
     if (deep)
         k_traverse<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], (int)P.nc, W.nodes,
             W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
@@ -869,22 +874,28 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
 void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
+    g_launches++;
     k_planes<<<g, kBlock, 0, s>>>(P, W.cand, W.plane_slot, (FacePlane*)W.planes, W.plane_cap, W.counters,
         W.poly_list, W.pair_bad);
+    if (W.tri_stride) g_launches++;
     if (W.tri_stride)
         k_triplets<<<grid_for(1024), kBlock, 0, s>>>(P, W.poly_list, W.counters, W.plane_slot, (FacePlane*)W.planes,
             (Trip*)W.tri_scratch, W.tri_scratch_cap, W.tri_stride, W.pair_status);
+    g_launches++;
     k_mark_vertices<<<g, kBlock, 0, s>>>(P, W.cand, W.vneed);
     cudaMemsetAsync(W.voff, 0, sizeof(uint32_t) * ((size_t)P.nv + 1), s);
+    g_launches++;
     k_vf_count<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff);
     exclusive_scan(W.voff, P.nv + 1, nullptr, W.scan_temp, s);
     cudaMemsetAsync(W.vcur, 0, sizeof(uint32_t) * (size_t)P.nv, s);
+    g_launches++;
     k_vf_fill<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff, W.vcur, W.vface, W.inc_cap);
 }
 
 void launch_tests(const Problem& P, Work& W, cudaStream_t s)
 {
     const int g = grid_for(W.pair_cap);
+    g_launches++;
     k_pair_tests<<<g, kBlock, 0, s>>>(P, W.fbox, W.pairs, W.counters, W.pair_cap, W.voff, W.vface, W.tests,
         W.test_cap, W.counters, W.pair_bad, W.pair_status);
 }
@@ -892,6 +903,7 @@ void launch_tests(const Problem& P, Work& W, cudaStream_t s)
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
 {
     const int g = grid_for(W.test_cap);
+    g_launches++;
     k_narrow<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
         W.pair_nrec);
@@ -904,6 +916,7 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
     // monotone in the pair index, so records come out grouped by pair
     const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1],
         nrec, 0, 64, W.sort_temp, s);
+    g_launches++;
     k_gather_records<<<grid_for(nrec), kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids,
         W.rec_pts);
     return buf;

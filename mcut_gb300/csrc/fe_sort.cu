@@ -12,6 +12,8 @@
 
 namespace mcgpu {
 
+unsigned long long g_launches = 0;
+
 namespace {
 constexpr int kThreads = 256;
 constexpr int kItems = 16;
@@ -186,6 +188,7 @@ void exclusive_scan(uint32_t* a, uint32_t n, uint32_t* total_out, uint32_t* temp
         return;
     }
     const uint32_t nb = (n + kScanTile - 1) / kScanTile;
+    g_launches += 3;
     k_block_reduce<<<nb, kScanThreads, 0, s>>>(a, n, temp);
     k_scan<<<1, 1024, 0, s>>>(temp, nb);
     k_block_scan<<<nb, kScanThreads, 0, s>>>(a, n, temp, total_out);
@@ -207,6 +210,7 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
     K* kb[2] = { keys, keys_alt };
     uint32_t* vb[2] = { vals, vals_alt };
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
+        g_launches += 3;
         k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);
         k_scan<<<1, 1024, 0, s>>>(temp, kDigits * tiles);
         k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles);

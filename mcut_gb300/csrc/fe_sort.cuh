@@ -5,6 +5,9 @@
 
 namespace mcgpu {
 
+// kernels launched by this library since load (reported per dispatch)
+extern unsigned long long g_launches;
+
 // Scratch (bytes) the sort needs for n keys.
 size_t radix_sort_temp_bytes(uint32_t n);
 

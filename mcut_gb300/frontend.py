@@ -39,6 +39,7 @@ class FrontEndResult:
     num_records: int
     escalations: tuple
     stage_ms: dict
+    kernel_launches: int
     record_ids: np.ndarray = field(default=None)     # [R,5] q, r, face, f0, f1
     record_points: np.ndarray = field(default=None)  # [R,3]
     pairs: np.ndarray = field(default=None)          # [P,2]
@@ -90,7 +91,8 @@ class Context:
         r = FrontEndResult(
             status=sm.status, status_name=L.STATUS_NAMES[sm.status], bad_face=sm.bad_face, cut_eps=sm.cut_eps,
             num_pairs=sm.num_pairs, num_tests=sm.num_tests, num_records=sm.num_records,
-            escalations=tuple(sm.escalations), stage_ms=dict(zip(L.STAGES, list(sm.stage_ms))))
+            escalations=tuple(sm.escalations), stage_ms=dict(zip(L.STAGES, list(sm.stage_ms))),
+            kernel_launches=sm.kernel_launches)
         if fetch:
             r.record_ids = self._get(L.DATA_RECORD_IDS, np.uint32, 5)
             r.record_points = self._get(L.DATA_RECORD_POINTS, np.float64, 3)

@@ -59,7 +59,8 @@ def test_records_carry_edge_faces(ctx):
     src_edge = ids[:, 3] < nsf
     assert np.all((ids[:, 2] >= nsf) == src_edge)
     assert np.all((ids[:, 4] == 0xFFFFFFFF) | ((ids[:, 4] < nsf) == src_edge))
-    assert np.all(ids[:, 3] < np.where(ids[:, 4] == 0xFFFFFFFF, 2**32, ids[:, 4]))
+    f1 = ids[:, 4].astype(np.int64)
+    assert np.all(ids[:, 3].astype(np.int64) < np.where(f1 == 0xFFFFFFFF, 2**32, f1))
 
 
 def test_deterministic_repeat(ctx):
