@@ -50,9 +50,24 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
 // ---------------------------------------------------------------------------
 // face boxes + per-mesh boxes (bvh.cpp:242-368)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void mesh_box_flush(unsigned long long* __restrict__ mesh_box, uint32_t key,
+    const unsigned long long* lo, const unsigned long long* hi)
+{
+    unsigned long long* mb = mesh_box + (size_t)key * 6;
+    for (int j = 0; j < 3; ++j) {
+        atomicMin(&mb[j], lo[j]);
+        atomicMax(&mb[3 + j], hi[j]);
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
     unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
 {
+    // per-mesh boxes (they only steer Morton codes): each thread folds its
+    // faces of one mesh in registers, a warp whose lanes all hold the same
+    // mesh folds once more with shuffles, then one atomic per value
+    uint32_t key = kNone;
+    unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         const uint32_t fp = P.face_pair[f];
         const uint32_t p = fp & ~kCutBit;
@@ -79,12 +94,29 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         d[0] = make_double2(b.mn[0], b.mn[1]);
         d[1] = make_double2(b.mn[2], b.mx[0]);
         d[2] = make_double2(b.mx[1], b.mx[2]);
-        // mesh box (only steers Morton codes: any order of min/max is exact)
-        unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
-        for (int j = 0; j < 3; ++j) {
-            atomicMin(&mb[j], ord_of(b.mn[j]));
-            atomicMax(&mb[3 + j], ord_of(b.mx[j]));
+        const uint32_t k = p * 2 + (is_cut ? 1u : 0u);
+        if (k != key) {
+            if (key != kNone) mesh_box_flush(mesh_box, key, lo, hi);
+            key = k;
+            for (int j = 0; j < 3; ++j) { lo[j] = ~0ull; hi[j] = 0ull; }
         }
+        for (int j = 0; j < 3; ++j) {
+            lo[j] = min(lo[j], ord_of(b.mn[j]));
+            hi[j] = max(hi[j], ord_of(b.mx[j]));
+        }
+    }
+    const unsigned full = 0xFFFFFFFFu;
+    const uint32_t k0 = __shfl_sync(full, key, 0);
+    if (__all_sync(full, key == k0)) {
+        if (key == kNone) return;
+        for (int off = 16; off; off >>= 1)
+            for (int j = 0; j < 3; ++j) {
+                lo[j] = min(lo[j], __shfl_xor_sync(full, lo[j], off));
+                hi[j] = max(hi[j], __shfl_xor_sync(full, hi[j], off));
+            }
+        if ((threadIdx.x & 31) == 0) mesh_box_flush(mesh_box, key, lo, hi);
+    } else if (key != kNone) {
+        mesh_box_flush(mesh_box, key, lo, hi);
     }
 }
 
@@ -668,7 +700,7 @@ __device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint
     double q[2];
     project2(pl.P, pt, q);
     int rc = 0, lc = 0;
-    double prv[2], first[2];
+    double prv[2];
     {
         double v[3];
         load_xyz(P.X, face_vertex(P, o, n, n - 1), v);
@@ -678,7 +710,6 @@ __device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint
         double v[3], c[2];
         load_xyz(P.X, face_vertex(P, o, n, i), v);
         project2(pl.P, v, c);
-        if (i == 0) { first[0] = c[0]; first[1] = c[1]; }
         const double xi = c[0] - q[0], yi = c[1] - q[1];
         if (xi == 0.0 && yi == 0.0) return 'v';
         const double xl = prv[0] - q[0], yl = prv[1] - q[1];
@@ -691,7 +722,6 @@ __device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint
         }
         prv[0] = c[0]; prv[1] = c[1];
     }
-    (void)first;
     if ((rc & 1) != (lc & 1)) return 'e';
     return (rc & 1) ? 'i' : 'o';
 }
