@@ -152,6 +152,28 @@ int mcgpu_get_batch_data(mcgpu_context ctx, uint32_t pair, uint32_t query, uint6
 int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut, double* src_out, double* cut_out,
     double* cut_eps_out);
 
+/* Front-end dispatch that allocates no GPU or pinned memory. No counterpart
+ * in the reference (MCUT allocates freely on the host). It is for callers
+ * that may not call cudaMalloc when they need the records: a thread that is
+ * recording a CUDA graph on its stream, a plugin that must stay inside its
+ * host application's own memory arena, a frame loop that cannot wait on the
+ * driver's allocator. All scratch sits in one file-scope __device__ array of
+ * about 11 MB that every GPU loading this library keeps until exit.
+ * Limits: triangles only; at most 16384 vertices and 16384 faces over both
+ * meshes, 32768 candidate pairs, 65536 edge-face tests -- anything larger
+ * returns MCGPU_TOO_LARGE. Every call shares that array and it keeps the
+ * previous call's contents (each call clears what it needs): calls whose GPU
+ * work overlaps race, so serialise them. The first call on a device looks up
+ * the array's address; make it outside any stream capture.
+ * src/cut: DEVICE pointers to internal (recentred) double coordinates and
+ * uint32 triangle indices (face_sizes NULL). record_ids (uint32[5*capacity])
+ * and record_points (double[3*capacity]) are device buffers filled as
+ * MCGPU_DATA_RECORD_IDS / _POINTS of mcgpu_dispatch. stream: a cudaStream_t,
+ * or NULL for the default stream. Returns MCGPU_OK when it ran; the front
+ * end's outcome is out->status. */
+int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
+    uint32_t* record_ids, double* record_points, uint64_t record_capacity, mcgpu_summary* out);
+
 /* Human-readable description of the last failure on this thread. */
 const char* mcgpu_last_error(void);
 

@@ -75,6 +75,8 @@ def load():
                                          C.POINTER(C.c_uint64)]
     lib.mcgpu_recentre.argtypes = [C.c_uint32, C.POINTER(Mesh), C.POINTER(Mesh), C.c_void_p, C.c_void_p,
                                    C.POINTER(C.c_double)]
+    lib.mcgpu_dispatch_noalloc.argtypes = [C.c_void_p, C.POINTER(Mesh), C.POINTER(Mesh), C.c_double, C.c_void_p,
+                                           C.c_void_p, C.c_uint64, C.POINTER(Summary)]
     lib.mcgpu_last_error.restype = C.c_char_p
     for name in exported_names_in_header():
         if name not in ("mcgpu_last_error",):
