@@ -30,8 +30,18 @@ struct Box {
     double mn[3], mx[3];
 };
 
-__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }  // std::max
-__device__ __forceinline__ double dmin_ref(double a, double b) { return (b < a) ? b : a; }  // std::min
+// (a < b) for non-NaN doubles on the integer pipe: order-preserving bits,
+// except that -0 and +0 compare equal as in IEEE. GB300's fp64 pipe runs at a
+// small fraction of its integer / fp32 rate, so box code avoids it.
+__device__ __forceinline__ bool dlt_int(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long oa = ia < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)ia) : ia;
+    const long long ob = ib < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)ib) : ib;
+    return oa < ob;
+}
+__device__ __forceinline__ double dmax_ref(double a, double b) { return dlt_int(a, b) ? b : a; }  // std::max
+__device__ __forceinline__ double dmin_ref(double a, double b) { return dlt_int(b, a) ? b : a; }  // std::min
 
 __device__ __forceinline__ bool box_overlap(const Box& a, const Box& b)
 {

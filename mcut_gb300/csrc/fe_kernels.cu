@@ -60,63 +60,90 @@ __device__ __forceinline__ void mesh_box_flush(unsigned long long* __restrict__ 
     }
 }
 
+constexpr int kBoundsItems = 8; // faces per thread per tile; a tile is kBlock * kBoundsItems consecutive faces
+
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
     unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
 {
-    // per-mesh boxes (they only steer Morton codes): each thread folds its
-    // faces of one mesh in registers, a warp whose lanes all hold the same
-    // mesh folds once more with shuffles, then one atomic per value
-    uint32_t key = kNone;
-    unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
-    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
-        const uint32_t fp = P.face_pair[f];
-        const uint32_t p = fp & ~kCutBit;
-        const bool is_cut = (fp & kCutBit) != 0;
-        const uint32_t o = face_o(P, f), n = face_n(P, f);
-        const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
-        Box b;
-        for (int j = 0; j < 3; ++j) { b.mn[j] = 1.7976931348623157e308; b.mx[j] = -1.7976931348623157e308; }
-        bool bad = false;
-        for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t v = P.fidx[o + k];
-            if (v < vlo || v >= vhi) { bad = true; continue; }
-            double x[3];
-            load_xyz(P.X, v, x);
-            for (int j = 0; j < 3; ++j) { b.mx[j] = dmax_ref(b.mx[j], x[j]); b.mn[j] = dmin_ref(b.mn[j], x[j]); }
-        }
-        if (bad) atomicOr(&pair_status[p], ST_INVALID);
-        if (is_cut) {
-            const double eps = P.pair_eps[p];
-            if (eps > 0.0)
-                for (int j = 0; j < 3; ++j) { b.mx[j] = b.mx[j] + eps; b.mn[j] = b.mn[j] - eps; }
-        }
-        double2* d = reinterpret_cast<double2*>(fbox + (size_t)f * 6);
-        d[0] = make_double2(b.mn[0], b.mn[1]);
-        d[1] = make_double2(b.mn[2], b.mx[0]);
-        d[2] = make_double2(b.mx[1], b.mx[2]);
-        const uint32_t k = p * 2 + (is_cut ? 1u : 0u);
-        if (k != key) {
-            if (key != kNone) mesh_box_flush(mesh_box, key, lo, hi);
-            key = k;
-            for (int j = 0; j < 3; ++j) { lo[j] = ~0ull; hi[j] = 0ull; }
-        }
-        for (int j = 0; j < 3; ++j) {
-            lo[j] = min(lo[j], ord_of(b.mn[j]));
-            hi[j] = max(hi[j], ord_of(b.mx[j]));
-        }
-    }
-    const unsigned full = 0xFFFFFFFFu;
-    const uint32_t k0 = __shfl_sync(full, key, 0);
-    if (__all_sync(full, key == k0)) {
-        if (key == kNone) return;
-        for (int off = 16; off; off >>= 1)
-            for (int j = 0; j < 3; ++j) {
-                lo[j] = min(lo[j], __shfl_xor_sync(full, lo[j], off));
-                hi[j] = max(hi[j], __shfl_xor_sync(full, hi[j], off));
+    // Per-mesh boxes only steer Morton codes. Tiles are runs of consecutive
+    // faces, so a tile almost always belongs to one mesh: each thread folds
+    // its faces in registers, the block folds in shared memory, and one
+    // thread issues the atomics. Tiles that straddle meshes fall back to
+    // per-lane atomics.
+    __shared__ unsigned long long red[kBlock / 32][6];
+    const uint32_t tiles = (P.nf + kBlock * kBoundsItems - 1) / (kBlock * kBoundsItems);
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t key = kNone;
+        bool mixed = false;
+        unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
+        for (int it = 0; it < kBoundsItems; ++it) {
+            const uint32_t f = tile * (kBlock * kBoundsItems) + it * kBlock + threadIdx.x;
+            if (f >= P.nf) break;
+            const uint32_t fp = P.face_pair[f];
+            const uint32_t p = fp & ~kCutBit;
+            const bool is_cut = (fp & kCutBit) != 0;
+            const uint32_t o = face_o(P, f), n = face_n(P, f);
+            const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
+            Box b;
+            for (int j = 0; j < 3; ++j) { b.mn[j] = 1.7976931348623157e308; b.mx[j] = -1.7976931348623157e308; }
+            bool bad = false;
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t v = P.fidx[o + k];
+                if (v < vlo || v >= vhi) { bad = true; continue; }
+                double x[3];
+                load_xyz(P.X, v, x);
+                for (int j = 0; j < 3; ++j) { b.mx[j] = dmax_ref(b.mx[j], x[j]); b.mn[j] = dmin_ref(b.mn[j], x[j]); }
             }
-        if ((threadIdx.x & 31) == 0) mesh_box_flush(mesh_box, key, lo, hi);
-    } else if (key != kNone) {
-        mesh_box_flush(mesh_box, key, lo, hi);
+            if (bad) atomicOr(&pair_status[p], ST_INVALID);
+            if (is_cut) {
+                const double eps = P.pair_eps[p];
+                if (eps > 0.0)
+                    for (int j = 0; j < 3; ++j) { b.mx[j] = b.mx[j] + eps; b.mn[j] = b.mn[j] - eps; }
+            }
+            double2* d = reinterpret_cast<double2*>(fbox + (size_t)f * 6);
+            d[0] = make_double2(b.mn[0], b.mn[1]);
+            d[1] = make_double2(b.mn[2], b.mx[0]);
+            d[2] = make_double2(b.mx[1], b.mx[2]);
+            const uint32_t k = p * 2 + (is_cut ? 1u : 0u);
+            if (key != kNone && k != key) {
+                mesh_box_flush(mesh_box, key, lo, hi);
+                for (int j = 0; j < 3; ++j) { lo[j] = ~0ull; hi[j] = 0ull; }
+                mixed = true;
+            }
+            key = k;
+            for (int j = 0; j < 3; ++j) {
+                lo[j] = min(lo[j], ord_of(b.mn[j]));
+                hi[j] = max(hi[j], ord_of(b.mx[j]));
+            }
+        }
+        // block-uniform key? (threads without faces count as matching)
+        __shared__ uint32_t skey;
+        if (threadIdx.x == 0) skey = key;
+        __syncthreads();
+        const uint32_t k0 = skey;
+        const bool uniform = __syncthreads_and(!mixed && (key == k0 || key == kNone)) && k0 != kNone;
+        if (uniform) {
+            const unsigned full = 0xFFFFFFFFu;
+            for (int off = 16; off; off >>= 1)
+                for (int j = 0; j < 3; ++j) {
+                    lo[j] = min(lo[j], __shfl_xor_sync(full, lo[j], off));
+                    hi[j] = max(hi[j], __shfl_xor_sync(full, hi[j], off));
+                }
+            if ((threadIdx.x & 31) == 0)
+                for (int j = 0; j < 3; ++j) { red[threadIdx.x >> 5][j] = lo[j]; red[threadIdx.x >> 5][3 + j] = hi[j]; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int w = 1; w < kBlock / 32; ++w)
+                    for (int j = 0; j < 3; ++j) {
+                        lo[j] = min(lo[j], red[w][j]);
+                        hi[j] = max(hi[j], red[w][3 + j]);
+                    }
+                mesh_box_flush(mesh_box, k0, lo, hi);
+            }
+        } else if (key != kNone) {
+            mesh_box_flush(mesh_box, key, lo, hi);
+        }
+        __syncthreads();
     }
 }
 
@@ -142,11 +169,14 @@ __global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __re
         const bool is_cut = (fp & kCutBit) != 0;
         const Box b = load_box(fbox, f);
         const unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
+        // the code only orders leaves (any order gives the same pair set), so
+        // it is formed in fp32: fp64 division is slow on this part
         uint32_t c[3];
         for (int j = 0; j < 3; ++j) {
             const double lo = of_ord(mb[j]), hi = of_ord(mb[3 + j]);
-            const double mid = (b.mn[j] + b.mx[j]) / 2.0;
-            float t = (float)((mid - lo) / (hi - lo));
+            const float ext = (float)(hi - lo);
+            const float mid = (float)((b.mn[j] + b.mx[j]) * 0.5 - lo);
+            float t = ext > 0.0f ? __fdividef(mid, ext) : 0.0f;
             t = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
             c[j] = expand_bits((uint32_t)t);
         }

@@ -197,7 +197,8 @@ void exclusive_scan(uint32_t* a, uint32_t n, uint32_t* total_out, uint32_t* temp
 size_t radix_sort_temp_bytes(uint32_t n)
 {
     const uint32_t tiles = (n + kTile - 1) / kTile;
-    return (size_t)kDigits * (tiles ? tiles : 1) * sizeof(uint32_t);
+    const size_t table = (size_t)kDigits * (tiles ? tiles : 1);
+    return (table + scan_temp_bytes((uint32_t)table) / sizeof(uint32_t) + 64) * sizeof(uint32_t);
 }
 
 template <typename K>
@@ -210,9 +211,9 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
     K* kb[2] = { keys, keys_alt };
     uint32_t* vb[2] = { vals, vals_alt };
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        g_launches += 3;
+        g_launches += 2;
         k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);
-        k_scan<<<1, 1024, 0, s>>>(temp, kDigits * tiles);
+        exclusive_scan(temp, kDigits * tiles, nullptr, temp + (size_t)kDigits * tiles, s);
         k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles);
         cur ^= 1;
     }
