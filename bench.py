@@ -190,6 +190,29 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_single():
+    """Two dispatches of the workload from device-resident inputs: the launches
+    of the second one are what a profiler capture should select (-s skips the
+    first dispatch's launches)."""
+    import ctypes as C
+    import torch
+    from mcut_gb300 import Context, recentre
+    from mcut_gb300 import _lib as L
+    src, cut = make_workload()
+    sx, cx, eps = recentre(src, cut)
+    ctx = Context(0)
+    lib = L.load()
+    d = [torch.from_numpy(a).cuda() for a in (sx, cx, src["f"].astype(np.int32), cut["f"].astype(np.int32))]
+    ms = L.Mesh(d[0].data_ptr(), d[2].data_ptr(), None, sx.shape[0], src["f"].shape[0] // 3)
+    mc = L.Mesh(d[1].data_ptr(), d[3].data_ptr(), None, cx.shape[0], cut["f"].shape[0] // 3)
+    sm = L.Summary()
+    for _ in range(2):
+        L.check(lib.mcgpu_dispatch(ctx._h, L.DEVICE_POINTERS, C.byref(ms), C.byref(mc), eps, C.byref(sm)), "dispatch")
+    torch.cuda.synchronize()
+    print(json.dumps({"single": True, "status": L.STATUS_NAMES[sm.status], "records": int(sm.num_records),
+                      "kernel_launches_per_dispatch": int(sm.kernel_launches)}))
+
+
 def run_gpu(args, world, rank, local):
     import torch
     import ctypes as C
@@ -333,9 +356,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--single", action="store_true",
+                    help="one warm-up dispatch + one dispatch of the workload, nothing else (for ncu captures)")
     args = ap.parse_args()
     world, rank, local = dist_init(args)
-    if args.impl == "reference":
+    if args.single:
+        run_single()
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_gpu(args, world, rank, local)

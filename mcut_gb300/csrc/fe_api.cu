@@ -89,15 +89,16 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
 struct Layout {
     uint32_t n_pairs = 0;
-    std::vector<uint32_t> vbase, vs, fbase, fs, sbase, cbase, ibase, is; // ibase: index base, is: src index count
+    std::vector<uint32_t> vbase, vs, fbase, fs, sbase, cbase, ibase, is, clbase; // ibase: index base, is: src index count
     std::vector<double> eps;
-    uint64_t nv = 0, nf = 0, ns = 0, nc = 0, nidx = 0;
+    uint64_t nv = 0, nf = 0, ns = 0, nc = 0, nidx = 0, ncl = 0;
+    uint32_t leaf_size = 4;
     bool all_tri = true;
     uint64_t tri_stride = 0, n_poly = 0;
     uint32_t max_face = 3;
@@ -119,6 +120,7 @@ struct mcgpu_context_t {
     uint64_t n_pairs_found = 0, n_tests = 0, n_records = 0;
     uint32_t flags = 0;
     int rec_buf = 0;
+    uint32_t leaf_size = 4;   // cut faces per tree leaf (MCGPU_LEAF_SIZE overrides, 1..16)
 };
 
 namespace {
@@ -264,6 +266,9 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
     L.n_pairs = n;
     L.vbase.resize(n + 1); L.vs.resize(n + 1); L.fbase.resize(n + 1); L.fs.resize(n + 1);
     L.sbase.resize(n + 1); L.cbase.resize(n + 1); L.ibase.resize(n + 1); L.is.resize(n + 1);
+    L.clbase.resize(n + 1);
+    L.leaf_size = c->leaf_size;
+    uint64_t cl = 0;
     L.eps.assign(n, 0.0);
     uint64_t v = 0, f = 0, sf = 0, cf = 0, ix = 0;
     for (uint32_t p = 0; p < n; ++p) {
@@ -275,6 +280,8 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
         L.vbase[p] = (uint32_t)v; L.vs[p] = S.num_vertices;
         L.fbase[p] = (uint32_t)f; L.fs[p] = S.num_faces;
         L.sbase[p] = (uint32_t)sf; L.cbase[p] = (uint32_t)cf; L.ibase[p] = (uint32_t)ix;
+        L.clbase[p] = (uint32_t)cl;
+        cl += (C.num_faces + L.leaf_size - 1) / L.leaf_size;
         uint64_t is = 0, ic = 0;
         for (int side = 0; side < 2; ++side) {
             const mcgpu_mesh& m = side ? C : S;
@@ -307,7 +314,8 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
     if (n > 65535) return fail(MCGPU_TOO_LARGE, "more than 65535 pairs in one batch");
     L.vbase[n] = (uint32_t)v; L.fbase[n] = (uint32_t)f; L.sbase[n] = (uint32_t)sf; L.cbase[n] = (uint32_t)cf;
     L.ibase[n] = (uint32_t)ix;
-    L.nv = v; L.nf = f; L.ns = sf; L.nc = cf; L.nidx = ix;
+    L.clbase[n] = (uint32_t)cl;
+    L.nv = v; L.nf = f; L.ns = sf; L.nc = cf; L.nidx = ix; L.ncl = cl;
     return MCGPU_OK;
 }
 
@@ -342,15 +350,18 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         ck(cudaMemcpyAsync(fidx + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, ikind, s), "H2D Is");
         ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, ikind, s), "H2D Ic");
     }
-    // per pair tables: ibase, is, vbase, vs, fbase, fs, sbase, cbase (n+1 each), eps
-    uint32_t* tab = c->pin_tab.get<uint32_t>((size_t)8 * (n + 1) + 2 * (size_t)(n + 1));
-    const std::vector<uint32_t>* rows[8] = { &L.ibase, &L.is, &L.vbase, &L.vs, &L.fbase, &L.fs, &L.sbase, &L.cbase };
-    for (int r = 0; r < 8; ++r) memcpy(tab + (size_t)r * (n + 1), rows[r]->data(), sizeof(uint32_t) * (n + 1));
-    double* teps = reinterpret_cast<double*>(tab + (size_t)8 * (n + 1) + ((8 * (n + 1)) & 1));
+    // per pair tables: ibase, is, vbase, vs, fbase, fs, sbase, cbase, clbase (n+1 each), eps
+    constexpr int kRows = 9;
+    const size_t rows_u32 = (size_t)kRows * (n + 1), eps_off = (rows_u32 + 1) & ~size_t(1);
+    uint32_t* tab = c->pin_tab.get<uint32_t>(eps_off + 2 * (size_t)(n + 1));
+    const std::vector<uint32_t>* rows[kRows] = { &L.ibase, &L.is, &L.vbase, &L.vs, &L.fbase, &L.fs, &L.sbase,
+        &L.cbase, &L.clbase };
+    for (int r = 0; r < kRows; ++r) memcpy(tab + (size_t)r * (n + 1), rows[r]->data(), sizeof(uint32_t) * (n + 1));
+    double* teps = reinterpret_cast<double*>(tab + eps_off);
     memcpy(teps, L.eps.data(), sizeof(double) * n);
-    uint32_t* dtab = c->buf[B_PTAB].get<uint32_t>((size_t)8 * (n + 1));
+    uint32_t* dtab = c->buf[B_PTAB].get<uint32_t>(rows_u32);
     double* deps = c->buf[B_EPS].get<double>(n);
-    ck(cudaMemcpyAsync(dtab, tab, sizeof(uint32_t) * 8 * (n + 1), cudaMemcpyHostToDevice, s), "H2D tab");
+    ck(cudaMemcpyAsync(dtab, tab, sizeof(uint32_t) * rows_u32, cudaMemcpyHostToDevice, s), "H2D tab");
     ck(cudaMemcpyAsync(deps, teps, sizeof(double) * n, cudaMemcpyHostToDevice, s), "H2D eps");
     uint32_t* foff = nullptr;
     if (!L.all_tri) {
@@ -390,7 +401,10 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.pair_sbase = dtab + 6 * (n + 1);
     P.pair_cbase = dtab + 7 * (n + 1);
     P.pair_eps = deps;
+    P.pair_clbase = dtab + 8 * (n + 1);
     P.all_triangles = L.all_tri ? 1 : 0;
+    P.leaf_size = L.leaf_size;
+    P.ncl = (uint32_t)L.ncl;
 }
 
 inline void rec(mcgpu_context_t* c, int i)
@@ -435,14 +449,19 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.ckeys[1] = c->buf[B_CK1].get<uint8_t>(L.nc * ksz);
     W.cvals[0] = c->buf[B_CV0].get<uint32_t>(L.nc);
     W.cvals[1] = c->buf[B_CV1].get<uint32_t>(L.nc);
-    W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.nc, 2) - 1);
-    W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.nc, 1));
-    W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.nc, 2));
+    W.cl_key = c->buf[B_CLKEY].get<uint8_t>(L.ncl * ksz);
+    W.cl_start = c->buf[B_CLSTART].get<uint32_t>(L.ncl);
+    W.cl_n = c->buf[B_CLN].get<uint8_t>(L.ncl);
+    W.leaf_key_box = c->buf[B_LKB].get<long long>(L.nc * 6);
+    W.packets = c->buf[B_PACKETS].get<uint2>(L.ns);
+    W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
+    W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));
+    W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
     W.counters = c->buf[B_COUNTERS].get<uint32_t>(16);
     W.cand = c->buf[B_CAND].get<uint8_t>(L.nf);
     W.pair_status = c->buf[B_PSTAT].get<uint32_t>(n);
     W.pair_bad = c->buf[B_PBAD].get<int32_t>(n);
-    W.pair_nrec = c->buf[B_PNREC].get<uint32_t>(n);
+    W.pair_nrec = c->buf[B_PNREC].get<uint32_t>(n + 1);
     W.scan_temp = c->buf[B_SCANTMP].get<uint32_t>(scan_temp_bytes((uint32_t)L.nv + 1) / 4 + 64);
     if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
@@ -454,7 +473,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
     ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
     ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
-    ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)n, s), "memset");
+    ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
 
     launch_bounds_morton(P, W, wide, s);
     rec(c, 2);
@@ -529,13 +548,15 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
     ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
     ck(cudaMemcpyAsync(hc + 16 + n, W.pair_bad, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H bad");
-    ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H nrec");
     ck(cudaStreamSynchronize(s), "sync narrow");
     c->n_tests = hc[1];
     c->n_records = hc[2];
     W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
     W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
     c->rec_buf = launch_records(P, W, (uint32_t)c->n_records, s);
+    // per-pair record ranges (first sorted record of each pair, then the total)
+    ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
+        "D2H ranges");
     rec(c, 7);
     ck(cudaStreamSynchronize(s), "sync records");
     ck(cudaGetLastError(), "kernel launch");
@@ -555,7 +576,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         } else if (st & ST_GP) m.status = MCGPU_GP_VIOLATION;
         else m.status = MCGPU_OK;
         m.cut_eps = L.eps[p];
-        m.num_records = hc[16 + 2 * n + p];
+        m.num_records = c->n_records ? hc[16 + 2 * n + p + 1] - hc[16 + 2 * n + p] : 0;
         c->rec_begin[p + 1] = c->rec_begin[p] + m.num_records;
     }
     if (n == 1) {
@@ -608,6 +629,10 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         mcgpu_context_t* c = new (std::nothrow) mcgpu_context_t();
         if (!c) return fail(MCGPU_OUT_OF_MEMORY, "host allocation");
         c->device = device;
+        if (const char* e = getenv("MCGPU_LEAF_SIZE")) {
+            const int v = atoi(e);
+            if (v >= 1 && v <= 16) c->leaf_size = (uint32_t)v;
+        }
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
         *out = c;

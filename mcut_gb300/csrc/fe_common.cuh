@@ -40,6 +40,30 @@ __device__ __forceinline__ bool dlt_int(double a, double b)
     const long long ob = ib < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)ib) : ib;
     return oa < ob;
 }
+// fp64 -> fp32 rounded toward -inf / +inf with integer operations (the fp64
+// pipe's conversions are slow here); values outside fp32's normal range take
+// the hardware conversion
+__device__ __forceinline__ float f32_round(double x, bool up)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    if (e < 1023u - 126u || e > 1023u + 127u) return up ? __double2float_ru(x) : __double2float_rd(x);
+    const unsigned sign = (unsigned)(b >> 63);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned fb = (sign << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
+    const bool inexact = (m & 0x1FFFFFFFull) != 0;
+    if (inexact && (sign != 0) != up) fb += 1u; // away from zero toward the requested infinity
+    return __uint_as_float(fb);
+}
+__device__ __forceinline__ float f32_rd(double x) { return f32_round(x, false); }
+__device__ __forceinline__ float f32_ru(double x) { return f32_round(x, true); }
+
+// the same order as a signed integer key: dlt_int(a, b) == (dkey(a) < dkey(b))
+__device__ __forceinline__ long long dkey(double a)
+{
+    const long long ia = __double_as_longlong(a);
+    return ia < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)ia) : ia;
+}
 __device__ __forceinline__ double dmax_ref(double a, double b) { return dlt_int(a, b) ? b : a; }  // std::max
 __device__ __forceinline__ double dmin_ref(double a, double b) { return dlt_int(b, a) ? b : a; }  // std::min
 

@@ -14,6 +14,10 @@
 // test. So the tree is a Karras LBVH with fp32 node boxes rounded outward,
 // not the reference's implicit complete tree.
 
+#include <climits>
+#include <cstdlib>
+#include <cstring>
+
 #include "fe_common.cuh"
 #include "fe_kernels.cuh"
 #include "fe_sort.cuh"
@@ -169,16 +173,23 @@ __global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __re
         const bool is_cut = (fp & kCutBit) != 0;
         const Box b = load_box(fbox, f);
         const unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
-        // the code only orders leaves (any order gives the same pair set), so
-        // it is formed in fp32: fp64 division is slow on this part
+        // The code only orders leaves (any order gives the same pair set), so
+        // it is formed on the integer pipe: positions are dkey() integers,
+        // monotone in the coordinate (piecewise linear within each binade),
+        // quantised to 10 bits per axis.
         uint32_t c[3];
         for (int j = 0; j < 3; ++j) {
-            const double lo = of_ord(mb[j]), hi = of_ord(mb[3 + j]);
-            const float ext = (float)(hi - lo);
-            const float mid = (float)((b.mn[j] + b.mx[j]) * 0.5 - lo);
-            float t = ext > 0.0f ? __fdividef(mid, ext) : 0.0f;
-            t = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
-            c[j] = expand_bits((uint32_t)t);
+            const long long lo = dkey(of_ord(mb[j])), hi = dkey(of_ord(mb[3 + j]));
+            const long long mid = (dkey(b.mn[j]) >> 1) + (dkey(b.mx[j]) >> 1);
+            const unsigned long long den = (unsigned long long)(hi - lo);
+            const unsigned long long num = mid > lo ? (unsigned long long)(mid - lo) : 0ull;
+            uint32_t q = 0;
+            if (den > 0) {
+                const int sh = max(0, 64 - __clzll((long long)den) - 20); // den >> sh < 2^20
+                const uint32_t d32 = (uint32_t)(den >> sh), n32 = (uint32_t)min(num >> sh, (unsigned long long)d32);
+                q = d32 ? (uint32_t)(((unsigned long long)n32 * 1023ull) / d32) : 0u;
+            }
+            c[j] = expand_bits(min(q, 1023u));
         }
         const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]);
         const uint32_t local = f - P.pair_fbase[p];
@@ -238,6 +249,74 @@ __global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, in
     }
 }
 
+// Query packets: the source faces are Morton-sorted too, and every Karras
+// subtree over them is a run of consecutive sorted faces split at a Morton
+// cell boundary, hence spatially compact. A packet is a maximal subtree of at
+// most 32 faces (its parent holds more); one warp walks the cut tree for it.
+template <typename K>
+__global__ void __launch_bounds__(kBlock) k_src_packets(const K* __restrict__ key, int n, uint2* __restrict__ packets,
+    uint32_t* __restrict__ counters)
+{
+    if (n <= 32) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
+            packets[0] = make_uint2(0u, (uint32_t)(n - 1));
+            counters[9] = 1;
+        }
+        return;
+    }
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n - 1; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + threadIdx.x;
+        bool emit0 = false, emit1 = false;
+        int gamma = 0, lo = 0, hi = 0;
+        if (i < n - 1) {
+        const int d = (delta(key, n, i, i + 1) - delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(key, n, i, i - d);
+        int lmax = 2;
+        while (delta(key, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(key, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        lo = min(i, j);
+        hi = max(i, j);
+        if (hi - lo + 1 > 32) {
+            const int dnode = delta(key, n, i, j);
+            int s = 0;
+            for (int t = (l + 1) >> 1;; t = (t + 1) >> 1) {
+                if (delta(key, n, i, i + (s + t) * d) > dnode) s += t;
+                if (t == 1) break;
+            }
+            gamma = i + s * d + min(d, 0);
+            emit0 = gamma - lo + 1 <= 32;
+            emit1 = hi - gamma <= 32;
+        }
+        }
+        const uint32_t p0 = warp_append(&counters[9], emit0);
+        if (emit0) packets[p0] = make_uint2((uint32_t)lo, (uint32_t)gamma);
+        const uint32_t p1 = warp_append(&counters[9], emit1);
+        if (emit1) packets[p1] = make_uint2((uint32_t)(gamma + 1), (uint32_t)hi);
+    }
+}
+
+// leaf clusters: `leaf_size` consecutive sorted cut faces of one pair
+template <typename K>
+__global__ void __launch_bounds__(kBlock) k_clusters(Problem P, const K* __restrict__ ckey, K* __restrict__ clkey,
+    uint32_t* __restrict__ cl_start, uint8_t* __restrict__ cl_n)
+{
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < P.ncl; c += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = P.n_pairs;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (P.pair_clbase[mid] <= c) lo = mid; else hi = mid;
+        }
+        const uint32_t start = P.pair_cbase[lo] + (c - P.pair_clbase[lo]) * P.leaf_size;
+        const uint32_t end = min(start + P.leaf_size, P.pair_cbase[lo + 1]);
+        clkey[c] = ckey[start];
+        cl_start[c] = start;
+        cl_n[c] = (uint8_t)(end - start);
+    }
+}
+
 struct FBox { float lo[3], hi[3]; uint32_t plo, phi; };
 
 __device__ __forceinline__ void put_child(Node* nd, int slot, const FBox& b)
@@ -263,27 +342,36 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
 
 // bottom-up refit: the second child to arrive at a node merges both boxes
 __global__ void __launch_bounds__(kBlock) k_refit(Problem P, const double* __restrict__ fbox,
-    const uint32_t* __restrict__ leaf_face, int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent,
-    uint32_t* __restrict__ flag)
+    const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n,
+    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, uint32_t* __restrict__ flag,
+    long long* __restrict__ leaf_key_box)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t f = leaf_face[i];
-        const Box b = load_box(fbox, f);
         FBox fb;
-        for (int j = 0; j < 3; ++j) {
-            fb.lo[j] = __double2float_rd(b.mn[j]);
-            fb.hi[j] = __double2float_ru(b.mx[j]);
+        for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
+        const uint32_t s0 = cl_start[i], cn = cl_n[i];
+        for (uint32_t t = 0; t < cn; ++t) {
+            const Box b = load_box(fbox, leaf_face[s0 + t]);
+            longlong2* kb = reinterpret_cast<longlong2*>(leaf_key_box + (size_t)(s0 + t) * 6);
+            kb[0] = make_longlong2(dkey(b.mn[0]), dkey(b.mn[1]));
+            kb[1] = make_longlong2(dkey(b.mn[2]), dkey(b.mx[0]));
+            kb[2] = make_longlong2(dkey(b.mx[1]), dkey(b.mx[2]));
+            for (int j = 0; j < 3; ++j) {
+                fb.lo[j] = fminf(fb.lo[j], f32_rd(b.mn[j]));
+                fb.hi[j] = fmaxf(fb.hi[j], f32_ru(b.mx[j]));
+            }
         }
-        fb.plo = fb.phi = P.face_pair[f] & ~kCutBit;
+        fb.plo = fb.phi = P.face_pair[leaf_face[s0]] & ~kCutBit;
         int child = ~i;
         int node = parent[(n - 1) + i];
         while (node >= 0) {
             Node* nd = &nodes[node];
             const int slot = (nd->child[0] == child) ? 0 : 1;
             put_child(nd, slot, fb);
-            __threadfence();
-            if (atomicAdd(&flag[node], 1u) == 0) break; // the sibling finishes this node
-            __threadfence();
+            // acq_rel arrival: releases this child's box, acquires the sibling's
+            unsigned prev;
+            asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&flag[node]) : "memory");
+            if (prev == 0) break; // the sibling finishes this node
             const FBox o = get_child(nd, slot ^ 1);
             for (int j = 0; j < 3; ++j) {
                 fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
@@ -297,25 +385,72 @@ __global__ void __launch_bounds__(kBlock) k_refit(Problem P, const double* __res
     }
 }
 
+__global__ void __launch_bounds__(kBlock) k_leaf_keys(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ leaf_face, long long* __restrict__ leaf_key_box)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nc; i += gridDim.x * blockDim.x) {
+        const Box b = load_box(fbox, leaf_face[i]);
+        long long* k = leaf_key_box + (size_t)i * 6;
+        for (int j = 0; j < 3; ++j) { k[j] = dkey(b.mn[j]); k[3 + j] = dkey(b.mx[j]); }
+    }
+}
+
 // ---------------------------------------------------------------------------
-// traversal: every source face queries the cut-face LBVH (intersectOIBVHs,
-// bvh.cpp:638-783). Queries run in Morton order so neighbouring threads walk
-// similar paths. Leaf tests are the reference's exact closed fp64 test.
+// packet traversal: a warp takes 32 Morton-consecutive source faces, walks
+// the tree ONCE with the union of their boxes (one shared-memory stack per
+// warp, node loads broadcast, no divergence in the walk) and, at each leaf
+// cluster the union reaches, every lane tests its own box exactly against
+// the cluster's faces. Exact tests compare dkey() integers, bit-for-bit the
+// reference's closed fp64 test (intersect_bounding_boxes, math.h:931-943).
 // ---------------------------------------------------------------------------
-template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __restrict__ fbox,
-    const uint32_t* __restrict__ qface, const uint32_t* __restrict__ leaf_face, int nleaf,
-    const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
+constexpr int kPacketStack = 64;
+
+__global__ void __launch_bounds__(kBlock) k_traverse_packet(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ qface, const uint2* __restrict__ packets, const uint32_t* __restrict__ leaf_face,
+    const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const long long* __restrict__ leaf_key_box,
+    int nleaf, const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
     uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
 {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < P.ns; t += gridDim.x * blockDim.x) {
-        const uint32_t s = qface[t];
-        const uint32_t p = P.face_pair[s] & ~kCutBit;
-        const Box qb = load_box(fbox, s);
+    __shared__ int stack_all[kBlock / 32][kPacketStack];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int* stack = stack_all[wib];
+    const unsigned full = 0xFFFFFFFFu;
+    const uint32_t npackets = counters[9];
+    for (;;) {
+        uint32_t pk = 0;
+        if (lane == 0) pk = atomicAdd(&counters[8], 1u);
+        pk = __shfl_sync(full, pk, 0);
+        if (pk >= npackets) break;
+        const uint2 range = packets[pk];
+        const uint32_t t = range.x + lane;
+        const bool active = t <= range.y;
+        uint32_t s = 0, p = 0;
+        long long qk[6];
         float ql[3], qh[3];
-        for (int j = 0; j < 3; ++j) {
-            ql[j] = __double2float_rd(qb.mn[j]);
-            qh[j] = __double2float_ru(qb.mx[j]);
+        if (active) {
+            s = qface[t];
+            p = P.face_pair[s] & ~kCutBit;
+            const Box qb = load_box(fbox, s);
+            for (int j = 0; j < 3; ++j) {
+                qk[j] = dkey(qb.mn[j]);
+                qk[3 + j] = dkey(qb.mx[j]);
+                ql[j] = f32_rd(qb.mn[j]);
+                qh[j] = f32_ru(qb.mx[j]);
+            }
+        } else {
+            for (int j = 0; j < 3; ++j) { qk[j] = LLONG_MAX; qk[3 + j] = LLONG_MIN; ql[j] = 3.4e38f; qh[j] = -3.4e38f; }
+            p = 0xFFFFu;
+        }
+        // packet box and pair range
+        float ul[3] = { ql[0], ql[1], ql[2] }, uh[3] = { qh[0], qh[1], qh[2] };
+        uint32_t pmin = active ? p : 0xFFFFu, pmax = active ? p : 0u;
+        for (int off = 16; off; off >>= 1) {
+            for (int j = 0; j < 3; ++j) {
+                ul[j] = fminf(ul[j], __shfl_xor_sync(full, ul[j], off));
+                uh[j] = fmaxf(uh[j], __shfl_xor_sync(full, uh[j], off));
+            }
+            pmin = min(pmin, __shfl_xor_sync(full, pmin, off));
+            pmax = max(pmax, __shfl_xor_sync(full, pmax, off));
         }
         unsigned long long buf[8];
         int nb = 0;
@@ -327,19 +462,361 @@ __global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __
                 if ((uint64_t)pos + k < cap) pairs[pos + k] = buf[k];
             nb = 0;
         };
+        // each lane tests its own query against one leaf cluster (fp32 pre-test, then exact)
+        auto leaf = [&](int li, float lx0, float ly0, float lz0, float hx0, float hy0, float hz0, uint32_t lp) {
+            if (!active || lp != p) return;
+            if (!(ql[0] <= hx0 && qh[0] >= lx0 && ql[1] <= hy0 && qh[1] >= ly0 && ql[2] <= hz0 && qh[2] >= lz0))
+                return;
+            const uint32_t s0 = __ldg(&cl_start[li]), cn = __ldg(&cl_n[li]);
+            for (uint32_t u = 0; u < cn; ++u) {
+                const longlong2* kb = reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
+                const longlong2 a = __ldg(kb), b = __ldg(kb + 1), c = __ldg(kb + 2);
+                // closed overlap: q.mn <= l.mx && q.mx >= l.mn on every axis
+                if (qk[0] <= b.y && qk[3] >= a.x && qk[1] <= c.x && qk[4] >= a.y && qk[2] <= c.y && qk[5] >= b.x) {
+                    const uint32_t c2 = __ldg(&leaf_face[s0 + u]);
+                    buf[nb++] = ((unsigned long long)s << 32) | c2;
+                    cand[c2] = 1;
+                    any = true;
+                    if (nb == 8) flush();
+                }
+            }
+        };
+        bool overflow = false;
+        if (nleaf == 1) {
+            // single cluster: its box is not stored in any node; test the faces directly
+            leaf(0, -3.4e38f, -3.4e38f, -3.4e38f, 3.4e38f, 3.4e38f, 3.4e38f, active ? p : 0xFFFFu);
+        } else {
+            int sp = 0;
+            if (lane == 0) stack[0] = 0;
+            sp = 1;
+            __syncwarp();
+            while (sp > 0) {
+                const int nd = stack[--sp];
+                __syncwarp();
+                const float4 a = __ldg(&nodes[nd].b0), b = __ldg(&nodes[nd].b1), c = __ldg(&nodes[nd].b2);
+                const int2 ch = __ldg(reinterpret_cast<const int2*>(&nodes[nd].child[0]));
+                const uint2 pr = __ldg(reinterpret_cast<const uint2*>(&nodes[nd].prange[0]));
+                const bool hit0 = (pr.x & 0xFFFFu) <= pmax && pmin <= (pr.x >> 16) && ul[0] <= a.w && uh[0] >= a.x
+                    && ul[1] <= b.x && uh[1] >= a.y && ul[2] <= b.y && uh[2] >= a.z;
+                const bool hit1 = (pr.y & 0xFFFFu) <= pmax && pmin <= (pr.y >> 16) && ul[0] <= c.y && uh[0] >= b.z
+                    && ul[1] <= c.z && uh[1] >= b.w && ul[2] <= c.w && uh[2] >= c.x;
+                if (hit0) {
+                    if (ch.x < 0) leaf(~ch.x, a.x, a.y, a.z, a.w, b.x, b.y, pr.x & 0xFFFFu);
+                    else {
+                        if (sp < kPacketStack) { if (lane == 0) stack[sp] = ch.x; ++sp; }
+                        else overflow = true;
+                    }
+                }
+                if (hit1) {
+                    if (ch.y < 0) leaf(~ch.y, b.z, b.w, c.x, c.y, c.z, c.w, pr.y & 0xFFFFu);
+                    else {
+                        if (sp < kPacketStack) { if (lane == 0) stack[sp] = ch.y; ++sp; }
+                        else overflow = true;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        flush();
+        if (any) cand[s] = 1;
+        if (overflow && lane == 0) atomicOr(&pair_status[pmin == 0xFFFFu ? 0 : pmin], ST_STACK);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wave traversal: one warp per query packet, breadth-first over the cut tree.
+// Each step the lanes take up to 32 frontier nodes at once (32 independent
+// node loads in flight instead of one long chain of dependent loads), test
+// both children against the packet's union box, and compact the surviving
+// internal children into the next frontier (ballot + popc). Leaf clusters
+// the union reaches are queued in shared memory; for each, every lane tests
+// its own query box (fp32 pre-test, then the exact integer-key test). A
+// frontier or queue overflow flags the pair for the per-thread deep re-run.
+// ---------------------------------------------------------------------------
+constexpr int kWaveFrontier = 256;
+constexpr int kWaveLeaves = 64;
+constexpr int kWaveWarps = kBlock / 32;
+
+struct WaveLeaf {
+    float lo[3], hi[3];
+    int id;
+    uint32_t pr;
+};
+
+// Output goes through a per-warp staging buffer in shared memory and reaches
+// the global pair list in blocks of up to kWaveOut pairs (one atomic each).
+//
+// Queued leaf clusters are tested lane-parallel: lane k takes queued leaf k
+// and tests every query of the packet (kept in shared memory) against it, so
+// a packet that reaches hundreds of leaves pays a few rounds of parallel
+// loads instead of hundreds of dependent ones.
+constexpr int kWaveOut = 224;
+
+struct WaveWarp {
+    int front[2][kWaveFrontier];
+    WaveLeaf leaves[kWaveLeaves];
+    unsigned long long out[kWaveOut + 32];
+    long long qk[32][6];
+    float qb[32][6];
+    uint32_t qs[32];
+    uint32_t qp[32];
+    int nout;
+    unsigned qhit; // queries of the current packet that produced a pair
+};
+constexpr size_t kWaveSmem = sizeof(WaveWarp) * kWaveWarps;
+
+__global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ qface, const uint2* __restrict__ packets, const uint32_t* __restrict__ leaf_face,
+    const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const long long* __restrict__ leaf_key_box,
+    int nleaf, const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
+    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
+{
+    extern __shared__ __align__(16) unsigned char wave_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WaveWarp& W = reinterpret_cast<WaveWarp*>(wave_smem)[wib];
+    const unsigned full = 0xFFFFFFFFu;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t npackets = counters[9];
+    if (lane == 0) W.nout = 0;
+    __syncwarp();
+    auto flush_out = [&]() {
+        __syncwarp();
+        const int nout = min(W.nout, kWaveOut + 32);
+        uint32_t base = 0;
+        if (lane == 0 && nout) base = atomicAdd(&counters[0], (uint32_t)nout);
+        base = __shfl_sync(full, base, 0);
+        for (int k = lane; k < nout; k += 32)
+            if ((uint64_t)base + k < cap) pairs[base + k] = W.out[k];
+        __syncwarp();
+        if (lane == 0) W.nout = 0;
+        __syncwarp();
+    };
+    for (;;) {
+        uint32_t pk = 0;
+        if (lane == 0) pk = atomicAdd(&counters[8], 1u);
+        pk = __shfl_sync(full, pk, 0);
+        if (pk >= npackets) break;
+        const uint2 range = packets[pk];
+        const int psize = (int)(range.y - range.x + 1);
+        const uint32_t t = range.x + lane;
+        const bool active = lane < psize;
+        uint32_t p = 0xFFFFu;
+        float ql[3], qh[3];
+        if (active) {
+            const uint32_t s = qface[t];
+            p = P.face_pair[s] & ~kCutBit;
+            const Box qb = load_box(fbox, s);
+            for (int j = 0; j < 3; ++j) {
+                W.qk[lane][j] = dkey(qb.mn[j]);
+                W.qk[lane][3 + j] = dkey(qb.mx[j]);
+                ql[j] = f32_rd(qb.mn[j]);
+                qh[j] = f32_ru(qb.mx[j]);
+                W.qb[lane][j] = ql[j];
+                W.qb[lane][3 + j] = qh[j];
+            }
+            W.qs[lane] = s;
+            W.qp[lane] = p;
+        } else {
+            for (int j = 0; j < 3; ++j) { ql[j] = 3.4e38f; qh[j] = -3.4e38f; }
+        }
+        float ul[3] = { ql[0], ql[1], ql[2] }, uh[3] = { qh[0], qh[1], qh[2] };
+        uint32_t pmin = active ? p : 0xFFFFu, pmax = active ? p : 0u;
+        for (int off = 16; off; off >>= 1) {
+            for (int j = 0; j < 3; ++j) {
+                ul[j] = fminf(ul[j], __shfl_xor_sync(full, ul[j], off));
+                uh[j] = fmaxf(uh[j], __shfl_xor_sync(full, uh[j], off));
+            }
+            pmin = min(pmin, __shfl_xor_sync(full, pmin, off));
+            pmax = max(pmax, __shfl_xor_sync(full, pmax, off));
+        }
+        if (lane == 0) W.qhit = 0;
+        __syncwarp();
+        bool overflow = false;
+        int nl = 0;         // queued leaves (uniform across the warp)
+        // lane k takes queued leaf k: a 32-bit mask of the packet's queries
+        // whose fp32 box meets the leaf's box, then exact tests of those
+        // queries against the leaf's faces; hits go to the warp's staging
+        // buffer through shared-memory atomics (global atomics past it)
+        auto drain = [&]() {
+            __syncwarp();
+            for (int base = 0; base < nl; base += 32) {
+                const int k = base + lane;
+                if (k < nl) {
+                    const WaveLeaf L = W.leaves[k];
+                    unsigned mask = 0;
+                    for (int j = 0; j < psize; ++j) {
+                        const bool ov = W.qp[j] == (L.pr & 0xFFFFu) && W.qb[j][0] <= L.hi[0] && W.qb[j][3] >= L.lo[0]
+                            && W.qb[j][1] <= L.hi[1] && W.qb[j][4] >= L.lo[1] && W.qb[j][2] <= L.hi[2]
+                            && W.qb[j][5] >= L.lo[2];
+                        mask |= (ov ? 1u : 0u) << j;
+                    }
+                    if (mask) {
+                        const uint32_t s0 = __ldg(&cl_start[L.id]), cn = __ldg(&cl_n[L.id]);
+                        for (uint32_t u = 0; u < cn; ++u) {
+                            const longlong2* b2 =
+                                reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
+                            const longlong2 ka = __ldg(b2), kb = __ldg(b2 + 1), kc = __ldg(b2 + 2);
+                            const uint32_t cf = __ldg(&leaf_face[s0 + u]);
+                            bool any_cf = false;
+                            for (unsigned mm = mask; mm; mm &= mm - 1) {
+                                const int j = __ffs(mm) - 1;
+                                const long long* q = W.qk[j];
+                                if (q[0] <= kb.y && q[3] >= ka.x && q[1] <= kc.x && q[4] >= ka.y && q[2] <= kc.y
+                                    && q[5] >= kb.x) {
+                                    const unsigned long long pr = ((unsigned long long)W.qs[j] << 32) | cf;
+                                    const int pos = atomicAdd(&W.nout, 1);
+                                    if (pos < kWaveOut + 32) {
+                                        W.out[pos] = pr;
+                                    } else {
+                                        const uint32_t g = atomicAdd(&counters[0], 1u);
+                                        if (g < cap) pairs[g] = pr;
+                                    }
+                                    atomicOr(&W.qhit, 1u << j);
+                                    any_cf = true;
+                                }
+                            }
+                            if (any_cf) cand[cf] = 1;
+                        }
+                    }
+                }
+                __syncwarp();
+                if (W.nout >= kWaveOut) flush_out();
+            }
+            nl = 0;
+            __syncwarp();
+        };
+        if (nleaf == 1) {
+            if (lane == 0) {
+                WaveLeaf& L = W.leaves[0];
+                for (int j = 0; j < 3; ++j) { L.lo[j] = -3.4e38f; L.hi[j] = 3.4e38f; }
+                L.id = 0;
+                L.pr = (P.face_pair[leaf_face[0]] & ~kCutBit) * 0x10001u;
+            }
+            nl = 1;
+            drain();
+        } else {
+            int cur = 0, nf = 1;
+            if (lane == 0) W.front[0][0] = 0;
+            __syncwarp();
+            while (nf > 0) {
+                int nn = 0;
+                for (int base = 0; base < nf; base += 32) {
+                    const int i = base + lane;
+                    const bool v = i < nf;
+                    bool hit[2] = { false, false };
+                    int ch[2] = { 0, 0 };
+                    float bx[2][6];
+                    uint32_t prr[2] = { 0, 0 };
+                    if (v) {
+                        const int nd = W.front[cur][i];
+                        const float4 a = __ldg(&nodes[nd].b0), b = __ldg(&nodes[nd].b1), c = __ldg(&nodes[nd].b2);
+                        const int2 cc = __ldg(reinterpret_cast<const int2*>(&nodes[nd].child[0]));
+                        const uint2 pr = __ldg(reinterpret_cast<const uint2*>(&nodes[nd].prange[0]));
+                        ch[0] = cc.x; ch[1] = cc.y; prr[0] = pr.x; prr[1] = pr.y;
+                        bx[0][0] = a.x; bx[0][1] = a.y; bx[0][2] = a.z; bx[0][3] = a.w; bx[0][4] = b.x; bx[0][5] = b.y;
+                        bx[1][0] = b.z; bx[1][1] = b.w; bx[1][2] = c.x; bx[1][3] = c.y; bx[1][4] = c.z; bx[1][5] = c.w;
+                        for (int k = 0; k < 2; ++k)
+                            hit[k] = (prr[k] & 0xFFFFu) <= pmax && pmin <= (prr[k] >> 16) && ul[0] <= bx[k][3]
+                                && uh[0] >= bx[k][0] && ul[1] <= bx[k][4] && uh[1] >= bx[k][1] && ul[2] <= bx[k][5]
+                                && uh[2] >= bx[k][2];
+                    }
+                    for (int k = 0; k < 2; ++k) {
+                        const bool inner = hit[k] && ch[k] >= 0, leaf = hit[k] && ch[k] < 0;
+                        const unsigned mi = __ballot_sync(full, inner), ml = __ballot_sync(full, leaf);
+                        if (nn + __popc(mi) > kWaveFrontier) {
+                            overflow = true;
+                        } else {
+                            if (inner) W.front[cur ^ 1][nn + __popc(mi & lt)] = ch[k];
+                            nn += __popc(mi);
+                        }
+                        if (nl + __popc(ml) > kWaveLeaves) drain(); // nl is uniform
+                        if (leaf) {
+                            WaveLeaf& L = W.leaves[nl + __popc(ml & lt)];
+                            for (int j = 0; j < 3; ++j) { L.lo[j] = bx[k][j]; L.hi[j] = bx[k][3 + j]; }
+                            L.id = ~ch[k];
+                            L.pr = prr[k];
+                        }
+                        nl += __popc(ml);
+                    }
+                }
+                __syncwarp();
+                cur ^= 1;
+                nf = nn;
+            }
+            drain();
+        }
+        __syncwarp();
+        if (active && (W.qhit >> lane) & 1u) cand[W.qs[lane]] = 1;
+        overflow = __any_sync(full, overflow);
+        if (overflow && lane == 0) atomicOr(&pair_status[pmin == 0xFFFFu ? 0 : pmin], ST_STACK);
+        __syncwarp();
+    }
+    flush_out();
+}
+
+// ---------------------------------------------------------------------------
+// traversal: every source face queries the cut-face LBVH (intersectOIBVHs,
+// bvh.cpp:638-783). Queries run in Morton order so neighbouring threads walk
+// similar paths. Leaf tests are the reference's exact closed fp64 test.
+// ---------------------------------------------------------------------------
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ qface, const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start,
+    const uint8_t* __restrict__ cl_n, const long long* __restrict__ leaf_key_box, int nleaf,
+    const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
+    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
+{
+    // queries cost very different amounts (far faces stop at the root), so
+    // warps take the next 32 Morton-ordered queries from a shared counter
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&counters[8], 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= P.ns) break;
+        const uint32_t t = base + lane;
+        if (t >= P.ns) continue;
+        const uint32_t s = qface[t];
+        const uint32_t p = P.face_pair[s] & ~kCutBit;
+        const Box qb = load_box(fbox, s);
+        float ql[3], qh[3];
+        long long qk[6];
+        for (int j = 0; j < 3; ++j) {
+            ql[j] = f32_rd(qb.mn[j]);
+            qh[j] = f32_ru(qb.mx[j]);
+            qk[j] = dkey(qb.mn[j]);
+            qk[3 + j] = dkey(qb.mx[j]);
+        }
+        unsigned long long buf[8];
+        int nb = 0;
+        bool any = false;
+        auto flush = [&]() {
+            if (nb == 0) return;
+            const uint32_t pos = atomicAdd(&counters[0], (uint32_t)nb);
+            for (int k = 0; k < nb; ++k)
+                if ((uint64_t)pos + k < cap) pairs[pos + k] = buf[k];
+            nb = 0;
+        };
+        // a leaf cluster's faces, tested exactly: the closed fp64 overlap of
+        // intersect_bounding_boxes (math.h:931-943) on dkey() integers. The
+        // cluster's pair was checked with its box (prange).
         auto leaf = [&](int li) {
-            const uint32_t c = leaf_face[li];
-            if ((P.face_pair[c] & ~kCutBit) != p) return;
-            const Box cb = load_box(fbox, c);
-            if (box_overlap(qb, cb)) {
-                buf[nb++] = ((unsigned long long)s << 32) | c;
-                cand[c] = 1;
-                any = true;
-                if (nb == 8) flush();
+            const uint32_t s0 = __ldg(&cl_start[li]), cn = __ldg(&cl_n[li]);
+            for (uint32_t u = 0; u < cn; ++u) {
+                const longlong2* kb = reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
+                const longlong2 a = __ldg(kb), b = __ldg(kb + 1), c = __ldg(kb + 2);
+                if (qk[0] <= b.y && qk[3] >= a.x && qk[1] <= c.x && qk[4] >= a.y && qk[2] <= c.y && qk[5] >= b.x) {
+                    const uint32_t cf = __ldg(&leaf_face[s0 + u]);
+                    buf[nb++] = ((unsigned long long)s << 32) | cf;
+                    cand[cf] = 1;
+                    any = true;
+                    if (nb == 8) flush();
+                }
             }
         };
         if (nleaf == 1) {
-            leaf(0);
+            if ((P.face_pair[__ldg(&leaf_face[0])] & ~kCutBit) == p) leaf(0);
         } else {
             int stack[STACK];
             int sp = 0;
@@ -426,8 +903,9 @@ __global__ void __launch_bounds__(kBlock) k_planes(Problem P, const uint8_t* __r
     uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, uint64_t plane_cap,
     uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad)
 {
-    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
-        const bool c = cand[f] != 0;
+    for (uint32_t f0 = blockIdx.x * blockDim.x; f0 < P.nf; f0 += gridDim.x * blockDim.x) {
+        const uint32_t f = f0 + threadIdx.x;
+        const bool c = f < P.nf && cand[f] != 0;
         const uint32_t slot = warp_append(&counters[3], c);
         if (!c) continue;
         plane_slot[f] = slot;
@@ -678,23 +1156,49 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
     const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vface, Test* __restrict__ tests, uint64_t test_cap,
     uint32_t* __restrict__ counters, const int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_status)
 {
+    __shared__ uint32_t s_nmax;
     const uint64_t np = min((uint64_t)counters_ro[0], pair_cap);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < np; i += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long pr = pairs[i];
-        const uint32_t sface = (uint32_t)(pr >> 32), cface = (uint32_t)pr;
-        const uint32_t p = P.face_pair[sface] & ~kCutBit;
-        if (pair_bad[p] != kNoBad) continue; // the reference stops before the narrow phase
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x; i0 < np; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + threadIdx.x;
+        bool live = i < np;
+        uint32_t sface = 0, cface = 0, p = 0;
+        if (live) {
+            const unsigned long long pr = pairs[i];
+            sface = (uint32_t)(pr >> 32);
+            cface = (uint32_t)pr;
+            p = P.face_pair[sface] & ~kCutBit;
+            live = pair_bad[p] == kNoBad; // the reference stops before the narrow phase
+        }
+        // edges of the source face against the cut face, then the reverse;
+        // the loop runs to the block's longest face so every thread reaches
+        // each block_append
+        uint32_t ns = live ? face_n(P, sface) : 0u, nc = live ? face_n(P, cface) : 0u;
+        if (P.all_triangles) {
+            if (threadIdx.x == 0) s_nmax = 3;
+        } else {
+            if (threadIdx.x == 0) s_nmax = 0;
+            __syncthreads();
+            atomicMax(&s_nmax, max(ns, nc));
+        }
+        __syncthreads();
+        const uint32_t nmax = s_nmax;
+        __syncthreads();
         for (int side = 0; side < 2; ++side) {
             const uint32_t F = side == 0 ? sface : cface;
             const uint32_t g = side == 0 ? cface : sface;
-            const Box gb = load_box(fbox, g);
-            const uint32_t o = face_o(P, F), n = face_n(P, F);
-            for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t a = P.fidx[o + k], b = P.fidx[o + (k + 1 == n ? 0 : k + 1)];
-                uint32_t oslot = kNone;
-                const uint32_t G = other_face(P, voff, vface, F, a, b, oslot);
-                bool emit = true;
-                if (G != kNone && G < F && box_overlap(load_box(fbox, G), gb)) emit = false;
+            const uint32_t n = side == 0 ? ns : nc;
+            Box gb;
+            if (live) gb = load_box(fbox, g);
+            const uint32_t o = live ? face_o(P, F) : 0u;
+            for (uint32_t k = 0; k < nmax; ++k) {
+                bool emit = k < n;
+                uint32_t a = 0, b = 0, oslot = kNone, G = kNone;
+                if (emit) {
+                    a = P.fidx[o + k];
+                    b = P.fidx[o + (k + 1 == n ? 0 : k + 1)];
+                    G = other_face(P, voff, vface, F, a, b, oslot);
+                    if (G != kNone && G < F && box_overlap(load_box(fbox, G), gb)) emit = false;
+                }
                 if (emit) {
                     double xa[3], xb[3];
                     load_xyz(P.X, a, xa);
@@ -760,12 +1264,18 @@ __global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __rest
     const uint32_t* __restrict__ counters_ro, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
     unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
-    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status, uint32_t* __restrict__ pair_nrec)
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status)
 {
     const uint64_t nt = min((uint64_t)counters_ro[1], test_cap);
     uint32_t esc[3] = { 0, 0, 0 };
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nt; i += (uint64_t)gridDim.x * blockDim.x) {
-        const Test t = tests[i];
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x; i0 < nt; i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + threadIdx.x;
+        // one block_append call site, reached by every thread of the block
+        bool rec = false;
+        Test t;
+        double pt[3] = { 0.0, 0.0, 0.0 };
+        if (i < nt) {
+        t = tests[i];
         const FacePlane pl = planes[plane_slot[t.g]];
         const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
         double q[3], r[3];
@@ -789,8 +1299,6 @@ __global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __rest
             else if ((sr < 0 && sq < 0) || (sr > 0 && sq > 0)) type = '0';
             else type = '1';
         }
-        bool rec = false;
-        double pt[3] = { 0.0, 0.0, 0.0 };
         if (type == 'q' || type == 'r') {
             pip = pip_face(P, pl, o, n, type == 'q' ? q : r);
         } else if (type == 'p') {
@@ -809,11 +1317,13 @@ __global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __rest
         }
         const uint32_t p = P.face_pair[t.g] & ~kCutBit;
         if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
-            || (type == '1' && (pip == 'v' || pip == 'e')))
-            atomicOr(&pair_status[p], ST_GP);
+            || (type == '1' && (pip == 'v' || pip == 'e'))) {
+            if (!(*(volatile uint32_t*)&pair_status[p] & ST_GP)) atomicOr(&pair_status[p], ST_GP);
+        }
         if (keep_tests) {
             char4 info = make_char4(sq, sr, type, pip);
             reinterpret_cast<char4*>(test_info)[i] = info;
+        }
         }
         const uint32_t pos = warp_append(&counters[2], rec);
         if (rec) {
@@ -822,13 +1332,39 @@ __global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __rest
             rec_pt[(size_t)i * 3 + 0] = pt[0];
             rec_pt[(size_t)i * 3 + 1] = pt[1];
             rec_pt[(size_t)i * 3 + 2] = pt[2];
-            atomicAdd(&pair_nrec[p], 1u);
         }
     }
     for (int k = 0; k < 3; ++k) {
         uint32_t v = esc[k];
         for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd(&counters[5 + k], v);
+    }
+}
+
+// records: (slot << 32 | face) -> (slot << gbits | face)
+__global__ void __launch_bounds__(kBlock) k_record_pack(unsigned long long* __restrict__ rec_key, uint32_t nrec,
+    int gbits)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += gridDim.x * blockDim.x) {
+        const unsigned long long k = rec_key[i];
+        rec_key[i] = ((k >> 32) << gbits) | (k & 0xFFFFFFFFull);
+    }
+}
+
+// first sorted record of every pair (and the total at n_pairs): the records
+// are grouped by pair, so a binary search over the sorted keys finds them
+__global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const unsigned long long* __restrict__ key,
+    uint32_t nrec, int gbits, uint32_t* __restrict__ rec_begin)
+{
+    const unsigned long long gmask = (1ull << gbits) - 1ull;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= P.n_pairs; p += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = nrec;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const uint32_t mp = P.face_pair[(uint32_t)(key[mid] & gmask)] & ~kCutBit;
+            if (mp < p) lo = mid + 1; else hi = mid;
+        }
+        rec_begin[p] = lo;
     }
 }
 
@@ -905,30 +1441,78 @@ int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t
 
 void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStream_t s)
 {
-    const int n = (int)P.nc;
-    if (n < 2) return;
+    const int n = (int)P.ncl;
+    const int gc = grid_for(n);
+    g_launches++;
+    if (wide)
+        k_clusters<unsigned long long><<<gc, kBlock, 0, s>>>(P, (const unsigned long long*)W.ckeys[cut_buf],
+            (unsigned long long*)W.cl_key, W.cl_start, W.cl_n);
+    else
+        k_clusters<uint32_t><<<gc, kBlock, 0, s>>>(P, (const uint32_t*)W.ckeys[cut_buf], (uint32_t*)W.cl_key,
+            W.cl_start, W.cl_n);
+    if (n < 2) {
+        g_launches++;
+        k_leaf_keys<<<grid_for(P.nc), kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], W.leaf_key_box);
+        return;
+    }
     const int g = grid_for(n);
     g_launches++;
     if (wide)
-        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.ckeys[cut_buf], n, W.nodes,
-            W.parent);
+        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.cl_key, n, W.nodes, W.parent);
     else
-        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.ckeys[cut_buf], n, W.nodes, W.parent);
+        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.cl_key, n, W.nodes, W.parent);
     cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
     g_launches++;
-    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], n, W.nodes, W.parent, W.refit_flag);
+    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], W.cl_start, W.cl_n, n, W.nodes, W.parent,
+        W.refit_flag, W.leaf_key_box);
 }
 
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
 {
-    const int g = grid_for(P.ns);
-    g_launches++;
-    if (deep)
-        k_traverse<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], (int)P.nc, W.nodes,
-            W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+    // Default: warp per query packet (a compact source subtree of <= 32
+    // faces). MCGPU_TRAVERSAL=thread selects one thread per source face; the
+    // deep re-run after a stack overflow is per thread with a 512-entry stack.
+    static const bool per_thread = [] {
+        const char* e = getenv("MCGPU_TRAVERSAL");
+        return e && strcmp(e, "thread") == 0;
+    }();
+    const bool wide = P.n_pairs > 1;
+    if (deep || per_thread) {
+        const int g = grid_for(P.ns);
+        g_launches++;
+        if (deep)
+            k_traverse<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], W.cl_start, W.cl_n,
+                W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+        else
+            k_traverse<64><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], W.cl_start, W.cl_n,
+                W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+        return;
+    }
+    g_launches += 2;
+    if (wide)
+        k_src_packets<unsigned long long><<<grid_for(P.ns), kBlock, 0, s>>>(
+            (const unsigned long long*)W.skeys[src_buf], (int)P.ns, W.packets, W.counters);
     else
-        k_traverse<64><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], (int)P.nc, W.nodes,
-            W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
+        k_src_packets<uint32_t><<<grid_for(P.ns), kBlock, 0, s>>>((const uint32_t*)W.skeys[src_buf], (int)P.ns,
+            W.packets, W.counters);
+    static const bool dfs = [] {
+        const char* e = getenv("MCGPU_TRAVERSAL");
+        return e && strcmp(e, "packet") == 0;
+    }();
+    if (dfs)
+        k_traverse_packet<<<grid_for(P.ns), kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
+            W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
+            W.counters, W.cand, W.pair_status);
+    else {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_traverse_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWaveSmem);
+            attr = true;
+        }
+        k_traverse_wave<<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
+            W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
+            W.counters, W.cand, W.pair_status);
+    }
 }
 
 void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
@@ -965,20 +1549,26 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     const int g = grid_for(W.test_cap);
     g_launches++;
     k_narrow<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
-        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
-        W.pair_nrec);
+        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status);
 }
 
 int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
 {
     if (nrec == 0) return 0;
-    // key = halfedge slot (edge creation order) << 32 | face: both global and
-    // monotone in the pair index, so records come out grouped by pair
-    const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1],
-        nrec, 0, 64, W.sort_temp, s);
+    // key = halfedge slot (edge creation order), then face: both global and
+    // monotone in the pair index, so records come out grouped by pair. The
+    // key is packed to the bits the ids need, which sets the radix passes.
+    const uint32_t nidx = P.all_triangles ? 3u * P.nf : 0xFFFFFFFFu;
+    const int sbits = nidx == 0xFFFFFFFFu ? 32 : 32 - __builtin_clz(nidx | 1u);
+    const int gbits = 32 - __builtin_clz(P.nf | 1u);
+    const int g = grid_for(nrec);
     g_launches++;
-    k_gather_records<<<grid_for(nrec), kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids,
-        W.rec_pts);
+    k_record_pack<<<g, kBlock, 0, s>>>(W.rec_key[0], nrec, gbits);
+    const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1],
+        nrec, 0, sbits + gbits, W.sort_temp, s);
+    g_launches += 2;
+    k_gather_records<<<g, kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids, W.rec_pts);
+    k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);
     return buf;
 }
 

@@ -8,7 +8,9 @@
 //   fidx       uint32[foff[nf]]   global vertex ids (cut-mesh ids already offset)
 //   face_pair  uint32[nf]         pair id | kCutBit for cut-mesh faces
 //   fbox       double[nf][6]      exact fp64 face boxes (cut boxes enlarged by eps)
-//   tree       Node[Nc-1]         LBVH over all cut faces, key = pair << 30 | Morton
+//   tree       Node[ncl-1]        LBVH over leaf clusters of `leaf_size` consecutive
+//                                 cut faces (Morton order, never across pairs),
+//                                 key = pair << 30 | Morton
 //   pairs      uint64[P]          (source face << 32 | cut face), global ids
 //   tests      Test[T]            culled edge-face tests
 //   records    Record[R]          intersection records, sorted by (edge, face)
@@ -53,7 +55,10 @@ struct Problem {
     const uint32_t* pair_sbase; // first position of the pair in the source-face list
     const uint32_t* pair_cbase; // first position of the pair in the cut-face list
     const double* pair_eps;     // cut-box enlargement
+    const uint32_t* pair_clbase;// first leaf cluster of the pair
     int all_triangles;          // foff[f] == 3f
+    uint32_t leaf_size;         // cut faces per tree leaf (consecutive in Morton order, one pair)
+    uint32_t ncl;               // total leaf clusters
 };
 
 struct Work {
@@ -65,12 +70,17 @@ struct Work {
     void* ckeys[2];                   // cut-face keys
     uint32_t* cvals[2];
     uint32_t* sort_temp;
-    Node* nodes;                      // [nc-1]
-    int32_t* parent;                  // [2nc-1]
-    uint32_t* refit_flag;             // [nc-1]
+    void* cl_key;                     // [ncl] key of each leaf cluster's first face
+    uint32_t* cl_start;               // [ncl] first sorted position of the cluster
+    uint8_t* cl_n;                    // [ncl] faces in the cluster
+    long long* leaf_key_box;          // [nc*6] cut-face boxes in leaf order as dkey() integers
+    Node* nodes;                      // [ncl-1]
+    int32_t* parent;                  // [2ncl-1]
+    uint32_t* refit_flag;             // [ncl-1]
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
-                                      //        5..7 escalations
+                                      //        5..7 escalations, 8 traversal work cursor, 9 packets
+    uint2* packets;                   // [ns] query packets: sorted source positions [x, y]
     uint8_t* cand;                    // [nf]
     uint32_t* plane_slot;             // [nf]
     void* planes;                     // FacePlane[cap]
@@ -89,7 +99,7 @@ struct Work {
     double* rec_pts;                  // [test_cap*3] final, sorted
     uint32_t* pair_status;            // [n_pairs] ST_* bits
     int32_t* pair_bad;                // [n_pairs] lowest degenerate ps face (local), INT_MAX if none
-    uint32_t* pair_nrec;              // [n_pairs]
+    uint32_t* pair_nrec;              // [n_pairs+1] first sorted record of each pair (+ total)
     double* tri_scratch;              // polygon triplet scratch (24-byte entries)
     uint64_t tri_scratch_cap;         // entries
     uint64_t tri_stride;              // entries per polygon (largest C(n,3)); 0: no polygons

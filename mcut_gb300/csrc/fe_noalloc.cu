@@ -11,7 +11,7 @@
 // What it does instead: every scratch buffer of the front end (face boxes,
 // sort keys, tree nodes, candidate pairs, planes, incidence, edge-face tests,
 // record keys) lives in ONE file-scope __device__ array of fixed size,
-// kScratchBytes (about 11 MB). Every GPU that loads this library holds that
+// kScratchBytes (about 12 MB). Every GPU that loads this library holds that
 // array until the process exits. The caller passes the inputs (device
 // pointers to the internal, recentred coordinates and triangle indices) and
 // the outputs (device buffers for the records). No cudaMalloc, cudaFree,
@@ -49,6 +49,7 @@ constexpr uint32_t kMaxVerts = 16384;
 constexpr uint32_t kMaxFaces = 16384;
 constexpr uint32_t kMaxPairs = 32768;
 constexpr uint32_t kMaxTests = 65536;
+constexpr uint32_t kLeafSize = 4;
 
 constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -58,7 +59,12 @@ constexpr size_t oFidx = oX + al(kMaxVerts * 24ull);
 constexpr size_t oFpair = oFidx + al(kMaxFaces * 12ull);
 constexpr size_t oTab = oFpair + al(kMaxFaces * 4ull);
 constexpr size_t oEps = oTab + al(8 * 2 * 4);
-constexpr size_t oFbox = oEps + al(8);
+constexpr size_t oClKey = oEps + al(8);
+constexpr size_t oClStart = oClKey + al(kMaxFaces * 4ull);
+constexpr size_t oClN = oClStart + al(kMaxFaces * 4ull);
+constexpr size_t oLkb = oClN + al(kMaxFaces);
+constexpr size_t oPackets = oLkb + al(kMaxFaces * 48ull);
+constexpr size_t oFbox = oPackets + al(kMaxFaces * 8ull);
 constexpr size_t oMbox = oFbox + al(kMaxFaces * 48ull);
 constexpr size_t oKeys = oMbox + al(12 * 8);             // 8 arrays of kMaxFaces x 4 B
 constexpr size_t oSortTmp = oKeys + al(8ull * kMaxFaces * 4);
@@ -153,8 +159,9 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     P.foff = nullptr;
     P.fidx = reinterpret_cast<uint32_t*>(base + oFidx);
     P.face_pair = reinterpret_cast<uint32_t*>(base + oFpair);
-    // per-pair table, two entries per row (pair 0, end): fbase | fs | vbase | vs | sbase | cbase
-    const uint32_t htab[12] = { 0, (uint32_t)nf, Fs, 0, 0, (uint32_t)nv, Vs, 0, 0, Fs, 0, P.nc };
+    // per-pair table, two entries per row (pair 0, end): fbase | fs | vbase | vs | sbase | cbase | clbase
+    const uint32_t ncl = (P.nc + kLeafSize - 1) / kLeafSize;
+    const uint32_t htab[14] = { 0, (uint32_t)nf, Fs, 0, 0, (uint32_t)nv, Vs, 0, 0, Fs, 0, P.nc, 0, ncl };
     uint32_t* tab = reinterpret_cast<uint32_t*>(base + oTab);
     P.pair_fbase = tab;
     P.pair_fs = tab + 2;
@@ -163,7 +170,10 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     P.pair_sbase = tab + 8;
     P.pair_cbase = tab + 10;
     P.pair_eps = reinterpret_cast<double*>(base + oEps);
+    P.pair_clbase = tab + 12;
     P.all_triangles = 1;
+    P.leaf_size = kLeafSize;
+    P.ncl = ncl;
 
     Work W {};
     W.fbox = reinterpret_cast<double*>(base + oFbox);
@@ -178,6 +188,11 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.cvals[0] = keys + 6 * kMaxFaces;
     W.cvals[1] = keys + 7 * kMaxFaces;
     W.sort_temp = reinterpret_cast<uint32_t*>(base + oSortTmp);
+    W.cl_key = base + oClKey;
+    W.cl_start = reinterpret_cast<uint32_t*>(base + oClStart);
+    W.cl_n = base + oClN;
+    W.leaf_key_box = reinterpret_cast<long long*>(base + oLkb);
+    W.packets = reinterpret_cast<uint2*>(base + oPackets);
     W.nodes = reinterpret_cast<Node*>(base + oNodes);
     W.parent = reinterpret_cast<int32_t*>(base + oParent);
     W.refit_flag = reinterpret_cast<uint32_t*>(base + oRflag);
@@ -217,7 +232,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     if (!ok(cudaMemcpyAsync(base + oX, src->vertices, (size_t)Vs * 24, cudaMemcpyDeviceToDevice, s))
         || !ok(cudaMemcpyAsync(base + oX + (size_t)Vs * 24, cut->vertices, (size_t)cut->num_vertices * 24,
             cudaMemcpyDeviceToDevice, s))
-        || !ok(cudaMemcpyAsync(tab, htab, sizeof(uint32_t) * 12, cudaMemcpyHostToDevice, s))
+        || !ok(cudaMemcpyAsync(tab, htab, sizeof(uint32_t) * 14, cudaMemcpyHostToDevice, s))
         || !ok(cudaMemcpyAsync(base + oEps, &cut_eps, sizeof(double), cudaMemcpyHostToDevice, s))
         || !ok(cudaMemsetAsync(W.counters, 0, 64, s)) || !ok(cudaMemsetAsync(W.cand, 0, nf, s))
         || !ok(cudaMemsetAsync(W.vneed, 0, nv, s)) || !ok(cudaMemsetAsync(W.pair_status, 0, 4, s))

@@ -61,16 +61,61 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ a, uint32_
     }
 }
 
+// one CTA per digit: exclusive scan of that digit's per-tile counts (in
+// place) and the digit's total
+__global__ void __launch_bounds__(kThreads) k_digit_scan(uint32_t* __restrict__ hist, uint32_t tiles,
+    uint32_t* __restrict__ totals)
+{
+    __shared__ uint32_t ws[kWarps];
+    uint32_t* row = hist + (size_t)blockIdx.x * tiles;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < tiles; base += kThreads) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < tiles ? row[i] : 0u;
+        uint32_t inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) ws[w] = inc;
+        __syncthreads();
+        uint32_t wpre = 0, tot = 0;
+        for (int k = 0; k < kWarps; ++k) {
+            if (k < w) wpre += ws[k];
+            tot += ws[k];
+        }
+        if (i < tiles) row[i] = carry + wpre + inc - v;
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
     K* __restrict__ okeys, uint32_t* __restrict__ ovals, uint32_t n, int shift, const uint32_t* __restrict__ hist,
-    uint32_t tiles)
+    uint32_t tiles, const uint32_t* __restrict__ totals)
 {
     __shared__ uint32_t wh[kWarps][kDigits];
     __shared__ uint32_t goff[kDigits];
+    __shared__ uint32_t wsum[kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kWarps * kDigits; i += kThreads) (&wh[0][0])[i] = 0;
-    for (int i = threadIdx.x; i < kDigits; i += kThreads) goff[i] = hist[(size_t)i * tiles + blockIdx.x];
+    {
+        // digit bases: exclusive scan of the 256 digit totals (kThreads == kDigits)
+        const uint32_t v = totals[threadIdx.x];
+        uint32_t inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t wpre = 0;
+        for (int k = 0; k < warp; ++k) wpre += wsum[k];
+        goff[threadIdx.x] = wpre + inc - v + hist[(size_t)threadIdx.x * tiles + blockIdx.x];
+    }
     __syncthreads();
 
     const size_t wbase = (size_t)blockIdx.x * kTile + (size_t)warp * 32 * kItems;
@@ -198,7 +243,7 @@ size_t radix_sort_temp_bytes(uint32_t n)
 {
     const uint32_t tiles = (n + kTile - 1) / kTile;
     const size_t table = (size_t)kDigits * (tiles ? tiles : 1);
-    return (table + scan_temp_bytes((uint32_t)table) / sizeof(uint32_t) + 64) * sizeof(uint32_t);
+    return (table + kDigits + 64) * sizeof(uint32_t);
 }
 
 template <typename K>
@@ -211,10 +256,12 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
     K* kb[2] = { keys, keys_alt };
     uint32_t* vb[2] = { vals, vals_alt };
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        g_launches += 2;
+        uint32_t* totals = temp + (size_t)kDigits * tiles;
+        g_launches += 3;
         k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);
-        exclusive_scan(temp, kDigits * tiles, nullptr, temp + (size_t)kDigits * tiles, s);
-        k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles);
+        k_digit_scan<<<kDigits, kThreads, 0, s>>>(temp, tiles, totals);
+        k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles,
+            totals);
         cur ^= 1;
     }
     return cur;
