@@ -158,7 +158,7 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
  * recording a CUDA graph on its stream, a plugin that must stay inside its
  * host application's own memory arena, a frame loop that cannot wait on the
  * driver's allocator. All scratch sits in one file-scope __device__ array of
- * about 11 MB that every GPU loading this library keeps until exit.
+ * about 12 MB that every GPU loading this library keeps until exit.
  * Limits: triangles only; at most 16384 vertices and 16384 faces over both
  * meshes, 32768 candidate pairs, 65536 edge-face tests -- anything larger
  * returns MCGPU_TOO_LARGE. Every call shares that array and it keeps the

@@ -439,6 +439,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     const int key_bits = kMortonBits + pbits;
     // stage-1 buffers
     W.fbox = c->buf[B_FBOX].get<double>(L.nf * 6);
+    W.fbox32 = c->buf[B_LKB].get<float>(L.nf * 6);
     W.mesh_box = c->buf[B_MESHBOX].get<unsigned long long>((size_t)n * 12);
     const size_t ksz = wide ? 8 : 4;
     W.skeys[0] = c->buf[B_SK0].get<uint8_t>(L.ns * ksz);
@@ -452,7 +453,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.cl_key = c->buf[B_CLKEY].get<uint8_t>(L.ncl * ksz);
     W.cl_start = c->buf[B_CLSTART].get<uint32_t>(L.ncl);
     W.cl_n = c->buf[B_CLN].get<uint8_t>(L.ncl);
-    W.leaf_key_box = c->buf[B_LKB].get<long long>(L.nc * 6);
+    W.leaf_key_box = nullptr;
     W.packets = c->buf[B_PACKETS].get<uint2>(L.ns);
     W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
     W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));

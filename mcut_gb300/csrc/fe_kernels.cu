@@ -67,7 +67,7 @@ __device__ __forceinline__ void mesh_box_flush(unsigned long long* __restrict__ 
 constexpr int kBoundsItems = 8; // faces per thread per tile; a tile is kBlock * kBoundsItems consecutive faces
 
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
-    unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
+    float* __restrict__ fbox32, unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
 {
     // Per-mesh boxes only steer Morton codes. Tiles are runs of consecutive
     // faces, so a tile almost always belongs to one mesh: each thread folds
@@ -108,6 +108,10 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
             d[0] = make_double2(b.mn[0], b.mn[1]);
             d[1] = make_double2(b.mn[2], b.mx[0]);
             d[2] = make_double2(b.mx[1], b.mx[2]);
+            float2* d32 = reinterpret_cast<float2*>(fbox32 + (size_t)f * 6);
+            d32[0] = make_float2(f32_rd(b.mn[0]), f32_rd(b.mn[1]));
+            d32[1] = make_float2(f32_rd(b.mn[2]), f32_ru(b.mx[0]));
+            d32[2] = make_float2(f32_ru(b.mx[1]), f32_ru(b.mx[2]));
             const uint32_t k = p * 2 + (is_cut ? 1u : 0u);
             if (key != kNone && k != key) {
                 mesh_box_flush(mesh_box, key, lo, hi);
@@ -298,6 +302,16 @@ __global__ void __launch_bounds__(kBlock) k_src_packets(const K* __restrict__ ke
     }
 }
 
+// a face's fp64 box as dkey() integers: (mn0,mn1) (mn2,mx0) (mx1,mx2)
+__device__ __forceinline__ void load_key_box(const double* __restrict__ fbox, uint32_t f, longlong2& a, longlong2& b,
+    longlong2& c)
+{
+    const Box x = load_box(fbox, f);
+    a = make_longlong2(dkey(x.mn[0]), dkey(x.mn[1]));
+    b = make_longlong2(dkey(x.mn[2]), dkey(x.mx[0]));
+    c = make_longlong2(dkey(x.mx[1]), dkey(x.mx[2]));
+}
+
 // leaf clusters: `leaf_size` consecutive sorted cut faces of one pair
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_clusters(Problem P, const K* __restrict__ ckey, K* __restrict__ clkey,
@@ -341,27 +355,23 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
 }
 
 // bottom-up refit: the second child to arrive at a node merges both boxes
-__global__ void __launch_bounds__(kBlock) k_refit(Problem P, const double* __restrict__ fbox,
+__global__ void __launch_bounds__(kBlock) k_refit(Problem P, const float* __restrict__ fbox32,
     const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n,
-    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, uint32_t* __restrict__ flag,
-    long long* __restrict__ leaf_key_box)
+    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, uint32_t* __restrict__ flag)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         FBox fb;
         for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
         const uint32_t s0 = cl_start[i], cn = cl_n[i];
+        uint32_t lf[16];
+        for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
         for (uint32_t t = 0; t < cn; ++t) {
-            const Box b = load_box(fbox, leaf_face[s0 + t]);
-            longlong2* kb = reinterpret_cast<longlong2*>(leaf_key_box + (size_t)(s0 + t) * 6);
-            kb[0] = make_longlong2(dkey(b.mn[0]), dkey(b.mn[1]));
-            kb[1] = make_longlong2(dkey(b.mn[2]), dkey(b.mx[0]));
-            kb[2] = make_longlong2(dkey(b.mx[1]), dkey(b.mx[2]));
-            for (int j = 0; j < 3; ++j) {
-                fb.lo[j] = fminf(fb.lo[j], f32_rd(b.mn[j]));
-                fb.hi[j] = fmaxf(fb.hi[j], f32_ru(b.mx[j]));
-            }
+            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
+            const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
+            fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
+            fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
         }
-        fb.plo = fb.phi = P.face_pair[leaf_face[s0]] & ~kCutBit;
+        fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
         int child = ~i;
         int node = parent[(n - 1) + i];
         while (node >= 0) {
@@ -382,16 +392,6 @@ __global__ void __launch_bounds__(kBlock) k_refit(Problem P, const double* __res
             child = node;
             node = node == 0 ? -1 : parent[node];
         }
-    }
-}
-
-__global__ void __launch_bounds__(kBlock) k_leaf_keys(Problem P, const double* __restrict__ fbox,
-    const uint32_t* __restrict__ leaf_face, long long* __restrict__ leaf_key_box)
-{
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nc; i += gridDim.x * blockDim.x) {
-        const Box b = load_box(fbox, leaf_face[i]);
-        long long* k = leaf_key_box + (size_t)i * 6;
-        for (int j = 0; j < 3; ++j) { k[j] = dkey(b.mn[j]); k[3 + j] = dkey(b.mx[j]); }
     }
 }
 
@@ -469,11 +469,11 @@ __global__ void __launch_bounds__(kBlock) k_traverse_packet(Problem P, const dou
                 return;
             const uint32_t s0 = __ldg(&cl_start[li]), cn = __ldg(&cl_n[li]);
             for (uint32_t u = 0; u < cn; ++u) {
-                const longlong2* kb = reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
-                const longlong2 a = __ldg(kb), b = __ldg(kb + 1), c = __ldg(kb + 2);
+                const uint32_t c2 = __ldg(&leaf_face[s0 + u]);
+                longlong2 a, b, c;
+                load_key_box(fbox, c2, a, b, c);
                 // closed overlap: q.mn <= l.mx && q.mx >= l.mn on every axis
                 if (qk[0] <= b.y && qk[3] >= a.x && qk[1] <= c.x && qk[4] >= a.y && qk[2] <= c.y && qk[5] >= b.x) {
-                    const uint32_t c2 = __ldg(&leaf_face[s0 + u]);
                     buf[nb++] = ((unsigned long long)s << 32) | c2;
                     cand[c2] = 1;
                     any = true;
@@ -654,10 +654,9 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                     if (mask) {
                         const uint32_t s0 = __ldg(&cl_start[L.id]), cn = __ldg(&cl_n[L.id]);
                         for (uint32_t u = 0; u < cn; ++u) {
-                            const longlong2* b2 =
-                                reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
-                            const longlong2 ka = __ldg(b2), kb = __ldg(b2 + 1), kc = __ldg(b2 + 2);
                             const uint32_t cf = __ldg(&leaf_face[s0 + u]);
+                            longlong2 ka, kb, kc;
+                            load_key_box(fbox, cf, ka, kb, kc);
                             bool any_cf = false;
                             for (unsigned mm = mask; mm; mm &= mm - 1) {
                                 const int j = __ffs(mm) - 1;
@@ -804,10 +803,10 @@ __global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __
         auto leaf = [&](int li) {
             const uint32_t s0 = __ldg(&cl_start[li]), cn = __ldg(&cl_n[li]);
             for (uint32_t u = 0; u < cn; ++u) {
-                const longlong2* kb = reinterpret_cast<const longlong2*>(leaf_key_box + (size_t)(s0 + u) * 6);
-                const longlong2 a = __ldg(kb), b = __ldg(kb + 1), c = __ldg(kb + 2);
+                const uint32_t cf = __ldg(&leaf_face[s0 + u]);
+                longlong2 a, b, c;
+                load_key_box(fbox, cf, a, b, c);
                 if (qk[0] <= b.y && qk[3] >= a.x && qk[1] <= c.x && qk[4] >= a.y && qk[2] <= c.y && qk[5] >= b.x) {
-                    const uint32_t cf = __ldg(&leaf_face[s0 + u]);
                     buf[nb++] = ((unsigned long long)s << 32) | cf;
                     cand[cf] = 1;
                     any = true;
@@ -1412,7 +1411,7 @@ void launch_bounds_morton(const Problem& P, Work& W, bool wide, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
     g_launches++;
-    k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, W.pair_status);
+    k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, W.mesh_box, W.pair_status);
     g_launches++;
     if (wide)
         k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box,
@@ -1450,11 +1449,7 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
     else
         k_clusters<uint32_t><<<gc, kBlock, 0, s>>>(P, (const uint32_t*)W.ckeys[cut_buf], (uint32_t*)W.cl_key,
             W.cl_start, W.cl_n);
-    if (n < 2) {
-        g_launches++;
-        k_leaf_keys<<<grid_for(P.nc), kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], W.leaf_key_box);
-        return;
-    }
+    if (n < 2) return;
     const int g = grid_for(n);
     g_launches++;
     if (wide)
@@ -1463,8 +1458,8 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
         k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.cl_key, n, W.nodes, W.parent);
     cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
     g_launches++;
-    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox, W.cvals[cut_buf], W.cl_start, W.cl_n, n, W.nodes, W.parent,
-        W.refit_flag, W.leaf_key_box);
+    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox32, W.cvals[cut_buf], W.cl_start, W.cl_n, n, W.nodes, W.parent,
+        W.refit_flag);
 }
 
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
@@ -1564,8 +1559,13 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
     const int g = grid_for(nrec);
     g_launches++;
     k_record_pack<<<g, kBlock, 0, s>>>(W.rec_key[0], nrec, gbits);
-    const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1],
-        nrec, 0, sbits + gbits, W.sort_temp, s);
+    int buf = 0;
+    if (nrec <= kSmallSort && sbits + gbits <= 50) {
+        sort_small_pairs(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1], nrec, sbits + gbits, s);
+        buf = 1;
+    } else
+        buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1], nrec, 0,
+            sbits + gbits, W.sort_temp, s);
     g_launches += 2;
     k_gather_records<<<g, kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids, W.rec_pts);
     k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);

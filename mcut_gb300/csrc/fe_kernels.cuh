@@ -63,6 +63,7 @@ struct Problem {
 
 struct Work {
     double* fbox;                     // [nf*6]
+    float* fbox32;                    // [nf*6] the same boxes rounded outward to fp32
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
     // sort buffers (keys u32 for one pair, u64 for batches)
     void* skeys[2];                   // source-face keys
@@ -73,7 +74,7 @@ struct Work {
     void* cl_key;                     // [ncl] key of each leaf cluster's first face
     uint32_t* cl_start;               // [ncl] first sorted position of the cluster
     uint8_t* cl_n;                    // [ncl] faces in the cluster
-    long long* leaf_key_box;          // [nc*6] cut-face boxes in leaf order as dkey() integers
+    long long* leaf_key_box;          // unused (kept null)
     Node* nodes;                      // [ncl-1]
     int32_t* parent;                  // [2ncl-1]
     uint32_t* refit_flag;             // [ncl-1]

@@ -191,7 +191,8 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.cl_key = base + oClKey;
     W.cl_start = reinterpret_cast<uint32_t*>(base + oClStart);
     W.cl_n = base + oClN;
-    W.leaf_key_box = reinterpret_cast<long long*>(base + oLkb);
+    W.leaf_key_box = nullptr;
+    W.fbox32 = reinterpret_cast<float*>(base + oLkb);
     W.packets = reinterpret_cast<uint2*>(base + oPackets);
     W.nodes = reinterpret_cast<Node*>(base + oNodes);
     W.parent = reinterpret_cast<int32_t*>(base + oParent);

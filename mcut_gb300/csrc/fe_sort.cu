@@ -27,11 +27,20 @@ __global__ void __launch_bounds__(kThreads) k_upsweep(const K* __restrict__ keys
 {
     __shared__ uint32_t h[kDigits];
     for (int i = threadIdx.x; i < kDigits; i += kThreads) h[i] = 0;
-    __syncthreads();
+    // all loads first: they are independent and overlap; the shared-memory
+    // atomics below would otherwise serialise them
+    K k[kItems];
     const size_t base = (size_t)blockIdx.x * kTile;
+#pragma unroll
     for (int i = 0; i < kItems; ++i) {
-        const size_t k = base + (size_t)i * kThreads + threadIdx.x;
-        if (k < n) atomicAdd(&h[(uint32_t)(keys[k] >> shift) & 0xFFu], 1u);
+        const size_t idx = base + (size_t)i * kThreads + threadIdx.x;
+        k[i] = idx < n ? keys[idx] : (K)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const size_t idx = base + (size_t)i * kThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(uint32_t)(k[i] >> shift) & 0xFFu], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kDigits; i += kThreads) hist[(size_t)i * tiles + blockIdx.x] = h[i];
@@ -122,12 +131,18 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ ke
     K k[kItems];
     uint32_t v[kItems], rank[kItems];
     const uint32_t lt = (1u << lane) - 1u;
+    // all loads first (independent, in flight together), then the ranking
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
         const size_t idx = wbase + (size_t)i * 32 + lane;
         const bool ok = idx < n;
         k[i] = ok ? keys[idx] : (K)0;
         v[i] = ok ? vals[idx] : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const size_t idx = wbase + (size_t)i * 32 + lane;
+        const bool ok = idx < n;
         const uint32_t d = ok ? ((uint32_t)(k[i] >> shift) & 0xFFu) : 0x100u; // 0x100: padding, no digit
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
         uint32_t prev = 0;
@@ -265,6 +280,103 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
         cur ^= 1;
     }
     return cur;
+}
+
+// One-CTA LSD radix sort for small inputs (n <= kSmallSort): every pass runs
+// in shared memory, so the whole sort is one launch instead of three per
+// pass. Keys carry their input position in the low 14 bits (composite
+// uint64, so end_bit + 14 <= 64); 16 warps, warp w ranks its contiguous chunk
+// in rounds of 32 keys (stable), digit offsets come from a (digit, warp) scan.
+constexpr int kSmallThreads = 512;
+constexpr int kSmallWarps = kSmallThreads / 32;
+constexpr int kSmallIdxBits = 14;
+
+__global__ void __launch_bounds__(kSmallThreads) k_sort_small(const unsigned long long* __restrict__ keys_in,
+    const uint32_t* __restrict__ vals_in, unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+    uint32_t n, int end_bit)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    unsigned long long* kb[2] = { reinterpret_cast<unsigned long long*>(sm),
+        reinterpret_cast<unsigned long long*>(sm) + kSmallSort };
+    uint32_t (*wh)[kDigits] = reinterpret_cast<uint32_t (*)[kDigits]>(kb[1] + kSmallSort);
+    uint32_t* dbase = reinterpret_cast<uint32_t*>(wh + kSmallWarps);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t i = threadIdx.x; i < n; i += kSmallThreads) kb[0][i] = (keys_in[i] << kSmallIdxBits) | i;
+    const uint32_t chunk = ((n + kSmallWarps - 1) / kSmallWarps + 31) & ~31u;
+    int cur = 0;
+    for (int shift = kSmallIdxBits; shift < end_bit + kSmallIdxBits; shift += 8) {
+        for (int i = threadIdx.x; i < kSmallWarps * kDigits; i += kSmallThreads) (&wh[0][0])[i] = 0;
+        __syncthreads();
+        uint32_t rank[kSmallSort / kSmallWarps / 32];
+        const uint32_t lo = w * chunk;
+        for (uint32_t r = 0; r * 32 < chunk; ++r) {
+            const uint32_t idx = lo + r * 32 + lane;
+            const bool ok = idx < n;
+            const uint32_t d = ok ? (uint32_t)(kb[cur][idx] >> shift) & 0xFFu : 0x100u;
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+            uint32_t prev = 0;
+            if (ok) prev = wh[w][d];
+            __syncwarp();
+            if (ok && (peers & lt) == 0) wh[w][d] = prev + __popc(peers);
+            __syncwarp();
+            rank[r] = prev + __popc(peers & lt);
+        }
+        __syncthreads();
+        if (threadIdx.x < kDigits) {
+            const int d = threadIdx.x;
+            uint32_t run = 0;
+            for (int k = 0; k < kSmallWarps; ++k) {
+                const uint32_t c = wh[k][d];
+                wh[k][d] = run;
+                run += c;
+            }
+            dbase[d] = run;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            // exclusive scan of the 256 digit totals by one warp (8 per lane)
+            uint32_t v[8], sum = 0;
+            for (int k = 0; k < 8; ++k) { v[k] = dbase[lane * 8 + k]; sum += v[k]; }
+            uint32_t inc = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            uint32_t run = inc - sum;
+            for (int k = 0; k < 8; ++k) { dbase[lane * 8 + k] = run; run += v[k]; }
+        }
+        __syncthreads();
+        for (uint32_t r = 0; r * 32 < chunk; ++r) {
+            const uint32_t idx = lo + r * 32 + lane;
+            if (idx < n) {
+                const unsigned long long k = kb[cur][idx];
+                const uint32_t d = (uint32_t)(k >> shift) & 0xFFu;
+                kb[cur ^ 1][dbase[d] + wh[w][d] + rank[r]] = k;
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += kSmallThreads) {
+        const unsigned long long c = kb[cur][i];
+        keys_out[i] = c >> kSmallIdxBits;
+        vals_out[i] = vals_in[c & ((1u << kSmallIdxBits) - 1u)];
+    }
+}
+
+size_t sort_small_smem() { return (size_t)kSmallSort * 16 + (size_t)kSmallWarps * kDigits * 4 + kDigits * 4; }
+
+void sort_small_pairs(const unsigned long long* keys_in, const uint32_t* vals_in, unsigned long long* keys_out,
+    uint32_t* vals_out, uint32_t n, int end_bit, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_small_smem());
+        attr = true;
+    }
+    g_launches++;
+    k_sort_small<<<1, kSmallThreads, sort_small_smem(), s>>>(keys_in, vals_in, keys_out, vals_out, n, end_bit);
 }
 
 template int radix_sort_pairs<uint32_t>(uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t, int, int, uint32_t*,
