@@ -109,7 +109,7 @@ struct Layout {
 struct mcgpu_context_t {
     int device = 0;
     cudaStream_t s = nullptr;
-    cudaEvent_t ev[9] = {};
+    cudaEvent_t ev[16] = {};  // begin / end of each stage (MCGPU_PROFILE)
     DevBuf buf[B_COUNT];
     PinBuf pin_counters, pin_tab, pin_stage;
     Layout L;
@@ -407,6 +407,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.ncl = (uint32_t)L.ncl;
 }
 
+// stage events: 2k at the start of stage k, 2k+1 at its end; the host
+// readbacks between stages fall outside every stage
 inline void rec(mcgpu_context_t* c, int i)
 {
     if (c->flags & MCGPU_PROFILE) ck(cudaEventRecord(c->ev[i], c->s), "event");
@@ -428,9 +430,9 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     if (rc != MCGPU_OK) return rc;
     Layout& L = c->L;
     cudaStream_t s = c->s;
-    rec(c, 0);
+    rec(c, 2 * MCGPU_STAGE_UPLOAD);
     upload(c, flags, srcs, cuts);
-    rec(c, 1);
+    rec(c, 2 * MCGPU_STAGE_UPLOAD + 1);
 
     Problem& P = c->P;
     Work& W = c->W;
@@ -468,6 +470,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
 
     // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
+    rec(c, 2 * MCGPU_STAGE_BOUNDS);
     g_launches++;
     k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
     ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
@@ -477,14 +480,19 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
 
     launch_bounds_morton(P, W, wide, s);
-    rec(c, 2);
+    rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
     W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(radix_sort_temp_bytes((uint32_t)std::max(L.ns, L.nc)) / 4 + 64);
     int cut_buf = 0;
+    rec(c, 2 * MCGPU_STAGE_SORT);
     const int src_buf = launch_sort(P, W, wide, key_bits, s, cut_buf);
-    rec(c, 3);
+    rec(c, 2 * MCGPU_STAGE_SORT + 1);
+    rec(c, 2 * MCGPU_STAGE_HIERARCHY);
     launch_hierarchy(P, W, wide, cut_buf, s);
-    rec(c, 4);
+    launch_packets(P, W, src_buf, s);
+    rec(c, 2 * MCGPU_STAGE_HIERARCHY + 1);
+    rec(c, 2 * MCGPU_STAGE_TRAVERSE);
     launch_traverse(P, W, src_buf, cut_buf, false, s);
+    rec(c, 2 * MCGPU_STAGE_TRAVERSE + 1);
 
     // readback 1: pair count and traversal flags
     uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
@@ -505,12 +513,12 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
         ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
         ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+        launch_packets(P, W, src_buf, s);
         launch_traverse(P, W, src_buf, cut_buf, deep, s);
         ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
         ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
         ck(cudaStreamSynchronize(s), "sync traverse");
     }
-    rec(c, 5);
     const uint64_t npairs = hc[0];
     c->n_pairs_found = npairs;
 
@@ -538,12 +546,14 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
     W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
         radix_sort_temp_bytes((uint32_t)std::max<uint64_t>({ L.ns, L.nc, W.test_cap })) / 4 + 64);
+    rec(c, 2 * MCGPU_STAGE_ADJACENCY);
     ck(cudaMemsetAsync(W.vneed, 0, L.nv, s), "memset");
-
     launch_adjacency_planes(P, W, s);
-    rec(c, 6);
+    rec(c, 2 * MCGPU_STAGE_ADJACENCY + 1);
+    rec(c, 2 * MCGPU_STAGE_NARROW);
     launch_tests(P, W, s);
     launch_narrow(P, W, (flags & MCGPU_KEEP_TESTS) != 0, s);
+    rec(c, 2 * MCGPU_STAGE_NARROW + 1);
 
     // readback 2: counters, per-pair status / degenerate face / record count
     ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
@@ -554,11 +564,12 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->n_records = hc[2];
     W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
     W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
+    rec(c, 2 * MCGPU_STAGE_DOWNLOAD);  // record sort + gather (added to the narrow stage)
     c->rec_buf = launch_records(P, W, (uint32_t)c->n_records, s);
+    rec(c, 2 * MCGPU_STAGE_DOWNLOAD + 1);
     // per-pair record ranges (first sorted record of each pair, then the total)
     ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
         "D2H ranges");
-    rec(c, 7);
     ck(cudaStreamSynchronize(s), "sync records");
     ck(cudaGetLastError(), "kernel launch");
 
@@ -587,11 +598,13 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         c->sums[0].escalations[1] = hc[6];
         c->sums[0].escalations[2] = hc[7];
         if (flags & MCGPU_PROFILE) {
-            for (int k = 0; k < 7; ++k) {
+            for (int k = 0; k < 8; ++k) {
                 float ms = 0.f;
-                cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+                cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]);
                 c->sums[0].stage_ms[k] = ms;
             }
+            c->sums[0].stage_ms[MCGPU_STAGE_NARROW] += c->sums[0].stage_ms[MCGPU_STAGE_DOWNLOAD];
+            c->sums[0].stage_ms[MCGPU_STAGE_DOWNLOAD] = 0.f;
         }
     }
     for (auto& m : c->sums) m.kernel_launches = (uint32_t)(g_launches - launches0);

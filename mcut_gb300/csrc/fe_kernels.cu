@@ -1462,16 +1462,26 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
         W.refit_flag);
 }
 
+void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)
+{
+    g_launches++;
+    if (P.n_pairs > 1)
+        k_src_packets<unsigned long long><<<grid_for(P.ns), kBlock, 0, s>>>(
+            (const unsigned long long*)W.skeys[src_buf], (int)P.ns, W.packets, W.counters);
+    else
+        k_src_packets<uint32_t><<<grid_for(P.ns), kBlock, 0, s>>>((const uint32_t*)W.skeys[src_buf], (int)P.ns,
+            W.packets, W.counters);
+}
+
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
 {
     // Default: warp per query packet (a compact source subtree of <= 32
-    // faces). MCGPU_TRAVERSAL=thread selects one thread per source face; the
+    // faces; launch_packets must have run since the counters were cleared). MCGPU_TRAVERSAL=thread selects one thread per source face; the
     // deep re-run after a stack overflow is per thread with a 512-entry stack.
     static const bool per_thread = [] {
         const char* e = getenv("MCGPU_TRAVERSAL");
         return e && strcmp(e, "thread") == 0;
     }();
-    const bool wide = P.n_pairs > 1;
     if (deep || per_thread) {
         const int g = grid_for(P.ns);
         g_launches++;
@@ -1483,13 +1493,7 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
                 W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
         return;
     }
-    g_launches += 2;
-    if (wide)
-        k_src_packets<unsigned long long><<<grid_for(P.ns), kBlock, 0, s>>>(
-            (const unsigned long long*)W.skeys[src_buf], (int)P.ns, W.packets, W.counters);
-    else
-        k_src_packets<uint32_t><<<grid_for(P.ns), kBlock, 0, s>>>((const uint32_t*)W.skeys[src_buf], (int)P.ns,
-            W.packets, W.counters);
+    g_launches++;
     static const bool dfs = [] {
         const char* e = getenv("MCGPU_TRAVERSAL");
         return e && strcmp(e, "packet") == 0;

@@ -111,6 +111,7 @@ struct Work {
 void launch_bounds_morton(const Problem& P, Work& W, bool wide_keys, cudaStream_t s);
 int launch_sort(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s, int& cut_buf);
 void launch_hierarchy(const Problem& P, Work& W, bool wide_keys, int cut_buf, cudaStream_t s);
+void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s);
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s);
 void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s);
 void launch_tests(const Problem& P, Work& W, cudaStream_t s);

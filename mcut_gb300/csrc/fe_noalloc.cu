@@ -247,6 +247,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     int cut_buf = 0;
     const int src_buf = launch_sort(P, W, false, kMortonBits, s, cut_buf);
     launch_hierarchy(P, W, false, cut_buf, s);
+    launch_packets(P, W, src_buf, s);
     launch_traverse(P, W, src_buf, cut_buf, false, s);
     uint32_t hc[16 + 3];
     if (!ok(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s))
