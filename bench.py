@@ -213,6 +213,103 @@ def run_single():
                       "kernel_launches_per_dispatch": int(sm.kernel_launches)}))
 
 
+BATCH_WORKLOAD = ("fracture batch: 4096 independent pairs, icosphere level U{2..5} r U(0.5,1.5) noise N(0,0.005) "
+                  "vs n x n crack grid n U{8..128}, random rotation, offset U(-0.3,0.3), z noise N(0,0.02)")
+
+
+def run_batch(ctx, lib, steps, world):
+    """The batched path against the plain per-dispatch path on the same
+    4096 fracture pairs, inputs resident in HBM (internal coordinates)."""
+    import ctypes as C
+    import torch
+    from mcut_gb300 import meshgen, pack_pairs
+    from mcut_gb300 import _lib as L
+
+    pairs = meshgen.batch_pairs(4096)
+    pk = pack_pairs(pairs)
+    n = len(pairs)
+    dv = torch.from_numpy(pk["v"]).cuda()
+    df = torch.from_numpy(pk["f"]).cuda()
+    dpk = dict(pk, v=dv, f=df)
+    nfaces = int(pk["counts"][:, 1].sum() + pk["counts"][:, 3].sum())
+
+    # batched: one packed pass over all pairs
+    launches = 0
+    for _ in range(2):
+        sums, _, _, _ = ctx.dispatch_packed(dpk, device=True, fetch=False)
+    torch.cuda.synchronize()
+    barrier(world)
+    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    bt = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        st.record()
+        sums, _, _, _ = ctx.dispatch_packed(dpk, device=True, fetch=False)
+        en.record()
+        torch.cuda.synchronize()
+        bt.append(st.elapsed_time(en))
+        launches += sums[0].kernel_launches
+    barrier(world)
+    b_ms = reduce_max(sum(bt), world) / steps
+    status = {}
+    nrec = 0
+    for i in range(n):
+        k = L.STATUS_NAMES[sums[i].status]
+        status[k] = status.get(k, 0) + 1
+        nrec += int(sums[i].num_records)
+
+    # end to end: packed host arrays -> records + offsets back on the host
+    et = []
+    for _ in range(1 + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, ids, pts, off = ctx.dispatch_packed(pk, device=False, fetch=True)
+        et.append(time.perf_counter() - t0)
+    e_s = reduce_max(sum(et[1:]), world) / steps
+
+    # plain: one mcgpu_dispatch per pair on the same device-resident arrays
+    cnt = pk["counts"].astype(np.int64)
+    vb = np.concatenate([[0], np.cumsum(cnt[:, 0] + cnt[:, 2])])
+    fb = np.concatenate([[0], np.cumsum(3 * (cnt[:, 1] + cnt[:, 3]))])
+    meshes = []
+    for i in range(n):
+        ms = L.Mesh(dv.data_ptr() + 24 * int(vb[i]), df.data_ptr() + 4 * int(fb[i]), None,
+                    int(cnt[i, 0]), int(cnt[i, 1]))
+        mc = L.Mesh(dv.data_ptr() + 24 * int(vb[i] + cnt[i, 0]), df.data_ptr() + 4 * int(fb[i] + 3 * cnt[i, 1]),
+                    None, int(cnt[i, 2]), int(cnt[i, 3]))
+        meshes.append((ms, mc, float(pk["eps"][i])))
+    sm = L.Summary()
+    for ms, mc, e in meshes[:32]:
+        L.check(lib.mcgpu_dispatch(ctx._h, L.DEVICE_POINTERS, C.byref(ms), C.byref(mc), e, C.byref(sm)), "dispatch")
+    torch.cuda.synchronize()
+    barrier(world)
+    lat = []
+    plain_rec = 0
+    t_all = time.perf_counter()
+    for ms, mc, e in meshes:
+        st.record()
+        L.check(lib.mcgpu_dispatch(ctx._h, L.DEVICE_POINTERS, C.byref(ms), C.byref(mc), e, C.byref(sm)), "dispatch")
+        en.record()
+        en.synchronize()
+        lat.append(st.elapsed_time(en))
+        plain_rec += int(sm.num_records)
+    t_all = time.perf_counter() - t_all
+    barrier(world)
+    p_s = reduce_max(t_all, world)
+    return {
+        "workload": BATCH_WORKLOAD, "pairs": n, "faces": nfaces, "status": status, "records": nrec,
+        "records_plain": plain_rec,
+        "batched": {"value": world * n / (b_ms / 1e3), "unit": UNIT, "ms_per_batch": b_ms,
+                    "kernel_launches_per_batch": launches // steps},
+        "batched_e2e": {"value": world * n / e_s, "unit": UNIT, "ms_per_batch": 1e3 * e_s,
+                        "h2d_bytes_per_step": int(pk["v"].nbytes + pk["f"].nbytes),
+                        "d2h_bytes_per_step": int(ids.nbytes + pts.nbytes + off.nbytes)},
+        "plain": {"value": world * n / p_s, "unit": UNIT,
+                  "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
+        "batched_over_plain": (n / (b_ms / 1e3)) / (n / p_s),
+    }
+
+
 def run_gpu(args, world, rank, local):
     import torch
     import ctypes as C
@@ -289,6 +386,7 @@ def run_gpu(args, world, rank, local):
         step_e2e()
         e2e_t.append(time.perf_counter() - t0)
     e2e_tot = reduce_max(sum(e2e_t), world)
+    batch = None if args.no_batch else run_batch(ctx, lib, 3, world)
     e2e_value = world * args.steps / e2e_tot
     h2d = sx.nbytes + cx.nbytes + fs_.nbytes + fc_.nbytes
     d2h = int(sm.num_records) * (20 + 24)
@@ -345,6 +443,7 @@ def run_gpu(args, world, rank, local):
                 "ms_per_step": 1e3 * e2e_tot / args.steps},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
+        "batch": batch,
     }
     print(json.dumps(line), flush=True)
 
@@ -356,6 +455,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 4096-pair batched vs plain measurement")
     ap.add_argument("--single", action="store_true",
                     help="one warm-up dispatch + one dispatch of the workload, nothing else (for ncu captures)")
     args = ap.parse_args()

@@ -110,7 +110,9 @@ typedef enum mcgpu_data {
     MCGPU_DATA_TESTS = 4,         /* uint32[3*T]: q, r, face; MCGPU_KEEP_TESTS */
     MCGPU_DATA_TEST_INFO = 5,     /* int8[4*T]: sign(orient3d q), sign(orient3d r), type char, pip char */
     MCGPU_DATA_VERTICES = 6,      /* double[3*(Vs+Vc)]: the ps coordinates used */
-    MCGPU_DATA_FACE_BOXES = 7     /* double[6*(Fs+Fc)]: min xyz, max xyz (cut boxes enlarged) */
+    MCGPU_DATA_FACE_BOXES = 7,    /* double[6*(Fs+Fc)]: min xyz, max xyz (cut boxes enlarged) */
+    MCGPU_DATA_RECORD_OFFSETS = 8 /* uint64[n_pairs+1]: first record of each pair of the last
+                                     dispatch (records of a batch are grouped by pair), then R */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.
@@ -144,6 +146,33 @@ int mcgpu_dispatch_batch(mcgpu_context ctx, uint32_t flags, uint32_t n_pairs, co
     const mcgpu_mesh* cuts, const double* cut_eps, mcgpu_summary* summaries);
 int mcgpu_get_batch_data(mcgpu_context ctx, uint32_t pair, uint32_t query, uint64_t bytes, void* mem,
     uint64_t* bytes_out);
+
+/* A batch of pairs packed end to end (the layout the library uses
+ * internally, so the upload is one copy per array). For pair i, in order:
+ * its source vertices then its cut vertices in `vertices`, and its source
+ * face indices then its cut face indices in `face_indices`, each mesh's
+ * indices LOCAL to that mesh (0-based), as mcDispatch takes them
+ * (mcut.h:1003-1040). mesh_counts[4*i .. 4*i+3] = source vertices, source
+ * faces, cut vertices, cut faces. face_sizes (NULL: triangles) follows the
+ * same order. cut_eps[i] as in mcgpu_dispatch (may be NULL with
+ * MCGPU_RECENTRE). With MCGPU_DEVICE_POINTERS the three arrays are device
+ * pointers and `vertices` is read in place (keep it alive while results of
+ * the dispatch are read). */
+typedef struct mcgpu_batch {
+    uint32_t num_pairs;
+    const void* vertices;
+    const uint32_t* face_indices;
+    const uint32_t* face_sizes;
+    const uint32_t* mesh_counts;
+    const double* cut_eps;
+} mcgpu_batch;
+
+/* mcgpu_dispatch_batch over a packed batch. Replaces num_pairs sequential
+ * mcDispatch front ends (the fracture use case: many independent uneven
+ * pairs). Summaries as mcgpu_dispatch_batch; records of every pair with
+ * mcgpu_get_data (grouped by pair, MCGPU_DATA_RECORD_OFFSETS) or per pair
+ * with mcgpu_get_batch_data. */
+int mcgpu_dispatch_packed(mcgpu_context ctx, uint32_t flags, const mcgpu_batch* batch, mcgpu_summary* summaries);
 
 /* The reference's recentring on the host (calculate_vertex_parameters +
  * client_input_arrays_to_hmesh, preproc.cpp:2124-2290, 147-181): writes the

@@ -25,8 +25,8 @@ KEEP_PAIRS = 1 << 3
 PROFILE = 1 << 4
 DEVICE_POINTERS = 1 << 5
 
-DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DATA_VERTICES, DATA_FACE_BOXES = \
-    range(1, 8)
+DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DATA_VERTICES, DATA_FACE_BOXES, \
+    DATA_RECORD_OFFSETS = range(1, 9)
 
 STAGES = ["upload", "bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow", "download"]
 
@@ -34,6 +34,11 @@ STAGES = ["upload", "bounds", "sort", "hierarchy", "traverse", "adjacency", "nar
 class Mesh(C.Structure):
     _fields_ = [("vertices", C.c_void_p), ("face_indices", C.c_void_p), ("face_sizes", C.c_void_p),
                 ("num_vertices", C.c_uint32), ("num_faces", C.c_uint32)]
+
+
+class Batch(C.Structure):
+    _fields_ = [("num_pairs", C.c_uint32), ("vertices", C.c_void_p), ("face_indices", C.c_void_p),
+                ("face_sizes", C.c_void_p), ("mesh_counts", C.c_void_p), ("cut_eps", C.c_void_p)]
 
 
 class Summary(C.Structure):
@@ -70,6 +75,7 @@ def load():
                                    C.POINTER(Summary)]
     lib.mcgpu_dispatch_batch.argtypes = [ctx, C.c_uint32, C.c_uint32, C.POINTER(Mesh), C.POINTER(Mesh),
                                          C.POINTER(C.c_double), C.POINTER(Summary)]
+    lib.mcgpu_dispatch_packed.argtypes = [ctx, C.c_uint32, C.POINTER(Batch), C.POINTER(Summary)]
     lib.mcgpu_get_data.argtypes = [ctx, C.c_uint32, C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64)]
     lib.mcgpu_get_batch_data.argtypes = [ctx, C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p,
                                          C.POINTER(C.c_uint64)]

@@ -319,33 +319,48 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
     return MCGPU_OK;
 }
 
+// a packed batch: the caller's arrays already follow the internal layout
+struct Packed {
+    const void* X;
+    const uint32_t* idx;
+};
+
 // upload ps arrays: coordinates (recentred on the host when asked), indices, offsets
-void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts)
+void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts, const Packed* pk)
 {
     Layout& L = c->L;
     const uint32_t n = L.n_pairs;
     cudaStream_t s = c->s;
-    double* X = c->buf[B_X].get<double>(L.nv * 3);
-    uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
     const bool fin = (flags & MCGPU_VERTEX_ARRAY_FLOAT) != 0;
     const bool dev = (flags & MCGPU_DEVICE_POINTERS) != 0;
-    if (flags & MCGPU_RECENTRE) {
+    // a packed device batch is read in place; everything else is copied
+    const double* X = (pk && dev) ? static_cast<const double*>(pk->X) : c->buf[B_X].get<double>(L.nv * 3);
+    uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
+    if (pk && dev) {
+        // read in place
+    } else if (pk && !(flags & MCGPU_RECENTRE)) {
+        ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
+            "H2D X");
+    } else if (flags & MCGPU_RECENTRE) {
         double* st = c->pin_stage.get<double>(L.nv * 3);
         for (uint32_t p = 0; p < n; ++p)
             recentre_pair(fin, srcs[p], cuts[p], st + (size_t)L.vbase[p] * 3,
                 st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
-        ck(cudaMemcpyAsync(X, st, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s), "H2D X");
+        ck(cudaMemcpyAsync(const_cast<double*>(X), st, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
+            "H2D X");
     } else {
         const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
         for (uint32_t p = 0; p < n; ++p) {
-            ck(cudaMemcpyAsync(X + (size_t)L.vbase[p] * 3, srcs[p].vertices, (size_t)L.vs[p] * 3 * sizeof(double),
-                   kind, s), "H2D Xs");
-            ck(cudaMemcpyAsync(X + ((size_t)L.vbase[p] + L.vs[p]) * 3, cuts[p].vertices,
+            ck(cudaMemcpyAsync(const_cast<double*>(X) + (size_t)L.vbase[p] * 3, srcs[p].vertices,
+                   (size_t)L.vs[p] * 3 * sizeof(double), kind, s), "H2D Xs");
+            ck(cudaMemcpyAsync(const_cast<double*>(X) + ((size_t)L.vbase[p] + L.vs[p]) * 3, cuts[p].vertices,
                    (size_t)cuts[p].num_vertices * 3 * sizeof(double), kind, s), "H2D Xc");
         }
     }
     const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    for (uint32_t p = 0; p < n; ++p) {
+    if (pk)
+        ck(cudaMemcpyAsync(fidx, pk->idx, (size_t)L.nidx * 4, ikind, s), "H2D idx");
+    else for (uint32_t p = 0; p < n; ++p) {
         const uint64_t ic = (uint64_t)(p + 1 < n + 1 ? L.ibase[p + 1] : L.nidx) - L.ibase[p] - L.is[p];
         ck(cudaMemcpyAsync(fidx + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, ikind, s), "H2D Is");
         ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, ikind, s), "H2D Ic");
@@ -415,7 +430,7 @@ inline void rec(mcgpu_context_t* c, int i)
 }
 
 int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts,
-    const double* eps, mcgpu_summary* out)
+    const double* eps, mcgpu_summary* out, const Packed* pk = nullptr)
 {
     if (!c || !srcs || !cuts || n == 0) return fail(MCGPU_INVALID_VALUE, "null argument");
     if (flags & MCGPU_DEVICE_POINTERS && flags & (MCGPU_RECENTRE | MCGPU_VERTEX_ARRAY_FLOAT))
@@ -431,7 +446,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     Layout& L = c->L;
     cudaStream_t s = c->s;
     rec(c, 2 * MCGPU_STAGE_UPLOAD);
-    upload(c, flags, srcs, cuts);
+    upload(c, flags, srcs, cuts, pk);
     rec(c, 2 * MCGPU_STAGE_UPLOAD + 1);
 
     Problem& P = c->P;
@@ -695,6 +710,49 @@ int mcgpu_dispatch_batch(mcgpu_context c, uint32_t flags, uint32_t n_pairs, cons
     }
 }
 
+int mcgpu_dispatch_packed(mcgpu_context c, uint32_t flags, const mcgpu_batch* b, mcgpu_summary* summaries)
+{
+    if (!c || !b || !b->vertices || !b->face_indices || !b->mesh_counts || b->num_pairs == 0)
+        return fail(MCGPU_INVALID_VALUE, "null argument");
+    try {
+        // per-pair views into the packed arrays (host side only: counts are host memory)
+        const uint32_t n = b->num_pairs;
+        std::vector<mcgpu_mesh> ms(n), mc(n);
+        const size_t vsz = (flags & MCGPU_VERTEX_ARRAY_FLOAT) ? 12 : 24;
+        const char* v = static_cast<const char*>(b->vertices);
+        const uint32_t* ix = b->face_indices;
+        const uint32_t* fs = b->face_sizes;
+        for (uint32_t p = 0; p < n; ++p) {
+            const uint32_t* k = b->mesh_counts + 4 * (size_t)p;
+            for (int side = 0; side < 2; ++side) {
+                mcgpu_mesh& m = side ? mc[p] : ms[p];
+                m.num_vertices = k[2 * side];
+                m.num_faces = k[2 * side + 1];
+                m.vertices = v;
+                m.face_indices = ix;
+                m.face_sizes = fs;
+                v += vsz * m.num_vertices;
+                uint64_t ni = 3ull * m.num_faces;
+                if (fs) {
+                    if (flags & MCGPU_DEVICE_POINTERS)
+                        return fail(MCGPU_INVALID_VALUE, "packed device batches hold triangles only");
+                    ni = 0;
+                    for (uint32_t f = 0; f < m.num_faces; ++f) ni += fs[f];
+                    fs += m.num_faces;
+                }
+                ix += ni;
+            }
+        }
+        // the per-mesh views are read one by one only by the host recentring;
+        // build_layout reads counts, the upload copies each packed array once
+        Packed pk { b->vertices, b->face_indices };
+        return run(c, flags, n, ms.data(), mc.data(), b->cut_eps, summaries, &pk);
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
 int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
@@ -747,6 +805,14 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
             return copy_out(c, c->P.X, c->L.nv * 24, bytes, mem, bytes_out);
         case MCGPU_DATA_FACE_BOXES:
             return copy_out(c, W.fbox, c->L.nf * 48, bytes, mem, bytes_out);
+        case MCGPU_DATA_RECORD_OFFSETS: {
+            const uint64_t need = c->rec_begin.size() * 8;
+            if (bytes_out) *bytes_out = need;
+            if (!mem && bytes == 0) return MCGPU_OK;
+            if (!mem || bytes < need) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+            memcpy(mem, c->rec_begin.data(), need);
+            return MCGPU_OK;
+        }
         default:
             return fail(MCGPU_INVALID_VALUE, "unknown query");
         }

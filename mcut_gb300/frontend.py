@@ -139,6 +139,28 @@ class Context:
                         ids, pts))
         return out
 
+    def dispatch_packed(self, packed, recentre: bool = False, device: bool = False, fetch: bool = True,
+                        profile: bool = False):
+        """One pass over a packed batch (see ``pack_pairs``). With ``device``
+        ``packed["v"]`` and ``packed["f"]`` are torch CUDA tensors (counts and
+        eps stay numpy). Returns (summaries
+        [n] structure array, record ids [R,5], points [R,3], offsets [n+1])."""
+        n = int(packed["counts"].shape[0])
+        ptr = (lambda a: a.data_ptr()) if device else (lambda a: a.ctypes.data)
+        eps = packed.get("eps")
+        b = L.Batch(n, ptr(packed["v"]), ptr(packed["f"]), None,
+                    packed["counts"].ctypes.data,
+                    None if (eps is None or recentre) else eps.ctypes.data)
+        sums = (L.Summary * n)()
+        flags = (L.RECENTRE if recentre else 0) | (L.DEVICE_POINTERS if device else 0) | (L.PROFILE if profile else 0)
+        L.check(self._lib.mcgpu_dispatch_packed(self._h, flags, C.byref(b), sums), "mcgpu_dispatch_packed")
+        if not fetch:
+            return sums, None, None, None
+        ids = self._get(L.DATA_RECORD_IDS, np.uint32, 5)
+        pts = self._get(L.DATA_RECORD_POINTS, np.float64, 3)
+        off = self._get(L.DATA_RECORD_OFFSETS, np.uint64, 1).reshape(-1)
+        return sums, ids, pts, off
+
     def _batch_get(self, pair, query, dtype, cols):
         n = C.c_uint64(0)
         L.check(self._lib.mcgpu_get_batch_data(self._h, pair, query, 0, None, C.byref(n)), "get_batch_data")
@@ -147,6 +169,25 @@ class Context:
             L.check(self._lib.mcgpu_get_batch_data(self._h, pair, query, n.value, out.ctypes.data, C.byref(n)),
                     "get_batch_data")
         return out.reshape(-1, cols)
+
+
+def pack_pairs(pairs, recentre_coords: bool = True):
+    """Pack (src, cut) triangle-mesh pairs end to end (the mcgpu_batch
+    layout). With ``recentre_coords`` the coordinates are the reference's
+    internal ones and ``eps`` the per-pair cut-box enlargement."""
+    vs, fs, counts, eps = [], [], [], []
+    for s, c in pairs:
+        assert s.get("fs") is None and c.get("fs") is None, "packed batches here hold triangles"
+        if recentre_coords:
+            sx, cx, e = recentre(s, c)
+        else:
+            sx, cx, e = s["v"], c["v"], 0.0
+        vs += [np.asarray(sx, np.float64).reshape(-1, 3), np.asarray(cx, np.float64).reshape(-1, 3)]
+        fs += [np.asarray(s["f"], np.uint32), np.asarray(c["f"], np.uint32)]
+        counts.append((sx.shape[0], s["f"].shape[0] // 3, cx.shape[0], c["f"].shape[0] // 3))
+        eps.append(e)
+    return dict(v=np.ascontiguousarray(np.concatenate(vs)), f=np.ascontiguousarray(np.concatenate(fs)),
+                counts=np.ascontiguousarray(np.array(counts, np.uint32)), eps=np.array(eps, np.float64))
 
 
 def recentre(src, cut, float_input: bool = False):

@@ -72,3 +72,26 @@ def test_null_arguments_are_errors_not_crashes():
     assert "null" in L.last_error()
     assert lib.mcgpu_context_create(None, 0) == L.INVALID_VALUE
     assert lib.mcgpu_get_data(None, L.DATA_RECORD_IDS, 0, None, None) == L.INVALID_VALUE
+    b = L.Batch(0, None, None, None, None, None)
+    assert lib.mcgpu_dispatch_packed(None, 0, C.byref(b), None) == L.INVALID_VALUE
+
+
+def test_pack_pairs_layout():
+    """The packed batch is the internal layout: per pair source then cut
+    vertices (recentred), source then cut local indices, counts per mesh."""
+    from mcut_gb300 import pack_pairs
+    pairs = meshgen.batch_pairs(5, seed=meshgen.SEED_BASE + 41)
+    pk = pack_pairs(pairs)
+    v0 = f0 = 0
+    for i, (s, c) in enumerate(pairs):
+        sx, cx, eps = recentre(s, c)
+        nsv, nsf, ncv, ncf = (int(x) for x in pk["counts"][i])
+        assert (nsv, ncv) == (s["v"].shape[0], c["v"].shape[0])
+        assert (nsf, ncf) == (meshgen.num_faces(s), meshgen.num_faces(c))
+        assert G.same_bits(pk["v"][v0:v0 + nsv], sx) and G.same_bits(pk["v"][v0 + nsv:v0 + nsv + ncv], cx)
+        assert np.array_equal(pk["f"][f0:f0 + 3 * nsf], s["f"])
+        assert np.array_equal(pk["f"][f0 + 3 * nsf:f0 + 3 * (nsf + ncf)], c["f"])
+        assert G.same_bits(pk["eps"][i], eps)
+        v0 += nsv + ncv
+        f0 += 3 * (nsf + ncf)
+    assert v0 == pk["v"].shape[0] and f0 == pk["f"].shape[0]
