@@ -233,6 +233,12 @@ def run_batch(ctx, lib, steps, world):
     dpk = dict(pk, v=dv, f=df)
     nfaces = int(pk["counts"][:, 1].sum() + pk["counts"][:, 3].sum())
 
+    # the autotuner picks leaf size / traversal / packet size on a 256-pair sample
+    spk = pack_pairs(pairs[:256])
+    spk = dict(spk, v=torch.from_numpy(spk["v"]).cuda(), f=torch.from_numpy(spk["f"]).cuda())
+    tuning, tune_ms = ctx.autotune(spk, device=True, repeats=2)
+    del spk
+
     # batched: one packed pass over all pairs
     launches = 0
     for _ in range(2):
@@ -307,6 +313,168 @@ def run_batch(ctx, lib, steps, world):
         "plain": {"value": world * n / p_s, "unit": UNIT,
                   "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
         "batched_over_plain": (n / (b_ms / 1e3)) / (n / p_s),
+        "autotuned": {"tuning": tuning, "sample_pairs": 256, "sample_ms": tune_ms},
+    }
+
+
+def run_configs(ctx, lib, world, cpu=True):
+    """C1 (the reference's CPU-runnable case: two level-3 icospheres) through
+    the C ABI from host arrays in user coordinates, as mcDispatch receives
+    them, against the CPU restatement; and C3x16 (lattice cube vs a grid
+    coincident with its top face, z nudged by U(-1e-12, 1e-12)): the
+    escalation rates of the orient3d filters."""
+    import torch
+    from mcut_gb300 import meshgen
+    out = {}
+    s, c = meshgen.two_spheres()
+    for _ in range(5):
+        r = ctx.dispatch(s, c)
+    n = 200
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        r = ctx.dispatch(s, c)
+    g = n / (time.perf_counter() - t0)
+    c1 = {"workload": "C1: level-3 icosphere r=1 vs level-3 icosphere r=0.8 at (0.5, 0.3, 0.1), fp64",
+          "gpu_e2e": {"value": world * g, "unit": UNIT, "records": int(r.num_records), "status": r.status_name}}
+    if cpu:
+        for th in (1, os.cpu_count() or 1):
+            ts = cpu_port_run(s, c, 20, 2, th)
+            c1[f"cpu_port_{th}_threads"] = {"value": len(ts) / sum(ts), "unit": UNIT}
+    out["c1"] = c1
+    s, c = meshgen.cube_coplanar(16.0)
+    for _ in range(2):
+        r = ctx.dispatch(s, c, profile=True, fetch=False)
+    st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        st.record()
+        r = ctx.dispatch(s, c, fetch=False)
+        en.record()
+        torch.cuda.synchronize()
+        t.append(st.elapsed_time(en))
+    esc = [int(x) for x in r.escalations]
+    tot = max(1, sum(esc))
+    out["c3"] = {"workload": "C3x16: 512^2-per-face lattice cube (3,145,728 tris) vs 256x256 grid on its top face "
+                             "plane, z + U(-1e-12, 1e-12), x16",
+                 "status": r.status_name, "pairs": int(r.num_pairs), "tests": int(r.num_tests),
+                 "records": int(r.num_records), "ms_per_dispatch": float(np.median(t)),
+                 "escalations": {"fp32_filter": esc[0], "fp64_filter": esc[1], "exact": esc[2],
+                                 "rates": [e / tot for e in esc]}}
+    return out
+
+
+SERVED_WORKLOAD = ("served: open-loop Poisson arrivals; each request one fracture pair with total triangles "
+                   "log-uniform in [1e3, 1e6]; 30% name one of 64 device-resident cut meshes; HBM budget 150 GiB")
+
+
+def make_served(n_pool=256, n_resident=64, n_req=1200):
+    from mcut_gb300 import meshgen
+    rng = np.random.default_rng(meshgen.SEED_BASE + 5)
+    logu = lambda k: np.exp(rng.uniform(np.log(1e3), np.log(1e6), k))  # noqa: E731
+    pool = [meshgen.crack_pair(rng, target_tris=int(t)) for t in logu(n_pool)]
+    resident = [meshgen.crack_pair(rng, target_tris=int(t))[1] for t in logu(n_resident)]
+    trace = []
+    for _ in range(n_req):
+        i = int(rng.integers(n_pool))
+        trace.append((i, int(rng.integers(n_resident)) if rng.random() < 0.3 else None))
+    return pool, resident, trace
+
+
+def run_served(ctx, world):
+    """Plain per-dispatch path vs the request server on the same request
+    trace: closed loop (all queued) for throughput, then Poisson arrivals at
+    fractions of that rate for p50/p99 latency (submission -> records on the
+    host)."""
+    import threading
+    from mcut_gb300 import Server
+
+    pool, resident, trace = make_served()
+    srv = Server(0, hbm_budget_bytes=150 << 30)
+    cids = [srv.add_cut(c) for c in resident]
+
+    def pair_of(i, r):
+        return pool[i][0], (resident[r] if r is not None else pool[i][1])
+
+    # plain: one mcgpu_dispatch per request from host arrays (recentred as
+    # mcDispatch does), records read back
+    n_plain = 300
+    for i, r in trace[:8]:
+        ctx.dispatch(*pair_of(i, r))
+    lat_p = []
+    t0 = time.perf_counter()
+    for i, r in trace[:n_plain]:
+        a = time.perf_counter()
+        ctx.dispatch(*pair_of(i, r))
+        lat_p.append(1e3 * (time.perf_counter() - a))
+    plain = n_plain / (time.perf_counter() - t0)
+
+    def submit(i, r):
+        s_, c_ = pool[i][0], pool[i][1]
+        return srv.submit(s_, cut_id=cids[r]) if r is not None else srv.submit(s_, c_)
+
+    def closed(n):
+        t0 = time.perf_counter()
+        ts = [submit(i, r) for i, r in trace[:n]]
+        lat = []
+        for t in ts:
+            lat.append(srv.wait(t)[1])
+            srv.release(t)
+        return n / (time.perf_counter() - t0), lat
+
+    closed(64)  # warm the worker pools
+    sat, lat_c = closed(len(trace))
+
+    def open_loop(rate, n):
+        rng = np.random.default_rng(7)
+        gaps = rng.exponential(1.0 / rate, n)
+        ts, lat = [], []
+        done = threading.Event()
+
+        def waiter():
+            k = 0
+            while k < n:
+                while k >= len(ts):
+                    time.sleep(0.0002)
+                lat.append(srv.wait(ts[k])[1])
+                srv.release(ts[k])
+                k += 1
+            done.set()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        nxt = t0
+        for k in range(n):
+            nxt += gaps[k]
+            while time.perf_counter() < nxt:
+                time.sleep(min(0.0005, max(0.0, nxt - time.perf_counter())))
+            i, r = trace[k % len(trace)]
+            ts.append(submit(i, r))
+        done.wait()
+        th.join()
+        el = time.perf_counter() - t0
+        return {"rate_per_s": rate, "requests": n, "throughput": n / el,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+
+    sweep = []
+    for frac in (0.25, 0.5, 0.8):
+        rate = frac * sat
+        sweep.append(open_loop(rate, int(min(len(trace), max(200, rate * 1.5)))))
+    st = srv.stats()
+    srv.close()
+    return {
+        "workload": SERVED_WORKLOAD, "requests": len(trace), "resident_cut_meshes": len(resident),
+        "plain": {"value": world * plain, "unit": UNIT, "requests": n_plain,
+                  "latency_ms": {"p50": float(np.percentile(lat_p, 50)), "p99": float(np.percentile(lat_p, 99))}},
+        "served_saturated": {"value": world * sat, "unit": UNIT,
+                             "latency_ms": {"p50": float(np.percentile(lat_c, 50)),
+                                            "p99": float(np.percentile(lat_c, 99))}},
+        "served_over_plain": sat / plain,
+        "open_loop": sweep,
+        "server": {"workers": 3, "batches": st["batches"], "peak_inflight_bytes": st["peak_inflight_bytes"],
+                   "resident_bytes": st["resident_bytes"]},
     }
 
 
@@ -333,16 +501,28 @@ def run_gpu(args, world, rank, local):
     mc = L.Mesh(d_cx.data_ptr(), d_fc.data_ptr(), None, cx.shape[0], fc_.shape[0] // 3)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     sm = L.Summary()
-    flags = L.DEVICE_POINTERS | L.PROFILE
 
-    def step_dev():
+    def step_dev(flags=L.DEVICE_POINTERS):
         L.check(lib.mcgpu_dispatch(ctx._h, flags, C.byref(ms), C.byref(mc), eps, C.byref(sm)), "dispatch")
+
+    # stage times: CUDA events on the context stream around each stage's
+    # launches (direct launches; the timed loop below replays launch graphs)
+    stage_acc = {k: 0.0 for k in L.STAGES}
+    n_prof = max(3, min(args.steps, 10))
+    for _ in range(2):
+        step_dev(L.DEVICE_POINTERS | L.PROFILE)
+    for _ in range(n_prof):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step_dev(L.DEVICE_POINTERS | L.PROFILE)
+        for k, v in zip(L.STAGES, sm.stage_ms):
+            stage_acc[k] += v / n_prof
 
     for _ in range(max(args.warmup, 3)):
         step_dev()
     torch.cuda.synchronize()
     barrier(world)
-    times, stage_acc, launches = [], {k: 0.0 for k in L.STAGES}, 0
+    times, launches = [], 0
     st, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -353,8 +533,6 @@ def run_gpu(args, world, rank, local):
             en.record()
             torch.cuda.synchronize()
             times.append(st.elapsed_time(en))
-            for k, v in zip(L.STAGES, sm.stage_ms):
-                stage_acc[k] += v
             launches += sm.kernel_launches
     barrier(world)
     tot_ms = reduce_max(sum(times), world)
@@ -387,6 +565,8 @@ def run_gpu(args, world, rank, local):
         e2e_t.append(time.perf_counter() - t0)
     e2e_tot = reduce_max(sum(e2e_t), world)
     batch = None if args.no_batch else run_batch(ctx, lib, 3, world)
+    served = None if args.no_batch else run_served(ctx, world)
+    configs = None if args.no_batch else run_configs(ctx, lib, world, cpu=not args.no_cpu_baseline)
     e2e_value = world * args.steps / e2e_tot
     h2d = sx.nbytes + cx.nbytes + fs_.nbytes + fc_.nbytes
     d2h = int(sm.num_records) * (20 + 24)
@@ -395,7 +575,7 @@ def run_gpu(args, world, rank, local):
         return
     # roofline of the dominant stage
     hbm, src_peak = peaks()
-    per = {k: v / args.steps for k, v in stage_acc.items()}
+    per = dict(stage_acc)
     comp = {k: per[k] for k in ("bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow")}
     dom = max(comp, key=comp.get)
     Fs, Fc = fs_.shape[0] // 3, fc_.shape[0] // 3
@@ -444,6 +624,8 @@ def run_gpu(args, world, rank, local):
         "clocks": clk.summary(),
         "gpu_launches": int(launches),
         "batch": batch,
+        "served": served,
+        "configs": configs,
     }
     print(json.dumps(line), flush=True)
 
@@ -455,7 +637,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batch", action="store_true", help="skip the 4096-pair batched vs plain measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched (4096 pairs) and served (request stream) measurements")
     ap.add_argument("--single", action="store_true",
                     help="one warm-up dispatch + one dispatch of the workload, nothing else (for ncu captures)")
     args = ap.parse_args()

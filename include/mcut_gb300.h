@@ -56,7 +56,8 @@ typedef enum mcgpu_status {
     MCGPU_CUDA_ERROR = 5,
     MCGPU_OUT_OF_MEMORY = 6,
     MCGPU_INVALID_VALUE = 7,       /* bad argument (null pointer, unknown query, ...) */
-    MCGPU_TOO_LARGE = 8            /* exceeds a fixed capacity of the entry point */
+    MCGPU_TOO_LARGE = 8,           /* exceeds a fixed capacity of the entry point */
+    MCGPU_NOT_READY = 9            /* a served request has not completed yet */
 } mcgpu_status;
 
 /* dispatch flags */
@@ -174,6 +175,30 @@ typedef struct mcgpu_batch {
  * with mcgpu_get_batch_data. */
 int mcgpu_dispatch_packed(mcgpu_context ctx, uint32_t flags, const mcgpu_batch* batch, mcgpu_summary* summaries);
 
+/* Launch tuning of a context. No setting changes any result (the pair set,
+ * tests and records are independent of the tree's shape and of the
+ * traversal order), only the speed. */
+typedef struct mcgpu_tuning {
+    uint32_t leaf_size;    /* cut faces per tree leaf, 1..16 (default 4) */
+    uint32_t traversal;    /* 0: one warp per source packet, breadth-first (default);
+                              1: one warp per source packet, depth-first;
+                              2: one thread per source face */
+    uint32_t packet_faces; /* source faces per packet = queries per warp, 1..32 (default 32) */
+    uint32_t stack_depth;  /* per-thread stack of traversal 2: 64 (default) or 512 */
+} mcgpu_tuning;
+
+int mcgpu_context_set_tuning(mcgpu_context ctx, const mcgpu_tuning* tuning);
+int mcgpu_context_get_tuning(mcgpu_context ctx, mcgpu_tuning* tuning);
+
+/* Autotuner: runs `sample` (a packed batch, as mcgpu_dispatch_packed with
+ * `flags`) under each candidate tuning -- leaf size {2, 4, 8} x {warp per
+ * packet of 16 or 32 faces breadth-first, warp per packet depth-first,
+ * thread per face with stack 64 or 512} -- `repeats` times each after one
+ * warm-up, keeps the fastest on ctx and returns it with its mean time.
+ * No counterpart in the reference. */
+int mcgpu_autotune(mcgpu_context ctx, uint32_t flags, const mcgpu_batch* sample, uint32_t repeats,
+    mcgpu_tuning* best, float* best_ms);
+
 /* The reference's recentring on the host (calculate_vertex_parameters +
  * client_input_arrays_to_hmesh, preproc.cpp:2124-2290, 147-181): writes the
  * internal coordinates of both meshes and the default cut-box enlargement
@@ -202,6 +227,58 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
  * end's outcome is out->status. */
 int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
     uint32_t* record_ids, double* record_points, uint64_t record_capacity, mcgpu_summary* out);
+
+/* ---- Request server: continuous batching on one GPU ------------------------
+ * Replaces MCUT's per-context task queue for the front end (mcEnqueueDispatch,
+ * mcut.cpp:459-552; frontend.h:548-580) when many independent dispatches
+ * arrive over time. `workers` threads each own a context (stream + device
+ * pool); a free worker takes the queued requests that fit its batch limits
+ * and the HBM admission budget, runs them as one batched dispatch, and
+ * completes them. Requests arriving meanwhile join the next batch, and the
+ * workers' batches overlap on the device. Meshes are user coordinates
+ * (double) and are recentred as mcDispatch does; like mcEnqueueDispatch,
+ * the caller's arrays must stay valid until the request completes
+ * (frontend.cpp:690-711). Cut meshes added with mcgpu_server_add_cut_mesh
+ * stay resident on the device: a request naming one uploads only its
+ * source mesh. Admission: the estimated device bytes of the requests in
+ * flight plus the resident meshes stay within hbm_budget_bytes (a request
+ * that alone exceeds it returns MCGPU_TOO_LARGE; one request on an idle
+ * device is always admitted). */
+typedef struct mcgpu_server_t* mcgpu_server;
+
+typedef struct mcgpu_server_config {
+    int device;
+    uint32_t workers;          /* batches in flight at once; 0 -> 3 */
+    uint32_t max_batch_pairs;  /* requests per batch; 0 -> 512 */
+    uint64_t max_batch_faces;  /* faces per batch (a larger request runs alone); 0 -> 16 Mi */
+    uint64_t hbm_budget_bytes; /* 0 -> 150 GiB */
+    uint32_t linger_us;        /* while other batches run, a short queue waits up to this long for
+                                  more requests; 0 -> 400, > 1e6 -> never wait */
+    uint32_t reserved;
+} mcgpu_server_config;
+
+typedef struct mcgpu_server_stats {
+    uint64_t submitted, completed, batches, pending;
+    uint64_t inflight_bytes, peak_inflight_bytes, resident_bytes, resident_meshes;
+} mcgpu_server_stats;
+
+int mcgpu_server_create(mcgpu_server* server, const mcgpu_server_config* config);
+/* Completes every queued request, then frees the server. */
+int mcgpu_server_release(mcgpu_server server);
+/* Keep a triangle cut mesh (double user coordinates) on the device. */
+int mcgpu_server_add_cut_mesh(mcgpu_server server, const mcgpu_mesh* cut, uint32_t* cut_id);
+/* Queue one request: `cut`, or NULL and a resident `cut_id`. */
+int mcgpu_server_submit(mcgpu_server server, const mcgpu_mesh* src, const mcgpu_mesh* cut, uint32_t cut_id,
+    uint64_t* ticket);
+/* Wait for a request (timeout_ms < 0: no limit; MCGPU_NOT_READY on timeout).
+ * latency_ms: submission to records on the host. */
+int mcgpu_server_wait(mcgpu_server server, uint64_t ticket, int timeout_ms, mcgpu_summary* out,
+    double* latency_ms);
+/* MCGPU_DATA_RECORD_IDS / _POINTS of a completed request (two-call size pattern). */
+int mcgpu_server_get_data(mcgpu_server server, uint64_t ticket, uint32_t query, uint64_t bytes, void* mem,
+    uint64_t* bytes_out);
+int mcgpu_server_release_request(mcgpu_server server, uint64_t ticket);
+int mcgpu_server_get_stats(mcgpu_server server, mcgpu_server_stats* out);
 
 /* Human-readable description of the last failure on this thread. */
 const char* mcgpu_last_error(void);

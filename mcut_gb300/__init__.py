@@ -5,4 +5,4 @@ product; this package is its Python host side: ctypes bindings
 (``_lib``), the front-end mirror of the reference seam (``frontend``),
 seeded synthetic workloads (``meshgen``) and the in-tree build (``build``).
 """
-from .frontend import Context, FrontEndResult, pack_pairs, recentre  # noqa: F401
+from .frontend import Context, FrontEndResult, Server, pack_pairs, recentre  # noqa: F401

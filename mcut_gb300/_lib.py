@@ -14,9 +14,10 @@ LIB_PATH = os.path.join(HERE, "libmcut_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "mcut_gb300.h")
 
 OK, GP_VIOLATION, DEGENERATE_SRC_FACE, DEGENERATE_CUT_FACE, INVALID_INPUT, CUDA_ERROR, OUT_OF_MEMORY, \
-    INVALID_VALUE, TOO_LARGE = range(9)
+    INVALID_VALUE, TOO_LARGE, NOT_READY = range(10)
 STATUS_NAMES = ["OK", "GP_VIOLATION", "DEGENERATE_SRC_FACE", "DEGENERATE_CUT_FACE", "INVALID_INPUT",
-                "CUDA_ERROR", "OUT_OF_MEMORY", "INVALID_VALUE", "TOO_LARGE"]
+                "CUDA_ERROR", "OUT_OF_MEMORY", "INVALID_VALUE", "TOO_LARGE", "NOT_READY"]
+NO_CUT = 0xFFFFFFFF
 
 VERTEX_ARRAY_FLOAT = 1 << 0
 RECENTRE = 1 << 1
@@ -46,6 +47,22 @@ class Summary(C.Structure):
                 ("num_pairs", C.c_uint64), ("num_tests", C.c_uint64), ("num_records", C.c_uint64),
                 ("escalations", C.c_uint64 * 3), ("stage_ms", C.c_float * 8),
                 ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("leaf_size", C.c_uint32), ("traversal", C.c_uint32), ("packet_faces", C.c_uint32),
+                ("stack_depth", C.c_uint32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("workers", C.c_uint32), ("max_batch_pairs", C.c_uint32),
+                ("max_batch_faces", C.c_uint64), ("hbm_budget_bytes", C.c_uint64), ("linger_us", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "batches", "pending", "inflight_bytes",
+                                          "peak_inflight_bytes", "resident_bytes", "resident_meshes")]
 
 
 class LibraryNotBuilt(RuntimeError):
@@ -83,6 +100,19 @@ def load():
                                    C.POINTER(C.c_double)]
     lib.mcgpu_dispatch_noalloc.argtypes = [C.c_void_p, C.POINTER(Mesh), C.POINTER(Mesh), C.c_double, C.c_void_p,
                                            C.c_void_p, C.c_uint64, C.POINTER(Summary)]
+    lib.mcgpu_context_set_tuning.argtypes = [ctx, C.POINTER(Tuning)]
+    lib.mcgpu_context_get_tuning.argtypes = [ctx, C.POINTER(Tuning)]
+    lib.mcgpu_autotune.argtypes = [ctx, C.c_uint32, C.POINTER(Batch), C.c_uint32, C.POINTER(Tuning),
+                                   C.POINTER(C.c_float)]
+    srv = C.c_void_p
+    lib.mcgpu_server_create.argtypes = [C.POINTER(srv), C.POINTER(ServerConfig)]
+    lib.mcgpu_server_release.argtypes = [srv]
+    lib.mcgpu_server_add_cut_mesh.argtypes = [srv, C.POINTER(Mesh), C.POINTER(C.c_uint32)]
+    lib.mcgpu_server_submit.argtypes = [srv, C.POINTER(Mesh), C.POINTER(Mesh), C.c_uint32, C.POINTER(C.c_uint64)]
+    lib.mcgpu_server_wait.argtypes = [srv, C.c_uint64, C.c_int, C.POINTER(Summary), C.POINTER(C.c_double)]
+    lib.mcgpu_server_get_data.argtypes = [srv, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.mcgpu_server_release_request.argtypes = [srv, C.c_uint64]
+    lib.mcgpu_server_get_stats.argtypes = [srv, C.POINTER(ServerStats)]
     lib.mcgpu_last_error.restype = C.c_char_p
     for name in exported_names_in_header():
         if name not in ("mcgpu_last_error",):

@@ -6,10 +6,14 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <atomic>
+#include <chrono>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fe_common.cuh"
+#include "fe_host.h"
 #include "fe_kernels.cuh"
 #include "fe_sort.cuh"
 #include "mcut_gb300.h"
@@ -111,7 +115,7 @@ struct mcgpu_context_t {
     cudaStream_t s = nullptr;
     cudaEvent_t ev[16] = {};  // begin / end of each stage (MCGPU_PROFILE)
     DevBuf buf[B_COUNT];
-    PinBuf pin_counters, pin_tab, pin_stage;
+    PinBuf pin_counters, pin_tab, pin_stage, pin_idx;
     Layout L;
     mcgpu::Problem P {};
     mcgpu::Work W {};
@@ -120,7 +124,15 @@ struct mcgpu_context_t {
     uint64_t n_pairs_found = 0, n_tests = 0, n_records = 0;
     uint32_t flags = 0;
     int rec_buf = 0;
-    uint32_t leaf_size = 4;   // cut faces per tree leaf (MCGPU_LEAF_SIZE overrides, 1..16)
+    mcgpu_tuning tune { 4, 0, 32, 64 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL override at creation
+    bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
+    struct Graph {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec = nullptr;
+        int seen = 0;
+        unsigned long long launches = 0;
+        int aux[2] = { 0, 0 };
+    } graphs[3];
 };
 
 namespace {
@@ -174,39 +186,78 @@ double hdot(const double* a, const double* b)
     return o;
 }
 
-void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out)
+} // namespace
+
+namespace mcgpu {
+
+void mesh_stats(const void* v, bool fin, uint32_t n, MeshStats& st) { vertex_bounds(v, fin, n, st.mn, st.mx, st.com); }
+
+// the pair's frame: com of the two centroids, t = (com - gmin) + its unit
+// vector (preproc.cpp:2124-2290)
+void pair_frame(const MeshStats& S, const MeshStats& Cm, double* com, double* t)
 {
-    double smn[3], smx[3], scom[3], cmn[3], cmx[3], ccom[3], com[3], gmn[3], tp[3], t[3];
-    vertex_bounds(S.vertices, fin, S.num_vertices, smn, smx, scom);
-    vertex_bounds(Cm.vertices, fin, Cm.num_vertices, cmn, cmx, ccom);
+    double tp[3];
     for (int j = 0; j < 3; ++j) {
-        com[j] = (scom[j] + ccom[j]) / 2.0;
-        gmn[j] = dminr(smn[j], cmn[j]);
-        tp[j] = com[j] - gmn[j];
+        com[j] = (S.com[j] + Cm.com[j]) / 2.0;
+        tp[j] = com[j] - dminr(S.mn[j], Cm.mn[j]);
     }
     const double len = std::sqrt(hdot(tp, tp));
     for (int j = 0; j < 3; ++j) t[j] = tp[j] + tp[j] / len;
-    auto conv = [&](const mcgpu_mesh& m, double* out) {
-        if (fin) {
-            const float* p = (const float*)m.vertices;
-            for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
-                const int j = (int)(k % 3);
-                const float x = (p[k] - (float)com[j]) + (float)t[j];
-                out[k] = (double)x;
-            }
-        } else {
-            const double* p = (const double*)m.vertices;
-            for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
-                const int j = (int)(k % 3);
-                out[k] = (p[k] - com[j]) + t[j];
-            }
+}
+
+// x' = (x - com) + t per coordinate (preproc.cpp:147-181)
+void apply_frame(bool fin, const mcgpu_mesh& m, const double* com, const double* t, double* out)
+{
+    if (fin) {
+        const float* p = (const float*)m.vertices;
+        for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
+            const int j = (int)(k % 3);
+            const float x = (p[k] - (float)com[j]) + (float)t[j];
+            out[k] = (double)x;
         }
-    };
-    conv(S, sx);
-    conv(Cm, cx);
+    } else {
+        const double* p = (const double*)m.vertices;
+        for (size_t k = 0; k < (size_t)m.num_vertices * 3; ++k) {
+            const int j = (int)(k % 3);
+            out[k] = (p[k] - com[j]) + t[j];
+        }
+    }
+}
+
+// |translated cut box diagonal| * 1e-4 (preproc.cpp:2518, 2667-2676)
+double frame_eps(const MeshStats& Cm, const double* t)
+{
     double d[3];
-    for (int j = 0; j < 3; ++j) d[j] = (cmx[j] + t[j]) - (cmn[j] + t[j]);
-    *eps_out = std::sqrt(hdot(d, d)) * 1e-4;
+    for (int j = 0; j < 3; ++j) d[j] = (Cm.mx[j] + t[j]) - (Cm.mn[j] + t[j]);
+    return std::sqrt(hdot(d, d)) * 1e-4;
+}
+
+} // namespace mcgpu
+
+namespace {
+
+void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out)
+{
+    MeshStats ss, cs;
+    mesh_stats(S.vertices, fin, S.num_vertices, ss);
+    mesh_stats(Cm.vertices, fin, Cm.num_vertices, cs);
+    double com[3], t[3];
+    pair_frame(ss, cs, com, t);
+    apply_frame(fin, S, com, t, sx);
+    apply_frame(fin, Cm, com, t, cx);
+    *eps_out = frame_eps(cs, t);
+}
+
+// resident cut mesh: its stored user coordinates mapped into the pair's frame
+__global__ void k_apply_frame(const double* __restrict__ in, double* __restrict__ out, uint64_t n3, double c0,
+    double c1, double c2, double t0, double t1, double t2)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n3; k += (uint64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(k % 3);
+        const double c = j == 0 ? c0 : (j == 1 ? c1 : c2);
+        const double t = j == 0 ? t0 : (j == 1 ? t1 : t2);
+        out[k] = __dadd_rn(__dsub_rn(in[k], c), t);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -267,7 +318,7 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
     L.vbase.resize(n + 1); L.vs.resize(n + 1); L.fbase.resize(n + 1); L.fs.resize(n + 1);
     L.sbase.resize(n + 1); L.cbase.resize(n + 1); L.ibase.resize(n + 1); L.is.resize(n + 1);
     L.clbase.resize(n + 1);
-    L.leaf_size = c->leaf_size;
+    L.leaf_size = c->tune.leaf_size;
     uint64_t cl = 0;
     L.eps.assign(n, 0.0);
     uint64_t v = 0, f = 0, sf = 0, cf = 0, ix = 0;
@@ -319,6 +370,26 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
     return MCGPU_OK;
 }
 
+// body(p) for p in [0, n) on up to `threads` host threads (dynamic, one pair at a time)
+template <typename F>
+void parallel_pairs(uint32_t n, uint64_t work, F body)
+{
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned want = (unsigned)std::min<uint64_t>({ (uint64_t)std::min(hw / 2u, 8u), n, work / 100000 + 1 });
+    if (want <= 1) {
+        for (uint32_t p = 0; p < n; ++p) body(p);
+        return;
+    }
+    std::atomic<uint32_t> next { 0 };
+    auto loop = [&] {
+        for (uint32_t p; (p = next.fetch_add(1)) < n;) body(p);
+    };
+    std::vector<std::thread> ts;
+    for (unsigned k = 1; k < want; ++k) ts.emplace_back(loop);
+    loop();
+    for (auto& t : ts) t.join();
+}
+
 // a packed batch: the caller's arrays already follow the internal layout
 struct Packed {
     const void* X;
@@ -326,7 +397,8 @@ struct Packed {
 };
 
 // upload ps arrays: coordinates (recentred on the host when asked), indices, offsets
-void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts, const Packed* pk)
+void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts, const Packed* pk,
+    const ResidentCut* const* res)
 {
     Layout& L = c->L;
     const uint32_t n = L.n_pairs;
@@ -342,12 +414,43 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
             "H2D X");
     } else if (flags & MCGPU_RECENTRE) {
+        // host recentring (and the index copy into one pinned stage) in
+        // parallel over the pairs; one H2D copy per array
         double* st = c->pin_stage.get<double>(L.nv * 3);
-        for (uint32_t p = 0; p < n; ++p)
-            recentre_pair(fin, srcs[p], cuts[p], st + (size_t)L.vbase[p] * 3,
-                st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
+        uint32_t* ist = dev ? nullptr : c->pin_idx.get<uint32_t>(L.nidx);
+        struct Job { double com[3], t[3]; };
+        std::vector<Job> jobs(res ? n : 0);
+        parallel_pairs(n, L.nv + L.nidx, [&](uint32_t p) {
+            double* sx = st + (size_t)L.vbase[p] * 3;
+            if (res && res[p]) {
+                // resident cut: only the source is mapped on the host
+                Job& j = jobs[p];
+                MeshStats ss;
+                mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
+                pair_frame(ss, res[p]->st, j.com, j.t);
+                apply_frame(fin, srcs[p], j.com, j.t, sx);
+                L.eps[p] = frame_eps(res[p]->st, j.t);
+            } else {
+                recentre_pair(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
+            }
+            if (ist) {
+                const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
+                memcpy(ist + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4);
+                if (!(res && res[p])) memcpy(ist + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4);
+            }
+        });
         ck(cudaMemcpyAsync(const_cast<double*>(X), st, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
             "H2D X");
+        if (ist) ck(cudaMemcpyAsync(fidx, ist, (size_t)L.nidx * 4, cudaMemcpyHostToDevice, s), "H2D idx");
+        for (uint32_t p = 0; res && p < n; ++p) {
+            if (!res[p]) continue;
+            const Job& j = jobs[p];
+            const ResidentCut& r = *res[p];
+            const uint64_t n3 = 3ull * r.nv;
+            g_launches++;
+            k_apply_frame<<<grid1(n3), 256, 0, s>>>(r.X, const_cast<double*>(X) + ((size_t)L.vbase[p] + L.vs[p]) * 3,
+                n3, j.com[0], j.com[1], j.com[2], j.t[0], j.t[1], j.t[2]);
+        }
     } else {
         const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
         for (uint32_t p = 0; p < n; ++p) {
@@ -358,12 +461,19 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         }
     }
     const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    if (pk)
+    const bool staged = (flags & MCGPU_RECENTRE) != 0; // indices went up with the recentred coordinates
+    if (pk && !staged)
         ck(cudaMemcpyAsync(fidx, pk->idx, (size_t)L.nidx * 4, ikind, s), "H2D idx");
     else for (uint32_t p = 0; p < n; ++p) {
-        const uint64_t ic = (uint64_t)(p + 1 < n + 1 ? L.ibase[p + 1] : L.nidx) - L.ibase[p] - L.is[p];
-        ck(cudaMemcpyAsync(fidx + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, ikind, s), "H2D Is");
-        ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, ikind, s), "H2D Ic");
+        const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
+        if (!staged)
+            ck(cudaMemcpyAsync(fidx + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, ikind, s), "H2D Is");
+        if (res && res[p])
+            ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], res[p]->idx, (size_t)ic * 4, cudaMemcpyDeviceToDevice, s),
+                "D2D Ic");
+        else if (!staged)
+            ck(cudaMemcpyAsync(fidx + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, ikind, s),
+                "H2D Ic");
     }
     // per pair tables: ibase, is, vbase, vs, fbase, fs, sbase, cbase, clbase (n+1 each), eps
     constexpr int kRows = 9;
@@ -429,8 +539,62 @@ inline void rec(mcgpu_context_t* c, int i)
     if (c->flags & MCGPU_PROFILE) ck(cudaEventRecord(c->ev[i], c->s), "event");
 }
 
+// Key of a launch segment: every value its launches read on the host.
+template <typename... T>
+std::vector<unsigned char> seg_key(const T&... v)
+{
+    std::vector<unsigned char> k;
+    auto add = [&](const auto& x) {
+        const unsigned char* b = reinterpret_cast<const unsigned char*>(&x);
+        k.insert(k.end(), b, b + sizeof(x));
+    };
+    (add(v), ...);
+    return k;
+}
+
+// Runs a launch segment. Without MCGPU_PROFILE: the first time a key is seen its launches run
+// directly; the second time they are captured into a CUDA graph (thread-local
+// capture: other threads' allocations are unaffected); after that the graph
+// is replayed. A key holds the Problem/Work values and sizes the launches
+// embed, so a replay sees the same buffers, sizes and parameters.
+template <typename F>
+void run_segment(mcgpu_context_t* c, int i, const std::vector<unsigned char>& key, F launches)
+{
+    auto& G = c->graphs[i];
+    // stage events (MCGPU_PROFILE) are timed only on direct launches
+    if (!c->use_graphs || (c->flags & MCGPU_PROFILE)) {
+        launches(G.aux);
+        return;
+    }
+    if (G.exec && G.key == key) {
+        g_launches += G.launches;
+        ck(cudaGraphLaunch(G.exec, c->s), "cudaGraphLaunch");
+        return;
+    }
+    if (G.key != key) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+        G.key = key;
+        G.seen = 0;
+    }
+    if (++G.seen < 2) {
+        launches(G.aux);
+        return;
+    }
+    ck(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    const unsigned long long l0 = g_launches;
+    launches(G.aux);
+    cudaGraph_t graph = nullptr;
+    ck(cudaStreamEndCapture(c->s, &graph), "cudaStreamEndCapture");
+    G.launches = g_launches - l0;
+    const cudaError_t e = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    ck(e, "cudaGraphInstantiate");
+    ck(cudaGraphLaunch(G.exec, c->s), "cudaGraphLaunch");
+}
+
 int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts,
-    const double* eps, mcgpu_summary* out, const Packed* pk = nullptr)
+    const double* eps, mcgpu_summary* out, const Packed* pk = nullptr, const ResidentCut* const* res = nullptr)
 {
     if (!c || !srcs || !cuts || n == 0) return fail(MCGPU_INVALID_VALUE, "null argument");
     if (flags & MCGPU_DEVICE_POINTERS && flags & (MCGPU_RECENTRE | MCGPU_VERTEX_ARRAY_FLOAT))
@@ -446,7 +610,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     Layout& L = c->L;
     cudaStream_t s = c->s;
     rec(c, 2 * MCGPU_STAGE_UPLOAD);
-    upload(c, flags, srcs, cuts, pk);
+    upload(c, flags, srcs, cuts, pk, res);
     rec(c, 2 * MCGPU_STAGE_UPLOAD + 1);
 
     Problem& P = c->P;
@@ -484,30 +648,37 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
 
-    // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
-    rec(c, 2 * MCGPU_STAGE_BOUNDS);
-    g_launches++;
-    k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
-    ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
-    ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
-    ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
-    ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
-    ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
-
-    launch_bounds_morton(P, W, wide, s);
-    rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
     W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(radix_sort_temp_bytes((uint32_t)std::max(L.ns, L.nc)) / 4 + 64);
-    int cut_buf = 0;
-    rec(c, 2 * MCGPU_STAGE_SORT);
-    const int src_buf = launch_sort(P, W, wide, key_bits, s, cut_buf);
-    rec(c, 2 * MCGPU_STAGE_SORT + 1);
-    rec(c, 2 * MCGPU_STAGE_HIERARCHY);
-    launch_hierarchy(P, W, wide, cut_buf, s);
-    launch_packets(P, W, src_buf, s);
-    rec(c, 2 * MCGPU_STAGE_HIERARCHY + 1);
-    rec(c, 2 * MCGPU_STAGE_TRAVERSE);
-    launch_traverse(P, W, src_buf, cut_buf, false, s);
-    rec(c, 2 * MCGPU_STAGE_TRAVERSE + 1);
+    W.traversal = c->tune.traversal;
+    W.packet_faces = c->tune.packet_faces;
+    W.stack_depth = c->tune.stack_depth;
+    const uint32_t prof = flags & MCGPU_PROFILE;
+    int src_buf = 0, cut_buf = 0;
+    run_segment(c, 0, seg_key(P, W, n, key_bits, prof), [&](int* aux) {
+        // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
+        rec(c, 2 * MCGPU_STAGE_BOUNDS);
+        g_launches++;
+        k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
+        ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
+        ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
+        ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+        ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
+        ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
+        launch_bounds_morton(P, W, wide, s);
+        rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
+        rec(c, 2 * MCGPU_STAGE_SORT);
+        aux[0] = launch_sort(P, W, wide, key_bits, s, aux[1]);
+        rec(c, 2 * MCGPU_STAGE_SORT + 1);
+        rec(c, 2 * MCGPU_STAGE_HIERARCHY);
+        launch_hierarchy(P, W, wide, aux[1], s);
+        launch_packets(P, W, aux[0], s);
+        rec(c, 2 * MCGPU_STAGE_HIERARCHY + 1);
+        rec(c, 2 * MCGPU_STAGE_TRAVERSE);
+        launch_traverse(P, W, aux[0], aux[1], false, s);
+        rec(c, 2 * MCGPU_STAGE_TRAVERSE + 1);
+    });
+    src_buf = c->graphs[0].aux[0];
+    cut_buf = c->graphs[0].aux[1];
 
     // readback 1: pair count and traversal flags
     uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
@@ -561,14 +732,17 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
     W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
         radix_sort_temp_bytes((uint32_t)std::max<uint64_t>({ L.ns, L.nc, W.test_cap })) / 4 + 64);
-    rec(c, 2 * MCGPU_STAGE_ADJACENCY);
-    ck(cudaMemsetAsync(W.vneed, 0, L.nv, s), "memset");
-    launch_adjacency_planes(P, W, s);
-    rec(c, 2 * MCGPU_STAGE_ADJACENCY + 1);
-    rec(c, 2 * MCGPU_STAGE_NARROW);
-    launch_tests(P, W, s);
-    launch_narrow(P, W, (flags & MCGPU_KEEP_TESTS) != 0, s);
-    rec(c, 2 * MCGPU_STAGE_NARROW + 1);
+    const uint32_t keep = flags & MCGPU_KEEP_TESTS;
+    run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) {
+        rec(c, 2 * MCGPU_STAGE_ADJACENCY);
+        ck(cudaMemsetAsync(W.vneed, 0, L.nv, s), "memset");
+        launch_adjacency_planes(P, W, s);
+        rec(c, 2 * MCGPU_STAGE_ADJACENCY + 1);
+        rec(c, 2 * MCGPU_STAGE_NARROW);
+        launch_tests(P, W, s);
+        launch_narrow(P, W, keep != 0, s);
+        rec(c, 2 * MCGPU_STAGE_NARROW + 1);
+    });
 
     // readback 2: counters, per-pair status / degenerate face / record count
     ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
@@ -579,9 +753,13 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->n_records = hc[2];
     W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
     W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
-    rec(c, 2 * MCGPU_STAGE_DOWNLOAD);  // record sort + gather (added to the narrow stage)
-    c->rec_buf = launch_records(P, W, (uint32_t)c->n_records, s);
-    rec(c, 2 * MCGPU_STAGE_DOWNLOAD + 1);
+    const uint32_t nrec = (uint32_t)c->n_records;
+    run_segment(c, 2, seg_key(P, W, n, nrec, prof), [&](int* aux) {
+        rec(c, 2 * MCGPU_STAGE_DOWNLOAD); // record sort + gather (added to the narrow stage)
+        aux[0] = launch_records(P, W, nrec, s);
+        rec(c, 2 * MCGPU_STAGE_DOWNLOAD + 1);
+    });
+    c->rec_buf = c->graphs[2].aux[0];
     // per-pair record ranges (first sorted record of each pair, then the total)
     ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
         "D2H ranges");
@@ -660,8 +838,13 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         c->device = device;
         if (const char* e = getenv("MCGPU_LEAF_SIZE")) {
             const int v = atoi(e);
-            if (v >= 1 && v <= 16) c->leaf_size = (uint32_t)v;
+            if (v >= 1 && v <= 16) c->tune.leaf_size = (uint32_t)v;
         }
+        if (const char* e = getenv("MCGPU_TRAVERSAL")) {
+            if (!strcmp(e, "packet")) c->tune.traversal = 1;
+            if (!strcmp(e, "thread")) c->tune.traversal = 2;
+        }
+        if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
         *out = c;
@@ -681,8 +864,11 @@ int mcgpu_context_release(mcgpu_context c)
     c->pin_counters.release();
     c->pin_tab.release();
     c->pin_stage.release();
+    c->pin_idx.release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& g : c->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     if (c->s) cudaStreamDestroy(c->s);
     delete c;
     return MCGPU_OK;
@@ -751,6 +937,68 @@ int mcgpu_dispatch_packed(mcgpu_context c, uint32_t flags, const mcgpu_batch* b,
         return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
             e.where + ": " + cudaGetErrorString(e.e));
     }
+}
+
+int mcgpu_context_set_tuning(mcgpu_context c, const mcgpu_tuning* t)
+{
+    if (!c || !t) return fail(MCGPU_INVALID_VALUE, "null argument");
+    if (t->leaf_size < 1 || t->leaf_size > 16 || t->traversal > 2 || t->packet_faces < 1 || t->packet_faces > 32
+        || (t->stack_depth != 64 && t->stack_depth != 512))
+        return fail(MCGPU_INVALID_VALUE, "tuning out of range");
+    c->tune = *t;
+    return MCGPU_OK;
+}
+
+int mcgpu_context_get_tuning(mcgpu_context c, mcgpu_tuning* t)
+{
+    if (!c || !t) return fail(MCGPU_INVALID_VALUE, "null argument");
+    *t = c->tune;
+    return MCGPU_OK;
+}
+
+int mcgpu_autotune(mcgpu_context c, uint32_t flags, const mcgpu_batch* sample, uint32_t repeats, mcgpu_tuning* best,
+    float* best_ms)
+{
+    if (!c || !sample || sample->num_pairs == 0) return fail(MCGPU_INVALID_VALUE, "null argument");
+    if (repeats == 0) repeats = 3;
+    std::vector<mcgpu_tuning> cand;
+    for (uint32_t leaf : { 2u, 4u, 8u }) {
+        cand.push_back({ leaf, 0, 32, 64 });
+        cand.push_back({ leaf, 0, 16, 64 });
+        cand.push_back({ leaf, 1, 32, 64 });
+        cand.push_back({ leaf, 2, 32, 64 });
+        cand.push_back({ leaf, 2, 32, 512 });
+    }
+    const mcgpu_tuning keep = c->tune;
+    std::vector<mcgpu_summary> sums(sample->num_pairs);
+    float best_t = 3.4e38f;
+    mcgpu_tuning best_c = keep;
+    for (const mcgpu_tuning& t : cand) {
+        c->tune = t;
+        for (int w = 0; w < 2; ++w) { // warm-up: pools sized, launch graph captured
+            const int rc = mcgpu_dispatch_packed(c, flags & ~(uint32_t)MCGPU_PROFILE, sample, sums.data());
+            if (rc != MCGPU_OK) {
+                c->tune = keep;
+                return rc;
+            }
+        }
+        const auto t0 = std::chrono::steady_clock::now();
+        for (uint32_t r = 0; r < repeats; ++r)
+            if (mcgpu_dispatch_packed(c, flags & ~(uint32_t)MCGPU_PROFILE, sample, sums.data()) != MCGPU_OK) {
+                c->tune = keep;
+                return fail(MCGPU_CUDA_ERROR, "autotune dispatch failed");
+            }
+        const float ms =
+            std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count() / repeats;
+        if (ms < best_t) {
+            best_t = ms;
+            best_c = t;
+        }
+    }
+    c->tune = best_c;
+    if (best) *best = best_c;
+    if (best_ms) *best_ms = best_t;
+    return MCGPU_OK;
 }
 
 int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
@@ -853,3 +1101,27 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
 const char* mcgpu_last_error(void) { return g_last_error.c_str(); }
 
 } // extern "C"
+
+namespace mcgpu {
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+int dispatch_with_resident(mcgpu_context c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs,
+    const mcgpu_mesh* cuts, const ResidentCut* const* resident, mcgpu_summary* out)
+{
+    if (!(flags & MCGPU_RECENTRE) || (flags & (MCGPU_DEVICE_POINTERS | MCGPU_VERTEX_ARRAY_FLOAT)))
+        return fail(MCGPU_INVALID_VALUE, "resident cut meshes take double user coordinates with MCGPU_RECENTRE");
+    try {
+        // stand-in views for resident cuts: counts for the layout, never dereferenced on the host
+        std::vector<mcgpu_mesh> cv(cuts, cuts + n);
+        for (uint32_t p = 0; p < n; ++p)
+            if (resident[p]) cv[p] = mcgpu_mesh { resident[p]->X, resident[p]->idx, nullptr, resident[p]->nv,
+                                                  resident[p]->nf };
+        return run(c, flags, n, srcs, cv.data(), nullptr, out, nullptr, resident);
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+} // namespace mcgpu

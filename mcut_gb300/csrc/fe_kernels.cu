@@ -259,9 +259,9 @@ __global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, in
 // most 32 faces (its parent holds more); one warp walks the cut tree for it.
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_src_packets(const K* __restrict__ key, int n, uint2* __restrict__ packets,
-    uint32_t* __restrict__ counters)
+    uint32_t* __restrict__ counters, int pmax)
 {
-    if (n <= 32) {
+    if (n <= pmax) {
         if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
             packets[0] = make_uint2(0u, (uint32_t)(n - 1));
             counters[9] = 1;
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kBlock) k_src_packets(const K* __restrict__ ke
         const int j = i + l * d;
         lo = min(i, j);
         hi = max(i, j);
-        if (hi - lo + 1 > 32) {
+        if (hi - lo + 1 > pmax) {
             const int dnode = delta(key, n, i, j);
             int s = 0;
             for (int t = (l + 1) >> 1;; t = (t + 1) >> 1) {
@@ -291,8 +291,8 @@ __global__ void __launch_bounds__(kBlock) k_src_packets(const K* __restrict__ ke
                 if (t == 1) break;
             }
             gamma = i + s * d + min(d, 0);
-            emit0 = gamma - lo + 1 <= 32;
-            emit1 = hi - gamma <= 32;
+            emit0 = gamma - lo + 1 <= pmax;
+            emit1 = hi - gamma <= pmax;
         }
         }
         const uint32_t p0 = warp_append(&counters[9], emit0);
@@ -1467,25 +1467,24 @@ void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)
     g_launches++;
     if (P.n_pairs > 1)
         k_src_packets<unsigned long long><<<grid_for(P.ns), kBlock, 0, s>>>(
-            (const unsigned long long*)W.skeys[src_buf], (int)P.ns, W.packets, W.counters);
+            (const unsigned long long*)W.skeys[src_buf], (int)P.ns, W.packets, W.counters, (int)W.packet_faces);
     else
         k_src_packets<uint32_t><<<grid_for(P.ns), kBlock, 0, s>>>((const uint32_t*)W.skeys[src_buf], (int)P.ns,
-            W.packets, W.counters);
+            W.packets, W.counters, (int)W.packet_faces);
 }
 
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
 {
-    // Default: warp per query packet (a compact source subtree of <= 32
-    // faces; launch_packets must have run since the counters were cleared). MCGPU_TRAVERSAL=thread selects one thread per source face; the
-    // deep re-run after a stack overflow is per thread with a 512-entry stack.
-    static const bool per_thread = [] {
-        const char* e = getenv("MCGPU_TRAVERSAL");
-        return e && strcmp(e, "thread") == 0;
-    }();
+    // W.traversal: 0 (default) one warp per query packet (a compact source
+    // subtree of <= W.packet_faces faces), breadth-first; 1 the same
+    // depth-first; 2 one thread per source face with a W.stack_depth stack.
+    // launch_packets must have run since the counters were cleared (0, 1).
+    // The deep re-run after a stack overflow is per thread, 512 entries.
+    const bool per_thread = W.traversal == 2;
     if (deep || per_thread) {
         const int g = grid_for(P.ns);
         g_launches++;
-        if (deep)
+        if (deep || W.stack_depth > 64)
             k_traverse<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.cvals[cut_buf], W.cl_start, W.cl_n,
                 W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand, W.pair_status);
         else
@@ -1494,20 +1493,14 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
         return;
     }
     g_launches++;
-    static const bool dfs = [] {
-        const char* e = getenv("MCGPU_TRAVERSAL");
-        return e && strcmp(e, "packet") == 0;
-    }();
+    const bool dfs = W.traversal == 1;
     if (dfs)
         k_traverse_packet<<<grid_for(P.ns), kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
             W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
             W.counters, W.cand, W.pair_status);
     else {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_traverse_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWaveSmem);
-            attr = true;
-        }
+        static std::atomic<unsigned long long> attr { 0 };
+        set_smem_once((const void*)k_traverse_wave, (int)kWaveSmem, attr);
         k_traverse_wave<<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
             W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
             W.counters, W.cand, W.pair_status);

@@ -105,6 +105,10 @@ struct Work {
     uint64_t tri_scratch_cap;         // entries
     uint64_t tri_stride;              // entries per polygon (largest C(n,3)); 0: no polygons
     uint64_t pair_cap, test_cap, inc_cap, plane_cap;
+    // tuning (results do not depend on it)
+    uint32_t traversal;               // 0 warp/packet breadth-first, 1 warp/packet depth-first, 2 thread/face
+    uint32_t packet_faces;            // source faces per query packet (1..32)
+    uint32_t stack_depth;             // per-thread stack of traversal 2 (64 or 512)
 };
 
 // stage launchers (all asynchronous on `s`)

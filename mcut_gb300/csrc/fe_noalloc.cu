@@ -176,6 +176,9 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     P.ncl = ncl;
 
     Work W {};
+    W.traversal = 0;
+    W.packet_faces = 32;
+    W.stack_depth = 64;
     W.fbox = reinterpret_cast<double*>(base + oFbox);
     W.mesh_box = reinterpret_cast<unsigned long long*>(base + oMbox);
     uint32_t* keys = reinterpret_cast<uint32_t*>(base + oKeys);

@@ -8,11 +8,22 @@
 //              their global rank.
 // A tile is 256 threads x 16 keys. Keys and values stream through HBM once
 // per launch; the histogram table stays in L2.
+#include <atomic>
 #include "fe_sort.cuh"
 
 namespace mcgpu {
 
-unsigned long long g_launches = 0;
+thread_local unsigned long long g_launches = 0;
+
+void set_smem_once(const void* func, int bytes, std::atomic<unsigned long long>& done)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
 
 namespace {
 constexpr int kThreads = 256;
@@ -370,11 +381,8 @@ size_t sort_small_smem() { return (size_t)kSmallSort * 16 + (size_t)kSmallWarps 
 void sort_small_pairs(const unsigned long long* keys_in, const uint32_t* vals_in, unsigned long long* keys_out,
     uint32_t* vals_out, uint32_t n, int end_bit, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sort_small_smem());
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr { 0 };
+    set_smem_once((const void*)k_sort_small, (int)sort_small_smem(), attr);
     g_launches++;
     k_sort_small<<<1, kSmallThreads, sort_small_smem(), s>>>(keys_in, vals_in, keys_out, vals_out, n, end_bit);
 }

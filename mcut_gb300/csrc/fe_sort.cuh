@@ -1,12 +1,15 @@
 // Device radix sort and scan used by the front-end kernels.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace mcgpu {
 
-// kernels launched by this library since load (reported per dispatch)
-extern unsigned long long g_launches;
+// kernels launched by the calling thread (each API call reports its own difference)
+extern thread_local unsigned long long g_launches;
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per device (`done`: bit per device)
+void set_smem_once(const void* func, int bytes, std::atomic<unsigned long long>& done);
 
 // Scratch (bytes) the sort needs for n keys.
 size_t radix_sort_temp_bytes(uint32_t n);

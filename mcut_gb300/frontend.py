@@ -103,6 +103,27 @@ class Context:
                 r.test_info = self._get(L.DATA_TEST_INFO, np.int8, 4)
         return r
 
+    def set_tuning(self, leaf_size=4, traversal=0, packet_faces=32, stack_depth=64):
+        t = L.Tuning(leaf_size, traversal, packet_faces, stack_depth)
+        L.check(self._lib.mcgpu_context_set_tuning(self._h, C.byref(t)), "mcgpu_context_set_tuning")
+
+    def tuning(self) -> dict:
+        t = L.Tuning()
+        L.check(self._lib.mcgpu_context_get_tuning(self._h, C.byref(t)), "mcgpu_context_get_tuning")
+        return {k: int(getattr(t, k)) for k, _ in L.Tuning._fields_}
+
+    def autotune(self, packed, device: bool = False, repeats: int = 3):
+        """Pick the fastest tuning for batches like ``packed`` (kept on this
+        context). Returns (tuning dict, mean ms per batch)."""
+        ptr = (lambda a: a.data_ptr()) if device else (lambda a: a.ctypes.data)
+        b = L.Batch(int(packed["counts"].shape[0]), ptr(packed["v"]), ptr(packed["f"]), None,
+                    packed["counts"].ctypes.data, packed["eps"].ctypes.data)
+        t = L.Tuning()
+        ms = C.c_float(0)
+        L.check(self._lib.mcgpu_autotune(self._h, L.DEVICE_POINTERS if device else 0, C.byref(b), repeats,
+                                         C.byref(t), C.byref(ms)), "mcgpu_autotune")
+        return {k: int(getattr(t, k)) for k, _ in L.Tuning._fields_}, ms.value
+
     def vertices(self):
         return self._get(L.DATA_VERTICES, np.float64, 3)
 
@@ -169,6 +190,89 @@ class Context:
             L.check(self._lib.mcgpu_get_batch_data(self._h, pair, query, n.value, out.ctypes.data, C.byref(n)),
                     "get_batch_data")
         return out.reshape(-1, cols)
+
+
+class Server:
+    """Continuous-batching request server on one GPU (mcgpu_server_*).
+
+        srv = Server(device=0)
+        cid = srv.add_cut(cut)                   # resident cut mesh
+        t = srv.submit(src, cut)                 # or srv.submit(src, cut_id=cid)
+        summary, latency_ms = srv.wait(t)
+        ids, pts = srv.records(t); srv.release(t)
+
+    Meshes are user coordinates (double); the server recentres them as
+    mcDispatch does. The numpy arrays of a request are kept alive here until
+    it is released.
+    """
+
+    def __init__(self, device: int = 0, workers: int = 0, max_batch_pairs: int = 0, max_batch_faces: int = 0,
+                 hbm_budget_bytes: int = 0, linger_us: int = 0):
+        self._lib = L.load()
+        self._h = C.c_void_p()
+        cfg = L.ServerConfig(device, workers, max_batch_pairs, max_batch_faces, hbm_budget_bytes, linger_us, 0)
+        L.check(self._lib.mcgpu_server_create(C.byref(self._h), C.byref(cfg)), "mcgpu_server_create")
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            self._lib.mcgpu_server_release(self._h)
+            self._h = C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_cut(self, cut) -> int:
+        m, keep = _as_mesh(cut)
+        cid = C.c_uint32(0)
+        L.check(self._lib.mcgpu_server_add_cut_mesh(self._h, C.byref(m), C.byref(cid)), "mcgpu_server_add_cut_mesh")
+        return cid.value
+
+    def submit(self, src, cut=None, cut_id: int | None = None) -> int:
+        ms, ks = _as_mesh(src)
+        keep = [ms, ks]
+        pc = None
+        if cut is not None:
+            mc, kc = _as_mesh(cut)
+            keep += [mc, kc]
+            pc = C.byref(mc)
+        t = C.c_uint64(0)
+        L.check(self._lib.mcgpu_server_submit(self._h, C.byref(ms), pc, L.NO_CUT if cut_id is None else int(cut_id),
+                                              C.byref(t)), "mcgpu_server_submit")
+        self._keep[t.value] = keep
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        sm = L.Summary()
+        lat = C.c_double(0)
+        L.check(self._lib.mcgpu_server_wait(self._h, ticket, timeout_ms, C.byref(sm), C.byref(lat)),
+                "mcgpu_server_wait")
+        return sm, lat.value
+
+    def records(self, ticket: int):
+        out = []
+        for q, dt, cols in ((L.DATA_RECORD_IDS, np.uint32, 5), (L.DATA_RECORD_POINTS, np.float64, 3)):
+            n = C.c_uint64(0)
+            L.check(self._lib.mcgpu_server_get_data(self._h, ticket, q, 0, None, C.byref(n)), "get_data")
+            a = np.empty(n.value // np.dtype(dt).itemsize, dt)
+            if n.value:
+                L.check(self._lib.mcgpu_server_get_data(self._h, ticket, q, n.value, a.ctypes.data, C.byref(n)),
+                        "get_data")
+            out.append(a.reshape(-1, cols))
+        return out[0], out[1]
+
+    def release(self, ticket: int):
+        L.check(self._lib.mcgpu_server_release_request(self._h, ticket), "mcgpu_server_release_request")
+        self._keep.pop(ticket, None)
+
+    def stats(self) -> dict:
+        st = L.ServerStats()
+        L.check(self._lib.mcgpu_server_get_stats(self._h, C.byref(st)), "mcgpu_server_get_stats")
+        return {k: int(getattr(st, k)) for k, _ in L.ServerStats._fields_}
 
 
 def pack_pairs(pairs, recentre_coords: bool = True):

@@ -78,6 +78,18 @@ def test_mid_size_against_oracle(ctx, level, n):
     check_against(r, want, meshgen.num_faces(s))
 
 
+@pytest.mark.parametrize("m,n", [(128, 64), (256, 40)])
+def test_coplanar_stress_against_oracle(ctx, m, n):
+    """The precision-stress config at reduced size: a grid coincident with
+    the cube's top face (z nudged by 1e-12): every test's signs, type and
+    point-in-polygon char, and the general-position outcome."""
+    s, c = meshgen.cube_coplanar(16.0, m=m, n=n)
+    want = oracle.front_end(s, c, impl="port", threads=8)
+    r = ctx.dispatch(s, c, keep_tests=True, keep_pairs=True)
+    check_against(r, want, meshgen.num_faces(s))
+    assert r.escalations[1] + r.escalations[2] > 0  # the near-coplanar signs leave the fp32 filter
+
+
 def test_full_size_sphere_heightfield_x16(ctx):
     """The single-large-pair workload at full size (327,680 vs 2,093,058 tris)."""
     s, c = meshgen.sphere_heightfield(16.0)

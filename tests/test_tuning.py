@@ -1,0 +1,97 @@
+"""Launch tuning and graph replay change speed only: every tuning and every
+replay of a captured launch graph gives bit-identical results."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+from mcut_gb300 import _lib as L
+from mcut_gb300 import meshgen
+
+TUNINGS = [dict(leaf_size=l, traversal=t, packet_faces=p, stack_depth=d)
+           for l in (1, 4, 16) for (t, p, d) in ((0, 32, 64), (0, 7, 64), (1, 32, 64), (1, 16, 64), (2, 32, 64),
+                                                 (2, 32, 512))]
+
+
+def test_tuning_arguments_checked_without_a_gpu():
+    lib = L.load()
+    t = L.Tuning(4, 0, 32, 64)
+    assert lib.mcgpu_context_set_tuning(None, C.byref(t)) == L.INVALID_VALUE
+    assert lib.mcgpu_context_get_tuning(None, C.byref(t)) == L.INVALID_VALUE
+    assert lib.mcgpu_autotune(None, 0, None, 1, None, None) == L.INVALID_VALUE
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from mcut_gb300 import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _key(r):
+    return r.status, r.num_pairs, r.num_tests, r.record_ids.tobytes(), r.record_points.tobytes(), \
+        r.pairs.tobytes() if r.pairs is not None else b""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["crack", "sphere_heightfield"])
+def test_every_tuning_gives_the_same_result(ctx, case):
+    if case == "crack":
+        s, c = meshgen.crack_pair(np.random.default_rng(11), target_tris=60000)
+    else:
+        s, c = meshgen.sphere_heightfield(16.0, level=5, n=300)
+    ctx.set_tuning()
+    want = _key(ctx.dispatch(s, c, keep_pairs=True))
+    for t in TUNINGS:
+        ctx.set_tuning(**t)
+        got = _key(ctx.dispatch(s, c, keep_pairs=True))
+        assert got[:3] == want[:3], t
+        assert got[3:5] == want[3:5], t
+        # the pair list is emitted in traversal order; compare as a set
+        a = np.frombuffer(got[5], np.uint32).reshape(-1, 2)
+        b = np.frombuffer(want[5], np.uint32).reshape(-1, 2)
+        assert np.array_equal(np.unique(a, axis=0), np.unique(b, axis=0)), t
+    ctx.set_tuning()
+
+
+@pytest.mark.gpu
+def test_graph_replay_is_identical(ctx):
+    """Dispatch 1 runs the launches directly, dispatch 2 captures them into
+    graphs, later ones replay; a different size in between changes the key."""
+    s, c = meshgen.crack_pair(np.random.default_rng(12), target_tris=20000)
+    s2, c2 = meshgen.crack_pair(np.random.default_rng(13), target_tris=5000)
+    first = ctx.dispatch(s, c)
+    for k in range(5):
+        r = ctx.dispatch(s, c)
+        assert r.status == first.status
+        assert np.array_equal(r.record_ids, first.record_ids)
+        assert G.same_bits(r.record_points, first.record_points)
+        assert r.kernel_launches == first.kernel_launches
+        if k == 2:
+            ctx.dispatch(s2, c2)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results(ctx):
+    from mcut_gb300 import pack_pairs
+    pairs = meshgen.batch_pairs(32, seed=meshgen.SEED_BASE + 42)
+    pk = pack_pairs(pairs)
+    sums0, ids0, pts0, off0 = ctx.dispatch_packed(pk)
+    best, ms = ctx.autotune(pk, repeats=1)
+    assert ms > 0 and ctx.tuning() == best
+    sums1, ids1, pts1, off1 = ctx.dispatch_packed(pk)
+    assert np.array_equal(off0, off1) and np.array_equal(ids0, ids1) and G.same_bits(pts0, pts1)
+    ctx.set_tuning()
+
+
+@pytest.mark.gpu
+def test_profiled_dispatches_repeat(ctx):
+    """Stage timing (direct launches) interleaved with graph replays."""
+    s, c = meshgen.crack_pair(np.random.default_rng(14), target_tris=20000)
+    for k in range(6):
+        r = ctx.dispatch(s, c, profile=(k % 2 == 0), fetch=False)
+        assert r.status in (0, 1)
+        if k % 2 == 0:
+            assert sum(r.stage_ms.values()) > 0
