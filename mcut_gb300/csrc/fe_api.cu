@@ -93,7 +93,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -712,6 +712,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.plane_cap = std::min<uint64_t>(L.nf, 2 * npairs + 1);
     W.plane_slot = c->buf[B_PSLOT].get<uint32_t>(L.nf);
     W.planes = c->buf[B_PLANES].get<FacePlane>(W.plane_cap);
+    W.proj_flag = c->buf[B_PFLAG].get<uint32_t>(W.plane_cap);
+    W.proj_list = c->buf[B_PLIST].get<uint32_t>(W.plane_cap);
     W.poly_list = c->buf[B_POLY].get<uint32_t>(L.all_tri ? 1 : L.nf);
     W.tri_stride = L.all_tri ? 0 : L.tri_stride;
     W.tri_scratch_cap = W.tri_stride * std::max<uint64_t>(L.n_poly, 1);

@@ -40,19 +40,34 @@ __device__ __forceinline__ bool dlt_int(double a, double b)
     const long long ob = ib < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)ib) : ib;
     return oa < ob;
 }
-// fp64 -> fp32 rounded toward -inf / +inf with integer operations (the fp64
-// pipe's conversions are slow here); values outside fp32's normal range take
-// the hardware conversion
+// fp64 -> fp32 rounded toward -inf / +inf with integer operations only (the
+// fp64 pipe's conversions are slow here, and a predicated conversion still
+// occupies it): normal results, subnormal results, overflow to +-FLT_MAX or
+// +-inf, and inf / NaN passed through.
 __device__ __forceinline__ float f32_round(double x, bool up)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    if (e < 1023u - 126u || e > 1023u + 127u) return up ? __double2float_ru(x) : __double2float_rd(x);
     const unsigned sign = (unsigned)(b >> 63);
     const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-    unsigned fb = (sign << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
-    const bool inexact = (m & 0x1FFFFFFFull) != 0;
-    if (inexact && (sign != 0) != up) fb += 1u; // away from zero toward the requested infinity
+    const bool away = (sign != 0) != up; // rounding away from zero is toward the requested infinity
+    unsigned fb;
+    if (e == 0x7FFu) {
+        fb = (sign << 31) | 0x7F800000u | (m ? 0x00400000u : 0u);
+    } else if (e > 1023u + 127u) {
+        fb = (sign << 31) | (away ? 0x7F800000u : 0x7F7FFFFFu);
+    } else if (e >= 1023u - 126u) {
+        fb = (sign << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
+        if (away && (m & 0x1FFFFFFFull) != 0) fb += 1u;
+    } else {
+        // below fp32's normal range: a multiple of 2^-149 (or zero)
+        const unsigned long long sig = e ? (m | (1ull << 52)) : m;
+        const unsigned sh = 926u - (e ? e : 1u);       // >= 30
+        const unsigned long long q = sh >= 64u ? 0ull : (sig >> sh);
+        const bool inexact = sh >= 64u ? sig != 0 : (sig & ((1ull << sh) - 1ull)) != 0;
+        fb = (sign << 31) | (unsigned)q;
+        if (away && inexact) fb += 1u;
+    }
     return __uint_as_float(fb);
 }
 __device__ __forceinline__ float f32_rd(double x) { return f32_round(x, false); }
@@ -263,18 +278,30 @@ static __device__ __noinline__ int orient3d_exact_sign(const double* pa, const d
 enum { ESC_F32 = 0, ESC_F64 = 1, ESC_EXACT = 2 };
 
 // FP32 filter. The nine differences are formed in fp64 and rounded once to
-// fp32, so each carries a relative error of at most u(1+2^-28) (u = 2^-24).
-// Shewchuk's stage-A analysis with that per-input error and u per fp32
-// operation gives |det - det_exact| <= (7u + 56u^2) * permanent; 8u covers
-// the slightly larger input error. The filter only runs when every nonzero
-// difference lies in [1e-12, 1e12]: then no fp32 product or sum can
-// underflow or overflow and the relative-error model holds for every
-// operation. Otherwise, or when the bound is not met, it escalates.
-__device__ __forceinline__ bool f32_ok(double d, float f)
+// fp32 to nearest (relative error <= u(1+2^-28), u = 2^-24), by integer
+// operations (fp64 conversions run at the fp64 rate). Shewchuk's stage-A
+// analysis with that per-input error and u per fp32 operation gives
+// |det - det_exact| <= (7u + 56u^2) * permanent; 8u covers the slightly
+// larger input error. The filter only runs when every nonzero difference
+// lies in [2^-39, 2^40): then no fp32 product or sum can overflow, no
+// product underflows, and the relative-error model holds for every
+// operation (a subnormal difference of products is exact). Otherwise, or
+// when the bound is not met, it escalates.
+__device__ __forceinline__ bool f32_filter_input(double d, float& f)
 {
-    const bool zero = ((unsigned long long)__double_as_longlong(d) << 1) == 0ull;
-    const float a = fabsf(f);
-    return (zero || a >= 1e-12f) && a <= 1e12f;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    if ((b << 1) == 0ull) {
+        f = 0.0f;
+        return true;
+    }
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    if (e < 1023u - 39u || e > 1023u + 39u) return false;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned fb = ((unsigned)(b >> 63) << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
+    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+    if (r > 0x10000000u || (r == 0x10000000u && (fb & 1u))) fb += 1u; // to nearest, ties to even
+    f = __uint_as_float(fb);
+    return true;
 }
 __device__ __forceinline__ int orient3d_sign_filtered(const double* pa, const double* pb, const double* pc,
     const double* pd, int& stage)
@@ -283,11 +310,10 @@ __device__ __forceinline__ int orient3d_sign_filtered(const double* pa, const do
     const double ady = pa[1] - pd[1], bdy = pb[1] - pd[1], cdy = pc[1] - pd[1];
     const double adz = pa[2] - pd[2], bdz = pb[2] - pd[2], cdz = pc[2] - pd[2];
     {
-        const float ax = (float)adx, bx = (float)bdx, cx = (float)cdx;
-        const float ay = (float)ady, by = (float)bdy, cy = (float)cdy;
-        const float az = (float)adz, bz = (float)bdz, cz = (float)cdz;
-        const bool ok = f32_ok(adx, ax) && f32_ok(bdx, bx) && f32_ok(cdx, cx) && f32_ok(ady, ay) && f32_ok(bdy, by)
-            && f32_ok(cdy, cy) && f32_ok(adz, az) && f32_ok(bdz, bz) && f32_ok(cdz, cz);
+        float ax, bx, cx, ay, by, cy, az, bz, cz;
+        const bool ok = f32_filter_input(adx, ax) & f32_filter_input(bdx, bx) & f32_filter_input(cdx, cx)
+            & f32_filter_input(ady, ay) & f32_filter_input(bdy, by) & f32_filter_input(cdy, cy)
+            & f32_filter_input(adz, az) & f32_filter_input(bdz, bz) & f32_filter_input(cdz, cz);
         if (ok) {
             const float bxcy = bx * cy, cxby = cx * by, cxay = cx * ay, axcy = ax * cy, axby = ax * by, bxay = bx * ay;
             const float det = az * (bxcy - cxby) + bz * (cxay - axcy) + cz * (axby - bxay);
@@ -380,7 +406,16 @@ struct FacePlane {
     int32_t tri[3];   // plane-defining vertex positions in the face's vertex list (-1: none)
 };
 
-// projection matrix P = K * R with the reference's operation order
+// projection matrix P = K * R (calculate_projection_matrix,
+// math.cpp:710-793), with the reference's rounding:
+//   a = n / |n|, b = sign(n[mc]) e_mc, R = 2 (a+b)(a+b)^T / (a.b) - diag(1,-1,1)
+// (R = diag(1,-1,1) when a == b), K picks rows i != mc of R. Here
+//   * a.b == |a[mc]| exactly (b has one nonzero component, +-1) and is at
+//     least 3^-1/2, so every entry of R is finite;
+//   * (K R)_ij = ((0 + K_i0 R_0j) + K_i1 R_1j) + K_i2 R_2j adds one selected
+//     entry to +0 and +-0 terms: it equals R_sj, except that -0 becomes +0;
+//   * apb_i apb_j == apb_j apb_i, so the two selected rows need 5 distinct
+//     quotients, each rounded exactly as the reference's.
 __device__ inline void projection_matrix(const double* nrm, int mc, double* P)
 {
     const double len = sqrt(dot3(nrm, nrm));
@@ -388,26 +423,25 @@ __device__ inline void projection_matrix(const double* nrm, int mc, double* P)
     double b[3] = { 0.0, 0.0, 0.0 };
     const int s = (0.0 < nrm[mc]) - (nrm[mc] < 0.0);
     b[mc] = 1.0 * (double)s;
-    double R[3][3] = { { 1.0, 0.0, 0.0 }, { 0.0, -1.0, 0.0 }, { 0.0, 0.0, 1.0 } };
+    const int r0 = mc == 0 ? 1 : 0, r1 = mc == 2 ? 1 : 2; // the rows K selects, r0 < r1
     if (a[0] != b[0] || a[1] != b[1] || a[2] != b[2]) {
         const double apb[3] = { a[0] + b[0], a[1] + b[1], a[2] + b[2] };
         const double adb = dot3(a, b);
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                const double I = (i == j) ? (i == 1 ? -1.0 : 1.0) : 0.0;
-                R[i][j] = (((apb[i] * apb[j]) / adb) * 2.0) - I;
-            }
-    }
-    double K[2][3] = { { 0.0, 0.0, 0.0 }, { 0.0, 0.0, 0.0 } };
-    if (mc == 0) { K[0][1] = 1.0; K[1][2] = 1.0; }
-    else if (mc == 1) { K[0][0] = 1.0; K[1][2] = 1.0; }
-    else { K[0][0] = 1.0; K[1][1] = 1.0; }
-    for (int i = 0; i < 2; ++i)
+        double q0[3], q1[3];
+        for (int j = 0; j < 3; ++j) q0[j] = (apb[r0] * apb[j]) / adb;
+        for (int j = 0; j < 3; ++j) q1[j] = (j == r0) ? q0[r1] : (apb[r1] * apb[j]) / adb;
         for (int j = 0; j < 3; ++j) {
-            double acc = 0.0;
-            for (int k = 0; k < 3; ++k) acc = acc + K[i][k] * R[k][j];
-            P[i * 3 + j] = acc;
+            const double e0 = (q0[j] * 2.0) - ((r0 == j) ? (r0 == 1 ? -1.0 : 1.0) : 0.0);
+            const double e1 = (q1[j] * 2.0) - ((r1 == j) ? (r1 == 1 ? -1.0 : 1.0) : 0.0);
+            P[j] = e0 == 0.0 ? 0.0 : e0;
+            P[3 + j] = e1 == 0.0 ? 0.0 : e1;
         }
+    } else {
+        for (int j = 0; j < 3; ++j) {
+            P[j] = (r0 == j) ? (r0 == 1 ? -1.0 : 1.0) : 0.0;
+            P[3 + j] = (r1 == j) ? (r1 == 1 ? -1.0 : 1.0) : 0.0;
+        }
+    }
 }
 
 // matrix_t * vec3 (math.h:508-520)

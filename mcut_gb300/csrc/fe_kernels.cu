@@ -248,8 +248,9 @@ __global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, in
         const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
         nodes[i].child[0] = left;
         nodes[i].child[1] = right;
+        // parent index | child slot << 31 (the refit climb needs no node read)
         parent[left >= 0 ? left : (n - 1) + ~left] = i;
-        parent[right >= 0 ? right : (n - 1) + ~right] = i;
+        parent[right >= 0 ? right : (n - 1) + ~right] = (int32_t)((uint32_t)i | 0x80000000u);
     }
 }
 
@@ -372,11 +373,12 @@ __global__ void __launch_bounds__(kBlock) k_refit(Problem P, const float* __rest
             fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
         }
         fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
-        int child = ~i;
-        int node = parent[(n - 1) + i];
-        while (node >= 0) {
+        uint32_t pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
+        for (;;) {
+            const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
+            // the next parent is read before the atomic (whose memory clobber orders every later load)
+            const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
             Node* nd = &nodes[node];
-            const int slot = (nd->child[0] == child) ? 0 : 1;
             put_child(nd, slot, fb);
             // acq_rel arrival: releases this child's box, acquires the sibling's
             unsigned prev;
@@ -389,8 +391,8 @@ __global__ void __launch_bounds__(kBlock) k_refit(Problem P, const float* __rest
             }
             fb.plo = min(fb.plo, o.plo);
             fb.phi = max(fb.phi, o.phi);
-            child = node;
-            node = node == 0 ? -1 : parent[node];
+            if (node == 0) break;
+            pe = next;
         }
     }
 }
@@ -942,7 +944,10 @@ __global__ void __launch_bounds__(kBlock) k_planes(Problem P, const uint8_t* __r
             const double t = fabs(pl.n[i]);
             if (t > big) { big = t; pl.mc = i; }
         }
-        projection_matrix(pl.n, pl.mc, pl.P);
+        // the projection is needed by the point-in-polygon test of the few
+        // faces a segment crosses (computed there for triangles) and by the
+        // triplet ranking of polygons (computed here)
+        if (n > 3) projection_matrix(pl.n, pl.mc, pl.P);
         pl.tri[0] = 0; pl.tri[1] = 1; pl.tri[2] = 2;
         planes[slot] = pl;
         if (n > 3) {
@@ -1228,21 +1233,21 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
 // ---------------------------------------------------------------------------
 // narrow phase (kernel.cpp:2456-2658; math.cpp:249-287, 391-427, 643-703, 851-902)
 // ---------------------------------------------------------------------------
-__device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint32_t n, const double* pt)
+__device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_t n, const double* pt)
 {
     double q[2];
-    project2(pl.P, pt, q);
+    project2(Pm, pt, q);
     int rc = 0, lc = 0;
     double prv[2];
     {
         double v[3];
         load_xyz(P.X, face_vertex(P, o, n, n - 1), v);
-        project2(pl.P, v, prv);
+        project2(Pm, v, prv);
     }
     for (uint32_t i = 0; i < n; ++i) {
         double v[3], c[2];
         load_xyz(P.X, face_vertex(P, o, n, i), v);
-        project2(pl.P, v, c);
+        project2(Pm, v, c);
         const double xi = c[0] - q[0], yi = c[1] - q[1];
         if (xi == 0.0 && yi == 0.0) return 'v';
         const double xl = prv[0] - q[0], yl = prv[1] - q[1];
@@ -1259,84 +1264,144 @@ __device__ char pip_face(const Problem& P, const FacePlane& pl, uint32_t o, uint
     return (rc & 1) ? 'i' : 'o';
 }
 
-__global__ void __launch_bounds__(kBlock) k_narrow(Problem P, const Test* __restrict__ tests,
+// Narrow phase, pass 1 (every culled test): both orient3d signs and the
+// type char (compute_segment_plane_intersection_type, math.cpp:391-427).
+// Tests whose segment meets the plane ('1', 'q', 'r', 'p') go to a compact
+// hit list for pass 2, so its fp64 work runs on full warps.
+__global__ void __launch_bounds__(kBlock) k_narrow_signs(Problem P, const Test* __restrict__ tests,
     const uint32_t* __restrict__ counters_ro, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
-    const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
-    unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
-    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status)
+    const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info, uint2* __restrict__ hits,
+    uint32_t* __restrict__ proj_flag, uint32_t* __restrict__ proj_list, uint32_t* __restrict__ counters)
 {
     const uint64_t nt = min((uint64_t)counters_ro[1], test_cap);
     uint32_t esc[3] = { 0, 0, 0 };
     for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x; i0 < nt; i0 += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i = i0 + threadIdx.x;
-        // one block_append call site, reached by every thread of the block
-        bool rec = false;
-        Test t;
-        double pt[3] = { 0.0, 0.0, 0.0 };
+        bool hit = false, first_hit = false;
+        uint32_t code = 0, slot = 0;
         if (i < nt) {
-        t = tests[i];
-        const FacePlane pl = planes[plane_slot[t.g]];
-        const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
-        double q[3], r[3];
-        load_xyz(P.X, t.q, q);
-        load_xyz(P.X, t.r, r);
-        int8_t sq = 0, sr = 0;
-        char type = '0', pip = 0;
-        if (pl.tri[0] >= 0) {
-            double a[3], b[3], c[3];
-            load_xyz(P.X, face_vertex(P, o, n, pl.tri[0]), a);
-            load_xyz(P.X, face_vertex(P, o, n, pl.tri[1]), b);
-            load_xyz(P.X, face_vertex(P, o, n, pl.tri[2]), c);
-            int st0, st1;
-            sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
-            sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
-            esc[st0]++;
-            esc[st1]++;
-            if (sq == 0 && sr == 0) type = 'p';
-            else if (sq == 0) type = 'q';
-            else if (sr == 0) type = 'r';
-            else if ((sr < 0 && sq < 0) || (sr > 0 && sq > 0)) type = '0';
-            else type = '1';
-        }
-        if (type == 'q' || type == 'r') {
-            pip = pip_face(P, pl, o, n, type == 'q' ? q : r);
-        } else if (type == 'p') {
-            pip = pip_face(P, pl, o, n, q);
-            if (!(pip == 'i' || pip == 'v' || pip == 'e')) pip = pip_face(P, pl, o, n, r);
-        } else if (type == '1') {
-            const double num = pl.d - dot3(q, pl.n);
-            const double rq[3] = { r[0] - q[0], r[1] - q[1], r[2] - q[2] };
-            const double den = dot3(rq, pl.n);
-            if (!(den == 0.0)) {
-                const double tt = num / den;
-                for (int k = 0; k < 3; ++k) pt[k] = q[k] + tt * (r[k] - q[k]);
+            const Test t = tests[i];
+            const int* tri = planes[plane_slot[t.g]].tri;
+            const int t0 = tri[0], t1 = tri[1], t2 = tri[2];
+            int8_t sq = 0, sr = 0;
+            char type = '0';
+            if (t0 >= 0) {
+                const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
+                double q[3], r[3], a[3], b[3], c[3];
+                load_xyz(P.X, t.q, q);
+                load_xyz(P.X, t.r, r);
+                load_xyz(P.X, face_vertex(P, o, n, t0), a);
+                load_xyz(P.X, face_vertex(P, o, n, t1), b);
+                load_xyz(P.X, face_vertex(P, o, n, t2), c);
+                int st0, st1;
+                sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
+                sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
+                esc[st0]++;
+                esc[st1]++;
+                if (sq == 0 && sr == 0) type = 'p';
+                else if (sq == 0) type = 'q';
+                else if (sr == 0) type = 'r';
+                else if ((sr < 0 && sq < 0) || (sr > 0 && sq > 0)) type = '0';
+                else type = '1';
             }
-            pip = pip_face(P, pl, o, n, pt);
-            rec = pip == 'i';
+            code = (uint32_t)(uint8_t)sq | ((uint32_t)(uint8_t)sr << 8) | ((uint32_t)(uint8_t)type << 16);
+            hit = type != '0';
+            if (!hit && keep_tests) reinterpret_cast<char4*>(test_info)[i] = make_char4(sq, sr, type, 0);
+            // the first hit on a triangle queues its projection matrix
+            if (hit && face_n(P, t.g) == 3) {
+                const uint32_t sl = plane_slot[t.g];
+                first_hit = atomicExch(&proj_flag[sl], 1u) == 0u;
+                slot = sl;
+            }
         }
-        const uint32_t p = P.face_pair[t.g] & ~kCutBit;
-        if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
-            || (type == '1' && (pip == 'v' || pip == 'e'))) {
-            if (!(*(volatile uint32_t*)&pair_status[p] & ST_GP)) atomicOr(&pair_status[p], ST_GP);
-        }
-        if (keep_tests) {
-            char4 info = make_char4(sq, sr, type, pip);
-            reinterpret_cast<char4*>(test_info)[i] = info;
-        }
-        }
-        const uint32_t pos = warp_append(&counters[2], rec);
-        if (rec) {
-            rec_key[pos] = ((unsigned long long)t.slot << 32) | t.g;
-            rec_val[pos] = (uint32_t)i;
-            rec_pt[(size_t)i * 3 + 0] = pt[0];
-            rec_pt[(size_t)i * 3 + 1] = pt[1];
-            rec_pt[(size_t)i * 3 + 2] = pt[2];
-        }
+        const uint32_t pos = warp_append(&counters[10], hit);
+        if (hit && pos < test_cap) hits[pos] = make_uint2((uint32_t)i, code);
+        const uint32_t k = warp_append(&counters[11], first_hit);
+        if (first_hit) proj_list[k] = slot;
     }
     for (int k = 0; k < 3; ++k) {
         uint32_t v = esc[k];
         for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd(&counters[5 + k], v);
+    }
+}
+
+// Projection matrices of the triangles that pass 1 queued (polygons got
+// theirs with the plane).
+__global__ void __launch_bounds__(kBlock) k_projections(FacePlane* __restrict__ planes,
+    const uint32_t* __restrict__ proj_list, const uint32_t* __restrict__ counters)
+{
+    const uint32_t n = counters[11];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        FacePlane& pl = planes[proj_list[k]];
+        const double nrm[3] = { pl.n[0], pl.n[1], pl.n[2] };
+        double Pm[6];
+        projection_matrix(nrm, pl.mc, Pm);
+        for (int j = 0; j < 6; ++j) pl.P[j] = Pm[j];
+    }
+}
+
+// Narrow phase, pass 2 (the hit list): segment-plane point
+// (compute_segment_plane_intersection, math.cpp:249-287), point-in-polygon
+// (math.cpp:851-902), general-position violations and records
+// (kernel.cpp:2456-2658).
+__global__ void __launch_bounds__(kBlock) k_narrow_hits(Problem P, const Test* __restrict__ tests,
+    const uint2* __restrict__ hits, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
+    const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
+    unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status)
+{
+    const uint64_t nh = min((uint64_t)counters[10], test_cap);
+    for (uint64_t h0 = blockIdx.x * (uint64_t)blockDim.x; h0 < nh; h0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = h0 + threadIdx.x;
+        bool rec = false;
+        Test t;
+        uint32_t i = 0;
+        double pt[3] = { 0.0, 0.0, 0.0 };
+        if (h < nh) {
+            const uint2 hv = hits[h];
+            i = hv.x;
+            const int8_t sq = (int8_t)(hv.y & 0xFFu), sr = (int8_t)((hv.y >> 8) & 0xFFu);
+            const char type = (char)((hv.y >> 16) & 0xFFu);
+            t = tests[i];
+            const FacePlane pl = planes[plane_slot[t.g]];
+            const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
+            const double* Pm = pl.P;
+            double q[3], r[3];
+            load_xyz(P.X, t.q, q);
+            load_xyz(P.X, t.r, r);
+            char pip = 0;
+            if (type == 'q' || type == 'r') {
+                pip = pip_face(P, Pm, o, n, type == 'q' ? q : r);
+            } else if (type == 'p') {
+                pip = pip_face(P, Pm, o, n, q);
+                if (!(pip == 'i' || pip == 'v' || pip == 'e')) pip = pip_face(P, Pm, o, n, r);
+            } else {
+                const double num = pl.d - dot3(q, pl.n);
+                const double rq[3] = { r[0] - q[0], r[1] - q[1], r[2] - q[2] };
+                const double den = dot3(rq, pl.n);
+                if (!(den == 0.0)) {
+                    const double tt = num / den;
+                    for (int k = 0; k < 3; ++k) pt[k] = q[k] + tt * (r[k] - q[k]);
+                }
+                pip = pip_face(P, Pm, o, n, pt);
+                rec = pip == 'i';
+            }
+            const uint32_t p = P.face_pair[t.g] & ~kCutBit;
+            if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
+                || (type == '1' && (pip == 'v' || pip == 'e'))) {
+                if (!(*(volatile uint32_t*)&pair_status[p] & ST_GP)) atomicOr(&pair_status[p], ST_GP);
+            }
+            if (keep_tests) reinterpret_cast<char4*>(test_info)[i] = make_char4(sq, sr, type, pip);
+        }
+        const uint32_t pos = warp_append(&counters[2], rec);
+        if (rec) {
+            rec_key[pos] = ((unsigned long long)t.slot << 32) | t.g;
+            rec_val[pos] = i;
+            rec_pt[(size_t)i * 3 + 0] = pt[0];
+            rec_pt[(size_t)i * 3 + 1] = pt[1];
+            rec_pt[(size_t)i * 3 + 2] = pt[2];
+        }
     }
 }
 
@@ -1364,6 +1429,60 @@ __global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const 
             if (mp < p) lo = mid + 1; else hi = mid;
         }
         rec_begin[p] = lo;
+    }
+}
+
+// Rank of every record key among all keys (keys are unique: one record per
+// (edge, face)). Block (x, y) compares its 256 records with key slice y,
+// staged in shared memory, and adds its counts into rank[] -- n^2 compares
+// spread over the whole GPU in one launch, cheaper than a multi-pass radix
+// sort for the few thousand records of a dispatch.
+constexpr int kRankChunk = 2048;
+__global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long long* __restrict__ key, uint32_t n,
+    uint32_t* __restrict__ rank)
+{
+    __shared__ unsigned long long sk[kRankChunk];
+    const uint32_t lo = blockIdx.y * kRankChunk, hi = min(n, lo + kRankChunk);
+    for (uint32_t j = lo + threadIdx.x; j < hi; j += kBlock) sk[j - lo] = key[j];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = key[i];
+    const int m = (int)(hi - lo);
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    int j = 0;
+    for (; j + 4 <= m; j += 4) {
+        c0 += sk[j] < k;
+        c1 += sk[j + 1] < k;
+        c2 += sk[j + 2] < k;
+        c3 += sk[j + 3] < k;
+    }
+    for (; j < m; ++j) c0 += sk[j] < k;
+    const uint32_t c = c0 + c1 + c2 + c3;
+    if (c) atomicAdd(&rank[i], c);
+}
+
+// records in rank order -> sorted keys and output arrays with per-pair local ids
+__global__ void __launch_bounds__(kBlock) k_scatter_records(Problem P, const unsigned long long* __restrict__ key,
+    const uint32_t* __restrict__ val, const uint32_t* __restrict__ rank, uint32_t nrec,
+    const Test* __restrict__ tests, const double* __restrict__ rec_pt, unsigned long long* __restrict__ skey,
+    uint32_t* __restrict__ rec_ids, double* __restrict__ rec_pts)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += gridDim.x * blockDim.x) {
+        const uint32_t r = rank[i];
+        const uint32_t ti = val[i];
+        skey[r] = key[i];
+        const Test t = tests[ti];
+        const uint32_t p = P.face_pair[t.g] & ~kCutBit;
+        const uint32_t vb = P.pair_vbase[p], fb = P.pair_fbase[p];
+        rec_ids[(size_t)r * 5 + 0] = t.q - vb;
+        rec_ids[(size_t)r * 5 + 1] = t.r - vb;
+        rec_ids[(size_t)r * 5 + 2] = t.g - fb;
+        rec_ids[(size_t)r * 5 + 3] = t.f0 - fb;
+        rec_ids[(size_t)r * 5 + 4] = t.f1 == kNone ? kNone : t.f1 - fb;
+        rec_pts[(size_t)r * 3 + 0] = rec_pt[(size_t)ti * 3 + 0];
+        rec_pts[(size_t)r * 3 + 1] = rec_pt[(size_t)ti * 3 + 1];
+        rec_pts[(size_t)r * 3 + 2] = rec_pt[(size_t)ti * 3 + 2];
     }
 }
 
@@ -1539,10 +1658,19 @@ void launch_tests(const Problem& P, Work& W, cudaStream_t s)
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
 {
     const int g = grid_for(W.test_cap);
-    g_launches++;
-    k_narrow<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
+    // the hit list lives in rec_key[1] (uint2 per test), free until the record sort
+    uint2* hits = reinterpret_cast<uint2*>(W.rec_key[1]);
+    g_launches += 3;
+    cudaMemsetAsync(W.proj_flag, 0, sizeof(uint32_t) * W.plane_cap, s);
+    k_narrow_signs<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
+        keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
+    k_projections<<<grid_for(W.plane_cap), kBlock, 0, s>>>((FacePlane*)W.planes, W.proj_list, W.counters);
+    k_narrow_hits<<<g, kBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status);
 }
+
+// records up to this many are ordered by k_rank_records (one launch)
+constexpr uint32_t kRankSortMax = 24576;
 
 int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
 {
@@ -1554,15 +1682,22 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
     const int sbits = nidx == 0xFFFFFFFFu ? 32 : 32 - __builtin_clz(nidx | 1u);
     const int gbits = 32 - __builtin_clz(P.nf | 1u);
     const int g = grid_for(nrec);
+    if (nrec <= kRankSortMax) {
+        // raw keys (slot << 32 | face) order like the packed ones
+        uint32_t* rank = W.rec_val[1];
+        cudaMemsetAsync(rank, 0, sizeof(uint32_t) * nrec, s);
+        g_launches += 3;
+        k_rank_records<<<dim3((nrec + kBlock - 1) / kBlock, (nrec + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
+            W.rec_key[0], nrec, rank);
+        k_scatter_records<<<g, kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, nrec, W.tests, W.rec_pt_raw,
+            W.rec_key[1], W.rec_ids, W.rec_pts);
+        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], nrec, 32, W.pair_nrec);
+        return 1;
+    }
     g_launches++;
     k_record_pack<<<g, kBlock, 0, s>>>(W.rec_key[0], nrec, gbits);
-    int buf = 0;
-    if (nrec <= kSmallSort && sbits + gbits <= 50) {
-        sort_small_pairs(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1], nrec, sbits + gbits, s);
-        buf = 1;
-    } else
-        buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1], nrec, 0,
-            sbits + gbits, W.sort_temp, s);
+    const int buf = radix_sort_pairs<unsigned long long>(W.rec_key[0], W.rec_val[0], W.rec_key[1], W.rec_val[1], nrec,
+        0, sbits + gbits, W.sort_temp, s);
     g_launches += 2;
     k_gather_records<<<g, kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids, W.rec_pts);
     k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);

@@ -80,11 +80,14 @@ struct Work {
     uint32_t* refit_flag;             // [ncl-1]
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
-                                      //        5..7 escalations, 8 traversal work cursor, 9 packets
+                                      //        5..7 escalations, 8 traversal work cursor, 9 packets, 10 narrow hits,
+                                      //        11 queued projections
     uint2* packets;                   // [ns] query packets: sorted source positions [x, y]
     uint8_t* cand;                    // [nf]
     uint32_t* plane_slot;             // [nf]
     void* planes;                     // FacePlane[cap]
+    uint32_t* proj_flag;              // [plane_cap] projection queued
+    uint32_t* proj_list;              // [plane_cap] plane slots whose projection is computed
     uint32_t* poly_list;              // [nf] faces with > 3 vertices among candidates
     uint8_t* vneed;                   // [nv]
     uint32_t* voff;                   // [nv+1]

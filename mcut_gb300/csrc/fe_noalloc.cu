@@ -88,7 +88,9 @@ constexpr size_t oRkey = oTinfo + al(4);
 constexpr size_t oRval = oRkey + al(2ull * kMaxTests * 8);
 constexpr size_t oRpt = oRval + al(2ull * kMaxTests * 4);
 constexpr size_t oPstat = oRpt + al(kMaxTests * 24ull);
-constexpr size_t kScratchBytes = oPstat + al(3 * 4);
+constexpr size_t oPflag = oPstat + al(3 * 4);
+constexpr size_t oPlist = oPflag + al(kMaxFaces * 4ull);
+constexpr size_t kScratchBytes = oPlist + al(kMaxFaces * 4ull);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -207,6 +209,8 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.plane_slot = reinterpret_cast<uint32_t*>(base + oPslot);
     W.planes = base + oPlanes;
     W.plane_cap = kMaxFaces;
+    W.proj_flag = reinterpret_cast<uint32_t*>(base + oPflag);
+    W.proj_list = reinterpret_cast<uint32_t*>(base + oPlist);
     W.poly_list = nullptr;
     W.vneed = base + oVneed;
     W.voff = reinterpret_cast<uint32_t*>(base + oVoff);

@@ -4,10 +4,12 @@
 //   upsweep  : per-tile digit histogram (shared-memory atomics)
 //   scan     : exclusive scan of the digit-major [256 x tiles] table (one CTA)
 //   downsweep: each warp ranks its keys with __match_any_sync in input order,
-//              warps are combined per digit in shared memory, keys scatter to
-//              their global rank.
+//              warps are combined per digit in shared memory, the tile is
+//              reordered by digit in shared memory and written out so that
+//              consecutive threads store consecutive slots of a digit's run.
 // A tile is 256 threads x 16 keys. Keys and values stream through HBM once
 // per launch; the histogram table stays in L2.
+#include <algorithm>
 #include <atomic>
 #include "fe_sort.cuh"
 
@@ -112,14 +114,27 @@ __global__ void __launch_bounds__(kThreads) k_digit_scan(uint32_t* __restrict__ 
     if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
+// Shared memory of the downsweep: the tile's keys and values in local
+// sorted order (reused for the per-warp digit counts before that).
+template <typename K>
+constexpr size_t downsweep_smem()
+{
+    return (size_t)kTile * (sizeof(K) + sizeof(uint32_t)) + 3 * kDigits * sizeof(uint32_t) + 2 * kWarps * 4;
+}
+
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
     K* __restrict__ okeys, uint32_t* __restrict__ ovals, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t tiles, const uint32_t* __restrict__ totals)
 {
-    __shared__ uint32_t wh[kWarps][kDigits];
-    __shared__ uint32_t goff[kDigits];
-    __shared__ uint32_t wsum[kWarps];
+    extern __shared__ __align__(16) unsigned char ds_smem[];
+    K* skeys = reinterpret_cast<K*>(ds_smem);                                // [kTile], after ranking
+    uint32_t* svals = reinterpret_cast<uint32_t*>(skeys + kTile);            // [kTile], after ranking
+    uint32_t (*wh)[kDigits] = reinterpret_cast<uint32_t (*)[kDigits]>(ds_smem); // [kWarps][kDigits], ranking only
+    uint32_t* goff = reinterpret_cast<uint32_t*>(svals + kTile);             // global offset of digit d's run
+    uint32_t* tstart = goff + kDigits;                                       // tile-local start of digit d
+    uint32_t* tcount = tstart + kDigits;
+    uint32_t* wsum = tcount + kDigits;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kWarps * kDigits; i += kThreads) (&wh[0][0])[i] = 0;
     {
@@ -137,8 +152,8 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ ke
         goff[threadIdx.x] = wpre + inc - v + hist[(size_t)threadIdx.x * tiles + blockIdx.x];
     }
     __syncthreads();
-
-    const size_t wbase = (size_t)blockIdx.x * kTile + (size_t)warp * 32 * kItems;
+    const size_t tbase = (size_t)blockIdx.x * kTile;
+    const size_t wbase = tbase + (size_t)warp * 32 * kItems;
     K k[kItems];
     uint32_t v[kItems], rank[kItems];
     const uint32_t lt = (1u << lane) - 1u;
@@ -164,25 +179,56 @@ __global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ ke
         rank[i] = prev + __popc(peers & lt);
     }
     __syncthreads();
-    // per digit: exclusive prefix across warps, plus the tile's global offset
-    for (int d = threadIdx.x; d < kDigits; d += kThreads) {
-        uint32_t run = goff[d];
+    // per digit: exclusive prefix across warps, and the digit's count in the tile
+    {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
         for (int w = 0; w < kWarps; ++w) {
             const uint32_t c = wh[w][d];
             wh[w][d] = run;
             run += c;
         }
+        tcount[d] = run;
+        // tile-local digit starts: exclusive scan of the counts over digits
+        uint32_t inc = run;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        __syncthreads();
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t wpre = 0;
+        for (int w = 0; w < warp; ++w) wpre += wsum[w];
+        tstart[d] = wpre + inc - run;
+    }
+    __syncthreads();
+    // tile-local sorted position of every key, then the keys go to shared
+    // memory in that order (over the digit counts, which are read first)
+    uint32_t pos[kItems];
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+        const uint32_t d = (uint32_t)(k[i] >> shift) & 0xFFu;
+        pos[i] = tstart[d] + wh[warp][d] + rank[i];
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
         const size_t idx = wbase + (size_t)i * 32 + lane;
         if (idx < n) {
-            const uint32_t d = (uint32_t)(k[i] >> shift) & 0xFFu;
-            const uint32_t dst = wh[warp][d] + rank[i];
-            okeys[dst] = k[i];
-            ovals[dst] = v[i];
+            skeys[pos[i]] = k[i];
+            svals[pos[i]] = v[i];
         }
+    }
+    __syncthreads();
+    // consecutive threads write consecutive slots of each digit's run
+    const uint32_t tn = (uint32_t)min((size_t)kTile, (size_t)n - tbase);
+    for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
+        const K key = skeys[j];
+        const uint32_t d = (uint32_t)(key >> shift) & 0xFFu;
+        const uint32_t dst = goff[d] + (j - tstart[d]);
+        okeys[dst] = key;
+        ovals[dst] = svals[j];
     }
 }
 } // namespace
@@ -277,6 +323,8 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
     uint32_t* temp, cudaStream_t s)
 {
     if (n == 0) return 0;
+    static std::atomic<unsigned long long> attr { 0 };
+    set_smem_once((const void*)k_downsweep<K>, (int)downsweep_smem<K>(), attr);
     const uint32_t tiles = (n + kTile - 1) / kTile;
     int cur = 0;
     K* kb[2] = { keys, keys_alt };
@@ -286,105 +334,11 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
         g_launches += 3;
         k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);
         k_digit_scan<<<kDigits, kThreads, 0, s>>>(temp, tiles, totals);
-        k_downsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n, shift, temp, tiles,
-            totals);
+        k_downsweep<K><<<tiles, kThreads, downsweep_smem<K>(), s>>>(kb[cur], vb[cur], kb[cur ^ 1], vb[cur ^ 1], n,
+            shift, temp, tiles, totals);
         cur ^= 1;
     }
     return cur;
-}
-
-// One-CTA LSD radix sort for small inputs (n <= kSmallSort): every pass runs
-// in shared memory, so the whole sort is one launch instead of three per
-// pass. Keys carry their input position in the low 14 bits (composite
-// uint64, so end_bit + 14 <= 64); 16 warps, warp w ranks its contiguous chunk
-// in rounds of 32 keys (stable), digit offsets come from a (digit, warp) scan.
-constexpr int kSmallThreads = 512;
-constexpr int kSmallWarps = kSmallThreads / 32;
-constexpr int kSmallIdxBits = 14;
-
-__global__ void __launch_bounds__(kSmallThreads) k_sort_small(const unsigned long long* __restrict__ keys_in,
-    const uint32_t* __restrict__ vals_in, unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-    uint32_t n, int end_bit)
-{
-    extern __shared__ __align__(16) unsigned char sm[];
-    unsigned long long* kb[2] = { reinterpret_cast<unsigned long long*>(sm),
-        reinterpret_cast<unsigned long long*>(sm) + kSmallSort };
-    uint32_t (*wh)[kDigits] = reinterpret_cast<uint32_t (*)[kDigits]>(kb[1] + kSmallSort);
-    uint32_t* dbase = reinterpret_cast<uint32_t*>(wh + kSmallWarps);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
-    for (uint32_t i = threadIdx.x; i < n; i += kSmallThreads) kb[0][i] = (keys_in[i] << kSmallIdxBits) | i;
-    const uint32_t chunk = ((n + kSmallWarps - 1) / kSmallWarps + 31) & ~31u;
-    int cur = 0;
-    for (int shift = kSmallIdxBits; shift < end_bit + kSmallIdxBits; shift += 8) {
-        for (int i = threadIdx.x; i < kSmallWarps * kDigits; i += kSmallThreads) (&wh[0][0])[i] = 0;
-        __syncthreads();
-        uint32_t rank[kSmallSort / kSmallWarps / 32];
-        const uint32_t lo = w * chunk;
-        for (uint32_t r = 0; r * 32 < chunk; ++r) {
-            const uint32_t idx = lo + r * 32 + lane;
-            const bool ok = idx < n;
-            const uint32_t d = ok ? (uint32_t)(kb[cur][idx] >> shift) & 0xFFu : 0x100u;
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-            uint32_t prev = 0;
-            if (ok) prev = wh[w][d];
-            __syncwarp();
-            if (ok && (peers & lt) == 0) wh[w][d] = prev + __popc(peers);
-            __syncwarp();
-            rank[r] = prev + __popc(peers & lt);
-        }
-        __syncthreads();
-        if (threadIdx.x < kDigits) {
-            const int d = threadIdx.x;
-            uint32_t run = 0;
-            for (int k = 0; k < kSmallWarps; ++k) {
-                const uint32_t c = wh[k][d];
-                wh[k][d] = run;
-                run += c;
-            }
-            dbase[d] = run;
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            // exclusive scan of the 256 digit totals by one warp (8 per lane)
-            uint32_t v[8], sum = 0;
-            for (int k = 0; k < 8; ++k) { v[k] = dbase[lane * 8 + k]; sum += v[k]; }
-            uint32_t inc = sum;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                if (lane >= o) inc += t;
-            }
-            uint32_t run = inc - sum;
-            for (int k = 0; k < 8; ++k) { dbase[lane * 8 + k] = run; run += v[k]; }
-        }
-        __syncthreads();
-        for (uint32_t r = 0; r * 32 < chunk; ++r) {
-            const uint32_t idx = lo + r * 32 + lane;
-            if (idx < n) {
-                const unsigned long long k = kb[cur][idx];
-                const uint32_t d = (uint32_t)(k >> shift) & 0xFFu;
-                kb[cur ^ 1][dbase[d] + wh[w][d] + rank[r]] = k;
-            }
-        }
-        __syncthreads();
-        cur ^= 1;
-    }
-    for (uint32_t i = threadIdx.x; i < n; i += kSmallThreads) {
-        const unsigned long long c = kb[cur][i];
-        keys_out[i] = c >> kSmallIdxBits;
-        vals_out[i] = vals_in[c & ((1u << kSmallIdxBits) - 1u)];
-    }
-}
-
-size_t sort_small_smem() { return (size_t)kSmallSort * 16 + (size_t)kSmallWarps * kDigits * 4 + kDigits * 4; }
-
-void sort_small_pairs(const unsigned long long* keys_in, const uint32_t* vals_in, unsigned long long* keys_out,
-    uint32_t* vals_out, uint32_t n, int end_bit, cudaStream_t s)
-{
-    static std::atomic<unsigned long long> attr { 0 };
-    set_smem_once((const void*)k_sort_small, (int)sort_small_smem(), attr);
-    g_launches++;
-    k_sort_small<<<1, kSmallThreads, sort_small_smem(), s>>>(keys_in, vals_in, keys_out, vals_out, n, end_bit);
 }
 
 template int radix_sort_pairs<uint32_t>(uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t, int, int, uint32_t*,

@@ -21,12 +21,6 @@ template <typename K>
 int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
     uint32_t* temp, cudaStream_t s);
 
-// Sort of n <= kSmallSort (uint64 key, uint32 value) pairs by key bits
-// [0, end_bit) (end_bit <= 50) into (keys_out, vals_out), in one CTA (one launch).
-constexpr uint32_t kSmallSort = 12288;
-void sort_small_pairs(const unsigned long long* keys_in, const uint32_t* vals_in, unsigned long long* keys_out,
-    uint32_t* vals_out, uint32_t n, int end_bit, cudaStream_t s);
-
 // In-place exclusive scan of n uint32 (n+1-th element receives the total if
 // total_out != nullptr). temp: scan_temp_bytes(n).
 size_t scan_temp_bytes(uint32_t n);
