@@ -93,7 +93,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -623,19 +623,18 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.fbox32 = c->buf[B_LKB].get<float>(L.nf * 6);
     W.mesh_box = c->buf[B_MESHBOX].get<unsigned long long>((size_t)n * 12);
     const size_t ksz = wide ? 8 : 4;
-    W.skeys[0] = c->buf[B_SK0].get<uint8_t>(L.ns * ksz);
-    W.skeys[1] = c->buf[B_SK1].get<uint8_t>(L.ns * ksz);
-    W.svals[0] = c->buf[B_SV0].get<uint32_t>(L.ns);
-    W.svals[1] = c->buf[B_SV1].get<uint32_t>(L.ns);
-    W.ckeys[0] = c->buf[B_CK0].get<uint8_t>(L.nc * ksz);
-    W.ckeys[1] = c->buf[B_CK1].get<uint8_t>(L.nc * ksz);
-    W.cvals[0] = c->buf[B_CV0].get<uint32_t>(L.nc);
-    W.cvals[1] = c->buf[B_CV1].get<uint32_t>(L.nc);
+    for (int b = 0; b < 2; ++b) {
+        W.skeys[b] = c->buf[b ? B_SK1 : B_SK0].get<uint8_t>((L.ns + L.nc) * ksz);
+        W.svals[b] = c->buf[b ? B_SV1 : B_SV0].get<uint32_t>(L.ns + L.nc);
+        W.ckeys[b] = static_cast<uint8_t*>(W.skeys[b]) + L.ns * ksz;
+        W.cvals[b] = W.svals[b] + L.ns;
+    }
     W.cl_key = c->buf[B_CLKEY].get<uint8_t>(L.ncl * ksz);
     W.cl_start = c->buf[B_CLSTART].get<uint32_t>(L.ncl);
     W.cl_n = c->buf[B_CLN].get<uint8_t>(L.ncl);
     W.leaf_key_box = nullptr;
     W.packets = c->buf[B_PACKETS].get<uint2>(L.ns);
+    W.top = c->buf[B_TOP].get<uint8_t>(64 * 32);
     W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
     W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));
     W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
@@ -648,7 +647,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
 
-    W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(radix_sort_temp_bytes((uint32_t)std::max(L.ns, L.nc)) / 4 + 64);
+    W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(radix_sort_temp_bytes((uint32_t)(L.ns + L.nc)) / 4 + 64);
     W.traversal = c->tune.traversal;
     W.packet_faces = c->tune.packet_faces;
     W.stack_depth = c->tune.stack_depth;
@@ -664,7 +663,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
         ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
         ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
-        launch_bounds_morton(P, W, wide, s);
+        launch_bounds_morton(P, W, wide, key_bits, s);
         rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
         rec(c, 2 * MCGPU_STAGE_SORT);
         aux[0] = launch_sort(P, W, wide, key_bits, s, aux[1]);
@@ -733,7 +732,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.rec_val[1] = c->buf[B_RV1].get<uint32_t>(W.test_cap);
     W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
     W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
-        radix_sort_temp_bytes((uint32_t)std::max<uint64_t>({ L.ns, L.nc, W.test_cap })) / 4 + 64);
+        radix_sort_temp_bytes((uint32_t)std::max<uint64_t>(L.ns + L.nc, W.test_cap)) / 4 + 64);
     const uint32_t keep = flags & MCGPU_KEEP_TESTS;
     run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) {
         rec(c, 2 * MCGPU_STAGE_ADJACENCY);
@@ -763,8 +762,13 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     });
     c->rec_buf = c->graphs[2].aux[0];
     // per-pair record ranges (first sorted record of each pair, then the total)
-    ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
-        "D2H ranges");
+    if (n > 1)
+        ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
+            "D2H ranges");
+    else {
+        hc[16 + 2] = 0;
+        hc[16 + 3] = (uint32_t)c->n_records;
+    }
     ck(cudaStreamSynchronize(s), "sync records");
     ck(cudaGetLastError(), "kernel launch");
 

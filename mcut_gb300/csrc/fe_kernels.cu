@@ -169,7 +169,7 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v)
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __restrict__ fbox,
     const unsigned long long* __restrict__ mesh_box, K* __restrict__ skey, uint32_t* __restrict__ sval,
-    K* __restrict__ ckey, uint32_t* __restrict__ cval)
+    K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit)
 {
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         const uint32_t fp = P.face_pair[f];
@@ -191,11 +191,13 @@ __global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __re
             if (den > 0) {
                 const int sh = max(0, 64 - __clzll((long long)den) - 20); // den >> sh < 2^20
                 const uint32_t d32 = (uint32_t)(den >> sh), n32 = (uint32_t)min(num >> sh, (unsigned long long)d32);
-                q = d32 ? (uint32_t)(((unsigned long long)n32 * 1023ull) / d32) : 0u;
+                // any monotone quantisation will do (the order only shapes the tree)
+                q = d32 ? (uint32_t)__fmul_rz(__uint2float_rz(n32), __fdiv_rz(1023.0f, __uint2float_rz(d32))) : 0u;
             }
             c[j] = expand_bits(min(q, 1023u));
         }
-        const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]);
+        // the mesh bit puts every source key before every cut key: one sort orders both meshes
+        const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]) | ((K)(is_cut ? 1 : 0) << mesh_bit);
         const uint32_t local = f - P.pair_fbase[p];
         if (is_cut) {
             const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);
@@ -537,7 +539,16 @@ __global__ void __launch_bounds__(kBlock) k_traverse_packet(Problem P, const dou
 // frontier or queue overflow flags the pair for the per-thread deep re-run.
 // ---------------------------------------------------------------------------
 constexpr int kWaveFrontier = 256;
-constexpr int kWaveLeaves = 64;
+#ifndef MCGPU_WAVE_LEAVES
+#define MCGPU_WAVE_LEAVES 64
+#endif
+#ifndef MCGPU_WAVE_OUT
+#define MCGPU_WAVE_OUT 96
+#endif
+#ifndef MCGPU_TOP_DEPTH
+#define MCGPU_TOP_DEPTH 6
+#endif
+constexpr int kWaveLeaves = MCGPU_WAVE_LEAVES;
 constexpr int kWaveWarps = kBlock / 32;
 
 struct WaveLeaf {
@@ -546,6 +557,59 @@ struct WaveLeaf {
     uint32_t pr;
 };
 
+// The top of the cut tree is the same for every packet: the tree cut at
+// depth kTopDepth (internal nodes at that depth, shallower leaves) is listed
+// once per dispatch with each entry's box, and every packet's walk starts by
+// testing that list -- kTopDepth fewer dependent levels per packet.
+constexpr int kTopDepth = MCGPU_TOP_DEPTH;
+constexpr int kTopMax = 1 << kTopDepth;
+struct WaveTop {
+    float lo[3], hi[3];
+    int id;       // >= 0 internal node, < 0 ~leaf
+    uint32_t pr;  // pair range lo | hi << 16
+};
+static_assert(sizeof(WaveTop) == 32, "the top-cut buffer holds 64 entries of 32 bytes");
+
+__global__ void __launch_bounds__(32) k_top_cut(const Node* __restrict__ nodes, int nleaf, WaveTop* __restrict__ top,
+    uint32_t* __restrict__ counters)
+{
+    __shared__ int cur[kTopMax], nxt[kTopMax];
+    __shared__ int ncur, nnxt, ntop;
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+        cur[0] = 0;
+        ncur = nleaf > 1 ? 1 : 0;
+        ntop = 0;
+    }
+    __syncwarp();
+    for (int depth = 1; depth <= kTopDepth && ncur > 0; ++depth) {
+        if (lane == 0) nnxt = 0;
+        __syncwarp();
+        for (int i = lane; i < ncur; i += 32) {
+            const Node nd = nodes[cur[i]];
+            const float* b = reinterpret_cast<const float*>(&nd.b0);
+            for (int k = 0; k < 2; ++k) {
+                const int c = nd.child[k];
+                if (c >= 0 && depth < kTopDepth) {
+                    nxt[atomicAdd(&nnxt, 1)] = c;
+                } else {
+                    WaveTop e;
+                    for (int j = 0; j < 3; ++j) { e.lo[j] = b[k * 6 + j]; e.hi[j] = b[k * 6 + 3 + j]; }
+                    e.id = c;
+                    e.pr = nd.prange[k];
+                    top[atomicAdd(&ntop, 1)] = e;
+                }
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < nnxt; i += 32) cur[i] = nxt[i];
+        __syncwarp();
+        if (lane == 0) ncur = nnxt;
+        __syncwarp();
+    }
+    if (lane == 0) counters[13] = (uint32_t)ntop;
+}
+
 // Output goes through a per-warp staging buffer in shared memory and reaches
 // the global pair list in blocks of up to kWaveOut pairs (one atomic each).
 //
@@ -553,7 +617,7 @@ struct WaveLeaf {
 // and tests every query of the packet (kept in shared memory) against it, so
 // a packet that reaches hundreds of leaves pays a few rounds of parallel
 // loads instead of hundreds of dependent ones.
-constexpr int kWaveOut = 224;
+constexpr int kWaveOut = MCGPU_WAVE_OUT;
 
 struct WaveWarp {
     int front[2][kWaveFrontier];
@@ -570,7 +634,7 @@ constexpr size_t kWaveSmem = sizeof(WaveWarp) * kWaveWarps;
 
 __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const double* __restrict__ fbox,
     const uint32_t* __restrict__ qface, const uint2* __restrict__ packets, const uint32_t* __restrict__ leaf_face,
-    const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const long long* __restrict__ leaf_key_box,
+    const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const WaveTop* __restrict__ top,
     int nleaf, const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
     uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
 {
@@ -654,9 +718,17 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                         mask |= (ov ? 1u : 0u) << j;
                     }
                     if (mask) {
-                        const uint32_t s0 = __ldg(&cl_start[L.id]), cn = __ldg(&cl_n[L.id]);
-                        for (uint32_t u = 0; u < cn; ++u) {
-                            const uint32_t cf = __ldg(&leaf_face[s0 + u]);
+                        // the cluster's faces: first position from the pair tables (as
+                        // k_clusters lays clusters out), face ids loaded four at a time
+                        const uint32_t lp = L.pr & 0xFFFFu;
+                        const uint32_t s0 = P.pair_cbase[lp] + ((uint32_t)L.id - P.pair_clbase[lp]) * P.leaf_size;
+                        const uint32_t cn = min(P.leaf_size, P.pair_cbase[lp + 1] - s0);
+                        for (uint32_t u0 = 0; u0 < cn; u0 += 4) {
+                            uint32_t cfs[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) cfs[u] = u0 + u < cn ? __ldg(&leaf_face[s0 + u0 + u]) : 0u;
+                        for (uint32_t u = 0; u < 4 && u0 + u < cn; ++u) {
+                            const uint32_t cf = cfs[u];
                             longlong2 ka, kb, kc;
                             load_key_box(fbox, cf, ka, kb, kc);
                             bool any_cf = false;
@@ -679,6 +751,7 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                             }
                             if (any_cf) cand[cf] = 1;
                         }
+                        }
                     }
                 }
                 __syncwarp();
@@ -697,8 +770,40 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
             nl = 1;
             drain();
         } else {
-            int cur = 0, nf = 1;
-            if (lane == 0) W.front[0][0] = 0;
+            int cur = 0, nf = 0;
+            // first wave: the listed top cut of the tree
+            const int ntop = (int)counters[13];
+            for (int base = 0; base < ntop; base += 32) {
+                const int i = base + lane;
+                bool hit = false;
+                int ch = 0;
+                float bx[6];
+                uint32_t prr = 0;
+                if (i < ntop) {
+                    const WaveTop e = top[i];
+                    ch = e.id;
+                    prr = e.pr;
+                    for (int j = 0; j < 3; ++j) { bx[j] = e.lo[j]; bx[3 + j] = e.hi[j]; }
+                    hit = (prr & 0xFFFFu) <= pmax && pmin <= (prr >> 16) && ul[0] <= bx[3] && uh[0] >= bx[0]
+                        && ul[1] <= bx[4] && uh[1] >= bx[1] && ul[2] <= bx[5] && uh[2] >= bx[2];
+                }
+                const bool inner = hit && ch >= 0, leaf = hit && ch < 0;
+                const unsigned mi = __ballot_sync(full, inner), ml = __ballot_sync(full, leaf);
+                if (nf + __popc(mi) > kWaveFrontier) {
+                    overflow = true;
+                } else {
+                    if (inner) W.front[0][nf + __popc(mi & lt)] = ch;
+                    nf += __popc(mi);
+                }
+                if (nl + __popc(ml) > kWaveLeaves) drain();
+                if (leaf) {
+                    WaveLeaf& L = W.leaves[nl + __popc(ml & lt)];
+                    for (int j = 0; j < 3; ++j) { L.lo[j] = bx[j]; L.hi[j] = bx[3 + j]; }
+                    L.id = ~ch;
+                    L.pr = prr;
+                }
+                nl += __popc(ml);
+            }
             __syncwarp();
             while (nf > 0) {
                 int nn = 0;
@@ -1526,7 +1631,7 @@ int grid_for(uint64_t n)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_bounds_morton(const Problem& P, Work& W, bool wide, cudaStream_t s)
+void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
     g_launches++;
@@ -1534,27 +1639,26 @@ void launch_bounds_morton(const Problem& P, Work& W, bool wide, cudaStream_t s)
     g_launches++;
     if (wide)
         k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box,
-            (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0]);
+            (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits);
     else
         k_morton<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, (uint32_t*)W.skeys[0], W.svals[0],
-            (uint32_t*)W.ckeys[0], W.cvals[0]);
+            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits);
 }
 
 int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)
 {
-    int src_buf;
-    if (wide) {
-        src_buf = radix_sort_pairs<unsigned long long>((unsigned long long*)W.skeys[0], W.svals[0],
-            (unsigned long long*)W.skeys[1], W.svals[1], P.ns, 0, key_bits, W.sort_temp, s);
-        cut_buf = radix_sort_pairs<unsigned long long>((unsigned long long*)W.ckeys[0], W.cvals[0],
-            (unsigned long long*)W.ckeys[1], W.cvals[1], P.nc, 0, key_bits, W.sort_temp, s);
-    } else {
-        src_buf = radix_sort_pairs<uint32_t>((uint32_t*)W.skeys[0], W.svals[0], (uint32_t*)W.skeys[1], W.svals[1],
-            P.ns, 0, key_bits, W.sort_temp, s);
-        cut_buf = radix_sort_pairs<uint32_t>((uint32_t*)W.ckeys[0], W.cvals[0], (uint32_t*)W.ckeys[1], W.cvals[1],
-            P.nc, 0, key_bits, W.sort_temp, s);
-    }
-    return src_buf;
+    // source and cut keys sit back to back (ckeys[b] == skeys[b] + ns) and the
+    // mesh bit above the key orders them apart: one sort for both meshes
+    const uint32_t n = P.ns + P.nc;
+    int buf;
+    if (wide)
+        buf = radix_sort_pairs<unsigned long long>((unsigned long long*)W.skeys[0], W.svals[0],
+            (unsigned long long*)W.skeys[1], W.svals[1], n, 0, key_bits + 1, W.sort_temp, s);
+    else
+        buf = radix_sort_pairs<uint32_t>((uint32_t*)W.skeys[0], W.svals[0], (uint32_t*)W.skeys[1], W.svals[1], n, 0,
+            key_bits + 1, W.sort_temp, s);
+    cut_buf = buf;
+    return buf;
 }
 
 void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStream_t s)
@@ -1620,9 +1724,12 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
     else {
         static std::atomic<unsigned long long> attr { 0 };
         set_smem_once((const void*)k_traverse_wave, (int)kWaveSmem, attr);
+        WaveTop* top = reinterpret_cast<WaveTop*>(W.top);
+        g_launches++;
+        k_top_cut<<<1, 32, 0, s>>>(W.nodes, (int)P.ncl, top, W.counters);
         k_traverse_wave<<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
-            W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
-            W.counters, W.cand, W.pair_status);
+            W.cvals[cut_buf], W.cl_start, W.cl_n, top, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand,
+            W.pair_status);
     }
 }
 
@@ -1669,7 +1776,8 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
         keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status);
 }
 
-// records up to this many are ordered by k_rank_records (one launch)
+// Records up to this many are ordered by k_rank_records (one launch). With
+// one pair W.pair_nrec is left alone: that pair owns records [0, nrec).
 constexpr uint32_t kRankSortMax = 24576;
 
 int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
@@ -1686,12 +1794,15 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
         // raw keys (slot << 32 | face) order like the packed ones
         uint32_t* rank = W.rec_val[1];
         cudaMemsetAsync(rank, 0, sizeof(uint32_t) * nrec, s);
-        g_launches += 3;
+        g_launches += 2;
         k_rank_records<<<dim3((nrec + kBlock - 1) / kBlock, (nrec + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
             W.rec_key[0], nrec, rank);
         k_scatter_records<<<g, kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, nrec, W.tests, W.rec_pt_raw,
             W.rec_key[1], W.rec_ids, W.rec_pts);
-        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], nrec, 32, W.pair_nrec);
+        if (P.n_pairs > 1) { // one pair owns every record (the caller knows the range)
+            g_launches++;
+            k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], nrec, 32, W.pair_nrec);
+        }
         return 1;
     }
     g_launches++;
@@ -1700,7 +1811,10 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
         0, sbits + gbits, W.sort_temp, s);
     g_launches += 2;
     k_gather_records<<<g, kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids, W.rec_pts);
-    k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);
+    if (P.n_pairs > 1)
+        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);
+    else
+        g_launches--;
     return buf;
 }
 

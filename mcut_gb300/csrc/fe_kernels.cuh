@@ -65,7 +65,8 @@ struct Work {
     double* fbox;                     // [nf*6]
     float* fbox32;                    // [nf*6] the same boxes rounded outward to fp32
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
-    // sort buffers (keys u32 for one pair, u64 for batches)
+    // sort buffers (keys u32 for one pair, u64 for batches); the cut keys and
+    // values follow the source ones in the same arrays (ckeys[b] = skeys[b] + ns)
     void* skeys[2];                   // source-face keys
     uint32_t* svals[2];
     void* ckeys[2];                   // cut-face keys
@@ -75,13 +76,14 @@ struct Work {
     uint32_t* cl_start;               // [ncl] first sorted position of the cluster
     uint8_t* cl_n;                    // [ncl] faces in the cluster
     long long* leaf_key_box;          // unused (kept null)
+    void* top;                        // [64] top cut of the cut tree (WaveTop, 32 B each)
     Node* nodes;                      // [ncl-1]
     int32_t* parent;                  // [2ncl-1]
     uint32_t* refit_flag;             // [ncl-1]
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
                                       //        5..7 escalations, 8 traversal work cursor, 9 packets, 10 narrow hits,
-                                      //        11 queued projections
+                                      //        11 queued projections, 13 top-cut entries
     uint2* packets;                   // [ns] query packets: sorted source positions [x, y]
     uint8_t* cand;                    // [nf]
     uint32_t* plane_slot;             // [nf]
@@ -115,7 +117,7 @@ struct Work {
 };
 
 // stage launchers (all asynchronous on `s`)
-void launch_bounds_morton(const Problem& P, Work& W, bool wide_keys, cudaStream_t s);
+void launch_bounds_morton(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s);
 int launch_sort(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s, int& cut_buf);
 void launch_hierarchy(const Problem& P, Work& W, bool wide_keys, int cut_buf, cudaStream_t s);
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s);

@@ -90,7 +90,8 @@ constexpr size_t oRpt = oRval + al(2ull * kMaxTests * 4);
 constexpr size_t oPstat = oRpt + al(kMaxTests * 24ull);
 constexpr size_t oPflag = oPstat + al(3 * 4);
 constexpr size_t oPlist = oPflag + al(kMaxFaces * 4ull);
-constexpr size_t kScratchBytes = oPlist + al(kMaxFaces * 4ull);
+constexpr size_t oTop = oPlist + al(kMaxFaces * 4ull);
+constexpr size_t kScratchBytes = oTop + al(64 * 32);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -184,14 +185,15 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.fbox = reinterpret_cast<double*>(base + oFbox);
     W.mesh_box = reinterpret_cast<unsigned long long*>(base + oMbox);
     uint32_t* keys = reinterpret_cast<uint32_t*>(base + oKeys);
+    // source then cut keys in one array per buffer (one sort orders both meshes)
     W.skeys[0] = keys;
     W.skeys[1] = keys + kMaxFaces;
     W.svals[0] = keys + 2 * kMaxFaces;
     W.svals[1] = keys + 3 * kMaxFaces;
-    W.ckeys[0] = keys + 4 * kMaxFaces;
-    W.ckeys[1] = keys + 5 * kMaxFaces;
-    W.cvals[0] = keys + 6 * kMaxFaces;
-    W.cvals[1] = keys + 7 * kMaxFaces;
+    W.ckeys[0] = keys + Fs;
+    W.ckeys[1] = keys + kMaxFaces + Fs;
+    W.cvals[0] = keys + 2 * kMaxFaces + Fs;
+    W.cvals[1] = keys + 3 * kMaxFaces + Fs;
     W.sort_temp = reinterpret_cast<uint32_t*>(base + oSortTmp);
     W.cl_key = base + oClKey;
     W.cl_start = reinterpret_cast<uint32_t*>(base + oClStart);
@@ -211,6 +213,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.plane_cap = kMaxFaces;
     W.proj_flag = reinterpret_cast<uint32_t*>(base + oPflag);
     W.proj_list = reinterpret_cast<uint32_t*>(base + oPlist);
+    W.top = base + oTop;
     W.poly_list = nullptr;
     W.vneed = base + oVneed;
     W.voff = reinterpret_cast<uint32_t*>(base + oVoff);
@@ -250,7 +253,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
         (uint32_t)nf, reinterpret_cast<uint32_t*>(base + oFidx), reinterpret_cast<uint32_t*>(base + oFpair),
         W.mesh_box);
 
-    launch_bounds_morton(P, W, false, s);
+    launch_bounds_morton(P, W, false, kMortonBits, s);
     int cut_buf = 0;
     const int src_buf = launch_sort(P, W, false, kMortonBits, s, cut_buf);
     launch_hierarchy(P, W, false, cut_buf, s);
