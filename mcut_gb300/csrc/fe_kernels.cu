@@ -167,34 +167,27 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v)
 // Morton code of the box centre in its mesh's box (morton3D, bvh.cpp:196-217),
 // written to the source-face or cut-face key list.
 template <typename K>
-__global__ void __launch_bounds__(kBlock) k_morton(Problem P, const double* __restrict__ fbox,
+__global__ void __launch_bounds__(kBlock) k_morton(Problem P, const float* __restrict__ fbox32,
     const unsigned long long* __restrict__ mesh_box, K* __restrict__ skey, uint32_t* __restrict__ sval,
     K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit)
 {
+    // The code only orders leaves (any order gives the same pair set), so it
+    // is formed in fp32 from the outward-rounded face boxes: centre relative
+    // to the mesh box, quantised to 10 bits per axis.
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         const uint32_t fp = P.face_pair[f];
         const uint32_t p = fp & ~kCutBit;
         const bool is_cut = (fp & kCutBit) != 0;
-        const Box b = load_box(fbox, f);
+        const float2* bp = reinterpret_cast<const float2*>(fbox32 + (size_t)f * 6);
+        const float2 x = __ldg(bp), y = __ldg(bp + 1), z = __ldg(bp + 2);
+        const float lo[3] = { x.x, x.y, y.x }, hi[3] = { y.y, z.x, z.y };
         const unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
-        // The code only orders leaves (any order gives the same pair set), so
-        // it is formed on the integer pipe: positions are dkey() integers,
-        // monotone in the coordinate (piecewise linear within each binade),
-        // quantised to 10 bits per axis.
         uint32_t c[3];
         for (int j = 0; j < 3; ++j) {
-            const long long lo = dkey(of_ord(mb[j])), hi = dkey(of_ord(mb[3 + j]));
-            const long long mid = (dkey(b.mn[j]) >> 1) + (dkey(b.mx[j]) >> 1);
-            const unsigned long long den = (unsigned long long)(hi - lo);
-            const unsigned long long num = mid > lo ? (unsigned long long)(mid - lo) : 0ull;
-            uint32_t q = 0;
-            if (den > 0) {
-                const int sh = max(0, 64 - __clzll((long long)den) - 20); // den >> sh < 2^20
-                const uint32_t d32 = (uint32_t)(den >> sh), n32 = (uint32_t)min(num >> sh, (unsigned long long)d32);
-                // any monotone quantisation will do (the order only shapes the tree)
-                q = d32 ? (uint32_t)__fmul_rz(__uint2float_rz(n32), __fdiv_rz(1023.0f, __uint2float_rz(d32))) : 0u;
-            }
-            c[j] = expand_bits(min(q, 1023u));
+            const float mlo = f32_rd(of_ord(__ldg(&mb[j]))), mhi = f32_ru(of_ord(__ldg(&mb[3 + j])));
+            const float ext = mhi - mlo;
+            const float t = ext > 0.0f ? (0.5f * (lo[j] + hi[j]) - mlo) * __fdiv_rn(1023.0f, ext) : 0.0f;
+            c[j] = expand_bits((uint32_t)fminf(fmaxf(t, 0.0f), 1023.0f));
         }
         // the mesh bit puts every source key before every cut key: one sort orders both meshes
         const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]) | ((K)(is_cut ? 1 : 0) << mesh_bit);
@@ -719,24 +712,41 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                     }
                     if (mask) {
                         // the cluster's faces: first position from the pair tables (as
-                        // k_clusters lays clusters out), face ids loaded four at a time
+                        // k_clusters lays clusters out). Their exact boxes are tested
+                        // first with no stores in the loop, the next face's box loading
+                        // while the current one is tested; pairs are emitted after.
                         const uint32_t lp = L.pr & 0xFFFFu;
                         const uint32_t s0 = P.pair_cbase[lp] + ((uint32_t)L.id - P.pair_clbase[lp]) * P.leaf_size;
                         const uint32_t cn = min(P.leaf_size, P.pair_cbase[lp + 1] - s0);
                         for (uint32_t u0 = 0; u0 < cn; u0 += 4) {
+                            const uint32_t m = min(4u, cn - u0);
                             uint32_t cfs[4];
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) cfs[u] = u0 + u < cn ? __ldg(&leaf_face[s0 + u0 + u]) : 0u;
-                        for (uint32_t u = 0; u < 4 && u0 + u < cn; ++u) {
-                            const uint32_t cf = cfs[u];
-                            longlong2 ka, kb, kc;
-                            load_key_box(fbox, cf, ka, kb, kc);
-                            bool any_cf = false;
-                            for (unsigned mm = mask; mm; mm &= mm - 1) {
-                                const int j = __ffs(mm) - 1;
-                                const long long* q = W.qk[j];
-                                if (q[0] <= kb.y && q[3] >= ka.x && q[1] <= kc.x && q[4] >= ka.y && q[2] <= kc.y
-                                    && q[5] >= kb.x) {
+                            for (int u = 0; u < 4; ++u) cfs[u] = (uint32_t)u < m ? __ldg(&leaf_face[s0 + u0 + u]) : 0u;
+                            unsigned hits[4] = { 0u, 0u, 0u, 0u };
+                            longlong2 na, nb, nc;
+                            load_key_box(fbox, cfs[0], na, nb, nc);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                if ((uint32_t)u >= m) break;
+                                const longlong2 ka = na, kb = nb, kc = nc;
+                                if ((uint32_t)u + 1 < m) load_key_box(fbox, cfs[u + 1], na, nb, nc);
+                                unsigned h = 0;
+                                for (unsigned mm = mask; mm; mm &= mm - 1) {
+                                    const int j = __ffs(mm) - 1;
+                                    const long long* q = W.qk[j];
+                                    if (q[0] <= kb.y && q[3] >= ka.x && q[1] <= kc.x && q[4] >= ka.y && q[2] <= kc.y
+                                        && q[5] >= kb.x)
+                                        h |= 1u << j;
+                                }
+                                hits[u] = h;
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                if (!hits[u]) continue;
+                                const uint32_t cf = cfs[u];
+                                for (unsigned mm = hits[u]; mm; mm &= mm - 1) {
+                                    const int j = __ffs(mm) - 1;
                                     const unsigned long long pr = ((unsigned long long)W.qs[j] << 32) | cf;
                                     const int pos = atomicAdd(&W.nout, 1);
                                     if (pos < kWaveOut + 32) {
@@ -745,12 +755,10 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                                         const uint32_t g = atomicAdd(&counters[0], 1u);
                                         if (g < cap) pairs[g] = pr;
                                     }
-                                    atomicOr(&W.qhit, 1u << j);
-                                    any_cf = true;
                                 }
+                                atomicOr(&W.qhit, hits[u]);
+                                cand[cf] = 1;
                             }
-                            if (any_cf) cand[cf] = 1;
-                        }
                         }
                     }
                 }
@@ -1638,10 +1646,10 @@ void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cu
     k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, W.mesh_box, W.pair_status);
     g_launches++;
     if (wide)
-        k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box,
+        k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox32, W.mesh_box,
             (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits);
     else
-        k_morton<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.mesh_box, (uint32_t*)W.skeys[0], W.svals[0],
+        k_morton<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox32, W.mesh_box, (uint32_t*)W.skeys[0], W.svals[0],
             (uint32_t*)W.ckeys[0], W.cvals[0], key_bits);
 }
 
