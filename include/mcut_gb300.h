@@ -68,7 +68,9 @@ typedef enum mcgpu_status {
 #define MCGPU_KEEP_TESTS (1u << 2)         /* keep every culled edge-face test and its predicates */
 #define MCGPU_KEEP_PAIRS (1u << 3)         /* keep the candidate face pairs */
 #define MCGPU_PROFILE (1u << 4)            /* time the stages with CUDA events */
-#define MCGPU_DEVICE_POINTERS (1u << 5)    /* mesh arrays are device pointers (recentred, double) */
+#define MCGPU_DEVICE_POINTERS (1u << 5)    /* mesh arrays are device pointers (recentred, double); a
+                                              single pair's and a packed batch's coordinates are read
+                                              in place, so keep them alive while results are read */
 
 typedef struct mcgpu_mesh {
     const void* vertices;         /* double[3*num_vertices], float with MCGPU_VERTEX_ARRAY_FLOAT */

@@ -263,8 +263,12 @@ __global__ void k_apply_frame(const double* __restrict__ in, double* __restrict_
 // ---------------------------------------------------------------------------
 // device helpers
 // ---------------------------------------------------------------------------
+// ps indices (local -> global vertex ids) and the face -> pair table. With
+// src_in / cut_in (a single pair from device arrays) the indices are read
+// from the caller's arrays; otherwise they were copied into fidx already.
 __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint32_t* __restrict__ fidx, uint64_t nidx,
-    uint32_t* __restrict__ face_pair, uint64_t nf)
+    uint32_t* __restrict__ face_pair, uint64_t nf, const uint32_t* __restrict__ src_in,
+    const uint32_t* __restrict__ cut_in)
 {
     // tab rows (n_pairs+1 each): ibase, is, vbase, vs, fbase, fs
     const uint32_t* ibase = tab;
@@ -282,7 +286,8 @@ __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint3
         }
         const uint32_t p = lo;
         const bool cut = (i - ibase[p]) >= is[p];
-        fidx[i] = fidx[i] + vbase[p] + (cut ? vs[p] : 0u);
+        const uint32_t local = src_in ? (cut ? cut_in[i - is[0]] : src_in[i]) : fidx[i];
+        fidx[i] = local + vbase[p] + (cut ? vs[p] : 0u);
     }
     for (uint64_t f = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; f < nf; f += stride) {
         uint32_t lo = 0, hi = n_pairs;
@@ -405,10 +410,13 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     cudaStream_t s = c->s;
     const bool fin = (flags & MCGPU_VERTEX_ARRAY_FLOAT) != 0;
     const bool dev = (flags & MCGPU_DEVICE_POINTERS) != 0;
-    // a packed device batch is read in place; everything else is copied
-    const double* X = (pk && dev) ? static_cast<const double*>(pk->X) : c->buf[B_X].get<double>(L.nv * 3);
+    // device inputs are read in place (a packed batch as one array, a single
+    // pair as its two arrays); everything else is copied
+    const bool split = dev && !pk && n == 1;
+    const double* X = (pk && dev) ? static_cast<const double*>(pk->X)
+        : split ? static_cast<const double*>(srcs[0].vertices) : c->buf[B_X].get<double>(L.nv * 3);
     uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
-    if (pk && dev) {
+    if ((pk && dev) || split) {
         // read in place
     } else if (pk && !(flags & MCGPU_RECENTRE)) {
         ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
@@ -462,7 +470,9 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     }
     const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const bool staged = (flags & MCGPU_RECENTRE) != 0; // indices went up with the recentred coordinates
-    if (pk && !staged)
+    if (split) {
+        // k_prep reads the caller's index arrays
+    } else if (pk && !staged)
         ck(cudaMemcpyAsync(fidx, pk->idx, (size_t)L.nidx * 4, ikind, s), "H2D idx");
     else for (uint32_t p = 0; p < n; ++p) {
         const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
@@ -507,7 +517,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     }
     uint32_t* face_pair = c->buf[B_FPAIR].get<uint32_t>(L.nf);
     g_launches++;
-    k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf);
+    k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf,
+        split ? srcs[0].face_indices : nullptr, split ? cuts[0].face_indices : nullptr);
 
     Problem& P = c->P;
     P.n_pairs = n;
@@ -516,6 +527,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.ns = (uint32_t)L.ns;
     P.nc = (uint32_t)L.nc;
     P.X = X;
+    P.Xc = split ? static_cast<const double*>(cuts[0].vertices) : nullptr;
+    P.xsplit = split ? L.vs[0] : 0xFFFFFFFFu;
     P.foff = foff;
     P.fidx = fidx;
     P.face_pair = face_pair;
@@ -1055,8 +1068,19 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
         case MCGPU_DATA_TEST_INFO:
             if (!(c->flags & MCGPU_KEEP_TESTS)) return fail(MCGPU_INVALID_VALUE, "dispatch without MCGPU_KEEP_TESTS");
             return copy_out(c, W.test_info, c->n_tests * 4, bytes, mem, bytes_out);
-        case MCGPU_DATA_VERTICES:
-            return copy_out(c, c->P.X, c->L.nv * 24, bytes, mem, bytes_out);
+        case MCGPU_DATA_VERTICES: {
+            if (c->P.xsplit == 0xFFFFFFFFu) return copy_out(c, c->P.X, c->L.nv * 24, bytes, mem, bytes_out);
+            // a single pair read in place from the caller's two device arrays
+            const uint64_t need = c->L.nv * 24, first = (uint64_t)c->P.xsplit * 24;
+            if (bytes_out) *bytes_out = need;
+            if (!mem && bytes == 0) return MCGPU_OK;
+            if (!mem || bytes < need) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+            ck(cudaMemcpyAsync(mem, c->P.X, first, cudaMemcpyDeviceToHost, c->s), "D2H vertices");
+            ck(cudaMemcpyAsync(static_cast<char*>(mem) + first, c->P.Xc, need - first, cudaMemcpyDeviceToHost, c->s),
+                "D2H vertices");
+            ck(cudaStreamSynchronize(c->s), "sync data");
+            return MCGPU_OK;
+        }
         case MCGPU_DATA_FACE_BOXES:
             return copy_out(c, W.fbox, c->L.nf * 48, bytes, mem, bytes_out);
         case MCGPU_DATA_RECORD_OFFSETS: {

@@ -82,10 +82,13 @@ __device__ __forceinline__ long long dkey(double a)
 __device__ __forceinline__ double dmax_ref(double a, double b) { return dlt_int(a, b) ? b : a; }  // std::max
 __device__ __forceinline__ double dmin_ref(double a, double b) { return dlt_int(b, a) ? b : a; }  // std::min
 
+// closed box overlap (intersect_bounding_boxes, math.h:931-943) on dkey()
+// integers: the IEEE order of non-NaN doubles (-0 == +0), off the fp64 pipe
 __device__ __forceinline__ bool box_overlap(const Box& a, const Box& b)
 {
-    return (a.mn[0] <= b.mx[0] && a.mx[0] >= b.mn[0]) && (a.mn[1] <= b.mx[1] && a.mx[1] >= b.mn[1])
-        && (a.mn[2] <= b.mx[2] && a.mx[2] >= b.mn[2]);
+    bool ov = true;
+    for (int j = 0; j < 3; ++j) ov &= dkey(a.mn[j]) <= dkey(b.mx[j]) && dkey(a.mx[j]) >= dkey(b.mn[j]);
+    return ov;
 }
 
 __device__ __forceinline__ Box load_box(const double* __restrict__ boxes, uint32_t f)

@@ -28,6 +28,13 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// vertex v of the dispatch (two segments when the caller's arrays are read in place)
+__device__ __forceinline__ void load_v(const Problem& P, uint32_t v, double* x)
+{
+    if (v < P.xsplit) load_xyz(P.X, v, x);
+    else load_xyz(P.Xc, v - P.xsplit, x);
+}
+
 __device__ __forceinline__ uint32_t face_n(const Problem& P, uint32_t f)
 {
     return P.all_triangles ? 3u : (P.foff[f + 1] - P.foff[f]);
@@ -95,7 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
                 const uint32_t v = P.fidx[o + k];
                 if (v < vlo || v >= vhi) { bad = true; continue; }
                 double x[3];
-                load_xyz(P.X, v, x);
+                load_v(P, v, x);
                 for (int j = 0; j < 3; ++j) { b.mx[j] = dmax_ref(b.mx[j], x[j]); b.mn[j] = dmin_ref(b.mn[j], x[j]); }
             }
             if (bad) atomicOr(&pair_status[p], ST_INVALID);
@@ -1028,10 +1035,10 @@ __global__ void __launch_bounds__(kBlock) k_planes(Problem P, const uint8_t* __r
         // Newell's normal over the rotated vertex list
         double nx = 0.0, ny = 0.0, nz = 0.0;
         double cur[3], nxt[3], first[3];
-        load_xyz(P.X, face_vertex(P, o, n, 0), first);
+        load_v(P, face_vertex(P, o, n, 0), first);
         cur[0] = first[0]; cur[1] = first[1]; cur[2] = first[2];
         for (uint32_t k = 0; k < n; ++k) {
-            if (k + 1 < n) load_xyz(P.X, face_vertex(P, o, n, k + 1), nxt);
+            if (k + 1 < n) load_v(P, face_vertex(P, o, n, k + 1), nxt);
             else { nxt[0] = first[0]; nxt[1] = first[1]; nxt[2] = first[2]; }
             nx = nx + (cur[1] - nxt[1]) * (cur[2] + nxt[2]);
             ny = ny + (cur[2] - nxt[2]) * (cur[0] + nxt[0]);
@@ -1218,15 +1225,15 @@ __global__ void k_triplets(Problem P, const uint32_t* __restrict__ poly_list, co
         long m = 0;
         for (uint32_t i = 0; i < n; ++i) {
             double vi[3], xi[2];
-            load_xyz(P.X, face_vertex(P, o, n, i), vi);
+            load_v(P, face_vertex(P, o, n, i), vi);
             project2(pl.P, vi, xi);
             for (uint32_t j = i + 1; j < n; ++j) {
                 double vj[3], xj[2];
-                load_xyz(P.X, face_vertex(P, o, n, j), vj);
+                load_v(P, face_vertex(P, o, n, j), vj);
                 project2(pl.P, vj, xj);
                 for (uint32_t k = j + 1; k < n; ++k) {
                     double vk[3], xk[2];
-                    load_xyz(P.X, face_vertex(P, o, n, k), vk);
+                    load_v(P, face_vertex(P, o, n, k), vk);
                     project2(pl.P, vk, xk);
                     const double r = orient2d(xi, xj, xk);
                     if (!(r == 0.0)) tr[m++] = Trip { r, (int)i, (int)j, (int)k, 0 };
@@ -1318,8 +1325,8 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
                 }
                 if (emit) {
                     double xa[3], xb[3];
-                    load_xyz(P.X, a, xa);
-                    load_xyz(P.X, b, xb);
+                    load_v(P, a, xa);
+                    load_v(P, b, xb);
                     Box eb;
                     for (int j = 0; j < 3; ++j) {
                         eb.mx[j] = dmax_ref(dmax_ref(-1.7976931348623157e308, xa[j]), xb[j]);
@@ -1354,12 +1361,12 @@ __device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_
     double prv[2];
     {
         double v[3];
-        load_xyz(P.X, face_vertex(P, o, n, n - 1), v);
+        load_v(P, face_vertex(P, o, n, n - 1), v);
         project2(Pm, v, prv);
     }
     for (uint32_t i = 0; i < n; ++i) {
         double v[3], c[2];
-        load_xyz(P.X, face_vertex(P, o, n, i), v);
+        load_v(P, face_vertex(P, o, n, i), v);
         project2(Pm, v, c);
         const double xi = c[0] - q[0], yi = c[1] - q[1];
         if (xi == 0.0 && yi == 0.0) return 'v';
@@ -1401,11 +1408,11 @@ __global__ void __launch_bounds__(kBlock) k_narrow_signs(Problem P, const Test* 
             if (t0 >= 0) {
                 const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
                 double q[3], r[3], a[3], b[3], c[3];
-                load_xyz(P.X, t.q, q);
-                load_xyz(P.X, t.r, r);
-                load_xyz(P.X, face_vertex(P, o, n, t0), a);
-                load_xyz(P.X, face_vertex(P, o, n, t1), b);
-                load_xyz(P.X, face_vertex(P, o, n, t2), c);
+                load_v(P, t.q, q);
+                load_v(P, t.r, r);
+                load_v(P, face_vertex(P, o, n, t0), a);
+                load_v(P, face_vertex(P, o, n, t1), b);
+                load_v(P, face_vertex(P, o, n, t2), c);
                 int st0, st1;
                 sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
                 sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
@@ -1481,8 +1488,8 @@ __global__ void __launch_bounds__(kBlock) k_narrow_hits(Problem P, const Test* _
             const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
             const double* Pm = pl.P;
             double q[3], r[3];
-            load_xyz(P.X, t.q, q);
-            load_xyz(P.X, t.r, r);
+            load_v(P, t.q, q);
+            load_v(P, t.r, r);
             char pip = 0;
             if (type == 'q' || type == 'r') {
                 pip = pip_face(P, Pm, o, n, type == 'q' ? q : r);

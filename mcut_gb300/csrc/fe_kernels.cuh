@@ -4,6 +4,8 @@
 // dispatch is a batch of one):
 //   X          double[nv][3]      ps vertex coordinates, pair after pair; within a
 //                                 pair the source vertices then the cut vertices
+//                                 (a single dispatch from device arrays reads the
+//                                 caller's two arrays in place: X and Xc)
 //   foff       uint32[nf+1]       CSR offsets of ps faces into fidx
 //   fidx       uint32[foff[nf]]   global vertex ids (cut-mesh ids already offset)
 //   face_pair  uint32[nf]         pair id | kCutBit for cut-mesh faces
@@ -44,6 +46,8 @@ struct Problem {
     uint32_t nv, nf;
     uint32_t ns, nc;            // total source / cut faces
     const double* X;
+    const double* Xc;           // with xsplit: vertices >= xsplit live here (index - xsplit)
+    uint32_t xsplit;            // 0xFFFFFFFF: every vertex in X
     const uint32_t* foff;
     const uint32_t* fidx;
     const uint32_t* face_pair;

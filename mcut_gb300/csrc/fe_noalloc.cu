@@ -159,6 +159,8 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     P.ns = Fs;
     P.nc = cut->num_faces;
     P.X = reinterpret_cast<double*>(base + oX);
+    P.Xc = nullptr;
+    P.xsplit = 0xFFFFFFFFu;
     P.foff = nullptr;
     P.fidx = reinterpret_cast<uint32_t*>(base + oFidx);
     P.face_pair = reinterpret_cast<uint32_t*>(base + oFpair);
