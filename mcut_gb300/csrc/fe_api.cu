@@ -93,7 +93,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -124,7 +124,7 @@ struct mcgpu_context_t {
     uint64_t n_pairs_found = 0, n_tests = 0, n_records = 0;
     uint32_t flags = 0;
     int rec_buf = 0;
-    mcgpu_tuning tune { 4, 0, 32, 64 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL override at creation
+    mcgpu_tuning tune { 4, 0, 32, 64 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL / MCGPU_PACKET_FACES override at creation
     bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
     struct Graph {
         std::vector<unsigned char> key;
@@ -651,6 +651,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
     W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));
     W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
+    W.node_range = c->buf[B_NRANGE].get<int2>(std::max<uint64_t>(L.ncl, 2));
     W.counters = c->buf[B_COUNTERS].get<uint32_t>(16);
     W.cand = c->buf[B_CAND].get<uint8_t>(L.nf);
     W.pair_status = c->buf[B_PSTAT].get<uint32_t>(n);
@@ -862,6 +863,10 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         if (const char* e = getenv("MCGPU_TRAVERSAL")) {
             if (!strcmp(e, "packet")) c->tune.traversal = 1;
             if (!strcmp(e, "thread")) c->tune.traversal = 2;
+        }
+        if (const char* e = getenv("MCGPU_PACKET_FACES")) {
+            const int v = atoi(e);
+            if (v >= 1 && v <= 32) c->tune.packet_faces = (uint32_t)v;
         }
         if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");

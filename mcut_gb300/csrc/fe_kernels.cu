@@ -15,6 +15,7 @@
 // not the reference's implicit complete tree.
 
 #include <climits>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 
@@ -227,7 +228,7 @@ __device__ __forceinline__ int delta(const K* __restrict__ key, int n, int i, in
 
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, int n, Node* __restrict__ nodes,
-    int32_t* __restrict__ parent)
+    int32_t* __restrict__ parent, int2* __restrict__ node_range)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
         const int d = (delta(key, n, i, i + 1) - delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -250,6 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, in
         const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
         nodes[i].child[0] = left;
         nodes[i].child[1] = right;
+        node_range[i] = make_int2(lo, hi);
         // parent index | child slot << 31 (the refit climb needs no node read)
         parent[left >= 0 ? left : (n - 1) + ~left] = i;
         parent[right >= 0 ? right : (n - 1) + ~right] = (int32_t)((uint32_t)i | 0x80000000u);
@@ -358,44 +360,71 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
 }
 
 // bottom-up refit: the second child to arrive at a node merges both boxes
-__global__ void __launch_bounds__(kBlock) k_refit(Problem P, const float* __restrict__ fbox32,
+// Bottom-up boxes. Block b owns leaf clusters [kRefitWin b, kRefitWin (b+1)): a node
+// whose leaf range lies inside that window has both children finished by
+// threads of the same block, so its arrival counter and the children's boxes
+// live in shared memory (block-scope ordering, no global round trip); the
+// nodes above the window use global acquire-release arrival counters. The
+// second thread to arrive at a node carries the union upward; every node's
+// child boxes are also written to the tree for the traversal.
+constexpr int kRefitWin = 256;
+__global__ void __launch_bounds__(kRefitWin) k_refit(Problem P, const float* __restrict__ fbox32,
     const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n,
-    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, uint32_t* __restrict__ flag)
+    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, const int2* __restrict__ node_range,
+    uint32_t* __restrict__ flag)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        FBox fb;
-        for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
-        const uint32_t s0 = cl_start[i], cn = cl_n[i];
-        uint32_t lf[16];
-        for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
-        for (uint32_t t = 0; t < cn; ++t) {
-            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
-            const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
-            fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
-            fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
-        }
-        fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
-        uint32_t pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
-        for (;;) {
-            const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
-            // the next parent is read before the atomic (whose memory clobber orders every later load)
-            const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
-            Node* nd = &nodes[node];
-            put_child(nd, slot, fb);
+    __shared__ uint32_t sflag[kRefitWin];
+    __shared__ FBox sbox[kRefitWin][2];
+    const int w0 = blockIdx.x * kRefitWin, w1 = min(n, w0 + kRefitWin) - 1;
+    sflag[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = w0 + threadIdx.x;
+    if (i >= n) return;
+    FBox fb;
+    for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
+    const uint32_t s0 = cl_start[i], cn = cl_n[i];
+    uint32_t lf[16];
+    for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
+    for (uint32_t t = 0; t < cn; ++t) {
+        const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
+        const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
+        fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
+        fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
+    }
+    fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
+    uint32_t pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
+    for (;;) {
+        const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
+        // the next parent and this node's range are read before the arrival
+        const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
+        const int2 rg = __ldg(&node_range[node]);
+        Node* nd = &nodes[node];
+        put_child(nd, slot, fb);
+        FBox o;
+        if (rg.x >= w0 && rg.y <= w1) {
+            // inside the window: node index in [w0, w1]
+            const int k = node - w0;
+            sbox[k][slot] = fb;
+            __threadfence_block();
+            const uint32_t prev = atomicAdd(&sflag[k], 1u);
+            __threadfence_block();
+            if (prev == 0) break;
+            o = sbox[k][slot ^ 1];
+        } else {
             // acq_rel arrival: releases this child's box, acquires the sibling's
             unsigned prev;
             asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&flag[node]) : "memory");
-            if (prev == 0) break; // the sibling finishes this node
-            const FBox o = get_child(nd, slot ^ 1);
-            for (int j = 0; j < 3; ++j) {
-                fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
-                fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
-            }
-            fb.plo = min(fb.plo, o.plo);
-            fb.phi = max(fb.phi, o.phi);
-            if (node == 0) break;
-            pe = next;
+            if (prev == 0) break;
+            o = get_child(nd, slot ^ 1);
         }
+        for (int j = 0; j < 3; ++j) {
+            fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
+            fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
+        }
+        fb.plo = min(fb.plo, o.plo);
+        fb.phi = max(fb.phi, o.phi);
+        if (node == 0) break;
+        pe = next;
     }
 }
 
@@ -619,18 +648,21 @@ __global__ void __launch_bounds__(32) k_top_cut(const Node* __restrict__ nodes, 
 // loads instead of hundreds of dependent ones.
 constexpr int kWaveOut = MCGPU_WAVE_OUT;
 
-struct WaveWarp {
+struct __align__(16) WaveWarp {
     int front[2][kWaveFrontier];
     WaveLeaf leaves[kWaveLeaves];
     unsigned long long out[kWaveOut + 32];
     long long qk[32][6];
-    float qb[32][6];
+    float qb[32][8];     // lo xyz, pad, hi xyz, pad (two float4 loads)
+    float sub[4][8];     // union boxes of queries 8g .. 8g+7
     uint32_t qs[32];
     uint32_t qp[32];
     int nout;
     unsigned qhit; // queries of the current packet that produced a pair
 };
 constexpr size_t kWaveSmem = sizeof(WaveWarp) * kWaveWarps;
+static_assert(sizeof(WaveWarp) % 16 == 0 && offsetof(WaveWarp, qb) % 16 == 0 && offsetof(WaveWarp, sub) % 16 == 0,
+    "float4 shared-memory loads of the query boxes need 16-byte alignment");
 
 __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const double* __restrict__ fbox,
     const uint32_t* __restrict__ qface, const uint2* __restrict__ packets, const uint32_t* __restrict__ leaf_face,
@@ -679,7 +711,7 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 ql[j] = f32_rd(qb.mn[j]);
                 qh[j] = f32_ru(qb.mx[j]);
                 W.qb[lane][j] = ql[j];
-                W.qb[lane][3 + j] = qh[j];
+                W.qb[lane][4 + j] = qh[j];
             }
             W.qs[lane] = s;
             W.qp[lane] = p;
@@ -688,7 +720,12 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
         }
         float ul[3] = { ql[0], ql[1], ql[2] }, uh[3] = { qh[0], qh[1], qh[2] };
         uint32_t pmin = active ? p : 0xFFFFu, pmax = active ? p : 0u;
-        for (int off = 16; off; off >>= 1) {
+        for (int off = 1; off < 32; off <<= 1) {
+            if (off == 8) {
+                // lanes 8g .. 8g+7 now hold their group's union: lane 8g writes it
+                if ((lane & 7) == 0)
+                    for (int j = 0; j < 3; ++j) { W.sub[lane >> 3][j] = ul[j]; W.sub[lane >> 3][4 + j] = uh[j]; }
+            }
             for (int j = 0; j < 3; ++j) {
                 ul[j] = fminf(ul[j], __shfl_xor_sync(full, ul[j], off));
                 uh[j] = fmaxf(uh[j], __shfl_xor_sync(full, uh[j], off));
@@ -710,26 +747,43 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 const int k = base + lane;
                 if (k < nl) {
                     const WaveLeaf L = W.leaves[k];
+                    // the cluster's faces: first position from the pair tables (as
+                    // k_clusters lays clusters out); their ids are requested before
+                    // the box tests so the loads overlap them
+                    const uint32_t lp = L.pr & 0xFFFFu;
+                    const uint32_t s0 = P.pair_cbase[lp] + ((uint32_t)L.id - P.pair_clbase[lp]) * P.leaf_size;
+                    const uint32_t cn = min(P.leaf_size, P.pair_cbase[lp + 1] - s0);
+                    uint32_t cf0[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) cf0[u] = (uint32_t)u < cn ? __ldg(&leaf_face[s0 + u]) : 0u;
+                    // queries whose fp32 box meets the leaf box, group by group of 8
+                    // (a group whose union misses the leaf is skipped)
                     unsigned mask = 0;
-                    for (int j = 0; j < psize; ++j) {
-                        const bool ov = W.qp[j] == (L.pr & 0xFFFFu) && W.qb[j][0] <= L.hi[0] && W.qb[j][3] >= L.lo[0]
-                            && W.qb[j][1] <= L.hi[1] && W.qb[j][4] >= L.lo[1] && W.qb[j][2] <= L.hi[2]
-                            && W.qb[j][5] >= L.lo[2];
-                        mask |= (ov ? 1u : 0u) << j;
+                    for (int g = 0; g * 8 < psize; ++g) {
+                        const float4 ga = *reinterpret_cast<const float4*>(&W.sub[g][0]);
+                        const float4 gb = *reinterpret_cast<const float4*>(&W.sub[g][4]);
+                        if (!(ga.x <= L.hi[0] && gb.x >= L.lo[0] && ga.y <= L.hi[1] && gb.y >= L.lo[1]
+                                && ga.z <= L.hi[2] && gb.z >= L.lo[2]))
+                            continue;
+                        const int je = min(psize, g * 8 + 8);
+                        for (int j = g * 8; j < je; ++j) {
+                            const float4 qa = *reinterpret_cast<const float4*>(&W.qb[j][0]);
+                            const float4 qb4 = *reinterpret_cast<const float4*>(&W.qb[j][4]);
+                            const bool ov = W.qp[j] == lp && qa.x <= L.hi[0] && qb4.x >= L.lo[0] && qa.y <= L.hi[1]
+                                && qb4.y >= L.lo[1] && qa.z <= L.hi[2] && qb4.z >= L.lo[2];
+                            mask |= (ov ? 1u : 0u) << j;
+                        }
                     }
                     if (mask) {
-                        // the cluster's faces: first position from the pair tables (as
-                        // k_clusters lays clusters out). Their exact boxes are tested
-                        // first with no stores in the loop, the next face's box loading
-                        // while the current one is tested; pairs are emitted after.
-                        const uint32_t lp = L.pr & 0xFFFFu;
-                        const uint32_t s0 = P.pair_cbase[lp] + ((uint32_t)L.id - P.pair_clbase[lp]) * P.leaf_size;
-                        const uint32_t cn = min(P.leaf_size, P.pair_cbase[lp + 1] - s0);
+                        // exact boxes tested first with no stores in the loop, the next
+                        // face's box loading while the current one is tested; pairs
+                        // are emitted after
                         for (uint32_t u0 = 0; u0 < cn; u0 += 4) {
                             const uint32_t m = min(4u, cn - u0);
                             uint32_t cfs[4];
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) cfs[u] = (uint32_t)u < m ? __ldg(&leaf_face[s0 + u0 + u]) : 0u;
+                            for (int u = 0; u < 4; ++u)
+                                cfs[u] = u0 == 0 ? cf0[u] : ((uint32_t)u < m ? __ldg(&leaf_face[s0 + u0 + u]) : 0u);
                             unsigned hits[4] = { 0u, 0u, 0u, 0u };
                             longlong2 na, nb, nc;
                             load_key_box(fbox, cfs[0], na, nb, nc);
@@ -1691,13 +1745,14 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
     const int g = grid_for(n);
     g_launches++;
     if (wide)
-        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.cl_key, n, W.nodes, W.parent);
+        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.cl_key, n, W.nodes, W.parent,
+            W.node_range);
     else
-        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.cl_key, n, W.nodes, W.parent);
+        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.cl_key, n, W.nodes, W.parent, W.node_range);
     cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
     g_launches++;
-    k_refit<<<g, kBlock, 0, s>>>(P, W.fbox32, W.cvals[cut_buf], W.cl_start, W.cl_n, n, W.nodes, W.parent,
-        W.refit_flag);
+    k_refit<<<(n + kRefitWin - 1) / kRefitWin, kRefitWin, 0, s>>>(P, W.fbox32, W.cvals[cut_buf], W.cl_start, W.cl_n, n,
+        W.nodes, W.parent, W.node_range, W.refit_flag);
 }
 
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)

@@ -83,6 +83,7 @@ struct Work {
     void* top;                        // [64] top cut of the cut tree (WaveTop, 32 B each)
     Node* nodes;                      // [ncl-1]
     int32_t* parent;                  // [2ncl-1]
+    int2* node_range;                 // [ncl-1] leaf range of each internal node
     uint32_t* refit_flag;             // [ncl-1]
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,

@@ -91,7 +91,8 @@ constexpr size_t oPstat = oRpt + al(kMaxTests * 24ull);
 constexpr size_t oPflag = oPstat + al(3 * 4);
 constexpr size_t oPlist = oPflag + al(kMaxFaces * 4ull);
 constexpr size_t oTop = oPlist + al(kMaxFaces * 4ull);
-constexpr size_t kScratchBytes = oTop + al(64 * 32);
+constexpr size_t oNrange = oTop + al(64 * 32);
+constexpr size_t kScratchBytes = oNrange + al(kMaxFaces * 8ull);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -216,6 +217,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.proj_flag = reinterpret_cast<uint32_t*>(base + oPflag);
     W.proj_list = reinterpret_cast<uint32_t*>(base + oPlist);
     W.top = base + oTop;
+    W.node_range = reinterpret_cast<int2*>(base + oNrange);
     W.poly_list = nullptr;
     W.vneed = base + oVneed;
     W.voff = reinterpret_cast<uint32_t*>(base + oVoff);
