@@ -100,7 +100,8 @@ typedef struct mcgpu_summary {
     uint64_t num_tests;       /* culled edge-face tests */
     uint64_t num_records;     /* intersection records (type '1', point inside) */
     uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, exact stage */
-    float stage_ms[8];        /* per-stage device time (MCGPU_PROFILE) */
+    float stage_ms[8];        /* per-stage device time of the call (MCGPU_PROFILE; a batch's
+                                 summaries all carry the batch's times) */
     uint32_t kernel_launches; /* CUDA kernels this call launched (whole batch) */
     uint32_t reserved;
 } mcgpu_summary;

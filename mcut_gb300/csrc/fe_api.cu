@@ -810,15 +810,17 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         c->sums[0].escalations[0] = hc[5];
         c->sums[0].escalations[1] = hc[6];
         c->sums[0].escalations[2] = hc[7];
-        if (flags & MCGPU_PROFILE) {
-            for (int k = 0; k < 8; ++k) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]);
-                c->sums[0].stage_ms[k] = ms;
-            }
-            c->sums[0].stage_ms[MCGPU_STAGE_NARROW] += c->sums[0].stage_ms[MCGPU_STAGE_DOWNLOAD];
-            c->sums[0].stage_ms[MCGPU_STAGE_DOWNLOAD] = 0.f;
+    }
+    if (flags & MCGPU_PROFILE) {
+        // stage times of the whole call (every summary of a batch carries them)
+        float st[8];
+        for (int k = 0; k < 8; ++k) {
+            st[k] = 0.f;
+            cudaEventElapsedTime(&st[k], c->ev[2 * k], c->ev[2 * k + 1]);
         }
+        st[MCGPU_STAGE_NARROW] += st[MCGPU_STAGE_DOWNLOAD];
+        st[MCGPU_STAGE_DOWNLOAD] = 0.f;
+        for (auto& m : c->sums) memcpy(m.stage_ms, st, sizeof st);
     }
     for (auto& m : c->sums) m.kernel_launches = (uint32_t)(g_launches - launches0);
     if (out) {

@@ -839,8 +839,14 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
             nl = 1;
             drain();
         } else {
-            int cur = 0, nf = 0;
-            // first wave: the listed top cut of the tree
+            // Nodes to expand sit on a warp-wide stack (both frontier arrays as one
+            // 512-entry array); each round pops up to 32 and pushes the children
+            // that meet the packet's union box, deepest first, which bounds the
+            // stack by the tree depth times 32 instead of by the widest level.
+            int* stk = &W.front[0][0];
+            constexpr int kStk = 2 * kWaveFrontier;
+            int sp = 0;
+            // first: the listed top cut of the tree
             const int ntop = (int)counters[13];
             for (int base = 0; base < ntop; base += 32) {
                 const int i = base + lane;
@@ -858,11 +864,11 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 }
                 const bool inner = hit && ch >= 0, leaf = hit && ch < 0;
                 const unsigned mi = __ballot_sync(full, inner), ml = __ballot_sync(full, leaf);
-                if (nf + __popc(mi) > kWaveFrontier) {
+                if (sp + __popc(mi) > kStk) {
                     overflow = true;
                 } else {
-                    if (inner) W.front[0][nf + __popc(mi & lt)] = ch;
-                    nf += __popc(mi);
+                    if (inner) stk[sp + __popc(mi & lt)] = ch;
+                    sp += __popc(mi);
                 }
                 if (nl + __popc(ml) > kWaveLeaves) drain();
                 if (leaf) {
@@ -874,50 +880,48 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 nl += __popc(ml);
             }
             __syncwarp();
-            while (nf > 0) {
-                int nn = 0;
-                for (int base = 0; base < nf; base += 32) {
-                    const int i = base + lane;
-                    const bool v = i < nf;
-                    bool hit[2] = { false, false };
-                    int ch[2] = { 0, 0 };
-                    float bx[2][6];
-                    uint32_t prr[2] = { 0, 0 };
-                    if (v) {
-                        const int nd = W.front[cur][i];
-                        const float4 a = __ldg(&nodes[nd].b0), b = __ldg(&nodes[nd].b1), c = __ldg(&nodes[nd].b2);
-                        const int2 cc = __ldg(reinterpret_cast<const int2*>(&nodes[nd].child[0]));
-                        const uint2 pr = __ldg(reinterpret_cast<const uint2*>(&nodes[nd].prange[0]));
-                        ch[0] = cc.x; ch[1] = cc.y; prr[0] = pr.x; prr[1] = pr.y;
-                        bx[0][0] = a.x; bx[0][1] = a.y; bx[0][2] = a.z; bx[0][3] = a.w; bx[0][4] = b.x; bx[0][5] = b.y;
-                        bx[1][0] = b.z; bx[1][1] = b.w; bx[1][2] = c.x; bx[1][3] = c.y; bx[1][4] = c.z; bx[1][5] = c.w;
-                        for (int k = 0; k < 2; ++k)
-                            hit[k] = (prr[k] & 0xFFFFu) <= pmax && pmin <= (prr[k] >> 16) && ul[0] <= bx[k][3]
-                                && uh[0] >= bx[k][0] && ul[1] <= bx[k][4] && uh[1] >= bx[k][1] && ul[2] <= bx[k][5]
-                                && uh[2] >= bx[k][2];
+            while (sp > 0) {
+                const int take = min(sp, 32);
+                const int base = sp - take;
+                const bool v = lane < take;
+                bool hit[2] = { false, false };
+                int ch[2] = { 0, 0 };
+                float bx[2][6];
+                uint32_t prr[2] = { 0, 0 };
+                const int nd = v ? stk[base + lane] : 0;
+                __syncwarp(); // every lane holds its entry before the pushes reuse the slots
+                sp = base;
+                if (v) {
+                    const float4 a = __ldg(&nodes[nd].b0), b = __ldg(&nodes[nd].b1), c = __ldg(&nodes[nd].b2);
+                    const int2 cc = __ldg(reinterpret_cast<const int2*>(&nodes[nd].child[0]));
+                    const uint2 pr = __ldg(reinterpret_cast<const uint2*>(&nodes[nd].prange[0]));
+                    ch[0] = cc.x; ch[1] = cc.y; prr[0] = pr.x; prr[1] = pr.y;
+                    bx[0][0] = a.x; bx[0][1] = a.y; bx[0][2] = a.z; bx[0][3] = a.w; bx[0][4] = b.x; bx[0][5] = b.y;
+                    bx[1][0] = b.z; bx[1][1] = b.w; bx[1][2] = c.x; bx[1][3] = c.y; bx[1][4] = c.z; bx[1][5] = c.w;
+                    for (int k = 0; k < 2; ++k)
+                        hit[k] = (prr[k] & 0xFFFFu) <= pmax && pmin <= (prr[k] >> 16) && ul[0] <= bx[k][3]
+                            && uh[0] >= bx[k][0] && ul[1] <= bx[k][4] && uh[1] >= bx[k][1] && ul[2] <= bx[k][5]
+                            && uh[2] >= bx[k][2];
+                }
+                for (int k = 0; k < 2; ++k) {
+                    const bool inner = hit[k] && ch[k] >= 0, leaf = hit[k] && ch[k] < 0;
+                    const unsigned mi = __ballot_sync(full, inner), ml = __ballot_sync(full, leaf);
+                    if (sp + __popc(mi) > kStk) {
+                        overflow = true;
+                    } else {
+                        if (inner) stk[sp + __popc(mi & lt)] = ch[k];
+                        sp += __popc(mi);
                     }
-                    for (int k = 0; k < 2; ++k) {
-                        const bool inner = hit[k] && ch[k] >= 0, leaf = hit[k] && ch[k] < 0;
-                        const unsigned mi = __ballot_sync(full, inner), ml = __ballot_sync(full, leaf);
-                        if (nn + __popc(mi) > kWaveFrontier) {
-                            overflow = true;
-                        } else {
-                            if (inner) W.front[cur ^ 1][nn + __popc(mi & lt)] = ch[k];
-                            nn += __popc(mi);
-                        }
-                        if (nl + __popc(ml) > kWaveLeaves) drain(); // nl is uniform
-                        if (leaf) {
-                            WaveLeaf& L = W.leaves[nl + __popc(ml & lt)];
-                            for (int j = 0; j < 3; ++j) { L.lo[j] = bx[k][j]; L.hi[j] = bx[k][3 + j]; }
-                            L.id = ~ch[k];
-                            L.pr = prr[k];
-                        }
-                        nl += __popc(ml);
+                    if (nl + __popc(ml) > kWaveLeaves) drain(); // nl is uniform
+                    if (leaf) {
+                        WaveLeaf& L = W.leaves[nl + __popc(ml & lt)];
+                        for (int j = 0; j < 3; ++j) { L.lo[j] = bx[k][j]; L.hi[j] = bx[k][3 + j]; }
+                        L.id = ~ch[k];
+                        L.pr = prr[k];
                     }
+                    nl += __popc(ml);
                 }
                 __syncwarp();
-                cur ^= 1;
-                nf = nn;
             }
             drain();
         }
