@@ -248,6 +248,59 @@ void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* 
     *eps_out = frame_eps(cs, t);
 }
 
+// memcpy on several host threads (large staging copies)
+void memcpy_mt(void* dst, const void* src, size_t bytes, unsigned threads)
+{
+    if (bytes < (8u << 20) || threads < 2) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t chunk = ((bytes + threads - 1) / threads + 4095) & ~size_t(4095);
+    std::vector<std::thread> ts;
+    for (size_t lo = 0; lo < bytes; lo += chunk) {
+        const size_t len = std::min(chunk, bytes - lo);
+        ts.emplace_back([=] { memcpy(static_cast<char*>(dst) + lo, static_cast<const char*>(src) + lo, len); });
+    }
+    for (auto& t : ts) t.join();
+}
+
+// recentre_pair for one large pair on several host threads: the two meshes'
+// stats run side by side (each centroid is still summed in vertex order, as
+// the reference sums it), then the coordinate maps run in chunks
+void recentre_pair_mt(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out,
+    unsigned threads)
+{
+    MeshStats ss, cs;
+    std::thread tc([&] { mesh_stats(Cm.vertices, fin, Cm.num_vertices, cs); });
+    mesh_stats(S.vertices, fin, S.num_vertices, ss);
+    tc.join();
+    double com[3], t[3];
+    pair_frame(ss, cs, com, t);
+    const uint64_t ns = S.num_vertices, nc = Cm.num_vertices, total = ns + nc;
+    const uint64_t chunk = (total + threads - 1) / threads;
+    std::vector<std::thread> ts;
+    for (unsigned k = 0; k < threads; ++k) {
+        const uint64_t lo = k * chunk, hi = std::min(total, lo + chunk);
+        if (lo >= hi) break;
+        ts.emplace_back([&, lo, hi] {
+            // vertices [lo, hi) of the concatenation (source then cut)
+            auto part = [&](const mcgpu_mesh& m, uint64_t base, double* out) {
+                const uint64_t a = std::max(lo, base), b = std::min(hi, base + m.num_vertices);
+                if (a >= b) return;
+                mcgpu_mesh sub = m;
+                const size_t vsz = fin ? 12 : 24;
+                sub.vertices = static_cast<const char*>(m.vertices) + (a - base) * vsz;
+                sub.num_vertices = (uint32_t)(b - a);
+                apply_frame(fin, sub, com, t, out + (a - base) * 3);
+            };
+            part(S, 0, sx);
+            part(Cm, ns, cx);
+        });
+    }
+    for (auto& th : ts) th.join();
+    *eps_out = frame_eps(cs, t);
+}
+
 // resident cut mesh: its stored user coordinates mapped into the pair's frame
 __global__ void k_apply_frame(const double* __restrict__ in, double* __restrict__ out, uint64_t n3, double c0,
     double c1, double c2, double t0, double t1, double t2)
@@ -438,13 +491,17 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
                 pair_frame(ss, res[p]->st, j.com, j.t);
                 apply_frame(fin, srcs[p], j.com, j.t, sx);
                 L.eps[p] = frame_eps(res[p]->st, j.t);
+            } else if (n == 1 && L.nv > 200000) {
+                const unsigned hw = std::max(2u, std::min(16u, std::thread::hardware_concurrency()));
+                recentre_pair_mt(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p], hw);
             } else {
                 recentre_pair(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
             }
             if (ist) {
                 const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
-                memcpy(ist + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4);
-                if (!(res && res[p])) memcpy(ist + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4);
+                const unsigned th = n == 1 ? std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1u;
+                memcpy_mt(ist + L.ibase[p], srcs[p].face_indices, (size_t)L.is[p] * 4, th);
+                if (!(res && res[p])) memcpy_mt(ist + L.ibase[p] + L.is[p], cuts[p].face_indices, (size_t)ic * 4, th);
             }
         });
         ck(cudaMemcpyAsync(const_cast<double*>(X), st, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),

@@ -286,10 +286,12 @@ enum { ESC_F32 = 0, ESC_F64 = 1, ESC_EXACT = 2 };
 // analysis with that per-input error and u per fp32 operation gives
 // |det - det_exact| <= (7u + 56u^2) * permanent; 8u covers the slightly
 // larger input error. The filter only runs when every nonzero difference
-// lies in [2^-39, 2^40): then no fp32 product or sum can overflow, no
-// product underflows, and the relative-error model holds for every
-// operation (a subnormal difference of products is exact). Otherwise, or
-// when the bound is not met, it escalates.
+// lies in [2^-40, 2^41). Then the permanent, a sum of six products each
+// < 2^123, stays below 2^126 (no overflow), and a nonzero permanent is at
+// least 2^-120: the bound's slack over 7u, u * permanent >= 2^-144, covers
+// the absolute error of the at most five operations whose result can be
+// subnormal (<= 2^-150 each; a subnormal difference of products is exact).
+// Otherwise, or when the bound is not met, it escalates.
 __device__ __forceinline__ bool f32_filter_input(double d, float& f)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(d);
@@ -298,7 +300,7 @@ __device__ __forceinline__ bool f32_filter_input(double d, float& f)
         return true;
     }
     const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-    if (e < 1023u - 39u || e > 1023u + 39u) return false;
+    if (e < 1023u - 40u || e > 1023u + 40u) return false;
     const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
     unsigned fb = ((unsigned)(b >> 63) << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
     const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
