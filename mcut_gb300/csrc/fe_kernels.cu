@@ -1078,7 +1078,10 @@ __device__ __forceinline__ uint32_t face_vertex(const Problem& P, uint32_t o, ui
     return P.fidx[o + (j == n ? 0 : j)];
 }
 
-__global__ void __launch_bounds__(kBlock) k_planes(Problem P, const uint8_t* __restrict__ cand,
+#ifndef MCGPU_PL_MINB
+#define MCGPU_PL_MINB 1
+#endif
+__global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, const uint8_t* __restrict__ cand,
     uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, uint64_t plane_cap,
     uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad)
 {
@@ -1446,7 +1449,10 @@ __device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_
 // type char (compute_segment_plane_intersection_type, math.cpp:391-427).
 // Tests whose segment meets the plane ('1', 'q', 'r', 'p') go to a compact
 // hit list for pass 2, so its fp64 work runs on full warps.
-__global__ void __launch_bounds__(kBlock) k_narrow_signs(Problem P, const Test* __restrict__ tests,
+#ifndef MCGPU_NS_MINB
+#define MCGPU_NS_MINB 2
+#endif
+__global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem P, const Test* __restrict__ tests,
     const uint32_t* __restrict__ counters_ro, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info, uint2* __restrict__ hits,
     uint32_t* __restrict__ proj_flag, uint32_t* __restrict__ proj_list, uint32_t* __restrict__ counters)
@@ -1523,7 +1529,10 @@ __global__ void __launch_bounds__(kBlock) k_projections(FacePlane* __restrict__ 
 // (compute_segment_plane_intersection, math.cpp:249-287), point-in-polygon
 // (math.cpp:851-902), general-position violations and records
 // (kernel.cpp:2456-2658).
-__global__ void __launch_bounds__(kBlock) k_narrow_hits(Problem P, const Test* __restrict__ tests,
+#ifndef MCGPU_NH_MINB
+#define MCGPU_NH_MINB 1
+#endif
+__global__ void __launch_bounds__(kBlock, MCGPU_NH_MINB) k_narrow_hits(Problem P, const Test* __restrict__ tests,
     const uint2* __restrict__ hits, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
     unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,

@@ -122,8 +122,12 @@ constexpr size_t downsweep_smem()
     return (size_t)kTile * (sizeof(K) + sizeof(uint32_t)) + 3 * kDigits * sizeof(uint32_t) + 2 * kWarps * 4;
 }
 
+// four blocks per SM (<= 64 registers): the pass is bandwidth-bound and needs the occupancy
+#ifndef MCGPU_DS_MINB
+#define MCGPU_DS_MINB 4
+#endif
 template <typename K>
-__global__ void __launch_bounds__(kThreads) k_downsweep(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
+__global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* __restrict__ keys, const uint32_t* __restrict__ vals,
     K* __restrict__ okeys, uint32_t* __restrict__ ovals, uint32_t n, int shift, const uint32_t* __restrict__ hist,
     uint32_t tiles, const uint32_t* __restrict__ totals)
 {
