@@ -1078,6 +1078,22 @@ __device__ __forceinline__ uint32_t face_vertex(const Problem& P, uint32_t o, ui
     return P.fidx[o + (j == n ? 0 : j)];
 }
 
+// unit normal, d and the largest component from the raw Newell normal in
+// pl.n (compute_polygon_plane_coefficients, math.cpp:130-239)
+__device__ __forceinline__ void finish_plane(FacePlane& pl, const double* first)
+{
+    const double nn[3] = { pl.n[0], pl.n[1], pl.n[2] };
+    const double len = sqrt(dot3(nn, nn));
+    pl.n[0] = nn[0] / len; pl.n[1] = nn[1] / len; pl.n[2] = nn[2] / len;
+    pl.d = dot3(first, pl.n);
+    double big = 0.0;
+    pl.mc = 0;
+    for (int i = 0; i < 3; ++i) {
+        const double t = fabs(pl.n[i]);
+        if (t > big) { big = t; pl.mc = i; }
+    }
+}
+
 #ifndef MCGPU_PL_MINB
 #define MCGPU_PL_MINB 1
 #endif
@@ -1116,20 +1132,18 @@ __global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, con
             planes[slot] = pl;
             continue;
         }
-        const double len = sqrt(sq);
-        pl.n[0] = nx / len; pl.n[1] = ny / len; pl.n[2] = nz / len;
-        pl.d = dot3(first, pl.n);
-        double big = 0.0;
-        pl.mc = 0;
-        for (int i = 0; i < 3; ++i) {
-            const double t = fabs(pl.n[i]);
-            if (t > big) { big = t; pl.mc = i; }
-        }
-        // the projection is needed by the point-in-polygon test of the few
-        // faces a segment crosses (computed there for triangles) and by the
-        // triplet ranking of polygons (computed here)
-        if (n > 3) projection_matrix(pl.n, pl.mc, pl.P);
         pl.tri[0] = 0; pl.tri[1] = 1; pl.tri[2] = 2;
+        pl.n[0] = nx; pl.n[1] = ny; pl.n[2] = nz;
+        if (n == 3) {
+            // a triangle keeps its raw Newell normal: the unit normal, d, the
+            // largest component and the projection are only needed if a
+            // segment meets its plane (k_finish_planes, once per such face)
+            planes[slot] = pl;
+            continue;
+        }
+        finish_plane(pl, first);
+        // the triplet ranking of polygons needs the projection now
+        projection_matrix(pl.n, pl.mc, pl.P);
         planes[slot] = pl;
         if (n > 3) {
             const uint32_t k = atomicAdd(&counters[4], 1u);
@@ -1491,11 +1505,10 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
             code = (uint32_t)(uint8_t)sq | ((uint32_t)(uint8_t)sr << 8) | ((uint32_t)(uint8_t)type << 16);
             hit = type != '0';
             if (!hit && keep_tests) reinterpret_cast<char4*>(test_info)[i] = make_char4(sq, sr, type, 0);
-            // the first hit on a triangle queues its projection matrix
+            // the first hit on a triangle queues the rest of its plane
             if (hit && face_n(P, t.g) == 3) {
-                const uint32_t sl = plane_slot[t.g];
-                first_hit = atomicExch(&proj_flag[sl], 1u) == 0u;
-                slot = sl;
+                first_hit = atomicExch(&proj_flag[plane_slot[t.g]], 1u) == 0u;
+                slot = t.g;
             }
         }
         const uint32_t pos = warp_append(&counters[10], hit);
@@ -1510,18 +1523,23 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
     }
 }
 
-// Projection matrices of the triangles that pass 1 queued (polygons got
-// theirs with the plane).
-__global__ void __launch_bounds__(kBlock) k_projections(FacePlane* __restrict__ planes,
-    const uint32_t* __restrict__ proj_list, const uint32_t* __restrict__ counters)
+// The triangles that pass 1 queued (a segment meets their plane): unit
+// normal, d, largest component and projection matrix, once per face
+// (polygons got theirs with the plane).
+__global__ void __launch_bounds__(kBlock) k_finish_planes(Problem P, FacePlane* __restrict__ planes,
+    const uint32_t* __restrict__ plane_slot, const uint32_t* __restrict__ proj_list,
+    const uint32_t* __restrict__ counters)
 {
     const uint32_t n = counters[11];
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        FacePlane& pl = planes[proj_list[k]];
-        const double nrm[3] = { pl.n[0], pl.n[1], pl.n[2] };
-        double Pm[6];
-        projection_matrix(nrm, pl.mc, Pm);
-        for (int j = 0; j < 6; ++j) pl.P[j] = Pm[j];
+        const uint32_t f = proj_list[k];
+        FacePlane& plr = planes[plane_slot[f]];
+        FacePlane pl = plr;
+        double first[3];
+        load_v(P, face_vertex(P, face_o(P, f), 3, 0), first);
+        finish_plane(pl, first);
+        projection_matrix(pl.n, pl.mc, pl.P);
+        plr = pl;
     }
 }
 
@@ -1854,7 +1872,8 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     cudaMemsetAsync(W.proj_flag, 0, sizeof(uint32_t) * W.plane_cap, s);
     k_narrow_signs<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
-    k_projections<<<grid_for(W.plane_cap), kBlock, 0, s>>>((FacePlane*)W.planes, W.proj_list, W.counters);
+    k_finish_planes<<<grid_for(W.plane_cap), kBlock, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot, W.proj_list,
+        W.counters);
     k_narrow_hits<<<g, kBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status);
 }

@@ -94,7 +94,7 @@ struct Work {
     uint32_t* plane_slot;             // [nf]
     void* planes;                     // FacePlane[cap]
     uint32_t* proj_flag;              // [plane_cap] projection queued
-    uint32_t* proj_list;              // [plane_cap] plane slots whose projection is computed
+    uint32_t* proj_list;              // [plane_cap] triangles whose plane is finished (face ids)
     uint32_t* poly_list;              // [nf] faces with > 3 vertices among candidates
     uint8_t* vneed;                   // [nv]
     uint32_t* voff;                   // [nv+1]
