@@ -169,3 +169,15 @@ def test_packed_fracture_batch_vs_oracle(ctx):
         assert G.same_bits(b, w_pts), i
         total += len(a)
     assert total > 0
+
+
+@pytest.mark.parametrize("name", ["two_spheres", "crack1", "bm014"])
+def test_face_boxes_and_vertices_match_oracle(ctx, name):
+    """The face boxes (cut boxes enlarged by eps) and ps coordinates the
+    dispatch used, bit for bit."""
+    c = CASES[name]
+    ctx.dispatch(c["src"], c["cut"], fetch=False)
+    want = oracle.front_end(c["src"], c["cut"], impl="port", threads=4)
+    assert G.same_bits(ctx.face_boxes(), want["face_boxes"].reshape(-1, 6))
+    v = ctx.vertices()
+    assert G.same_bits(v, np.concatenate([want["src_xyz"].reshape(-1, 3), want["cut_xyz"].reshape(-1, 3)]))
