@@ -140,11 +140,13 @@ def dist_init(args):
 
 
 def reduce_max(x, world):
+    """Max over ranks (NCCL on the GPU arm, gloo on CPU)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
