@@ -188,6 +188,8 @@ typedef struct mcgpu_tuning {
                               2: one thread per source face */
     uint32_t packet_faces; /* source faces per packet = queries per warp, 1..32 (default 32) */
     uint32_t stack_depth;  /* per-thread stack of traversal 2: 64 (default) or 512 */
+    uint32_t split_round;  /* traversal 0: walk rounds after which a packet with work left is split
+                              across warps (a second launch); 0 never splits (default 2) */
 } mcgpu_tuning;
 
 int mcgpu_context_set_tuning(mcgpu_context ctx, const mcgpu_tuning* tuning);
@@ -197,7 +199,8 @@ int mcgpu_context_get_tuning(mcgpu_context ctx, mcgpu_tuning* tuning);
  * `flags`) under each candidate tuning -- leaf size {2, 4, 8} x {warp per
  * packet of 16 or 32 faces breadth-first, warp per packet depth-first,
  * thread per face with stack 64 or 512} -- `repeats` times each after one
- * warm-up, keeps the fastest on ctx and returns it with its mean time.
+ * warm-up, plus packet splitting on / off for the breadth-first walk;
+ * keeps the fastest on ctx and returns it with its mean time.
  * No counterpart in the reference. */
 int mcgpu_autotune(mcgpu_context ctx, uint32_t flags, const mcgpu_batch* sample, uint32_t repeats,
     mcgpu_tuning* best, float* best_ms);

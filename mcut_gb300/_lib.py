@@ -51,7 +51,7 @@ class Summary(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("leaf_size", C.c_uint32), ("traversal", C.c_uint32), ("packet_faces", C.c_uint32),
-                ("stack_depth", C.c_uint32)]
+                ("stack_depth", C.c_uint32), ("split_round", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):

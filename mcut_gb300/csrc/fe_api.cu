@@ -93,7 +93,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -124,8 +124,9 @@ struct mcgpu_context_t {
     uint64_t n_pairs_found = 0, n_tests = 0, n_records = 0;
     uint32_t flags = 0;
     int rec_buf = 0;
-    mcgpu_tuning tune { 4, 0, 32, 64 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL / MCGPU_PACKET_FACES override at creation
+    mcgpu_tuning tune { 4, 0, 32, 64, 2 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL / MCGPU_PACKET_FACES override at creation
     bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
+    uint64_t split_cap = 0;               // MCGPU_SPLIT_CAP: fixed split-entry capacity (0: by size)
     struct Graph {
         std::vector<unsigned char> key;
         cudaGraphExec_t exec = nullptr;
@@ -705,6 +706,10 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.leaf_key_box = nullptr;
     W.packets = c->buf[B_PACKETS].get<uint2>(L.ns);
     W.top = c->buf[B_TOP].get<uint8_t>(64 * 32);
+    // slow packets split for the second traversal launch (one entry per two
+    // queries and 32 subtree roots; past the cap a packet finishes its own walk)
+    W.split_cap = c->split_cap ? c->split_cap : std::min<uint64_t>(std::max<uint64_t>(4096, L.ns), 4u << 20);
+    W.split = c->buf[B_SPLIT].get<uint8_t>(W.split_cap * 144);
     W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
     W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));
     W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
@@ -722,6 +727,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.traversal = c->tune.traversal;
     W.packet_faces = c->tune.packet_faces;
     W.stack_depth = c->tune.stack_depth;
+    W.split_round = c->tune.split_round;
     const uint32_t prof = flags & MCGPU_PROFILE;
     int src_buf = 0, cut_buf = 0;
     run_segment(c, 0, seg_key(P, W, n, key_bits, prof), [&](int* aux) {
@@ -928,6 +934,7 @@ int mcgpu_context_create(mcgpu_context* out, int device)
             if (v >= 1 && v <= 32) c->tune.packet_faces = (uint32_t)v;
         }
         if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
+        if (const char* e = getenv("MCGPU_SPLIT_CAP")) c->split_cap = strtoull(e, nullptr, 10);
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
         *out = c;
@@ -1026,7 +1033,7 @@ int mcgpu_context_set_tuning(mcgpu_context c, const mcgpu_tuning* t)
 {
     if (!c || !t) return fail(MCGPU_INVALID_VALUE, "null argument");
     if (t->leaf_size < 1 || t->leaf_size > 16 || t->traversal > 2 || t->packet_faces < 1 || t->packet_faces > 32
-        || (t->stack_depth != 64 && t->stack_depth != 512))
+        || (t->stack_depth != 64 && t->stack_depth != 512) || t->split_round > 64)
         return fail(MCGPU_INVALID_VALUE, "tuning out of range");
     c->tune = *t;
     return MCGPU_OK;
@@ -1046,11 +1053,12 @@ int mcgpu_autotune(mcgpu_context c, uint32_t flags, const mcgpu_batch* sample, u
     if (repeats == 0) repeats = 3;
     std::vector<mcgpu_tuning> cand;
     for (uint32_t leaf : { 2u, 4u, 8u }) {
-        cand.push_back({ leaf, 0, 32, 64 });
-        cand.push_back({ leaf, 0, 16, 64 });
-        cand.push_back({ leaf, 1, 32, 64 });
-        cand.push_back({ leaf, 2, 32, 64 });
-        cand.push_back({ leaf, 2, 32, 512 });
+        cand.push_back({ leaf, 0, 32, 64, 2 });
+        cand.push_back({ leaf, 0, 32, 64, 0 });
+        cand.push_back({ leaf, 0, 16, 64, 2 });
+        cand.push_back({ leaf, 1, 32, 64, 0 });
+        cand.push_back({ leaf, 2, 32, 64, 0 });
+        cand.push_back({ leaf, 2, 32, 512, 0 });
     }
     const mcgpu_tuning keep = c->tune;
     std::vector<mcgpu_summary> sums(sample->num_pairs);

@@ -599,6 +599,23 @@ struct WaveTop {
 };
 static_assert(sizeof(WaveTop) == 32, "the top-cut buffer holds 64 entries of 32 bytes");
 
+// A slow packet's remaining walk, handed from the first traversal launch to
+// the second: a group of its queries and up to 32 subtree roots to expand.
+#ifndef MCGPU_SPLIT_STACK
+#define MCGPU_SPLIT_STACK 8     // ... if more than this many nodes are still to expand
+#endif
+#ifndef MCGPU_SPLIT_GROUP
+#define MCGPU_SPLIT_GROUP 2     // queries per split entry (1, 2, 4, 8, 16 or 32)
+#endif
+struct SplitEntry {
+    uint32_t packet;
+    uint32_t qmask;   // queries of the packet (lanes) this entry walks for
+    uint32_t count;   // subtree roots in nodes[]
+    uint32_t pad;
+    int nodes[32];
+};
+static_assert(sizeof(SplitEntry) == 144, "split entries are 144 bytes");
+
 __global__ void __launch_bounds__(32) k_top_cut(const Node* __restrict__ nodes, int nleaf, WaveTop* __restrict__ top,
     uint32_t* __restrict__ counters)
 {
@@ -664,11 +681,17 @@ constexpr size_t kWaveSmem = sizeof(WaveWarp) * kWaveWarps;
 static_assert(sizeof(WaveWarp) % 16 == 0 && offsetof(WaveWarp, qb) % 16 == 0 && offsetof(WaveWarp, sub) % 16 == 0,
     "float4 shared-memory loads of the query boxes need 16-byte alignment");
 
+// SPLIT = false: one packet per work item, the walk starting at the top cut;
+// a packet still far from done after `split_round` rounds is split into
+// entries (its queries in groups of 8 x its remaining subtree roots in
+// chunks of 32) for the second launch. SPLIT = true: one entry per work item.
+template <bool SPLIT>
 __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const double* __restrict__ fbox,
     const uint32_t* __restrict__ qface, const uint2* __restrict__ packets, const uint32_t* __restrict__ leaf_face,
     const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const WaveTop* __restrict__ top,
     int nleaf, const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
-    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
+    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status,
+    SplitEntry* __restrict__ split, uint32_t split_cap, int split_round)
 {
     extern __shared__ __align__(16) unsigned char wave_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -690,17 +713,25 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
         if (lane == 0) W.nout = 0;
         __syncwarp();
     };
+    const uint32_t nitems = SPLIT ? min(counters[14], split_cap) : npackets;
     for (;;) {
-        uint32_t pk = 0;
-        if (lane == 0) pk = atomicAdd(&counters[8], 1u);
-        pk = __shfl_sync(full, pk, 0);
-        if (pk >= npackets) break;
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(&counters[SPLIT ? 15 : 8], 1u);
+        it = __shfl_sync(full, it, 0);
+        if (it >= nitems) break;
+        const uint32_t pk = SPLIT ? split[it].packet : it;
+        const uint32_t qmask = SPLIT ? split[it].qmask : 0xFFFFFFFFu;
         const uint2 range = packets[pk];
         const int psize = (int)(range.y - range.x + 1);
         const uint32_t t = range.x + lane;
-        const bool active = lane < psize;
+        const bool active = lane < psize && ((qmask >> lane) & 1u);
         uint32_t p = 0xFFFFu;
         float ql[3], qh[3];
+        if (!active) {
+            // a query this item does not walk for matches nothing
+            for (int j = 0; j < 3; ++j) { W.qb[lane][j] = 3.4e38f; W.qb[lane][4 + j] = -3.4e38f; }
+            W.qp[lane] = 0xFFFFFFFFu;
+        }
         if (active) {
             const uint32_t s = qface[t];
             p = P.face_pair[s] & ~kCutBit;
@@ -846,8 +877,13 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
             int* stk = &W.front[0][0];
             constexpr int kStk = 2 * kWaveFrontier;
             int sp = 0;
+            if (SPLIT) {
+                const int cnt = (int)split[it].count;
+                if (lane < cnt) stk[lane] = split[it].nodes[lane];
+                sp = cnt;
+            }
             // first: the listed top cut of the tree
-            const int ntop = (int)counters[13];
+            const int ntop = SPLIT ? 0 : (int)counters[13];
             for (int base = 0; base < ntop; base += 32) {
                 const int i = base + lane;
                 bool hit = false;
@@ -880,7 +916,51 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 nl += __popc(ml);
             }
             __syncwarp();
+            int rounds = 0;
             while (sp > 0) {
+                if (!SPLIT && split_round > 0 && ++rounds > split_round && sp > MCGPU_SPLIT_STACK) {
+                    // a slow packet: its groups of 8 queries x chunks of 32 roots go
+                    // to the second launch, each walked by its own warp
+                    constexpr int kG = MCGPU_SPLIT_GROUP;
+                    constexpr unsigned kGm = kG == 32 ? 0xFFFFFFFFu : ((1u << kG) - 1u);
+                    unsigned am = __ballot_sync(full, active);
+                    const int chunks = (sp + 31) / 32;
+                    int ng = 0;
+                    for (int g = 0; g < 32 / kG; ++g) ng += ((am >> (kG * g)) & kGm) ? 1 : 0;
+                    uint32_t base_e = 0;
+                    if (lane == 0) base_e = atomicAdd(&counters[14], (uint32_t)(ng * chunks));
+                    base_e = __shfl_sync(full, base_e, 0);
+                    if (base_e + (uint32_t)(ng * chunks) > split_cap) {
+                        // no room: the reserved entries below the cap are left empty
+                        // and this packet finishes its own walk
+                        for (uint32_t e = base_e + lane; e < split_cap && e < base_e + (uint32_t)(ng * chunks); e += 32) {
+                            split[e].packet = pk;
+                            split[e].qmask = 0u;
+                            split[e].count = 0u;
+                        }
+                        rounds = -(1 << 30);
+                    } else {
+                        uint32_t e = base_e;
+                        for (int g = 0; g < 32 / kG; ++g) {
+                            const uint32_t gm = am & (kGm << (kG * g));
+                            if (!gm) continue;
+                            for (int c = 0; c < chunks; ++c, ++e) {
+                                const int cnt = min(32, sp - 32 * c);
+                                if (lane == 0) {
+                                    split[e].packet = pk;
+                                    split[e].qmask = gm;
+                                    split[e].count = (uint32_t)cnt;
+                                }
+                                if (lane < cnt) split[e].nodes[lane] = stk[32 * c + lane];
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    if (rounds >= 0) {
+                        sp = 0;
+                        break;
+                    }
+                }
                 const int take = min(sp, 32);
                 const int base = sp - take;
                 const bool v = lane < take;
@@ -1823,14 +1903,22 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
             W.cvals[cut_buf], W.cl_start, W.cl_n, W.leaf_key_box, (int)P.ncl, W.nodes, W.pairs, W.pair_cap,
             W.counters, W.cand, W.pair_status);
     else {
-        static std::atomic<unsigned long long> attr { 0 };
-        set_smem_once((const void*)k_traverse_wave, (int)kWaveSmem, attr);
+        static std::atomic<unsigned long long> attr { 0 }, attr2 { 0 };
+        set_smem_once((const void*)k_traverse_wave<false>, (int)kWaveSmem, attr);
+        set_smem_once((const void*)k_traverse_wave<true>, (int)kWaveSmem, attr2);
         WaveTop* top = reinterpret_cast<WaveTop*>(W.top);
-        g_launches++;
+        SplitEntry* split = reinterpret_cast<SplitEntry*>(W.split);
+        g_launches += 2; // top cut + first walk
         k_top_cut<<<1, 32, 0, s>>>(W.nodes, (int)P.ncl, top, W.counters);
-        k_traverse_wave<<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
+        k_traverse_wave<false><<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
             W.cvals[cut_buf], W.cl_start, W.cl_n, top, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand,
-            W.pair_status);
+            W.pair_status, split, (uint32_t)W.split_cap, (int)W.split_round);
+        if (W.split_round > 0) {
+            g_launches++;
+            k_traverse_wave<true><<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
+                W.cvals[cut_buf], W.cl_start, W.cl_n, top, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters,
+                W.cand, W.pair_status, split, (uint32_t)W.split_cap, 0);
+        }
     }
 }
 

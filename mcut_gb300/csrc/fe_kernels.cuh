@@ -81,6 +81,8 @@ struct Work {
     uint8_t* cl_n;                    // [ncl] faces in the cluster
     long long* leaf_key_box;          // unused (kept null)
     void* top;                        // [64] top cut of the cut tree (WaveTop, 32 B each)
+    void* split;                      // [split_cap] slow packets' remaining walks (144 B each)
+    uint64_t split_cap;
     Node* nodes;                      // [ncl-1]
     int32_t* parent;                  // [2ncl-1]
     int2* node_range;                 // [ncl-1] leaf range of each internal node
@@ -88,7 +90,8 @@ struct Work {
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
                                       //        5..7 escalations, 8 traversal work cursor, 9 packets, 10 narrow hits,
-                                      //        11 queued projections, 13 top-cut entries
+                                      //        11 queued projections, 13 top-cut entries, 14 split entries,
+//        15 second-launch work cursor
     uint2* packets;                   // [ns] query packets: sorted source positions [x, y]
     uint8_t* cand;                    // [nf]
     uint32_t* plane_slot;             // [nf]
@@ -119,6 +122,7 @@ struct Work {
     uint32_t traversal;               // 0 warp/packet breadth-first, 1 warp/packet depth-first, 2 thread/face
     uint32_t packet_faces;            // source faces per query packet (1..32)
     uint32_t stack_depth;             // per-thread stack of traversal 2 (64 or 512)
+    uint32_t split_round;             // traversal 0: rounds before a slow packet is split (0: never)
 };
 
 // stage launchers (all asynchronous on `s`)

@@ -91,7 +91,9 @@ constexpr size_t oPstat = oRpt + al(kMaxTests * 24ull);
 constexpr size_t oPflag = oPstat + al(3 * 4);
 constexpr size_t oPlist = oPflag + al(kMaxFaces * 4ull);
 constexpr size_t oTop = oPlist + al(kMaxFaces * 4ull);
-constexpr size_t oNrange = oTop + al(64 * 32);
+constexpr size_t kSplitCap = 2048;
+constexpr size_t oSplit = oTop + al(64 * 32);
+constexpr size_t oNrange = oSplit + al(kSplitCap * 144ull);
 constexpr size_t kScratchBytes = oNrange + al(kMaxFaces * 8ull);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -185,6 +187,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.traversal = 0;
     W.packet_faces = 32;
     W.stack_depth = 64;
+    W.split_round = 2;
     W.fbox = reinterpret_cast<double*>(base + oFbox);
     W.mesh_box = reinterpret_cast<unsigned long long*>(base + oMbox);
     uint32_t* keys = reinterpret_cast<uint32_t*>(base + oKeys);
@@ -217,6 +220,8 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.proj_flag = reinterpret_cast<uint32_t*>(base + oPflag);
     W.proj_list = reinterpret_cast<uint32_t*>(base + oPlist);
     W.top = base + oTop;
+    W.split = base + oSplit;
+    W.split_cap = kSplitCap;
     W.node_range = reinterpret_cast<int2*>(base + oNrange);
     W.poly_list = nullptr;
     W.vneed = base + oVneed;

@@ -103,8 +103,8 @@ class Context:
                 r.test_info = self._get(L.DATA_TEST_INFO, np.int8, 4)
         return r
 
-    def set_tuning(self, leaf_size=4, traversal=0, packet_faces=32, stack_depth=64):
-        t = L.Tuning(leaf_size, traversal, packet_faces, stack_depth)
+    def set_tuning(self, leaf_size=4, traversal=0, packet_faces=32, stack_depth=64, split_round=2):
+        t = L.Tuning(leaf_size, traversal, packet_faces, stack_depth, split_round)
         L.check(self._lib.mcgpu_context_set_tuning(self._h, C.byref(t)), "mcgpu_context_set_tuning")
 
     def tuning(self) -> dict:

@@ -9,14 +9,14 @@ import golden_cases as G
 from mcut_gb300 import _lib as L
 from mcut_gb300 import meshgen
 
-TUNINGS = [dict(leaf_size=l, traversal=t, packet_faces=p, stack_depth=d)
-           for l in (1, 4, 16) for (t, p, d) in ((0, 32, 64), (0, 7, 64), (1, 32, 64), (1, 16, 64), (2, 32, 64),
-                                                 (2, 32, 512))]
+TUNINGS = [dict(leaf_size=l, traversal=t, packet_faces=p, stack_depth=d, split_round=r)
+           for l in (1, 4, 16) for (t, p, d, r) in ((0, 32, 64, 2), (0, 32, 64, 0), (0, 7, 64, 1), (1, 32, 64, 0),
+                                                    (1, 16, 64, 0), (2, 32, 64, 0), (2, 32, 512, 0))]
 
 
 def test_tuning_arguments_checked_without_a_gpu():
     lib = L.load()
-    t = L.Tuning(4, 0, 32, 64)
+    t = L.Tuning(4, 0, 32, 64, 2)
     assert lib.mcgpu_context_set_tuning(None, C.byref(t)) == L.INVALID_VALUE
     assert lib.mcgpu_context_get_tuning(None, C.byref(t)) == L.INVALID_VALUE
     assert lib.mcgpu_autotune(None, 0, None, 1, None, None) == L.INVALID_VALUE
@@ -95,3 +95,26 @@ def test_profiled_dispatches_repeat(ctx):
         assert r.status in (0, 1)
         if k % 2 == 0:
             assert sum(r.stage_ms.values()) > 0
+
+
+@pytest.mark.gpu
+def test_split_capacity_overflow_is_harmless():
+    """Slow packets hand their remaining walk to a second launch; with the
+    entry capacity forced tiny most of them must finish their own walk, with
+    the same result."""
+    import os
+    from mcut_gb300 import Context
+    s, c = meshgen.sphere_heightfield(16.0, level=6, n=512)
+    a = Context(0)
+    want = a.dispatch(s, c, keep_pairs=True)
+    os.environ["MCGPU_SPLIT_CAP"] = "3"
+    try:
+        b = Context(0)
+    finally:
+        del os.environ["MCGPU_SPLIT_CAP"]
+    got = b.dispatch(s, c, keep_pairs=True)
+    assert got.num_pairs == want.num_pairs and got.status == want.status
+    assert np.array_equal(np.unique(got.pairs, axis=0), np.unique(want.pairs, axis=0))
+    assert np.array_equal(got.record_ids, want.record_ids) and G.same_bits(got.record_points, want.record_points)
+    a.close()
+    b.close()
