@@ -113,6 +113,8 @@ struct Layout {
 struct mcgpu_context_t {
     int device = 0;
     cudaStream_t s = nullptr;
+    cudaStream_t s2 = nullptr; // independent launches run here beside s (fork / join by events)
+    cudaEvent_t fork[2] = {}, join[2] = {};
     cudaEvent_t ev[16] = {};  // begin / end of each stage (MCGPU_PROFILE)
     DevBuf buf[B_COUNT];
     PinBuf pin_counters, pin_tab, pin_stage, pin_idx;
@@ -746,8 +748,13 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         aux[0] = launch_sort(P, W, wide, key_bits, s, aux[1]);
         rec(c, 2 * MCGPU_STAGE_SORT + 1);
         rec(c, 2 * MCGPU_STAGE_HIERARCHY);
+        // the query packets (source keys) beside the cut tree's build
+        ck(cudaEventRecord(c->fork[0], s), "fork");
+        ck(cudaStreamWaitEvent(c->s2, c->fork[0], 0), "fork");
+        launch_packets(P, W, aux[0], c->s2);
+        ck(cudaEventRecord(c->join[0], c->s2), "join");
         launch_hierarchy(P, W, wide, aux[1], s);
-        launch_packets(P, W, aux[0], s);
+        ck(cudaStreamWaitEvent(s, c->join[0], 0), "join");
         rec(c, 2 * MCGPU_STAGE_HIERARCHY + 1);
         rec(c, 2 * MCGPU_STAGE_TRAVERSE);
         launch_traverse(P, W, aux[0], aux[1], false, s);
@@ -813,8 +820,13 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     const uint32_t keep = flags & MCGPU_KEEP_TESTS;
     run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) {
         rec(c, 2 * MCGPU_STAGE_ADJACENCY);
-        ck(cudaMemsetAsync(W.vneed, 0, L.nv, s), "memset");
-        launch_adjacency_planes(P, W, s);
+        // vertex -> face incidence beside the candidate-face planes
+        ck(cudaEventRecord(c->fork[1], s), "fork");
+        ck(cudaStreamWaitEvent(c->s2, c->fork[1], 0), "fork");
+        launch_incidence(P, W, c->s2);
+        ck(cudaEventRecord(c->join[1], c->s2), "join");
+        launch_planes(P, W, s);
+        ck(cudaStreamWaitEvent(s, c->join[1], 0), "join");
         rec(c, 2 * MCGPU_STAGE_ADJACENCY + 1);
         rec(c, 2 * MCGPU_STAGE_NARROW);
         launch_tests(P, W, s);
@@ -936,6 +948,11 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
         if (const char* e = getenv("MCGPU_SPLIT_CAP")) c->split_cap = strtoull(e, nullptr, 10);
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
+        ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");
+        for (int k = 0; k < 2; ++k) {
+            ck(cudaEventCreateWithFlags(&c->fork[k], cudaEventDisableTiming), "event");
+            ck(cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming), "event");
+        }
         for (auto& e : c->ev) ck(cudaEventCreate(&e), "event");
         *out = c;
         return MCGPU_OK;
@@ -959,6 +976,12 @@ int mcgpu_context_release(mcgpu_context c)
         if (e) cudaEventDestroy(e);
     for (auto& g : c->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (c->s2) cudaStreamSynchronize(c->s2);
+    for (int k = 0; k < 2; ++k) {
+        if (c->fork[k]) cudaEventDestroy(c->fork[k]);
+        if (c->join[k]) cudaEventDestroy(c->join[k]);
+    }
+    if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s) cudaStreamDestroy(c->s);
     delete c;
     return MCGPU_OK;

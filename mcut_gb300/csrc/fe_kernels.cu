@@ -1922,7 +1922,7 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
     }
 }
 
-void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
+void launch_planes(const Problem& P, Work& W, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
     g_launches++;
@@ -1932,6 +1932,12 @@ void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
     if (W.tri_stride)
         k_triplets<<<grid_for(1024), kBlock, 0, s>>>(P, W.poly_list, W.counters, W.plane_slot, (FacePlane*)W.planes,
             (Trip*)W.tri_scratch, W.tri_scratch_cap, W.tri_stride, W.pair_status);
+}
+
+void launch_incidence(const Problem& P, Work& W, cudaStream_t s)
+{
+    const int g = grid_for(P.nf);
+    cudaMemsetAsync(W.vneed, 0, (size_t)P.nv, s);
     g_launches++;
     k_mark_vertices<<<g, kBlock, 0, s>>>(P, W.cand, W.vneed);
     cudaMemsetAsync(W.voff, 0, sizeof(uint32_t) * ((size_t)P.nv + 1), s);
@@ -1941,6 +1947,12 @@ void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
     cudaMemsetAsync(W.vcur, 0, sizeof(uint32_t) * (size_t)P.nv, s);
     g_launches++;
     k_vf_fill<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff, W.vcur, W.vface, W.inc_cap);
+}
+
+void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s)
+{
+    launch_planes(P, W, s);
+    launch_incidence(P, W, s);
 }
 
 void launch_tests(const Problem& P, Work& W, cudaStream_t s)

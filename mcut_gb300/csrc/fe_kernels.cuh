@@ -131,7 +131,9 @@ int launch_sort(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStr
 void launch_hierarchy(const Problem& P, Work& W, bool wide_keys, int cut_buf, cudaStream_t s);
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s);
 void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s);
-void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s);
+void launch_adjacency_planes(const Problem& P, Work& W, cudaStream_t s); // planes + incidence on one stream
+void launch_planes(const Problem& P, Work& W, cudaStream_t s);           // candidate-face planes (+ triplets)
+void launch_incidence(const Problem& P, Work& W, cudaStream_t s);        // vertex -> face incidence
 void launch_tests(const Problem& P, Work& W, cudaStream_t s);
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s);
 int launch_records(const Problem& P, Work& W, uint32_t n_records, cudaStream_t s);
