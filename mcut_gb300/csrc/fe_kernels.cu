@@ -96,15 +96,29 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
             const bool is_cut = (fp & kCutBit) != 0;
             const uint32_t o = face_o(P, f), n = face_n(P, f);
             const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
+            // std::min / std::max folds from +-DBL_MAX in vertex order
+            // (bvh.cpp:242-314): each running extreme is kept with its dkey(),
+            // so a step converts only the new coordinate; a strict compare
+            // keeps the first of equal keys, as the reference's fold does
             Box b;
-            for (int j = 0; j < 3; ++j) { b.mn[j] = 1.7976931348623157e308; b.mx[j] = -1.7976931348623157e308; }
+            long long kmn[3], kmx[3];
+            for (int j = 0; j < 3; ++j) {
+                b.mn[j] = 1.7976931348623157e308;
+                b.mx[j] = -1.7976931348623157e308;
+                kmn[j] = dkey(b.mn[j]);
+                kmx[j] = dkey(b.mx[j]);
+            }
             bool bad = false;
             for (uint32_t k = 0; k < n; ++k) {
                 const uint32_t v = P.fidx[o + k];
                 if (v < vlo || v >= vhi) { bad = true; continue; }
                 double x[3];
                 load_v(P, v, x);
-                for (int j = 0; j < 3; ++j) { b.mx[j] = dmax_ref(b.mx[j], x[j]); b.mn[j] = dmin_ref(b.mn[j], x[j]); }
+                for (int j = 0; j < 3; ++j) {
+                    const long long kx = dkey(x[j]);
+                    if (kmx[j] < kx) { kmx[j] = kx; b.mx[j] = x[j]; }
+                    if (kx < kmn[j]) { kmn[j] = kx; b.mn[j] = x[j]; }
+                }
             }
             if (bad) atomicOr(&pair_status[p], ST_INVALID);
             if (is_cut) {
