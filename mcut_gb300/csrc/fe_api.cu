@@ -93,7 +93,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -695,6 +695,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.fbox = c->buf[B_FBOX].get<double>(L.nf * 6);
     W.fbox32 = c->buf[B_LKB].get<float>(L.nf * 6);
     W.mesh_box = c->buf[B_MESHBOX].get<unsigned long long>((size_t)n * 12);
+    W.mesh_frame = c->buf[B_FRAME].get<uint8_t>((size_t)n * 64);
     const size_t ksz = wide ? 8 : 4;
     for (int b = 0; b < 2; ++b) {
         W.skeys[b] = c->buf[b ? B_SK1 : B_SK0].get<uint8_t>((L.ns + L.nc) * ksz);

@@ -1,7 +1,7 @@
 // Kernels of the GB300 intersection front end.
 //
 // Stage map (reference function -> kernel):
-//   bvh.cpp:242-433  face boxes, mesh box, Morton codes   -> k_face_bounds, k_morton
+//   bvh.cpp:242-433  face boxes, mesh box, Morton codes   -> k_vertex_bounds, k_mesh_frames, k_face_bounds
 //   bvh.cpp:437-442  std::sort by Morton code             -> radix_sort_pairs (fe_sort.cu)
 //   bvh.cpp:444-635  implicit-tree build + refit          -> k_karras, k_refit (LBVH)
 //   bvh.cpp:638-783  intersectOIBVHs                       -> k_traverse
@@ -72,69 +72,46 @@ __device__ __forceinline__ void mesh_box_flush(unsigned long long* __restrict__ 
     }
 }
 
-constexpr int kBoundsItems = 8; // faces per thread per tile; a tile is kBlock * kBoundsItems consecutive faces
+constexpr int kBoundsItems = 8; // vertices per thread per tile; a tile is kBlock * kBoundsItems consecutive vertices
 
-__global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
-    float* __restrict__ fbox32, unsigned long long* __restrict__ mesh_box, uint32_t* __restrict__ pair_status)
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v)
 {
-    // Per-mesh boxes only steer Morton codes. Tiles are runs of consecutive
-    // faces, so a tile almost always belongs to one mesh: each thread folds
-    // its faces in registers, the block folds in shared memory, and one
-    // thread issues the atomics. Tiles that straddle meshes fall back to
-    // per-lane atomics.
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// Mesh boxes (the union of each mesh's vertices; they only steer the Morton
+// codes, so a vertex no face uses may widen them harmlessly). Tiles are runs
+// of consecutive vertices, almost always of one mesh: each thread folds in
+// registers, the block folds in shared memory, one thread issues the
+// atomics; a tile that straddles meshes falls back to per-thread atomics.
+__global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned long long* __restrict__ mesh_box)
+{
     __shared__ unsigned long long red[kBlock / 32][6];
-    const uint32_t tiles = (P.nf + kBlock * kBoundsItems - 1) / (kBlock * kBoundsItems);
+    __shared__ uint32_t skey;
+    const uint32_t tiles = (P.nv + kBlock * kBoundsItems - 1) / (kBlock * kBoundsItems);
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        uint32_t key = kNone;
+        uint32_t key = kNone, p = 0;
         bool mixed = false;
         unsigned long long lo[3] = { ~0ull, ~0ull, ~0ull }, hi[3] = { 0ull, 0ull, 0ull };
         for (int it = 0; it < kBoundsItems; ++it) {
-            const uint32_t f = tile * (kBlock * kBoundsItems) + it * kBlock + threadIdx.x;
-            if (f >= P.nf) break;
-            const uint32_t fp = P.face_pair[f];
-            const uint32_t p = fp & ~kCutBit;
-            const bool is_cut = (fp & kCutBit) != 0;
-            const uint32_t o = face_o(P, f), n = face_n(P, f);
-            const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
-            // std::min / std::max folds from +-DBL_MAX in vertex order
-            // (bvh.cpp:242-314): each running extreme is kept with its dkey(),
-            // so a step converts only the new coordinate; a strict compare
-            // keeps the first of equal keys, as the reference's fold does
-            Box b;
-            long long kmn[3], kmx[3];
-            for (int j = 0; j < 3; ++j) {
-                b.mn[j] = 1.7976931348623157e308;
-                b.mx[j] = -1.7976931348623157e308;
-                kmn[j] = dkey(b.mn[j]);
-                kmx[j] = dkey(b.mx[j]);
-            }
-            bool bad = false;
-            for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t v = P.fidx[o + k];
-                if (v < vlo || v >= vhi) { bad = true; continue; }
-                double x[3];
-                load_v(P, v, x);
-                for (int j = 0; j < 3; ++j) {
-                    const long long kx = dkey(x[j]);
-                    if (kmx[j] < kx) { kmx[j] = kx; b.mx[j] = x[j]; }
-                    if (kx < kmn[j]) { kmn[j] = kx; b.mn[j] = x[j]; }
+            const uint32_t v = tile * (kBlock * kBoundsItems) + it * kBlock + threadIdx.x;
+            if (v >= P.nv) break;
+            if (it == 0) { // the pair of the thread's first vertex, then a forward walk
+                uint32_t l = 0, h = P.n_pairs;
+                while (h - l > 1) {
+                    const uint32_t mid = (l + h) >> 1;
+                    if (P.pair_vbase[mid] <= v) l = mid; else h = mid;
                 }
+                p = l;
             }
-            if (bad) atomicOr(&pair_status[p], ST_INVALID);
-            if (is_cut) {
-                const double eps = P.pair_eps[p];
-                if (eps > 0.0)
-                    for (int j = 0; j < 3; ++j) { b.mx[j] = b.mx[j] + eps; b.mn[j] = b.mn[j] - eps; }
-            }
-            double2* d = reinterpret_cast<double2*>(fbox + (size_t)f * 6);
-            d[0] = make_double2(b.mn[0], b.mn[1]);
-            d[1] = make_double2(b.mn[2], b.mx[0]);
-            d[2] = make_double2(b.mx[1], b.mx[2]);
-            float2* d32 = reinterpret_cast<float2*>(fbox32 + (size_t)f * 6);
-            d32[0] = make_float2(f32_rd(b.mn[0]), f32_rd(b.mn[1]));
-            d32[1] = make_float2(f32_rd(b.mn[2]), f32_ru(b.mx[0]));
-            d32[2] = make_float2(f32_ru(b.mx[1]), f32_ru(b.mx[2]));
-            const uint32_t k = p * 2 + (is_cut ? 1u : 0u);
+            while (v >= P.pair_vbase[p + 1]) ++p;
+            const uint32_t k = p * 2 + ((v - P.pair_vbase[p]) >= P.pair_vs[p] ? 1u : 0u);
+            double x[3];
+            load_v(P, v, x);
             if (key != kNone && k != key) {
                 mesh_box_flush(mesh_box, key, lo, hi);
                 for (int j = 0; j < 3; ++j) { lo[j] = ~0ull; hi[j] = 0ull; }
@@ -142,12 +119,10 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
             }
             key = k;
             for (int j = 0; j < 3; ++j) {
-                lo[j] = min(lo[j], ord_of(b.mn[j]));
-                hi[j] = max(hi[j], ord_of(b.mx[j]));
+                lo[j] = min(lo[j], ord_of(x[j]));
+                hi[j] = max(hi[j], ord_of(x[j]));
             }
         }
-        // block-uniform key? (threads without faces count as matching)
-        __shared__ uint32_t skey;
         if (threadIdx.x == 0) skey = key;
         __syncthreads();
         const uint32_t k0 = skey;
@@ -177,42 +152,90 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
     }
 }
 
-__device__ __forceinline__ uint32_t expand_bits(uint32_t v)
+// Per mesh: the fp32 frame the Morton codes are quantised in -- the mesh
+// box rounded outward, and 1023 / extent per axis (0 for a flat axis).
+__global__ void k_mesh_frames(const unsigned long long* __restrict__ mesh_box, uint32_t nmesh,
+    float4* __restrict__ frame)
 {
-    v = (v * 0x00010001u) & 0xFF0000FFu;
-    v = (v * 0x00000101u) & 0x0F00F00Fu;
-    v = (v * 0x00000011u) & 0xC30C30C3u;
-    v = (v * 0x00000005u) & 0x49249249u;
-    return v;
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < nmesh; m += gridDim.x * blockDim.x) {
+        const unsigned long long* mb = mesh_box + (size_t)m * 6;
+        float lo[3], sc[3];
+        for (int j = 0; j < 3; ++j) {
+            lo[j] = f32_rd(of_ord(mb[j]));
+            const float ext = f32_ru(of_ord(mb[3 + j])) - lo[j];
+            sc[j] = ext > 0.0f ? __fdiv_rn(1023.0f, ext) : 0.0f;
+        }
+        frame[2 * m] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        frame[2 * m + 1] = make_float4(sc[0], sc[1], sc[2], 0.0f);
+    }
 }
 
-// Morton code of the box centre in its mesh's box (morton3D, bvh.cpp:196-217),
-// written to the source-face or cut-face key list.
+// Face boxes (bvh.cpp:242-314, cut boxes enlarged as preproc.cpp:2693) and
+// each face's Morton key (bvh.cpp:370-433). The code only orders leaves --
+// any order gives the same pair set -- so it is formed in fp32 from the
+// outward-rounded box: centre relative to the mesh frame, 10 bits per axis;
+// the mesh bit above the key puts every source key before every cut key so
+// one sort orders both meshes.
 template <typename K>
-__global__ void __launch_bounds__(kBlock) k_morton(Problem P, const float* __restrict__ fbox32,
-    const unsigned long long* __restrict__ mesh_box, K* __restrict__ skey, uint32_t* __restrict__ sval,
-    K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit)
+__global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
+    float* __restrict__ fbox32, const float4* __restrict__ frame, K* __restrict__ skey, uint32_t* __restrict__ sval,
+    K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit, uint32_t* __restrict__ pair_status)
 {
-    // The code only orders leaves (any order gives the same pair set), so it
-    // is formed in fp32 from the outward-rounded face boxes: centre relative
-    // to the mesh box, quantised to 10 bits per axis.
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         const uint32_t fp = P.face_pair[f];
         const uint32_t p = fp & ~kCutBit;
         const bool is_cut = (fp & kCutBit) != 0;
-        const float2* bp = reinterpret_cast<const float2*>(fbox32 + (size_t)f * 6);
-        const float2 x = __ldg(bp), y = __ldg(bp + 1), z = __ldg(bp + 2);
-        const float lo[3] = { x.x, x.y, y.x }, hi[3] = { y.y, z.x, z.y };
-        const unsigned long long* mb = mesh_box + ((size_t)p * 2 + (is_cut ? 1 : 0)) * 6;
-        uint32_t c[3];
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
+        // std::min / std::max folds from +-DBL_MAX in vertex order: each
+        // running extreme is kept with its dkey(), so a step converts only
+        // the new coordinate; a strict compare keeps the first of equal keys,
+        // as the reference's fold does
+        Box b;
+        long long kmn[3], kmx[3];
         for (int j = 0; j < 3; ++j) {
-            const float mlo = f32_rd(of_ord(__ldg(&mb[j]))), mhi = f32_ru(of_ord(__ldg(&mb[3 + j])));
-            const float ext = mhi - mlo;
-            const float t = ext > 0.0f ? (0.5f * (lo[j] + hi[j]) - mlo) * __fdiv_rn(1023.0f, ext) : 0.0f;
-            c[j] = expand_bits((uint32_t)fminf(fmaxf(t, 0.0f), 1023.0f));
+            b.mn[j] = 1.7976931348623157e308;
+            b.mx[j] = -1.7976931348623157e308;
+            kmn[j] = dkey(b.mn[j]);
+            kmx[j] = dkey(b.mx[j]);
         }
-        // the mesh bit puts every source key before every cut key: one sort orders both meshes
-        const K key = ((K)p << kMortonBits) | (K)(c[0] * 4 + c[1] * 2 + c[2]) | ((K)(is_cut ? 1 : 0) << mesh_bit);
+        bool bad = false;
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = P.fidx[o + k];
+            if (v < vlo || v >= vhi) { bad = true; continue; }
+            double x[3];
+            load_v(P, v, x);
+            for (int j = 0; j < 3; ++j) {
+                const long long kx = dkey(x[j]);
+                if (kmx[j] < kx) { kmx[j] = kx; b.mx[j] = x[j]; }
+                if (kx < kmn[j]) { kmn[j] = kx; b.mn[j] = x[j]; }
+            }
+        }
+        if (bad) atomicOr(&pair_status[p], ST_INVALID);
+        if (is_cut) {
+            const double eps = P.pair_eps[p];
+            if (eps > 0.0)
+                for (int j = 0; j < 3; ++j) { b.mx[j] = b.mx[j] + eps; b.mn[j] = b.mn[j] - eps; }
+        }
+        double2* d = reinterpret_cast<double2*>(fbox + (size_t)f * 6);
+        d[0] = make_double2(b.mn[0], b.mn[1]);
+        d[1] = make_double2(b.mn[2], b.mx[0]);
+        d[2] = make_double2(b.mx[1], b.mx[2]);
+        float lo[3], hi[3];
+        for (int j = 0; j < 3; ++j) { lo[j] = f32_rd(b.mn[j]); hi[j] = f32_ru(b.mx[j]); }
+        float2* d32 = reinterpret_cast<float2*>(fbox32 + (size_t)f * 6);
+        d32[0] = make_float2(lo[0], lo[1]);
+        d32[1] = make_float2(lo[2], hi[0]);
+        d32[2] = make_float2(hi[1], hi[2]);
+        const uint32_t m = p * 2 + (is_cut ? 1u : 0u);
+        const float4 fl = __ldg(&frame[2 * m]), fs = __ldg(&frame[2 * m + 1]);
+        const float c0 = (0.5f * (lo[0] + hi[0]) - fl.x) * fs.x;
+        const float c1 = (0.5f * (lo[1] + hi[1]) - fl.y) * fs.y;
+        const float c2 = (0.5f * (lo[2] + hi[2]) - fl.z) * fs.z;
+        const uint32_t m0 = expand_bits((uint32_t)fminf(fmaxf(c0, 0.0f), 1023.0f));
+        const uint32_t m1 = expand_bits((uint32_t)fminf(fmaxf(c1, 0.0f), 1023.0f));
+        const uint32_t m2 = expand_bits((uint32_t)fminf(fmaxf(c2, 0.0f), 1023.0f));
+        const K key = ((K)p << kMortonBits) | (K)(m0 * 4 + m1 * 2 + m2) | ((K)(is_cut ? 1 : 0) << mesh_bit);
         const uint32_t local = f - P.pair_fbase[p];
         if (is_cut) {
             const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);
@@ -226,6 +249,9 @@ __global__ void __launch_bounds__(kBlock) k_morton(Problem P, const float* __res
     }
 }
 
+
+// Morton code of the box centre in its mesh's box (morton3D, bvh.cpp:196-217),
+// written to the source-face or cut-face key list.
 // ---------------------------------------------------------------------------
 // Karras (HPG 2012) hierarchy over the sorted cut-face keys; duplicate keys
 // are ordered by position.
@@ -1573,12 +1599,20 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
         uint32_t code = 0, slot = 0;
         if (i < nt) {
             const Test t = tests[i];
-            const int* tri = planes[plane_slot[t.g]].tri;
-            const int t0 = tri[0], t1 = tri[1], t2 = tri[2];
+            const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
+            // a triangle's plane-defining vertices are its own three (a
+            // degenerate triangle makes its whole pair degenerate, and the hit
+            // pass drops that pair's results); a polygon's come from k_triplets
+            int t0 = 0, t1 = 1, t2 = 2;
+            if (n != 3) {
+                const int* tri = planes[plane_slot[t.g]].tri;
+                t0 = tri[0];
+                t1 = tri[1];
+                t2 = tri[2];
+            }
             int8_t sq = 0, sr = 0;
             char type = '0';
             if (t0 >= 0) {
-                const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
                 double q[3], r[3], a[3], b[3], c[3];
                 load_v(P, t.q, q);
                 load_v(P, t.r, r);
@@ -1600,7 +1634,7 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
             hit = type != '0';
             if (!hit && keep_tests) reinterpret_cast<char4*>(test_info)[i] = make_char4(sq, sr, type, 0);
             // the first hit on a triangle queues the rest of its plane
-            if (hit && face_n(P, t.g) == 3) {
+            if (hit && n == 3) {
                 first_hit = atomicExch(&proj_flag[plane_slot[t.g]], 1u) == 0u;
                 slot = t.g;
             }
@@ -1648,7 +1682,7 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NH_MINB) k_narrow_hits(Problem P
     const uint2* __restrict__ hits, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
     unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
-    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status)
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ pair_status, const int32_t* __restrict__ pair_bad)
 {
     const uint64_t nh = min((uint64_t)counters[10], test_cap);
     for (uint64_t h0 = blockIdx.x * (uint64_t)blockDim.x; h0 < nh; h0 += (uint64_t)gridDim.x * blockDim.x) {
@@ -1687,7 +1721,12 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NH_MINB) k_narrow_hits(Problem P
                 rec = pip == 'i';
             }
             const uint32_t p = P.face_pair[t.g] & ~kCutBit;
-            if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
+            if (pair_bad[p] != kNoBad) {
+                // a pair with a degenerate face has no narrow phase (the reference
+                // stops before it): no records, no flags
+                rec = false;
+                pip = 0;
+            } else if (((type == 'q' || type == 'r' || type == 'p') && (pip == 'i' || pip == 'v' || pip == 'e'))
                 || (type == '1' && (pip == 'v' || pip == 'e'))) {
                 if (!(*(volatile uint32_t*)&pair_status[p] & ST_GP)) atomicOr(&pair_status[p], ST_GP);
             }
@@ -1827,16 +1866,18 @@ int grid_for(uint64_t n)
 // ---------------------------------------------------------------------------
 void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s)
 {
+    float4* frame = reinterpret_cast<float4*>(W.mesh_frame);
+    g_launches += 3;
+    k_vertex_bounds<<<grid_for(P.nv / kBoundsItems + 1), kBlock, 0, s>>>(P, W.mesh_box);
+    k_mesh_frames<<<(2 * P.n_pairs + 255) / 256, 256, 0, s>>>(W.mesh_box, 2 * P.n_pairs, frame);
     const int g = grid_for(P.nf);
-    g_launches++;
-    k_face_bounds<<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, W.mesh_box, W.pair_status);
-    g_launches++;
     if (wide)
-        k_morton<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox32, W.mesh_box,
-            (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits);
+        k_face_bounds<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame,
+            (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits,
+            W.pair_status);
     else
-        k_morton<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox32, W.mesh_box, (uint32_t*)W.skeys[0], W.svals[0],
-            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits);
+        k_face_bounds<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame, (uint32_t*)W.skeys[0], W.svals[0],
+            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status);
 }
 
 int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)
@@ -1989,7 +2030,8 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     k_finish_planes<<<grid_for(W.plane_cap), kBlock, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot, W.proj_list,
         W.counters);
     k_narrow_hits<<<g, kBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
-        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status);
+        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
+        W.pair_bad);
 }
 
 // Records up to this many are ordered by k_rank_records (one launch). With

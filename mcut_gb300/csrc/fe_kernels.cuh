@@ -69,6 +69,7 @@ struct Work {
     double* fbox;                     // [nf*6]
     float* fbox32;                    // [nf*6] the same boxes rounded outward to fp32
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
+    void* mesh_frame;                 // [n_pairs*2*2] float4: fp32 box low corner, 1023 / extent
     // sort buffers (keys u32 for one pair, u64 for batches); the cut keys and
     // values follow the source ones in the same arrays (ckeys[b] = skeys[b] + ns)
     void* skeys[2];                   // source-face keys

@@ -94,7 +94,8 @@ constexpr size_t oTop = oPlist + al(kMaxFaces * 4ull);
 constexpr size_t kSplitCap = 2048;
 constexpr size_t oSplit = oTop + al(64 * 32);
 constexpr size_t oNrange = oSplit + al(kSplitCap * 144ull);
-constexpr size_t kScratchBytes = oNrange + al(kMaxFaces * 8ull);
+constexpr size_t oFrame = oNrange + al(kMaxFaces * 8ull);
+constexpr size_t kScratchBytes = oFrame + al(64);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -223,6 +224,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.split = base + oSplit;
     W.split_cap = kSplitCap;
     W.node_range = reinterpret_cast<int2*>(base + oNrange);
+    W.mesh_frame = base + oFrame;
     W.poly_list = nullptr;
     W.vneed = base + oVneed;
     W.voff = reinterpret_cast<uint32_t*>(base + oVoff);
