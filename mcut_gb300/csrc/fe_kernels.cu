@@ -399,15 +399,18 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
     return b;
 }
 
-// bottom-up refit: the second child to arrive at a node merges both boxes
-// Bottom-up boxes. Block b owns leaf clusters [kRefitWin b, kRefitWin (b+1)): a node
-// whose leaf range lies inside that window has both children finished by
-// threads of the same block, so its arrival counter and the children's boxes
-// live in shared memory (block-scope ordering, no global round trip); the
-// nodes above the window use global acquire-release arrival counters. The
-// second thread to arrive at a node carries the union upward; every node's
-// child boxes are also written to the tree for the traversal.
-constexpr int kRefitWin = 256;
+// Bottom-up boxes. Block b owns leaf clusters [kRefitWin b, kRefitWin (b+1)): a
+// node whose leaf range lies inside that window has both children finished
+// by threads of the same block, so its arrival counter and its children's
+// boxes live in shared memory, and the climb through the window touches no
+// global memory (a fence then waits on shared memory only). The block then
+// writes its finished nodes with vector stores, and the threads that reached
+// a node above the window carry on through global acquire-release arrival
+// counters, the second to arrive at a node carrying the union upward.
+#ifndef MCGPU_REFIT_WIN
+#define MCGPU_REFIT_WIN 256
+#endif
+constexpr int kRefitWin = MCGPU_REFIT_WIN;
 __global__ void __launch_bounds__(kRefitWin) k_refit(Problem P, const float* __restrict__ fbox32,
     const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n,
     int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, const int2* __restrict__ node_range,
@@ -419,44 +422,69 @@ __global__ void __launch_bounds__(kRefitWin) k_refit(Problem P, const float* __r
     sflag[threadIdx.x] = 0;
     __syncthreads();
     const int i = w0 + threadIdx.x;
-    if (i >= n) return;
+    bool carry = false; // holds a box for a node above the window
     FBox fb;
-    for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
-    const uint32_t s0 = cl_start[i], cn = cl_n[i];
-    uint32_t lf[16];
-    for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
-    for (uint32_t t = 0; t < cn; ++t) {
-        const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
-        const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
-        fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
-        fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
-    }
-    fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
-    uint32_t pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
-    for (;;) {
-        const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
-        // the next parent and this node's range are read before the arrival
-        const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
-        const int2 rg = __ldg(&node_range[node]);
-        Node* nd = &nodes[node];
-        put_child(nd, slot, fb);
-        FBox o;
-        if (rg.x >= w0 && rg.y <= w1) {
-            // inside the window: node index in [w0, w1]
-            const int k = node - w0;
+    uint32_t pe = 0;
+    if (i < n) {
+        for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
+        const uint32_t s0 = cl_start[i], cn = cl_n[i];
+        uint32_t lf[16];
+        for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
+        for (uint32_t t = 0; t < cn; ++t) {
+            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
+            const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
+            fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
+            fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
+        }
+        fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
+        pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
+        for (;;) {
+            const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
+            const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
+            const int2 rg = __ldg(&node_range[node]);
+            if (rg.x < w0 || rg.y > w1) { carry = true; break; }
+            const int k = node - w0; // a node's index is one end of its range
             sbox[k][slot] = fb;
             __threadfence_block();
             const uint32_t prev = atomicAdd(&sflag[k], 1u);
             __threadfence_block();
             if (prev == 0) break;
-            o = sbox[k][slot ^ 1];
-        } else {
-            // acq_rel arrival: releases this child's box, acquires the sibling's
-            unsigned prev;
-            asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&flag[node]) : "memory");
-            if (prev == 0) break;
-            o = get_child(nd, slot ^ 1);
+            const FBox o = sbox[k][slot ^ 1];
+            for (int j = 0; j < 3; ++j) {
+                fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
+                fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
+            }
+            fb.plo = min(fb.plo, o.plo);
+            fb.phi = max(fb.phi, o.phi);
+            if (node == 0) break;
+            pe = next;
         }
+    }
+    __syncthreads();
+    {
+        // every node inside the window has had both arrivals
+        const int k = threadIdx.x, node = w0 + k;
+        if (node < n - 1 && sflag[k] == 2u) {
+            const FBox& l = sbox[k][0];
+            const FBox& r = sbox[k][1];
+            Node* nd = &nodes[node];
+            nd->b0 = make_float4(l.lo[0], l.lo[1], l.lo[2], l.hi[0]);
+            nd->b1 = make_float4(l.hi[1], l.hi[2], r.lo[0], r.lo[1]);
+            nd->b2 = make_float4(r.lo[2], r.hi[0], r.hi[1], r.hi[2]);
+            *reinterpret_cast<uint2*>(nd->prange) = make_uint2(l.plo | (l.phi << 16), r.plo | (r.phi << 16));
+        }
+    }
+    if (!carry) return;
+    for (;;) {
+        const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
+        const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
+        Node* nd = &nodes[node];
+        put_child(nd, slot, fb);
+        // acq_rel arrival: releases this child's box, acquires the sibling's
+        unsigned prev;
+        asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&flag[node]) : "memory");
+        if (prev == 0) break;
+        const FBox o = get_child(nd, slot ^ 1);
         for (int j = 0; j < 3; ++j) {
             fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
             fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
