@@ -68,7 +68,7 @@ constexpr size_t oFbox = oPackets + al(kMaxFaces * 8ull);
 constexpr size_t oMbox = oFbox + al(kMaxFaces * 48ull);
 constexpr size_t oKeys = oMbox + al(12 * 8);             // 8 arrays of kMaxFaces x 4 B
 constexpr size_t oSortTmp = oKeys + al(8ull * kMaxFaces * 4);
-constexpr size_t kSortTmpBytes = 256ull * ((kMaxTests + 4095) / 4096) * 4 + 4096; // table + scan block sums
+constexpr size_t kSortTmpBytes = radix_sort_temp_bytes(kMaxTests) + 4096; // table + scan block sums
 constexpr size_t oNodes = oSortTmp + al(kSortTmpBytes);
 constexpr size_t oParent = oNodes + al(kMaxFaces * sizeof(Node));
 constexpr size_t oRflag = oParent + al(2ull * kMaxFaces * 4);

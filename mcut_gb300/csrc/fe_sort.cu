@@ -1,12 +1,15 @@
-// LSD radix sort of (key, uint32 value) pairs, 8-bit digits, stable.
+// LSD radix sort of (key, uint32 value) pairs, kSortDigitBits-bit digits,
+// stable.
 //
 // One pass = three launches:
 //   upsweep  : per-tile digit histogram (shared-memory atomics)
-//   scan     : exclusive scan of the digit-major [256 x tiles] table (one CTA)
-//   downsweep: each warp ranks its keys with __match_any_sync in input order,
-//              warps are combined per digit in shared memory, the tile is
-//              reordered by digit in shared memory and written out so that
-//              consecutive threads store consecutive slots of a digit's run.
+//   scan     : exclusive scan of the digit-major [digits x tiles] table, one
+//              CTA per digit
+//   downsweep: each warp ranks its keys in input order (lanes of equal digit
+//              found by one ballot per digit bit), warps are combined per
+//              digit in shared memory, the tile is reordered by digit in
+//              shared memory and written out so that consecutive threads
+//              store consecutive slots of a digit's run.
 // A tile is 256 threads x 16 keys. Keys and values stream through HBM once
 // per launch; the histogram table stays in L2.
 #include <algorithm>
@@ -32,7 +35,14 @@ constexpr int kThreads = 256;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;
 constexpr int kWarps = kThreads / 32;
-constexpr int kDigits = 256;
+constexpr int kBits = kSortDigitBits;
+constexpr int kDigits = (int)kSortDigits;
+constexpr uint32_t kMask = kSortDigits - 1u;
+constexpr int kPer = kDigits / kThreads; // consecutive digits a thread owns in the block-wide scans
+static_assert(kTile == (int)kSortTile, "tile size");
+static_assert(kDigits >= kThreads && kDigits % kThreads == 0, "digits per thread");
+// the per-warp digit counts alias the tile's key area
+static_assert((size_t)kWarps * kDigits * 4 <= (size_t)kTile * 8, "per-warp counts fit the tile buffer");
 
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_upsweep(const K* __restrict__ keys, uint32_t n, int shift,
@@ -53,7 +63,7 @@ __global__ void __launch_bounds__(kThreads) k_upsweep(const K* __restrict__ keys
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
         const size_t idx = base + (size_t)i * kThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(uint32_t)(k[i] >> shift) & 0xFFu], 1u);
+        if (idx < n) atomicAdd(&h[(uint32_t)(k[i] >> shift) & kMask], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kDigits; i += kThreads) hist[(size_t)i * tiles + blockIdx.x] = h[i];
@@ -114,12 +124,31 @@ __global__ void __launch_bounds__(kThreads) k_digit_scan(uint32_t* __restrict__ 
     if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
+// block-wide exclusive scan of one value per thread (wsum: kWarps words;
+// every thread must call it)
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t x, uint32_t* wsum)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = x;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    __syncthreads();
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += wsum[w];
+    return wpre + inc - x;
+}
+
 // Shared memory of the downsweep: the tile's keys and values in local
-// sorted order (reused for the per-warp digit counts before that).
+// sorted order (the per-warp digit counts before that), then the digits'
+// global and tile-local run starts.
 template <typename K>
 constexpr size_t downsweep_smem()
 {
-    return (size_t)kTile * (sizeof(K) + sizeof(uint32_t)) + 3 * kDigits * sizeof(uint32_t) + 2 * kWarps * 4;
+    return (size_t)kTile * (sizeof(K) + sizeof(uint32_t)) + 2 * kDigits * sizeof(uint32_t) + kWarps * 4;
 }
 
 // four blocks per SM (<= 64 registers): the pass is bandwidth-bound and needs the occupancy
@@ -137,23 +166,21 @@ __global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* 
     uint32_t (*wh)[kDigits] = reinterpret_cast<uint32_t (*)[kDigits]>(ds_smem); // [kWarps][kDigits], ranking only
     uint32_t* goff = reinterpret_cast<uint32_t*>(svals + kTile);             // global offset of digit d's run
     uint32_t* tstart = goff + kDigits;                                       // tile-local start of digit d
-    uint32_t* tcount = tstart + kDigits;
-    uint32_t* wsum = tcount + kDigits;
+    uint32_t* wsum = tstart + kDigits;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int d0 = threadIdx.x * kPer; // the digits this thread owns in the scans
     for (int i = threadIdx.x; i < kWarps * kDigits; i += kThreads) (&wh[0][0])[i] = 0;
     {
-        // digit bases: exclusive scan of the 256 digit totals (kThreads == kDigits)
-        const uint32_t v = totals[threadIdx.x];
-        uint32_t inc = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-            if (lane >= o) inc += t;
+        // digit bases: exclusive scan of the digit totals
+        uint32_t tv[kPer], sum = 0;
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) { tv[r] = totals[d0 + r]; sum += tv[r]; }
+        uint32_t run = block_exclusive(sum, wsum);
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            goff[d0 + r] = run + hist[(size_t)(d0 + r) * tiles + blockIdx.x];
+            run += tv[r];
         }
-        if (lane == 31) wsum[warp] = inc;
-        __syncthreads();
-        uint32_t wpre = 0;
-        for (int k = 0; k < warp; ++k) wpre += wsum[k];
-        goff[threadIdx.x] = wpre + inc - v + hist[(size_t)threadIdx.x * tiles + blockIdx.x];
     }
     __syncthreads();
     const size_t tbase = (size_t)blockIdx.x * kTile;
@@ -173,8 +200,16 @@ __global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* 
     for (int i = 0; i < kItems; ++i) {
         const size_t idx = wbase + (size_t)i * 32 + lane;
         const bool ok = idx < n;
-        const uint32_t d = ok ? ((uint32_t)(k[i] >> shift) & 0xFFu) : 0x100u; // 0x100: padding, no digit
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t d = (uint32_t)(k[i] >> shift) & kMask;
+        // lanes with the same digit: one ballot per digit bit (padding lanes
+        // are left out by the first ballot and never use their own mask)
+        uint32_t peers = __ballot_sync(0xFFFFFFFFu, ok);
+#pragma unroll
+        for (int b = 0; b < kBits; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, bit);
+            peers &= bit ? m : ~m;
+        }
         uint32_t prev = 0;
         if (ok) prev = wh[warp][d];
         __syncwarp();
@@ -183,28 +218,27 @@ __global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* 
         rank[i] = prev + __popc(peers & lt);
     }
     __syncthreads();
-    // per digit: exclusive prefix across warps, and the digit's count in the tile
+    // per digit: exclusive prefix across warps; tile-local digit starts:
+    // exclusive scan of the digits' tile counts
     {
-        const int d = threadIdx.x;
-        uint32_t run = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = wh[w][d];
-            wh[w][d] = run;
-            run += c;
+        uint32_t cnt[kPer], tot = 0;
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            uint32_t run = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t c = wh[w][d0 + r];
+                wh[w][d0 + r] = run;
+                run += c;
+            }
+            cnt[r] = run;
+            tot += run;
         }
-        tcount[d] = run;
-        // tile-local digit starts: exclusive scan of the counts over digits
-        uint32_t inc = run;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-            if (lane >= o) inc += t;
+        uint32_t start = block_exclusive(tot, wsum);
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            tstart[d0 + r] = start;
+            start += cnt[r];
         }
-        __syncthreads();
-        if (lane == 31) wsum[warp] = inc;
-        __syncthreads();
-        uint32_t wpre = 0;
-        for (int w = 0; w < warp; ++w) wpre += wsum[w];
-        tstart[d] = wpre + inc - run;
     }
     __syncthreads();
     // tile-local sorted position of every key, then the keys go to shared
@@ -212,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* 
     uint32_t pos[kItems];
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-        const uint32_t d = (uint32_t)(k[i] >> shift) & 0xFFu;
+        const uint32_t d = (uint32_t)(k[i] >> shift) & kMask;
         pos[i] = tstart[d] + wh[warp][d] + rank[i];
     }
     __syncthreads();
@@ -229,7 +263,7 @@ __global__ void __launch_bounds__(kThreads, MCGPU_DS_MINB) k_downsweep(const K* 
     const uint32_t tn = (uint32_t)min((size_t)kTile, (size_t)n - tbase);
     for (uint32_t j = threadIdx.x; j < tn; j += kThreads) {
         const K key = skeys[j];
-        const uint32_t d = (uint32_t)(key >> shift) & 0xFFu;
+        const uint32_t d = (uint32_t)(key >> shift) & kMask;
         const uint32_t dst = goff[d] + (j - tstart[d]);
         okeys[dst] = key;
         ovals[dst] = svals[j];
@@ -315,13 +349,6 @@ void exclusive_scan(uint32_t* a, uint32_t n, uint32_t* total_out, uint32_t* temp
     k_block_scan<<<nb, kScanThreads, 0, s>>>(a, n, temp, total_out);
 }
 
-size_t radix_sort_temp_bytes(uint32_t n)
-{
-    const uint32_t tiles = (n + kTile - 1) / kTile;
-    const size_t table = (size_t)kDigits * (tiles ? tiles : 1);
-    return (table + kDigits + 64) * sizeof(uint32_t);
-}
-
 template <typename K>
 int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, uint32_t n, int begin_bit, int end_bit,
     uint32_t* temp, cudaStream_t s)
@@ -333,7 +360,7 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, u
     int cur = 0;
     K* kb[2] = { keys, keys_alt };
     uint32_t* vb[2] = { vals, vals_alt };
-    for (int shift = begin_bit; shift < end_bit; shift += 8) {
+    for (int shift = begin_bit; shift < end_bit; shift += kBits) {
         uint32_t* totals = temp + (size_t)kDigits * tiles;
         g_launches += 3;
         k_upsweep<K><<<tiles, kThreads, 0, s>>>(kb[cur], n, shift, temp, tiles);

@@ -11,8 +11,20 @@ extern thread_local unsigned long long g_launches;
 // cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per device (`done`: bit per device)
 void set_smem_once(const void* func, int bytes, std::atomic<unsigned long long>& done);
 
-// Scratch (bytes) the sort needs for n keys.
-size_t radix_sort_temp_bytes(uint32_t n);
+// Digit width of one radix pass and keys per tile.
+#ifndef MCGPU_SORT_BITS
+#define MCGPU_SORT_BITS 8
+#endif
+constexpr int kSortDigitBits = MCGPU_SORT_BITS;
+constexpr uint32_t kSortDigits = 1u << kSortDigitBits;
+constexpr uint32_t kSortTile = 4096;
+
+// Scratch (bytes) the sort needs for n keys: the [digit x tile] count table
+// and the digit totals.
+constexpr size_t radix_sort_temp_bytes(uint32_t n)
+{
+    return ((size_t)kSortDigits * (n ? (n + kSortTile - 1) / kSortTile : 1) + kSortDigits + 64) * sizeof(uint32_t);
+}
 
 // Sorts (keys, vals) by bits [begin_bit, end_bit) of the key, stably.
 // Ping-pongs between (keys, vals) and (keys_alt, vals_alt); returns 0 if the
