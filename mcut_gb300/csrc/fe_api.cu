@@ -91,7 +91,7 @@ struct PinBuf {
 
 enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
-    B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_RFLAG, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
+    B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_COUNT
 };
@@ -714,9 +714,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.split_cap = c->split_cap ? c->split_cap : std::min<uint64_t>(std::max<uint64_t>(4096, L.ns), 4u << 20);
     W.split = c->buf[B_SPLIT].get<uint8_t>(W.split_cap * 144);
     W.nodes = c->buf[B_NODES].get<Node>(std::max<uint64_t>(L.ncl, 2) - 1);
-    W.parent = c->buf[B_PARENT].get<int32_t>(2 * std::max<uint64_t>(L.ncl, 1));
-    W.refit_flag = c->buf[B_RFLAG].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
-    W.node_range = c->buf[B_NRANGE].get<int2>(std::max<uint64_t>(L.ncl, 2));
+    W.split_far = c->buf[B_PARENT].get<uint32_t>(std::max<uint64_t>(L.ncl, 2));
+    W.split_box = c->buf[B_NRANGE].get<uint8_t>(64 * std::max<uint64_t>(L.ncl, 2));
     W.counters = c->buf[B_COUNTERS].get<uint32_t>(16);
     W.cand = c->buf[B_CAND].get<uint8_t>(L.nf);
     W.pair_status = c->buf[B_PSTAT].get<uint32_t>(n);

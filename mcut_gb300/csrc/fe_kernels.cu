@@ -3,7 +3,7 @@
 // Stage map (reference function -> kernel):
 //   bvh.cpp:242-433  face boxes, mesh box, Morton codes   -> k_vertex_bounds, k_mesh_frames, k_face_bounds
 //   bvh.cpp:437-442  std::sort by Morton code             -> radix_sort_pairs (fe_sort.cu)
-//   bvh.cpp:444-635  implicit-tree build + refit          -> k_karras, k_refit (LBVH)
+//   bvh.cpp:444-635  implicit-tree build + refit          -> k_build (LBVH, built bottom-up with its boxes)
 //   bvh.cpp:638-783  intersectOIBVHs                       -> k_traverse
 //   kernel.cpp:1781-2177 edge->faces, edge boxes, culling -> k_pair_tests
 //   kernel.cpp:2184-2356 tested-face planes               -> k_planes, k_triplets
@@ -266,38 +266,6 @@ __device__ __forceinline__ int delta(const K* __restrict__ key, int n, int i, in
     return __clz((unsigned)((uint32_t)a ^ (uint32_t)b));
 }
 
-template <typename K>
-__global__ void __launch_bounds__(kBlock) k_karras(const K* __restrict__ key, int n, Node* __restrict__ nodes,
-    int32_t* __restrict__ parent, int2* __restrict__ node_range)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
-        const int d = (delta(key, n, i, i + 1) - delta(key, n, i, i - 1)) >= 0 ? 1 : -1;
-        const int dmin = delta(key, n, i, i - d);
-        int lmax = 2;
-        while (delta(key, n, i, i + lmax * d) > dmin) lmax <<= 1;
-        int l = 0;
-        for (int t = lmax >> 1; t >= 1; t >>= 1)
-            if (delta(key, n, i, i + (l + t) * d) > dmin) l += t;
-        const int j = i + l * d;
-        const int dnode = delta(key, n, i, j);
-        int s = 0;
-        for (int t = (l + 1) >> 1;; t = (t + 1) >> 1) {
-            if (delta(key, n, i, i + (s + t) * d) > dnode) s += t;
-            if (t == 1) break;
-        }
-        const int gamma = i + s * d + min(d, 0);
-        const int lo = min(i, j), hi = max(i, j);
-        const int left = (lo == gamma) ? ~gamma : gamma;
-        const int right = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-        nodes[i].child[0] = left;
-        nodes[i].child[1] = right;
-        node_range[i] = make_int2(lo, hi);
-        // parent index | child slot << 31 (the refit climb needs no node read)
-        parent[left >= 0 ? left : (n - 1) + ~left] = i;
-        parent[right >= 0 ? right : (n - 1) + ~right] = (int32_t)((uint32_t)i | 0x80000000u);
-    }
-}
-
 // Query packets: the source faces are Morton-sorted too, and every Karras
 // subtree over them is a run of consecutive sorted faces split at a Morton
 // cell boundary, hence spatially compact. A packet is a maximal subtree of at
@@ -399,100 +367,169 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
     return b;
 }
 
-// Bottom-up boxes. Block b owns leaf clusters [kRefitWin b, kRefitWin (b+1)): a
-// node whose leaf range lies inside that window has both children finished
-// by threads of the same block, so its arrival counter and its children's
-// boxes live in shared memory, and the climb through the window touches no
-// global memory (a fence then waits on shared memory only). The block then
-// writes its finished nodes with vector stores, and the threads that reached
-// a node above the window carry on through global acquire-release arrival
-// counters, the second to arrive at a node carrying the union upward.
+// Bottom-up build of the binary radix tree over the sorted leaf clusters,
+// boxes included (agglomerative LBVH, Apetrei, EG 2014). D(j), the boundary
+// between sorted clusters j and j+1, is the XOR of their keys with the XOR of
+// the positions below it (distinct keys, duplicates ordered by position, as
+// the Karras construction orders them). The tree is the Cartesian tree of D:
+// a node [l, r] is the left child of its parent when D(r) < D(l-1), and
+// splits at its largest inner boundary. Every leaf thread climbs: at the
+// parent's split position s the first child to arrive deposits its box and
+// far end and stops; the second builds the parent. Nodes keep the Karras
+// numbering (a left child is numbered by its right end, a right child by its
+// left end, the root is 0), so the walk is unchanged.
+//
+// Block b owns clusters [W b, W (b+1)), W = kRefitWin. A split whose node lies
+// inside the window -- D(s) is below some boundary on each side within the
+// window, found by prefix and suffix maxima -- is exchanged through shared
+// memory: the climb through a window touches no global memory. Splits whose
+// node leaves the window use global acquire-release exchanges.
 #ifndef MCGPU_REFIT_WIN
 #define MCGPU_REFIT_WIN 256
 #endif
 constexpr int kRefitWin = MCGPU_REFIT_WIN;
-__global__ void __launch_bounds__(kRefitWin) k_refit(Problem P, const float* __restrict__ fbox32,
-    const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n,
-    int n, Node* __restrict__ nodes, const int32_t* __restrict__ parent, const int2* __restrict__ node_range,
-    uint32_t* __restrict__ flag)
+constexpr uint32_t kNoFar = 0xFFFFFFFFu;
+
+struct Dlt { unsigned long long x; uint32_t i; };
+__device__ __forceinline__ bool dlt_less(const Dlt& a, const Dlt& b)
 {
-    __shared__ uint32_t sflag[kRefitWin];
+    return a.x < b.x || (a.x == b.x && a.i < b.i);
+}
+template <typename K>
+__device__ __forceinline__ Dlt boundary_delta(const K* __restrict__ key, int n, int j)
+{
+    if (j < 0 || j >= n - 1) return Dlt { ~0ull, ~0u };
+    return Dlt { (unsigned long long)(__ldg(&key[j]) ^ __ldg(&key[j + 1])), (uint32_t)(j ^ (j + 1)) };
+}
+__device__ __forceinline__ Dlt dlt_shfl_up(const Dlt& d, int o)
+{
+    return Dlt { __shfl_up_sync(0xFFFFFFFFu, d.x, o), __shfl_up_sync(0xFFFFFFFFu, d.i, o) };
+}
+__device__ __forceinline__ Dlt dlt_shfl_down(const Dlt& d, int o)
+{
+    return Dlt { __shfl_down_sync(0xFFFFFFFFu, d.x, o), __shfl_down_sync(0xFFFFFFFFu, d.i, o) };
+}
+__device__ __forceinline__ void store_fbox(FBox* p, const FBox& b)
+{
+    float4* q = reinterpret_cast<float4*>(p);
+    q[0] = make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]);
+    q[1] = make_float4(b.hi[1], b.hi[2], __uint_as_float(b.plo), __uint_as_float(b.phi));
+}
+__device__ __forceinline__ FBox load_fbox_cg(const FBox* p)
+{
+    const float4 a = __ldcg(reinterpret_cast<const float4*>(p)), c = __ldcg(reinterpret_cast<const float4*>(p) + 1);
+    FBox b;
+    b.lo[0] = a.x; b.lo[1] = a.y; b.lo[2] = a.z; b.hi[0] = a.w;
+    b.hi[1] = c.x; b.hi[2] = c.y; b.plo = __float_as_uint(c.z); b.phi = __float_as_uint(c.w);
+    return b;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restrict__ key, int n,
+    const float* __restrict__ fbox32, const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start,
+    const uint8_t* __restrict__ cl_n, Node* __restrict__ nodes, uint32_t* __restrict__ split_far,
+    FBox* __restrict__ split_box)
+{
+    constexpr int kW = kRefitWin / 32;
+    __shared__ Dlt sd[kRefitWin + 1];  // sd[t] = D(w0 - 1 + t)
+    __shared__ Dlt wagg[2][kW];
+    __shared__ uint32_t sfar[kRefitWin];
+    __shared__ uint8_t sinw[kRefitWin];
     __shared__ FBox sbox[kRefitWin][2];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int w0 = blockIdx.x * kRefitWin, w1 = min(n, w0 + kRefitWin) - 1;
-    sflag[threadIdx.x] = 0;
+    const int i = w0 + t;
+    const bool valid = i <= w1;
+    const Dlt lowest { 0ull, 0u }; // below every boundary (a boundary's position XOR is >= 1)
+    const Dlt dm = valid ? boundary_delta(key, n, i) : lowest;
+    sd[t + 1] = dm;
+    if (t == 0) sd[0] = boundary_delta(key, n, w0 - 1);
+    sfar[t] = kNoFar;
+    // inclusive max-scans of D over the window, from the left and from the right
+    Dlt pre = dm, suf = dm;
+    for (int o = 1; o < 32; o <<= 1) {
+        const Dlt a = dlt_shfl_up(pre, o), b = dlt_shfl_down(suf, o);
+        if (lane >= o && dlt_less(pre, a)) pre = a;
+        if (lane + o < 32 && dlt_less(suf, b)) suf = b;
+    }
+    if (lane == 31) wagg[0][warp] = pre;
+    if (lane == 0) wagg[1][warp] = suf;
+    Dlt epre = dlt_shfl_up(pre, 1), esuf = dlt_shfl_down(suf, 1);
     __syncthreads();
-    const int i = w0 + threadIdx.x;
-    bool carry = false; // holds a box for a node above the window
+    if (lane == 0) epre = sd[0];
+    else if (dlt_less(epre, sd[0])) epre = sd[0];
+    if (lane == 31) esuf = lowest;
+    for (int w = 0; w < warp; ++w)
+        if (dlt_less(epre, wagg[0][w])) epre = wagg[0][w];
+    for (int w = warp + 1; w < kW; ++w)
+        if (dlt_less(esuf, wagg[1][w])) esuf = wagg[1][w];
+    // split i closes inside the window: a larger boundary on each side of it
+    sinw[t] = (valid && i < w1 && dlt_less(dm, epre) && dlt_less(dm, esuf)) ? 1 : 0;
+    __syncthreads();
+    if (!valid) return;
+
     FBox fb;
-    uint32_t pe = 0;
-    if (i < n) {
-        for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
+    for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
+    {
         const uint32_t s0 = cl_start[i], cn = cl_n[i];
         uint32_t lf[16];
-        for (uint32_t t = 0; t < cn; ++t) lf[t] = __ldg(&leaf_face[s0 + t]);
-        for (uint32_t t = 0; t < cn; ++t) {
-            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[t] * 6);
+        for (uint32_t u = 0; u < cn; ++u) lf[u] = __ldg(&leaf_face[s0 + u]);
+        for (uint32_t u = 0; u < cn; ++u) {
+            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[u] * 6);
             const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
             fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
             fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
         }
         fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
-        pe = (uint32_t)__ldg(&parent[(n - 1) + i]);
-        for (;;) {
-            const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
-            const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
-            const int2 rg = __ldg(&node_range[node]);
-            if (rg.x < w0 || rg.y > w1) { carry = true; break; }
-            const int k = node - w0; // a node's index is one end of its range
-            sbox[k][slot] = fb;
-            __threadfence_block();
-            const uint32_t prev = atomicAdd(&sflag[k], 1u);
-            __threadfence_block();
-            if (prev == 0) break;
-            const FBox o = sbox[k][slot ^ 1];
-            for (int j = 0; j < 3; ++j) {
-                fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
-                fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
-            }
-            fb.plo = min(fb.plo, o.plo);
-            fb.phi = max(fb.phi, o.phi);
-            if (node == 0) break;
-            pe = next;
-        }
     }
-    __syncthreads();
-    {
-        // every node inside the window has had both arrivals
-        const int k = threadIdx.x, node = w0 + k;
-        if (node < n - 1 && sflag[k] == 2u) {
-            const FBox& l = sbox[k][0];
-            const FBox& r = sbox[k][1];
-            Node* nd = &nodes[node];
-            nd->b0 = make_float4(l.lo[0], l.lo[1], l.lo[2], l.hi[0]);
-            nd->b1 = make_float4(l.hi[1], l.hi[2], r.lo[0], r.lo[1]);
-            nd->b2 = make_float4(r.lo[2], r.hi[0], r.hi[1], r.hi[2]);
-            *reinterpret_cast<uint2*>(nd->prange) = make_uint2(l.plo | (l.phi << 16), r.plo | (r.phi << 16));
-        }
-    }
-    if (!carry) return;
+    int l = i, r = i;
+    Dlt dl = sd[t], dr = sd[t + 1]; // D(l-1), D(r)
     for (;;) {
-        const int node = (int)(pe & 0x7FFFFFFFu), slot = (int)(pe >> 31);
-        const uint32_t next = node == 0 ? 0xFFFFFFFFu : (uint32_t)__ldg(&parent[node]);
-        Node* nd = &nodes[node];
-        put_child(nd, slot, fb);
-        // acq_rel arrival: releases this child's box, acquires the sibling's
-        unsigned prev;
-        asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&flag[node]) : "memory");
-        if (prev == 0) break;
-        const FBox o = get_child(nd, slot ^ 1);
+        const bool right = dlt_less(dr, dl); // the parent extends to the right: this node is its left child
+        const int s = right ? r : l - 1;
+        const int slot = right ? 0 : 1;
+        const uint32_t far = (uint32_t)(right ? l : r);
+        uint32_t prev;
+        FBox o;
+        const int ks = s - w0;
+        if (ks >= 0 && ks < kRefitWin && sinw[ks]) {
+            sbox[ks][slot] = fb;
+            __threadfence_block();
+            prev = atomicExch(&sfar[ks], far);
+            __threadfence_block();
+            if (prev == kNoFar) return;
+            o = sbox[ks][slot ^ 1];
+        } else {
+            store_fbox(&split_box[2 * (size_t)s + slot], fb);
+            // acq_rel exchange: releases this child's box, acquires the sibling's
+            asm volatile("atom.exch.acq_rel.gpu.b32 %0, [%1], %2;" : "=r"(prev) : "l"(split_far + s), "r"(far) : "memory");
+            if (prev == kNoFar) return;
+            o = load_fbox_cg(&split_box[2 * (size_t)s + (slot ^ 1)]);
+        }
+        const int pl = right ? l : (int)prev, pr = right ? (int)prev : r;
+        const Dlt pdl = (pl >= w0 && pl <= w1 + 1) ? sd[pl - w0] : boundary_delta(key, n, pl - 1);
+        const Dlt pdr = (pr >= w0 - 1 && pr <= w1) ? sd[pr - w0 + 1] : boundary_delta(key, n, pr);
+        const bool root = pl == 0 && pr == n - 1;
+        const int pidx = root ? 0 : (dlt_less(pdr, pdl) ? pr : pl);
+        const FBox& lb = right ? fb : o;
+        const FBox& rb = right ? o : fb;
+        Node* nd = &nodes[pidx];
+        nd->b0 = make_float4(lb.lo[0], lb.lo[1], lb.lo[2], lb.hi[0]);
+        nd->b1 = make_float4(lb.hi[1], lb.hi[2], rb.lo[0], rb.lo[1]);
+        nd->b2 = make_float4(rb.lo[2], rb.hi[0], rb.hi[1], rb.hi[2]);
+        *reinterpret_cast<int4*>(nd->child) = make_int4(pl == s ? ~s : s, s + 1 == pr ? ~(s + 1) : s + 1,
+            (int)(lb.plo | (lb.phi << 16)), (int)(rb.plo | (rb.phi << 16)));
         for (int j = 0; j < 3; ++j) {
             fb.lo[j] = fminf(fb.lo[j], o.lo[j]);
             fb.hi[j] = fmaxf(fb.hi[j], o.hi[j]);
         }
         fb.plo = min(fb.plo, o.plo);
         fb.phi = max(fb.phi, o.phi);
-        if (node == 0) break;
-        pe = next;
+        if (root) return;
+        l = pl;
+        r = pr;
+        dl = pdl;
+        dr = pdr;
     }
 }
 
@@ -1936,17 +1973,15 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
         k_clusters<uint32_t><<<gc, kBlock, 0, s>>>(P, (const uint32_t*)W.ckeys[cut_buf], (uint32_t*)W.cl_key,
             W.cl_start, W.cl_n);
     if (n < 2) return;
-    const int g = grid_for(n);
+    cudaMemsetAsync(W.split_far, 0xFF, sizeof(uint32_t) * (size_t)(n - 1), s);
     g_launches++;
+    const int g = (n + kRefitWin - 1) / kRefitWin;
     if (wide)
-        k_karras<unsigned long long><<<g, kBlock, 0, s>>>((const unsigned long long*)W.cl_key, n, W.nodes, W.parent,
-            W.node_range);
+        k_build<unsigned long long><<<g, kRefitWin, 0, s>>>(P, (const unsigned long long*)W.cl_key, n, W.fbox32,
+            W.cvals[cut_buf], W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box);
     else
-        k_karras<uint32_t><<<g, kBlock, 0, s>>>((const uint32_t*)W.cl_key, n, W.nodes, W.parent, W.node_range);
-    cudaMemsetAsync(W.refit_flag, 0, sizeof(uint32_t) * (size_t)(n - 1), s);
-    g_launches++;
-    k_refit<<<(n + kRefitWin - 1) / kRefitWin, kRefitWin, 0, s>>>(P, W.fbox32, W.cvals[cut_buf], W.cl_start, W.cl_n, n,
-        W.nodes, W.parent, W.node_range, W.refit_flag);
+        k_build<uint32_t><<<g, kRefitWin, 0, s>>>(P, (const uint32_t*)W.cl_key, n, W.fbox32, W.cvals[cut_buf],
+            W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box);
 }
 
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)

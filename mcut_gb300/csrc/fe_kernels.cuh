@@ -85,9 +85,8 @@ struct Work {
     void* split;                      // [split_cap] slow packets' remaining walks (144 B each)
     uint64_t split_cap;
     Node* nodes;                      // [ncl-1]
-    int32_t* parent;                  // [2ncl-1]
-    int2* node_range;                 // [ncl-1] leaf range of each internal node
-    uint32_t* refit_flag;             // [ncl-1]
+    uint32_t* split_far;              // [ncl-1] per split position: far leaf of the first child to arrive
+    void* split_box;                  // [2(ncl-1)] per split position and side: that child's box (32 B)
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
                                       //        5..7 escalations, 8 traversal work cursor, 9 packets, 10 narrow hits,

@@ -70,9 +70,8 @@ constexpr size_t oKeys = oMbox + al(12 * 8);             // 8 arrays of kMaxFace
 constexpr size_t oSortTmp = oKeys + al(8ull * kMaxFaces * 4);
 constexpr size_t kSortTmpBytes = radix_sort_temp_bytes(kMaxTests) + 4096; // table + scan block sums
 constexpr size_t oNodes = oSortTmp + al(kSortTmpBytes);
-constexpr size_t oParent = oNodes + al(kMaxFaces * sizeof(Node));
-constexpr size_t oRflag = oParent + al(2ull * kMaxFaces * 4);
-constexpr size_t oPairs = oRflag + al(kMaxFaces * 4ull);
+constexpr size_t oParent = oNodes + al(kMaxFaces * sizeof(Node)); // split_far
+constexpr size_t oPairs = oParent + al(kMaxFaces * 4ull);
 constexpr size_t oCounters = oPairs + al(kMaxPairs * 8ull);
 constexpr size_t oCand = oCounters + al(16 * 4);
 constexpr size_t oPslot = oCand + al(kMaxFaces);
@@ -94,7 +93,7 @@ constexpr size_t oTop = oPlist + al(kMaxFaces * 4ull);
 constexpr size_t kSplitCap = 2048;
 constexpr size_t oSplit = oTop + al(64 * 32);
 constexpr size_t oNrange = oSplit + al(kSplitCap * 144ull);
-constexpr size_t oFrame = oNrange + al(kMaxFaces * 8ull);
+constexpr size_t oFrame = oNrange + al(kMaxFaces * 64ull); // split_box
 constexpr size_t kScratchBytes = oFrame + al(64);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -209,8 +208,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.fbox32 = reinterpret_cast<float*>(base + oLkb);
     W.packets = reinterpret_cast<uint2*>(base + oPackets);
     W.nodes = reinterpret_cast<Node*>(base + oNodes);
-    W.parent = reinterpret_cast<int32_t*>(base + oParent);
-    W.refit_flag = reinterpret_cast<uint32_t*>(base + oRflag);
+    W.split_far = reinterpret_cast<uint32_t*>(base + oParent);
     W.pairs = reinterpret_cast<unsigned long long*>(base + oPairs);
     W.pair_cap = kMaxPairs;
     W.counters = reinterpret_cast<uint32_t*>(base + oCounters);
@@ -223,7 +221,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.top = base + oTop;
     W.split = base + oSplit;
     W.split_cap = kSplitCap;
-    W.node_range = reinterpret_cast<int2*>(base + oNrange);
+    W.split_box = base + oNrange;
     W.mesh_frame = base + oFrame;
     W.poly_list = nullptr;
     W.vneed = base + oVneed;
