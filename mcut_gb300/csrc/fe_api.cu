@@ -128,14 +128,19 @@ struct mcgpu_context_t {
     int rec_buf = 0;
     mcgpu_tuning tune { 4, 0, 32, 64, 2 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL / MCGPU_PACKET_FACES override at creation
     bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
+    bool use_fuse = true;                 // MCGPU_FUSE=0: every call stage by stage
     uint64_t split_cap = 0;               // MCGPU_SPLIT_CAP: fixed split-entry capacity (0: by size)
     struct Graph {
         std::vector<unsigned char> key;
         cudaGraphExec_t exec = nullptr;
         int seen = 0;
         unsigned long long launches = 0;
-        int aux[2] = { 0, 0 };
-    } graphs[3];
+        int aux[3] = { 0, 0, 0 };
+    } graphs[4];
+    // the fused call (one graph, one readback) follows a call with the same segment-0 key
+    std::vector<unsigned char> fuse_key;
+    bool fuse_ok = false;
+    uint64_t fuse_nrec = 0;
 };
 
 namespace {
@@ -731,8 +736,10 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.stack_depth = c->tune.stack_depth;
     W.split_round = c->tune.split_round;
     const uint32_t prof = flags & MCGPU_PROFILE;
+    const uint32_t keep = flags & MCGPU_KEEP_TESTS;
     int src_buf = 0, cut_buf = 0;
-    run_segment(c, 0, seg_key(P, W, n, key_bits, prof), [&](int* aux) {
+    uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
+    auto seg0 = [&](int* aux) {
         // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
         rec(c, 2 * MCGPU_STAGE_BOUNDS);
         g_launches++;
@@ -759,66 +766,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         rec(c, 2 * MCGPU_STAGE_TRAVERSE);
         launch_traverse(P, W, aux[0], aux[1], false, s);
         rec(c, 2 * MCGPU_STAGE_TRAVERSE + 1);
-    });
-    src_buf = c->graphs[0].aux[0];
-    cut_buf = c->graphs[0].aux[1];
-
-    // readback 1: pair count and traversal flags
-    uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
-    ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
-    ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
-    ck(cudaStreamSynchronize(s), "sync traverse");
-    bool deep = false;
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        bool stack = false;
-        for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
-        const uint64_t np = hc[0];
-        if (!stack && np <= W.pair_cap) break;
-        if (np > W.pair_cap) {
-            W.pair_cap = np + np / 8 + 1024;
-            W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
-        }
-        deep = deep || stack;
-        ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
-        ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
-        ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
-        launch_packets(P, W, src_buf, s);
-        launch_traverse(P, W, src_buf, cut_buf, deep, s);
-        ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
-        ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
-        ck(cudaStreamSynchronize(s), "sync traverse");
-    }
-    const uint64_t npairs = hc[0];
-    c->n_pairs_found = npairs;
-
-    // stage-3 buffers sized from the pair count
-    W.plane_cap = std::min<uint64_t>(L.nf, 2 * npairs + 1);
-    W.plane_slot = c->buf[B_PSLOT].get<uint32_t>(L.nf);
-    W.planes = c->buf[B_PLANES].get<FacePlane>(W.plane_cap);
-    W.proj_flag = c->buf[B_PFLAG].get<uint32_t>(W.plane_cap);
-    W.proj_list = c->buf[B_PLIST].get<uint32_t>(W.plane_cap);
-    W.poly_list = c->buf[B_POLY].get<uint32_t>(L.all_tri ? 1 : L.nf);
-    W.tri_stride = L.all_tri ? 0 : L.tri_stride;
-    W.tri_scratch_cap = W.tri_stride * std::max<uint64_t>(L.n_poly, 1);
-    W.tri_scratch = c->buf[B_TRI].get<double>(W.tri_scratch_cap * 3 + 1);
-    W.vneed = c->buf[B_VNEED].get<uint8_t>(L.nv);
-    W.voff = c->buf[B_VOFF].get<uint32_t>(L.nv + 1);
-    W.vcur = c->buf[B_VCUR].get<uint32_t>(L.nv);
-    W.inc_cap = L.nidx;
-    W.vface = c->buf[B_VFACE].get<uint32_t>(L.nidx);
-    W.test_cap = std::max<uint64_t>(1, 2ull * L.max_face * npairs);
-    if (W.test_cap > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "edge-face tests exceed 2^32");
-    W.tests = c->buf[B_TESTS].get<Test>(W.test_cap);
-    W.test_info = c->buf[B_TINFO].get<int8_t>((flags & MCGPU_KEEP_TESTS) ? W.test_cap * 4 : 4);
-    W.rec_key[0] = c->buf[B_RK0].get<unsigned long long>(W.test_cap);
-    W.rec_key[1] = c->buf[B_RK1].get<unsigned long long>(W.test_cap);
-    W.rec_val[0] = c->buf[B_RV0].get<uint32_t>(W.test_cap);
-    W.rec_val[1] = c->buf[B_RV1].get<uint32_t>(W.test_cap);
-    W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
-    W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
-        radix_sort_temp_bytes((uint32_t)std::max<uint64_t>(L.ns + L.nc, W.test_cap)) / 4 + 64);
-    const uint32_t keep = flags & MCGPU_KEEP_TESTS;
-    run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) {
+    };
+    auto seg1 = [&]() {
         rec(c, 2 * MCGPU_STAGE_ADJACENCY);
         // vertex -> face incidence beside the candidate-face planes
         ck(cudaEventRecord(c->fork[1], s), "fork");
@@ -832,33 +781,168 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         launch_tests(P, W, s);
         launch_narrow(P, W, keep != 0, s);
         rec(c, 2 * MCGPU_STAGE_NARROW + 1);
-    });
-
-    // readback 2: counters, per-pair status / degenerate face / record count
-    ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
-    ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
-    ck(cudaMemcpyAsync(hc + 16 + n, W.pair_bad, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H bad");
-    ck(cudaStreamSynchronize(s), "sync narrow");
-    c->n_tests = hc[1];
-    c->n_records = hc[2];
-    W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
-    W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
-    const uint32_t nrec = (uint32_t)c->n_records;
-    run_segment(c, 2, seg_key(P, W, n, nrec, prof), [&](int* aux) {
-        rec(c, 2 * MCGPU_STAGE_DOWNLOAD); // record sort + gather (added to the narrow stage)
-        aux[0] = launch_records(P, W, nrec, s);
-        rec(c, 2 * MCGPU_STAGE_DOWNLOAD + 1);
-    });
-    c->rec_buf = c->graphs[2].aux[0];
-    // per-pair record ranges (first sorted record of each pair, then the total)
-    if (n > 1)
-        ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
-            "D2H ranges");
-    else {
-        hc[16 + 2] = 0;
-        hc[16 + 3] = (uint32_t)c->n_records;
+    };
+    // stage-3 buffers for np candidate pairs (all_planes: a plane slot for every face)
+    auto size_stage3 = [&](uint64_t np, bool all_planes) -> int {
+        W.plane_cap = all_planes ? std::max<uint64_t>(L.nf, 1) : std::min<uint64_t>(L.nf, 2 * np + 1);
+        W.plane_slot = c->buf[B_PSLOT].get<uint32_t>(L.nf);
+        W.planes = c->buf[B_PLANES].get<FacePlane>(W.plane_cap);
+        W.proj_flag = c->buf[B_PFLAG].get<uint32_t>(W.plane_cap);
+        W.proj_list = c->buf[B_PLIST].get<uint32_t>(W.plane_cap);
+        W.poly_list = c->buf[B_POLY].get<uint32_t>(L.all_tri ? 1 : L.nf);
+        W.tri_stride = L.all_tri ? 0 : L.tri_stride;
+        W.tri_scratch_cap = W.tri_stride * std::max<uint64_t>(L.n_poly, 1);
+        W.tri_scratch = c->buf[B_TRI].get<double>(W.tri_scratch_cap * 3 + 1);
+        W.vneed = c->buf[B_VNEED].get<uint8_t>(L.nv);
+        W.voff = c->buf[B_VOFF].get<uint32_t>(L.nv + 1);
+        W.vcur = c->buf[B_VCUR].get<uint32_t>(L.nv);
+        W.inc_cap = L.nidx;
+        W.vface = c->buf[B_VFACE].get<uint32_t>(L.nidx);
+        W.test_cap = std::max<uint64_t>(1, 2ull * L.max_face * np);
+        if (W.test_cap > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "edge-face tests exceed 2^32");
+        W.tests = c->buf[B_TESTS].get<Test>(W.test_cap);
+        W.test_info = c->buf[B_TINFO].get<int8_t>((flags & MCGPU_KEEP_TESTS) ? W.test_cap * 4 : 4);
+        W.rec_key[0] = c->buf[B_RK0].get<unsigned long long>(W.test_cap);
+        W.rec_key[1] = c->buf[B_RK1].get<unsigned long long>(W.test_cap);
+        W.rec_val[0] = c->buf[B_RV0].get<uint32_t>(W.test_cap);
+        W.rec_val[1] = c->buf[B_RV1].get<uint32_t>(W.test_cap);
+        W.rec_pt_raw = c->buf[B_RPTRAW].get<double>(W.test_cap * 3);
+        W.sort_temp = c->buf[B_SORTTMP].get<uint32_t>(
+            radix_sort_temp_bytes((uint32_t)std::max<uint64_t>(L.ns + L.nc, W.test_cap)) / 4 + 64);
+        return MCGPU_OK;
+    };
+    // record segment from the host's record count, then the per-pair ranges
+    auto record_segment = [&]() {
+        W.rec_ids = c->buf[B_RIDS].get<uint32_t>(std::max<uint64_t>(c->n_records, 1) * 5);
+        W.rec_pts = c->buf[B_RPTS].get<double>(std::max<uint64_t>(c->n_records, 1) * 3);
+        const uint32_t nrec = (uint32_t)c->n_records;
+        run_segment(c, 2, seg_key(P, W, n, nrec, prof), [&](int* aux) {
+            rec(c, 2 * MCGPU_STAGE_DOWNLOAD); // record sort + gather (added to the narrow stage)
+            aux[0] = launch_records(P, W, nrec, s);
+            rec(c, 2 * MCGPU_STAGE_DOWNLOAD + 1);
+        });
+        c->rec_buf = c->graphs[2].aux[0];
+        // per-pair record ranges (first sorted record of each pair, then the total)
+        if (n > 1)
+            ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
+                "D2H ranges");
+        else {
+            hc[16 + 2] = 0;
+            hc[16 + 3] = (uint32_t)c->n_records;
+        }
+        ck(cudaStreamSynchronize(s), "sync records");
+    };
+    auto read_status = [&](bool ranges) {
+        ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+        ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+        ck(cudaMemcpyAsync(hc + 16 + n, W.pair_bad, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H bad");
+        if (ranges)
+            ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
+                "D2H ranges");
+    };
+    // The stage-3 buffers of the previous call stay out of the segment keys.
+    W.plane_slot = W.proj_flag = W.proj_list = W.poly_list = W.voff = W.vcur = W.vface = W.rec_ids = nullptr;
+    W.planes = nullptr;
+    W.vneed = nullptr;
+    W.tri_scratch = nullptr;
+    W.tests = nullptr;
+    W.test_info = nullptr;
+    W.rec_key[0] = W.rec_key[1] = nullptr;
+    W.rec_val[0] = W.rec_val[1] = nullptr;
+    W.rec_pt_raw = W.rec_pts = nullptr;
+    W.tri_scratch_cap = W.tri_stride = W.test_cap = W.inc_cap = W.plane_cap = 0;
+    const std::vector<unsigned char> key0 = seg_key(P, W, n, key_bits, prof);
+    uint64_t npairs = 0;
+    bool done = false;
+    // Fused call: after a call of the same shape, the three segments run as
+    // one graph with one readback. Stage 3 is sized for the pair capacity (a
+    // plane slot for every face, tests for every pair the buffer holds), so
+    // nothing overflows whatever the pair count, and the records are ordered
+    // from the count left on the device. A pair overflow or a traversal stack
+    // overflow reruns the call stage by stage; a record count past the
+    // one-launch ordering reruns only the record segment.
+    if (c->use_graphs && c->use_fuse && !prof && c->fuse_ok && c->fuse_key == key0) {
+        rc = size_stage3(W.pair_cap, true);
+        if (rc != MCGPU_OK) return rc;
+        const uint32_t rec_cap = (uint32_t)std::min<uint64_t>(W.test_cap, kRankSortMax);
+        const bool dev_rec = c->fuse_nrec <= rec_cap;
+        if (dev_rec) {
+            W.rec_ids = c->buf[B_RIDS].get<uint32_t>((size_t)rec_cap * 5);
+            W.rec_pts = c->buf[B_RPTS].get<double>((size_t)rec_cap * 3);
+        }
+        run_segment(c, 3, seg_key(P, W, n, key_bits, keep, dev_rec, rec_cap), [&](int* aux) {
+            seg0(aux);
+            seg1();
+            aux[2] = dev_rec ? launch_records_dev(P, W, rec_cap, s) : 0;
+        });
+        src_buf = c->graphs[3].aux[0];
+        cut_buf = c->graphs[3].aux[1];
+        read_status(dev_rec && n > 1);
+        ck(cudaStreamSynchronize(s), "sync fused");
+        bool stack = false;
+        for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
+        if (!stack && hc[0] <= W.pair_cap) {
+            npairs = hc[0];
+            c->n_pairs_found = npairs;
+            c->n_tests = hc[1];
+            c->n_records = hc[2];
+            if (dev_rec && c->n_records <= rec_cap) {
+                c->rec_buf = c->graphs[3].aux[2];
+                if (n == 1) {
+                    hc[16 + 2] = 0;
+                    hc[16 + 3] = (uint32_t)c->n_records;
+                }
+            } else {
+                record_segment();
+            }
+            done = true;
+        }
     }
-    ck(cudaStreamSynchronize(s), "sync records");
+    if (!done) {
+        run_segment(c, 0, key0, seg0);
+        src_buf = c->graphs[0].aux[0];
+        cut_buf = c->graphs[0].aux[1];
+
+        // readback 1: pair count and traversal flags
+        ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+        ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+        ck(cudaStreamSynchronize(s), "sync traverse");
+        bool deep = false;
+        for (int attempt = 0; attempt < 4; ++attempt) {
+            bool stack = false;
+            for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
+            const uint64_t np = hc[0];
+            if (!stack && np <= W.pair_cap) break;
+            if (np > W.pair_cap) {
+                W.pair_cap = np + np / 8 + 1024;
+                W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
+            }
+            deep = deep || stack;
+            ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
+            ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
+            ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+            launch_packets(P, W, src_buf, s);
+            launch_traverse(P, W, src_buf, cut_buf, deep, s);
+            ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+            ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+            ck(cudaStreamSynchronize(s), "sync traverse");
+        }
+        npairs = hc[0];
+        c->n_pairs_found = npairs;
+        rc = size_stage3(npairs, false);
+        if (rc != MCGPU_OK) return rc;
+        run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) { seg1(); });
+
+        // readback 2: counters, per-pair status / degenerate face / record count
+        read_status(false);
+        ck(cudaStreamSynchronize(s), "sync narrow");
+        c->n_tests = hc[1];
+        c->n_records = hc[2];
+        record_segment();
+    }
+    c->fuse_key = key0;
+    c->fuse_ok = true;
+    c->fuse_nrec = c->n_records;
     ck(cudaGetLastError(), "kernel launch");
 
     c->sums.assign(n, mcgpu_summary());
@@ -946,6 +1030,7 @@ int mcgpu_context_create(mcgpu_context* out, int device)
             if (v >= 1 && v <= 32) c->tune.packet_faces = (uint32_t)v;
         }
         if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
+        if (const char* e = getenv("MCGPU_FUSE")) c->use_fuse = atoi(e) != 0;
         if (const char* e = getenv("MCGPU_SPLIT_CAP")) c->split_cap = strtoull(e, nullptr, 10);
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");

@@ -390,16 +390,35 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
 constexpr int kRefitWin = MCGPU_REFIT_WIN;
 constexpr uint32_t kNoFar = 0xFFFFFFFFu;
 
+// D for 32-bit keys: key XOR above position XOR in one 64-bit word; for
+// 64-bit keys the pair compared lexicographically
 struct Dlt { unsigned long long x; uint32_t i; };
 __device__ __forceinline__ bool dlt_less(const Dlt& a, const Dlt& b)
 {
     return a.x < b.x || (a.x == b.x && a.i < b.i);
 }
-template <typename K>
-__device__ __forceinline__ Dlt boundary_delta(const K* __restrict__ key, int n, int j)
+__device__ __forceinline__ bool dlt_less(unsigned long long a, unsigned long long b) { return a < b; }
+__device__ __forceinline__ unsigned long long dlt_make(uint32_t a, uint32_t b, int j)
 {
-    if (j < 0 || j >= n - 1) return Dlt { ~0ull, ~0u };
-    return Dlt { (unsigned long long)(__ldg(&key[j]) ^ __ldg(&key[j + 1])), (uint32_t)(j ^ (j + 1)) };
+    return ((unsigned long long)(a ^ b) << 32) | (uint32_t)(j ^ (j + 1));
+}
+__device__ __forceinline__ Dlt dlt_make(unsigned long long a, unsigned long long b, int j)
+{
+    return Dlt { a ^ b, (uint32_t)(j ^ (j + 1)) };
+}
+template <typename T> __device__ __forceinline__ T dlt_top();
+template <> __device__ __forceinline__ unsigned long long dlt_top<unsigned long long>() { return ~0ull; }
+template <> __device__ __forceinline__ Dlt dlt_top<Dlt>() { return Dlt { ~0ull, ~0u }; }
+template <typename T> __device__ __forceinline__ T dlt_bottom();
+template <> __device__ __forceinline__ unsigned long long dlt_bottom<unsigned long long>() { return 0ull; }
+template <> __device__ __forceinline__ Dlt dlt_bottom<Dlt>() { return Dlt { 0ull, 0u }; }
+__device__ __forceinline__ unsigned long long dlt_shfl_up(unsigned long long d, int o)
+{
+    return __shfl_up_sync(0xFFFFFFFFu, d, o);
+}
+__device__ __forceinline__ unsigned long long dlt_shfl_down(unsigned long long d, int o)
+{
+    return __shfl_down_sync(0xFFFFFFFFu, d, o);
 }
 __device__ __forceinline__ Dlt dlt_shfl_up(const Dlt& d, int o)
 {
@@ -408,6 +427,15 @@ __device__ __forceinline__ Dlt dlt_shfl_up(const Dlt& d, int o)
 __device__ __forceinline__ Dlt dlt_shfl_down(const Dlt& d, int o)
 {
     return Dlt { __shfl_down_sync(0xFFFFFFFFu, d.x, o), __shfl_down_sync(0xFFFFFFFFu, d.i, o) };
+}
+template <typename K>
+using DltOf = decltype(dlt_make(K(), K(), 0));
+// D(j); the mesh ends (j = -1, j = n-1) are above every boundary
+template <typename K>
+__device__ __forceinline__ DltOf<K> boundary_delta(const K* __restrict__ key, int n, int j)
+{
+    if (j < 0 || j >= n - 1) return dlt_top<DltOf<K>>();
+    return dlt_make(__ldg(&key[j]), __ldg(&key[j + 1]), j);
 }
 __device__ __forceinline__ void store_fbox(FBox* p, const FBox& b)
 {
@@ -430,9 +458,10 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
     const uint8_t* __restrict__ cl_n, Node* __restrict__ nodes, uint32_t* __restrict__ split_far,
     FBox* __restrict__ split_box)
 {
+    using D = DltOf<K>;
     constexpr int kW = kRefitWin / 32;
-    __shared__ Dlt sd[kRefitWin + 1];  // sd[t] = D(w0 - 1 + t)
-    __shared__ Dlt wagg[2][kW];
+    __shared__ D sd[kRefitWin + 1];  // sd[t] = D(w0 - 1 + t)
+    __shared__ D wagg[2][kW];
     __shared__ uint32_t sfar[kRefitWin];
     __shared__ uint8_t sinw[kRefitWin];
     __shared__ FBox sbox[kRefitWin][2];
@@ -440,21 +469,21 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
     const int w0 = blockIdx.x * kRefitWin, w1 = min(n, w0 + kRefitWin) - 1;
     const int i = w0 + t;
     const bool valid = i <= w1;
-    const Dlt lowest { 0ull, 0u }; // below every boundary (a boundary's position XOR is >= 1)
-    const Dlt dm = valid ? boundary_delta(key, n, i) : lowest;
+    const D lowest = dlt_bottom<D>(); // below every boundary (a boundary's position XOR is >= 1)
+    const D dm = valid ? boundary_delta(key, n, i) : lowest;
     sd[t + 1] = dm;
     if (t == 0) sd[0] = boundary_delta(key, n, w0 - 1);
     sfar[t] = kNoFar;
     // inclusive max-scans of D over the window, from the left and from the right
-    Dlt pre = dm, suf = dm;
+    D pre = dm, suf = dm;
     for (int o = 1; o < 32; o <<= 1) {
-        const Dlt a = dlt_shfl_up(pre, o), b = dlt_shfl_down(suf, o);
+        const D a = dlt_shfl_up(pre, o), b = dlt_shfl_down(suf, o);
         if (lane >= o && dlt_less(pre, a)) pre = a;
         if (lane + o < 32 && dlt_less(suf, b)) suf = b;
     }
     if (lane == 31) wagg[0][warp] = pre;
     if (lane == 0) wagg[1][warp] = suf;
-    Dlt epre = dlt_shfl_up(pre, 1), esuf = dlt_shfl_down(suf, 1);
+    D epre = dlt_shfl_up(pre, 1), esuf = dlt_shfl_down(suf, 1);
     __syncthreads();
     if (lane == 0) epre = sd[0];
     else if (dlt_less(epre, sd[0])) epre = sd[0];
@@ -472,18 +501,24 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
     for (int j = 0; j < 3; ++j) { fb.lo[j] = 3.4e38f; fb.hi[j] = -3.4e38f; }
     {
         const uint32_t s0 = cl_start[i], cn = cl_n[i];
-        uint32_t lf[16];
-        for (uint32_t u = 0; u < cn; ++u) lf[u] = __ldg(&leaf_face[s0 + u]);
-        for (uint32_t u = 0; u < cn; ++u) {
-            const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[u] * 6);
-            const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
-            fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
-            fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
+        const uint32_t f0 = __ldg(&leaf_face[s0]);
+        fb.plo = fb.phi = P.face_pair[f0] & ~kCutBit;
+        // four faces at a time, their loads in flight together
+        for (uint32_t c0 = 0; c0 < cn; c0 += 4) {
+            uint32_t lf[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) lf[u] = c0 + u < cn ? __ldg(&leaf_face[s0 + c0 + u]) : f0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float2* b = reinterpret_cast<const float2*>(fbox32 + (size_t)lf[u] * 6);
+                const float2 x = __ldg(b), y = __ldg(b + 1), z = __ldg(b + 2);
+                fb.lo[0] = fminf(fb.lo[0], x.x); fb.lo[1] = fminf(fb.lo[1], x.y); fb.lo[2] = fminf(fb.lo[2], y.x);
+                fb.hi[0] = fmaxf(fb.hi[0], y.y); fb.hi[1] = fmaxf(fb.hi[1], z.x); fb.hi[2] = fmaxf(fb.hi[2], z.y);
+            }
         }
-        fb.plo = fb.phi = P.face_pair[lf[0]] & ~kCutBit;
     }
     int l = i, r = i;
-    Dlt dl = sd[t], dr = sd[t + 1]; // D(l-1), D(r)
+    D dl = sd[t], dr = sd[t + 1]; // D(l-1), D(r)
     for (;;) {
         const bool right = dlt_less(dr, dl); // the parent extends to the right: this node is its left child
         const int s = right ? r : l - 1;
@@ -507,8 +542,8 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
             o = load_fbox_cg(&split_box[2 * (size_t)s + (slot ^ 1)]);
         }
         const int pl = right ? l : (int)prev, pr = right ? (int)prev : r;
-        const Dlt pdl = (pl >= w0 && pl <= w1 + 1) ? sd[pl - w0] : boundary_delta(key, n, pl - 1);
-        const Dlt pdr = (pr >= w0 - 1 && pr <= w1) ? sd[pr - w0 + 1] : boundary_delta(key, n, pr);
+        const D pdl = (pl >= w0 && pl <= w1 + 1) ? sd[pl - w0] : boundary_delta(key, n, pl - 1);
+        const D pdr = (pr >= w0 - 1 && pr <= w1) ? sd[pr - w0 + 1] : boundary_delta(key, n, pr);
         const bool root = pl == 0 && pr == n - 1;
         const int pidx = root ? 0 : (dlt_less(pdr, pdl) ? pr : pl);
         const FBox& lb = right ? fb : o;
@@ -1284,7 +1319,8 @@ __device__ __forceinline__ void finish_plane(FacePlane& pl, const double* first)
 #endif
 __global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, const uint8_t* __restrict__ cand,
     uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, uint64_t plane_cap,
-    uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad)
+    uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad,
+    uint32_t* __restrict__ proj_flag)
 {
     for (uint32_t f0 = blockIdx.x * blockDim.x; f0 < P.nf; f0 += gridDim.x * blockDim.x) {
         const uint32_t f = f0 + threadIdx.x;
@@ -1293,6 +1329,7 @@ __global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, con
         if (!c) continue;
         plane_slot[f] = slot;
         if (slot >= plane_cap) continue;
+        proj_flag[slot] = 0u; // the narrow phase queues the slot's projection once
         const uint32_t o = face_o(P, f), n = face_n(P, f);
         // Newell's normal over the rotated vertex list
         double nx = 0.0, ny = 0.0, nz = 0.0;
@@ -1820,9 +1857,18 @@ __global__ void __launch_bounds__(kBlock) k_record_pack(unsigned long long* __re
 
 // first sorted record of every pair (and the total at n_pairs): the records
 // are grouped by pair, so a binary search over the sorted keys finds them
-__global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const unsigned long long* __restrict__ key,
-    uint32_t nrec, int gbits, uint32_t* __restrict__ rec_begin)
+// record count: the host's, or (ndev) the device's when it is within cap (else 0)
+__device__ __forceinline__ uint32_t record_count(uint32_t n, const uint32_t* ndev, uint32_t cap)
 {
+    if (!ndev) return n;
+    const uint32_t v = *ndev;
+    return v <= cap ? v : 0u;
+}
+
+__global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const unsigned long long* __restrict__ key,
+    uint32_t nrec_host, const uint32_t* __restrict__ ndev, uint32_t cap, int gbits, uint32_t* __restrict__ rec_begin)
+{
+    const uint32_t nrec = record_count(nrec_host, ndev, cap);
     const unsigned long long gmask = (1ull << gbits) - 1ull;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= P.n_pairs; p += gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = nrec;
@@ -1841,11 +1887,14 @@ __global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const 
 // spread over the whole GPU in one launch, cheaper than a multi-pass radix
 // sort for the few thousand records of a dispatch.
 constexpr int kRankChunk = 2048;
-__global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long long* __restrict__ key, uint32_t n,
-    uint32_t* __restrict__ rank)
+__global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long long* __restrict__ key, uint32_t n_host,
+    const uint32_t* __restrict__ ndev, uint32_t cap, uint32_t* __restrict__ rank)
 {
     __shared__ unsigned long long sk[kRankChunk];
-    const uint32_t lo = blockIdx.y * kRankChunk, hi = min(n, lo + kRankChunk);
+    const uint32_t n = record_count(n_host, ndev, cap);
+    const uint32_t lo = blockIdx.y * kRankChunk;
+    if (lo >= n || blockIdx.x * kBlock >= n) return; // grids sized for a capacity
+    const uint32_t hi = min(n, lo + kRankChunk);
     for (uint32_t j = lo + threadIdx.x; j < hi; j += kBlock) sk[j - lo] = key[j];
     __syncthreads();
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
@@ -1867,10 +1916,11 @@ __global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long lon
 
 // records in rank order -> sorted keys and output arrays with per-pair local ids
 __global__ void __launch_bounds__(kBlock) k_scatter_records(Problem P, const unsigned long long* __restrict__ key,
-    const uint32_t* __restrict__ val, const uint32_t* __restrict__ rank, uint32_t nrec,
-    const Test* __restrict__ tests, const double* __restrict__ rec_pt, unsigned long long* __restrict__ skey,
-    uint32_t* __restrict__ rec_ids, double* __restrict__ rec_pts)
+    const uint32_t* __restrict__ val, const uint32_t* __restrict__ rank, uint32_t nrec_host,
+    const uint32_t* __restrict__ ndev, uint32_t cap, const Test* __restrict__ tests, const double* __restrict__ rec_pt,
+    unsigned long long* __restrict__ skey, uint32_t* __restrict__ rec_ids, double* __restrict__ rec_pts)
 {
+    const uint32_t nrec = record_count(nrec_host, ndev, cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += gridDim.x * blockDim.x) {
         const uint32_t r = rank[i];
         const uint32_t ti = val[i];
@@ -2045,7 +2095,7 @@ void launch_planes(const Problem& P, Work& W, cudaStream_t s)
     const int g = grid_for(P.nf);
     g_launches++;
     k_planes<<<g, kBlock, 0, s>>>(P, W.cand, W.plane_slot, (FacePlane*)W.planes, W.plane_cap, W.counters,
-        W.poly_list, W.pair_bad);
+        W.poly_list, W.pair_bad, W.proj_flag);
     if (W.tri_stride) g_launches++;
     if (W.tri_stride)
         k_triplets<<<grid_for(1024), kBlock, 0, s>>>(P, W.poly_list, W.counters, W.plane_slot, (FacePlane*)W.planes,
@@ -2087,7 +2137,6 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     // the hit list lives in rec_key[1] (uint2 per test), free until the record sort
     uint2* hits = reinterpret_cast<uint2*>(W.rec_key[1]);
     g_launches += 3;
-    cudaMemsetAsync(W.proj_flag, 0, sizeof(uint32_t) * W.plane_cap, s);
     k_narrow_signs<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
     k_finish_planes<<<grid_for(W.plane_cap), kBlock, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot, W.proj_list,
@@ -2097,9 +2146,8 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
         W.pair_bad);
 }
 
-// Records up to this many are ordered by k_rank_records (one launch). With
+// Records up to kRankSortMax are ordered by k_rank_records (one launch). With
 // one pair W.pair_nrec is left alone: that pair owns records [0, nrec).
-constexpr uint32_t kRankSortMax = 24576;
 
 int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
 {
@@ -2117,12 +2165,13 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
         cudaMemsetAsync(rank, 0, sizeof(uint32_t) * nrec, s);
         g_launches += 2;
         k_rank_records<<<dim3((nrec + kBlock - 1) / kBlock, (nrec + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
-            W.rec_key[0], nrec, rank);
-        k_scatter_records<<<g, kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, nrec, W.tests, W.rec_pt_raw,
-            W.rec_key[1], W.rec_ids, W.rec_pts);
+            W.rec_key[0], nrec, nullptr, 0, rank);
+        k_scatter_records<<<g, kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, nrec, nullptr, 0, W.tests,
+            W.rec_pt_raw, W.rec_key[1], W.rec_ids, W.rec_pts);
         if (P.n_pairs > 1) { // one pair owns every record (the caller knows the range)
             g_launches++;
-            k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], nrec, 32, W.pair_nrec);
+            k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], nrec, nullptr, 0, 32,
+                W.pair_nrec);
         }
         return 1;
     }
@@ -2133,10 +2182,31 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
     g_launches += 2;
     k_gather_records<<<g, kBlock, 0, s>>>(P, W.rec_val[buf], nrec, W.tests, W.rec_pt_raw, W.rec_ids, W.rec_pts);
     if (P.n_pairs > 1)
-        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, gbits, W.pair_nrec);
+        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[buf], nrec, nullptr, 0, gbits,
+            W.pair_nrec);
     else
         g_launches--;
     return buf;
+}
+
+// The same one-launch ordering with the record count left on the device
+// (counters[2]): grids are sized for `cap` records, and a count above it
+// leaves everything untouched for the host to order from its own count.
+int launch_records_dev(const Problem& P, Work& W, uint32_t cap, cudaStream_t s)
+{
+    const uint32_t* nd = W.counters + 2;
+    uint32_t* rank = W.rec_val[1];
+    cudaMemsetAsync(rank, 0, sizeof(uint32_t) * cap, s);
+    g_launches += 2;
+    k_rank_records<<<dim3((cap + kBlock - 1) / kBlock, (cap + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
+        W.rec_key[0], 0, nd, cap, rank);
+    k_scatter_records<<<grid_for(cap), kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, 0, nd, cap, W.tests,
+        W.rec_pt_raw, W.rec_key[1], W.rec_ids, W.rec_pts);
+    if (P.n_pairs > 1) {
+        g_launches++;
+        k_pair_record_ranges<<<grid_for(P.n_pairs + 1), kBlock, 0, s>>>(P, W.rec_key[1], 0, nd, cap, 32, W.pair_nrec);
+    }
+    return 1;
 }
 
 } // namespace mcgpu

@@ -137,5 +137,9 @@ void launch_incidence(const Problem& P, Work& W, cudaStream_t s);        // vert
 void launch_tests(const Problem& P, Work& W, cudaStream_t s);
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s);
 int launch_records(const Problem& P, Work& W, uint32_t n_records, cudaStream_t s);
+// record ordering from the device's record count (at most cap = kRankSortMax
+// records; above cap nothing is written); returns the sorted-key buffer
+int launch_records_dev(const Problem& P, Work& W, uint32_t cap, cudaStream_t s);
+constexpr uint32_t kRankSortMax = 24576; // records ordered by one rank launch
 
 } // namespace mcgpu

@@ -70,8 +70,9 @@ uint64_t mesh_indices(const mcgpu_mesh& m)
 
 // Device bytes one request adds to a batch: the dispatch's per-face and
 // per-vertex buffers (face boxes f64 + f32, keys, values, tree, incidence,
-// planes, pairs, tests and records at their usual sizes) plus slack.
-uint64_t estimate_bytes(uint64_t faces, uint64_t verts) { return (1ull << 20) + faces * 640 + verts * 64; }
+// pairs, tests and records at their usual sizes, and a plane slot for every
+// face, 104 B, as a repeated dispatch shape sizes them) plus slack.
+uint64_t estimate_bytes(uint64_t faces, uint64_t verts) { return (1ull << 20) + faces * 744 + verts * 64; }
 
 } // namespace
 

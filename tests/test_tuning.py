@@ -118,3 +118,55 @@ def test_split_capacity_overflow_is_harmless():
     assert np.array_equal(got.record_ids, want.record_ids) and G.same_bits(got.record_points, want.record_points)
     a.close()
     b.close()
+
+
+def _lifted(m, dz):
+    return dict(v=m["v"] + np.array([0.0, 0.0, dz]), f=m["f"], fs=m["fs"])
+
+
+def _same_result(a, b):
+    assert (a.status, a.num_pairs, a.num_tests, a.num_records) == (b.status, b.num_pairs, b.num_tests, b.num_records)
+    assert np.array_equal(a.record_ids, b.record_ids)
+    assert G.same_bits(a.record_points, b.record_points)
+
+
+@pytest.mark.gpu
+def test_fused_call_reorders_records_past_the_one_launch_sort(ctx):
+    """A call of the same shape as the one before runs as one graph; when its
+    records outnumber the one-launch ordering (24,576), the record segment
+    runs again from the host's count. Stage-timed calls take the stage-by-
+    stage path: both give the same records."""
+    src = meshgen.grid(200, 1.5, lambda X, Y: 0.02 * np.sin(40.0 * X) * np.sin(40.0 * Y))
+    cut = meshgen.grid(200, 1.5, lambda X, Y: np.full_like(X, 0.001))
+    far = ctx.dispatch(src, _lifted(cut, 1.0))
+    assert far.num_records == 0
+    fused = ctx.dispatch(src, cut)
+    exact = ctx.dispatch(src, cut, profile=True)
+    assert exact.num_records > 24576
+    _same_result(fused, exact)
+    again = ctx.dispatch(src, cut)
+    _same_result(again, exact)
+
+
+@pytest.mark.gpu
+def test_fused_call_reruns_on_pair_overflow():
+    """A fresh context holds 2 (source + cut faces) pairs; near-coplanar grids
+    overlap about 18 faces each, so the fused call after a disjoint one
+    overflows and reruns stage by stage (the pair buffer grows)."""
+    from mcut_gb300 import Context
+    rng = np.random.default_rng(77)
+    src = meshgen.grid(80, 1.0)
+    src["v"][:, 2] = rng.uniform(-2e-4, 2e-4, size=src["v"].shape[0])
+    cut = meshgen.grid(80, 1.0, lambda X, Y: np.full_like(X, 3e-5))
+    c = Context(0)
+    try:
+        far = c.dispatch(src, _lifted(cut, 5.0))
+        assert far.num_pairs == 0
+        over = c.dispatch(src, cut)
+        assert over.num_pairs > 2 * (meshgen.num_faces(src) + meshgen.num_faces(cut))
+        exact = c.dispatch(src, cut, profile=True)
+        _same_result(over, exact)
+        for _ in range(3):  # the grown buffers, then fused calls at that size
+            _same_result(c.dispatch(src, cut), exact)
+    finally:
+        c.close()
