@@ -129,6 +129,7 @@ struct mcgpu_context_t {
     mcgpu_tuning tune { 4, 0, 32, 64, 2 };  // MCGPU_LEAF_SIZE / MCGPU_TRAVERSAL / MCGPU_PACKET_FACES override at creation
     bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
     bool use_fuse = true;                 // MCGPU_FUSE=0: every call stage by stage
+    bool host_reads = false;              // the device reads pageable host memory (MCGPU_HOST_READS=0: never)
     uint64_t split_cap = 0;               // MCGPU_SPLIT_CAP: fixed split-entry capacity (0: by size)
     struct Graph {
         std::vector<unsigned char> key;
@@ -309,6 +310,29 @@ void recentre_pair_mt(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, doubl
     *eps_out = frame_eps(cs, t);
 }
 
+// Host arrays read in place by the device (it walks the host's page tables:
+// cudaDevAttrPageableMemoryAccess): one launch moves every segment at the
+// host link's bandwidth, with no staging copy by the driver. 8-byte words
+// where both ends and the size allow, else 4-byte words.
+struct HostSeg { const void* src; void* dst; uint64_t bytes; };
+struct HostSegs { HostSeg s[4]; int n; };
+__global__ void __launch_bounds__(256) k_host_copy(HostSegs g)
+{
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, st = (uint64_t)gridDim.x * blockDim.x;
+    for (int k = 0; k < g.n; ++k) {
+        const HostSeg h = g.s[k];
+        if ((((uintptr_t)h.src | (uintptr_t)h.dst | h.bytes) & 7u) == 0) {
+            const uint2* a = static_cast<const uint2*>(h.src);
+            uint2* b = static_cast<uint2*>(h.dst);
+            for (uint64_t i = t0; i < h.bytes / 8; i += st) b[i] = a[i];
+        } else {
+            const uint32_t* a = static_cast<const uint32_t*>(h.src);
+            uint32_t* b = static_cast<uint32_t*>(h.dst);
+            for (uint64_t i = t0; i < h.bytes / 4; i += st) b[i] = a[i];
+        }
+    }
+}
+
 // resident cut mesh: its stored user coordinates mapped into the pair's frame
 __global__ void k_apply_frame(const double* __restrict__ in, double* __restrict__ out, uint64_t n3, double c0,
     double c1, double c2, double t0, double t1, double t2)
@@ -477,8 +501,24 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     const double* X = (pk && dev) ? static_cast<const double*>(pk->X)
         : split ? static_cast<const double*>(srcs[0].vertices) : c->buf[B_X].get<double>(L.nv * 3);
     uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
-    if ((pk && dev) || split) {
-        // read in place
+    // a single pair from host arrays, copied by the device reading them
+    const bool host_read = c->host_reads && !dev && !pk && !res && n == 1 && !(flags & MCGPU_RECENTRE)
+        && ((uintptr_t)srcs[0].vertices & 3) == 0 && ((uintptr_t)cuts[0].vertices & 3) == 0
+        && ((uintptr_t)srcs[0].face_indices & 3) == 0 && ((uintptr_t)cuts[0].face_indices & 3) == 0;
+    if (host_read) {
+        HostSegs g {};
+        const uint64_t ic = (uint64_t)L.ibase[1] - L.is[0];
+        g.s[0] = HostSeg { srcs[0].vertices, const_cast<double*>(X), (uint64_t)L.vs[0] * 24 };
+        g.s[1] = HostSeg { cuts[0].vertices, const_cast<double*>(X) + (size_t)L.vs[0] * 3,
+            (uint64_t)cuts[0].num_vertices * 24 };
+        g.s[2] = HostSeg { srcs[0].face_indices, fidx, (uint64_t)L.is[0] * 4 };
+        g.s[3] = HostSeg { cuts[0].face_indices, fidx + L.is[0], ic * 4 };
+        g.n = 4;
+        g_launches++;
+        k_host_copy<<<grid1((L.nv * 24 + L.nidx * 4) / 8), 256, 0, s>>>(g);
+    }
+    if ((pk && dev) || split || host_read) {
+        // read in place, or copied above
     } else if (pk && !(flags & MCGPU_RECENTRE)) {
         ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
             "H2D X");
@@ -535,8 +575,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     }
     const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const bool staged = (flags & MCGPU_RECENTRE) != 0; // indices went up with the recentred coordinates
-    if (split) {
-        // k_prep reads the caller's index arrays
+    if (split || host_read) {
+        // k_prep reads the caller's index arrays, or they were copied above
     } else if (pk && !staged)
         ck(cudaMemcpyAsync(fidx, pk->idx, (size_t)L.nidx * 4, ikind, s), "H2D idx");
     else for (uint32_t p = 0; p < n; ++p) {
@@ -1031,6 +1071,9 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         }
         if (const char* e = getenv("MCGPU_GRAPHS")) c->use_graphs = atoi(e) != 0;
         if (const char* e = getenv("MCGPU_FUSE")) c->use_fuse = atoi(e) != 0;
+        int pma = 0;
+        if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess) c->host_reads = pma != 0;
+        if (const char* e = getenv("MCGPU_HOST_READS")) c->host_reads = c->host_reads && atoi(e) != 0;
         if (const char* e = getenv("MCGPU_SPLIT_CAP")) c->split_cap = strtoull(e, nullptr, 10);
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");
