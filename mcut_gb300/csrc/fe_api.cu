@@ -363,16 +363,30 @@ __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint3
     const uint32_t* fbase = tab + 4 * (n_pairs + 1);
     const uint32_t* fs = tab + 5 * (n_pairs + 1);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nidx; i += stride) {
-        uint32_t lo = 0, hi = n_pairs; // last pair with ibase <= i
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (ibase[mid] <= i) lo = mid; else hi = mid;
+    // four independent elements per thread and step: their loads are in flight together
+    for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < nidx; i0 += 4 * stride) {
+        uint32_t local[4], add[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t i = i0 + k * stride;
+            local[k] = 0u;
+            add[k] = 0u;
+            if (i >= nidx) continue;
+            uint32_t lo = 0, hi = n_pairs; // last pair with ibase <= i
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (ibase[mid] <= i) lo = mid; else hi = mid;
+            }
+            const uint32_t p = lo;
+            const bool cut = (i - ibase[p]) >= is[p];
+            local[k] = src_in ? (cut ? cut_in[i - is[0]] : src_in[i]) : fidx[i];
+            add[k] = vbase[p] + (cut ? vs[p] : 0u);
         }
-        const uint32_t p = lo;
-        const bool cut = (i - ibase[p]) >= is[p];
-        const uint32_t local = src_in ? (cut ? cut_in[i - is[0]] : src_in[i]) : fidx[i];
-        fidx[i] = local + vbase[p] + (cut ? vs[p] : 0u);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t i = i0 + k * stride;
+            if (i < nidx) fidx[i] = local[k] + add[k];
+        }
     }
     for (uint64_t f = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; f < nf; f += stride) {
         uint32_t lo = 0, hi = n_pairs;

@@ -385,7 +385,7 @@ __device__ __forceinline__ FBox get_child(const Node* nd, int slot)
 // memory: the climb through a window touches no global memory. Splits whose
 // node leaves the window use global acquire-release exchanges.
 #ifndef MCGPU_REFIT_WIN
-#define MCGPU_REFIT_WIN 256
+#define MCGPU_REFIT_WIN 128
 #endif
 constexpr int kRefitWin = MCGPU_REFIT_WIN;
 constexpr uint32_t kNoFar = 0xFFFFFFFFu;
@@ -1317,10 +1317,12 @@ __device__ __forceinline__ void finish_plane(FacePlane& pl, const double* first)
 #ifndef MCGPU_PL_MINB
 #define MCGPU_PL_MINB 1
 #endif
-__global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, const uint8_t* __restrict__ cand,
-    uint32_t* __restrict__ plane_slot, FacePlane* __restrict__ planes, uint64_t plane_cap,
-    uint32_t* __restrict__ counters, uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad,
-    uint32_t* __restrict__ proj_flag)
+// Candidate faces -> dense plane slots, and the slot -> face list (slot_face)
+// the plane kernel walks: its fp64 work then runs in full warps however
+// sparsely the candidates lie among the faces.
+__global__ void __launch_bounds__(kBlock) k_plane_slots(Problem P, const uint8_t* __restrict__ cand,
+    uint32_t* __restrict__ plane_slot, uint64_t plane_cap, uint32_t* __restrict__ counters,
+    uint32_t* __restrict__ slot_face, uint32_t* __restrict__ proj_flag)
 {
     for (uint32_t f0 = blockIdx.x * blockDim.x; f0 < P.nf; f0 += gridDim.x * blockDim.x) {
         const uint32_t f = f0 + threadIdx.x;
@@ -1329,7 +1331,18 @@ __global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, con
         if (!c) continue;
         plane_slot[f] = slot;
         if (slot >= plane_cap) continue;
+        slot_face[slot] = f;
         proj_flag[slot] = 0u; // the narrow phase queues the slot's projection once
+    }
+}
+
+__global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, const uint32_t* __restrict__ slot_face,
+    FacePlane* __restrict__ planes, uint64_t plane_cap, uint32_t* __restrict__ counters,
+    uint32_t* __restrict__ poly_list, int32_t* __restrict__ pair_bad)
+{
+    const uint32_t nslots = (uint32_t)min((uint64_t)counters[3], plane_cap);
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslots; slot += gridDim.x * blockDim.x) {
+        const uint32_t f = slot_face[slot];
         const uint32_t o = face_o(P, f), n = face_n(P, f);
         // Newell's normal over the rotated vertex list
         double nx = 0.0, ny = 0.0, nz = 0.0;
@@ -1756,7 +1769,11 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
 // The triangles that pass 1 queued (a segment meets their plane): unit
 // normal, d, largest component and projection matrix, once per face
 // (polygons got theirs with the plane).
-__global__ void __launch_bounds__(kBlock) k_finish_planes(Problem P, FacePlane* __restrict__ planes,
+// Narrow-phase kernels over short lists (hit triangles, hits) run long fp64
+// chains per item: launched in blocks of kSpread threads so that a list of a
+// few thousand items still occupies every SM.
+constexpr int kSpread = 64;
+__global__ void __launch_bounds__(kSpread) k_finish_planes(Problem P, FacePlane* __restrict__ planes,
     const uint32_t* __restrict__ plane_slot, const uint32_t* __restrict__ proj_list,
     const uint32_t* __restrict__ counters)
 {
@@ -1780,7 +1797,7 @@ __global__ void __launch_bounds__(kBlock) k_finish_planes(Problem P, FacePlane* 
 #ifndef MCGPU_NH_MINB
 #define MCGPU_NH_MINB 1
 #endif
-__global__ void __launch_bounds__(kBlock, MCGPU_NH_MINB) k_narrow_hits(Problem P, const Test* __restrict__ tests,
+__global__ void __launch_bounds__(kSpread, MCGPU_NH_MINB) k_narrow_hits(Problem P, const Test* __restrict__ tests,
     const uint2* __restrict__ hits, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
     unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
@@ -1886,7 +1903,10 @@ __global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const 
 // staged in shared memory, and adds its counts into rank[] -- n^2 compares
 // spread over the whole GPU in one launch, cheaper than a multi-pass radix
 // sort for the few thousand records of a dispatch.
-constexpr int kRankChunk = 2048;
+#ifndef MCGPU_RANK_CHUNK
+#define MCGPU_RANK_CHUNK 512
+#endif
+constexpr int kRankChunk = MCGPU_RANK_CHUNK;
 __global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long long* __restrict__ key, uint32_t n_host,
     const uint32_t* __restrict__ ndev, uint32_t cap, uint32_t* __restrict__ rank)
 {
@@ -1960,7 +1980,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_records(Problem P, const uint
     }
 }
 
-int grid_for(uint64_t n)
+static int sm_count()
 {
     static int sms = 0;
     if (!sms) {
@@ -1969,8 +1989,21 @@ int grid_for(uint64_t n)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
+    return sms;
+}
+
+int grid_for(uint64_t n)
+{
     const uint64_t want = (n + kBlock - 1) / kBlock;
-    const uint64_t cap = (uint64_t)sms * 8;
+    const uint64_t cap = (uint64_t)sm_count() * 8;
+    return (int)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+// blocks of kSpread threads for n items, at most 32 per SM
+int grid_spread(uint64_t n)
+{
+    const uint64_t want = (n + kSpread - 1) / kSpread;
+    const uint64_t cap = (uint64_t)sm_count() * 32;
     return (int)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
@@ -2093,9 +2126,11 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
 void launch_planes(const Problem& P, Work& W, cudaStream_t s)
 {
     const int g = grid_for(P.nf);
-    g_launches++;
-    k_planes<<<g, kBlock, 0, s>>>(P, W.cand, W.plane_slot, (FacePlane*)W.planes, W.plane_cap, W.counters,
-        W.poly_list, W.pair_bad, W.proj_flag);
+    g_launches += 2;
+    // the slot -> face list lives in proj_list until the narrow phase queues projections there
+    k_plane_slots<<<g, kBlock, 0, s>>>(P, W.cand, W.plane_slot, W.plane_cap, W.counters, W.proj_list, W.proj_flag);
+    k_planes<<<grid_for(W.plane_cap), kBlock, 0, s>>>(P, W.proj_list, (FacePlane*)W.planes, W.plane_cap, W.counters,
+        W.poly_list, W.pair_bad);
     if (W.tri_stride) g_launches++;
     if (W.tri_stride)
         k_triplets<<<grid_for(1024), kBlock, 0, s>>>(P, W.poly_list, W.counters, W.plane_slot, (FacePlane*)W.planes,
@@ -2139,9 +2174,10 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     g_launches += 3;
     k_narrow_signs<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
-    k_finish_planes<<<grid_for(W.plane_cap), kBlock, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot, W.proj_list,
-        W.counters);
-    k_narrow_hits<<<g, kBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
+    k_finish_planes<<<grid_spread(W.plane_cap), kSpread, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot,
+        W.proj_list, W.counters);
+    k_narrow_hits<<<grid_spread(W.test_cap), kSpread, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot,
+        (const FacePlane*)W.planes,
         keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
         W.pair_bad);
 }
