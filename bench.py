@@ -47,12 +47,27 @@ UNIT = "pairs/s"
 
 # algorithmic bytes per unit of work, per stage
 BYTES = {
-    "bounds": ("face", 80),        # read idx 12 + positions ~12, write box 48 + key 4 + id 4
+    "bounds": ("face", 116),       # read idx 12 + positions ~12 (twice: mesh boxes, face boxes), write
+                                   # fp64 box 48 + fp32 box 24 + key 4 + id 4
     "sort": ("face", 68),          # 4 passes x (8 read + 8 write) + histogram
-    "hierarchy": ("node", 160),    # children/parent 12, 2 child boxes read, box write, flag
+    "hierarchy": ("node", 184),    # node write 64 + the leaf cluster's 4 face ids and fp32 boxes 112 + keys 8
     "traverse": ("pair-of-trees", None),
     "adjacency": ("face", 40),     # incidence count + fill over indices, planes of candidates
     "narrow": ("test", 152),       # edge 2x24 + face 3x24 + plane 32 (+40 per record)
+}
+
+
+# the kernels each stage's CUDA events bracket (k_src_packets and the incidence
+# kernels run on the second stream inside the hierarchy and adjacency stages)
+STAGE_KERNELS = {
+    "upload": ["k_prep"],
+    "bounds": ["k_init_meshbox", "k_vertex_bounds", "k_mesh_frames", "k_face_bounds"],
+    "sort": ["k_upsweep", "k_digit_scan", "k_downsweep"],
+    "hierarchy": ["k_clusters", "k_build", "k_src_packets"],
+    "traverse": ["k_top_cut", "k_traverse_wave"],
+    "adjacency": ["k_plane_slots", "k_planes", "k_triplets", "k_mark_vertices", "k_vf_count", "k_vf_fill"],
+    "narrow": ["k_pair_tests", "k_narrow_signs", "k_finish_planes", "k_narrow_hits", "k_rank_records",
+               "k_scatter_records"],
 }
 
 
@@ -603,8 +618,8 @@ def run_gpu(args, world, rank, local):
         algo = 152 * summ["tests"] + 40 * summ["records"]
         units = f"152 B x {summ['tests']} tests + 40 B x {summ['records']} records"
     elif dom == "hierarchy":
-        algo = 160 * (Fc - 1)
-        units = f"160 B x {Fc - 1} nodes"
+        algo = 184 * (Fc // 4)
+        units = f"184 B x {Fc // 4} leaf clusters of 4 faces"
     else:
         algo = BYTES[dom][1] * (Fs + Fc)
         units = f"{BYTES[dom][1]} B x {Fs + Fc} faces"
@@ -630,7 +645,8 @@ def run_gpu(args, world, rank, local):
         "config": {"workload": WORKLOAD, "l2": "flushed (256 MB write) before every step",
                    "parallelism": f"replicas x{world}", "path": "plain GPU per-dispatch path"},
         "latency_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": dom, "stage_kernels": STAGE_KERNELS[dom], "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "algorithmic_bytes": algo,
                      "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)"},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
