@@ -130,6 +130,8 @@ struct mcgpu_context_t {
     bool use_graphs = true;               // MCGPU_GRAPHS=0 disables
     bool use_fuse = true;                 // MCGPU_FUSE=0: every call stage by stage
     bool host_reads = false;              // the device reads pageable host memory (MCGPU_HOST_READS=0: never)
+    uint32_t inc_slots = 16;              // vertex -> face slots per vertex (MCGPU_INC_SLOTS; 0: CSR lists)
+    bool csr_incidence = false;           // a vertex of this layout had more faces than slots
     uint64_t split_cap = 0;               // MCGPU_SPLIT_CAP: fixed split-entry capacity (0: by size)
     struct Graph {
         std::vector<unsigned char> key;
@@ -850,8 +852,9 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         W.vneed = c->buf[B_VNEED].get<uint8_t>(L.nv);
         W.voff = c->buf[B_VOFF].get<uint32_t>(L.nv + 1);
         W.vcur = c->buf[B_VCUR].get<uint32_t>(L.nv);
-        W.inc_cap = L.nidx;
-        W.vface = c->buf[B_VFACE].get<uint32_t>(L.nidx);
+        W.inc_slots = c->csr_incidence ? 0u : c->inc_slots;
+        W.inc_cap = W.inc_slots ? (uint64_t)L.nv * W.inc_slots : L.nidx;
+        W.vface = c->buf[B_VFACE].get<uint32_t>(std::max<uint64_t>(W.inc_cap, 1));
         W.test_cap = std::max<uint64_t>(1, 2ull * L.max_face * np);
         if (W.test_cap > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "edge-face tests exceed 2^32");
         W.tests = c->buf[B_TESTS].get<Test>(W.test_cap);
@@ -894,105 +897,118 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
             ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
                 "D2H ranges");
     };
-    // The stage-3 buffers of the previous call stay out of the segment keys.
-    W.plane_slot = W.proj_flag = W.proj_list = W.poly_list = W.voff = W.vcur = W.vface = W.rec_ids = nullptr;
-    W.planes = nullptr;
-    W.vneed = nullptr;
-    W.tri_scratch = nullptr;
-    W.tests = nullptr;
-    W.test_info = nullptr;
-    W.rec_key[0] = W.rec_key[1] = nullptr;
-    W.rec_val[0] = W.rec_val[1] = nullptr;
-    W.rec_pt_raw = W.rec_pts = nullptr;
-    W.tri_scratch_cap = W.tri_stride = W.test_cap = W.inc_cap = W.plane_cap = 0;
-    const std::vector<unsigned char> key0 = seg_key(P, W, n, key_bits, prof);
+    // the stage-3 buffers of the previous call stay out of the segment keys
+    auto clear_stage3 = [&]() {
+        W.plane_slot = W.proj_flag = W.proj_list = W.poly_list = W.voff = W.vcur = W.vface = W.rec_ids = nullptr;
+        W.planes = nullptr;
+        W.vneed = nullptr;
+        W.tri_scratch = nullptr;
+        W.tests = nullptr;
+        W.test_info = nullptr;
+        W.rec_key[0] = W.rec_key[1] = nullptr;
+        W.rec_val[0] = W.rec_val[1] = nullptr;
+        W.rec_pt_raw = W.rec_pts = nullptr;
+        W.tri_scratch_cap = W.tri_stride = W.test_cap = W.inc_cap = W.plane_cap = 0;
+        W.inc_slots = 0;
+    };
+    clear_stage3();
+    if (seg_key(P, W, n, key_bits, prof) != c->fuse_key) c->csr_incidence = false; // a new layout
     uint64_t npairs = 0;
-    bool done = false;
-    // Fused call: after a call of the same shape, the three segments run as
-    // one graph with one readback. Stage 3 is sized for the pair capacity (a
-    // plane slot for every face, tests for every pair the buffer holds), so
-    // nothing overflows whatever the pair count, and the records are ordered
-    // from the count left on the device. A pair overflow or a traversal stack
-    // overflow reruns the call stage by stage; a record count past the
-    // one-launch ordering reruns only the record segment.
-    if (c->use_graphs && c->use_fuse && !prof && c->fuse_ok && c->fuse_key == key0) {
-        rc = size_stage3(W.pair_cap, true);
-        if (rc != MCGPU_OK) return rc;
-        const uint32_t rec_cap = (uint32_t)std::min<uint64_t>(W.test_cap, kRankSortMax);
-        const bool dev_rec = c->fuse_nrec <= rec_cap;
-        if (dev_rec) {
-            W.rec_ids = c->buf[B_RIDS].get<uint32_t>((size_t)rec_cap * 5);
-            W.rec_pts = c->buf[B_RPTS].get<double>((size_t)rec_cap * 3);
-        }
-        run_segment(c, 3, seg_key(P, W, n, key_bits, keep, dev_rec, rec_cap), [&](int* aux) {
-            seg0(aux);
-            seg1();
-            aux[2] = dev_rec ? launch_records_dev(P, W, rec_cap, s) : 0;
-        });
-        src_buf = c->graphs[3].aux[0];
-        cut_buf = c->graphs[3].aux[1];
-        read_status(dev_rec && n > 1);
-        ck(cudaStreamSynchronize(s), "sync fused");
-        bool stack = false;
-        for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
-        if (!stack && hc[0] <= W.pair_cap) {
-            npairs = hc[0];
-            c->n_pairs_found = npairs;
-            c->n_tests = hc[1];
-            c->n_records = hc[2];
-            if (dev_rec && c->n_records <= rec_cap) {
-                c->rec_buf = c->graphs[3].aux[2];
-                if (n == 1) {
-                    hc[16 + 2] = 0;
-                    hc[16 + 3] = (uint32_t)c->n_records;
-                }
-            } else {
-                record_segment();
+    std::vector<unsigned char> key0;
+    // a vertex with more incident faces than the fixed incidence slots reruns
+    // the call with CSR incidence (kept for the layout's later calls)
+    for (;;) {
+        clear_stage3();
+        key0 = seg_key(P, W, n, key_bits, prof);
+        bool done = false;
+        // Fused call: after a call of the same shape, the three segments run as
+        // one graph with one readback. Stage 3 is sized for the pair capacity (a
+        // plane slot for every face, tests for every pair the buffer holds), so
+        // nothing overflows whatever the pair count, and the records are ordered
+        // from the count left on the device. A pair overflow or a traversal stack
+        // overflow reruns the call stage by stage; a record count past the
+        // one-launch ordering reruns only the record segment.
+        if (c->use_graphs && c->use_fuse && !prof && c->fuse_ok && c->fuse_key == key0) {
+            rc = size_stage3(W.pair_cap, true);
+            if (rc != MCGPU_OK) return rc;
+            const uint32_t rec_cap = (uint32_t)std::min<uint64_t>(W.test_cap, kRankSortMax);
+            const bool dev_rec = c->fuse_nrec <= rec_cap;
+            if (dev_rec) {
+                W.rec_ids = c->buf[B_RIDS].get<uint32_t>((size_t)rec_cap * 5);
+                W.rec_pts = c->buf[B_RPTS].get<double>((size_t)rec_cap * 3);
             }
-            done = true;
-        }
-    }
-    if (!done) {
-        run_segment(c, 0, key0, seg0);
-        src_buf = c->graphs[0].aux[0];
-        cut_buf = c->graphs[0].aux[1];
-
-        // readback 1: pair count and traversal flags
-        ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
-        ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
-        ck(cudaStreamSynchronize(s), "sync traverse");
-        bool deep = false;
-        for (int attempt = 0; attempt < 4; ++attempt) {
+            run_segment(c, 3, seg_key(P, W, n, key_bits, keep, dev_rec, rec_cap), [&](int* aux) {
+                seg0(aux);
+                seg1();
+                aux[2] = dev_rec ? launch_records_dev(P, W, rec_cap, s) : 0;
+            });
+            src_buf = c->graphs[3].aux[0];
+            cut_buf = c->graphs[3].aux[1];
+            read_status(dev_rec && n > 1);
+            ck(cudaStreamSynchronize(s), "sync fused");
             bool stack = false;
             for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
-            const uint64_t np = hc[0];
-            if (!stack && np <= W.pair_cap) break;
-            if (np > W.pair_cap) {
-                W.pair_cap = np + np / 8 + 1024;
-                W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
+            if (!stack && hc[0] <= W.pair_cap) {
+                npairs = hc[0];
+                c->n_pairs_found = npairs;
+                c->n_tests = hc[1];
+                c->n_records = hc[2];
+                if (dev_rec && c->n_records <= rec_cap) {
+                    c->rec_buf = c->graphs[3].aux[2];
+                    if (n == 1) {
+                        hc[16 + 2] = 0;
+                        hc[16 + 3] = (uint32_t)c->n_records;
+                    }
+                } else {
+                    record_segment();
+                }
+                done = true;
             }
-            deep = deep || stack;
-            ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
-            ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
-            ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
-            launch_packets(P, W, src_buf, s);
-            launch_traverse(P, W, src_buf, cut_buf, deep, s);
+        }
+        if (!done) {
+            run_segment(c, 0, key0, seg0);
+            src_buf = c->graphs[0].aux[0];
+            cut_buf = c->graphs[0].aux[1];
+
+            // readback 1: pair count and traversal flags
             ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
             ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
             ck(cudaStreamSynchronize(s), "sync traverse");
-        }
-        npairs = hc[0];
-        c->n_pairs_found = npairs;
-        rc = size_stage3(npairs, false);
-        if (rc != MCGPU_OK) return rc;
-        run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) { seg1(); });
+            bool deep = false;
+            for (int attempt = 0; attempt < 4; ++attempt) {
+                bool stack = false;
+                for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
+                const uint64_t np = hc[0];
+                if (!stack && np <= W.pair_cap) break;
+                if (np > W.pair_cap) {
+                    W.pair_cap = np + np / 8 + 1024;
+                    W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
+                }
+                deep = deep || stack;
+                ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
+                ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
+                ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+                launch_packets(P, W, src_buf, s);
+                launch_traverse(P, W, src_buf, cut_buf, deep, s);
+                ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");
+                ck(cudaMemcpyAsync(hc + 16, W.pair_status, 4 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H status");
+                ck(cudaStreamSynchronize(s), "sync traverse");
+            }
+            npairs = hc[0];
+            c->n_pairs_found = npairs;
+            rc = size_stage3(npairs, false);
+            if (rc != MCGPU_OK) return rc;
+            run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) { seg1(); });
 
-        // readback 2: counters, per-pair status / degenerate face / record count
-        read_status(false);
-        ck(cudaStreamSynchronize(s), "sync narrow");
-        c->n_tests = hc[1];
-        c->n_records = hc[2];
-        record_segment();
+            // readback 2: counters, per-pair status / degenerate face / record count
+            read_status(false);
+            ck(cudaStreamSynchronize(s), "sync narrow");
+            c->n_tests = hc[1];
+            c->n_records = hc[2];
+            record_segment();
+        }
+        if (hc[12] == 0 || W.inc_slots == 0) break;
+        c->csr_incidence = true;
     }
     c->fuse_key = key0;
     c->fuse_ok = true;
@@ -1088,6 +1104,7 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         int pma = 0;
         if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess) c->host_reads = pma != 0;
         if (const char* e = getenv("MCGPU_HOST_READS")) c->host_reads = c->host_reads && atoi(e) != 0;
+        if (const char* e = getenv("MCGPU_INC_SLOTS")) c->inc_slots = (uint32_t)std::min(64, std::max(0, atoi(e)));
         if (const char* e = getenv("MCGPU_SPLIT_CAP")) c->split_cap = strtoull(e, nullptr, 10);
         ck(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "stream");
         ck(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "stream");

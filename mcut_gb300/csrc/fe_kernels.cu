@@ -1274,6 +1274,25 @@ __global__ void __launch_bounds__(kBlock) k_vf_count(Problem P, const uint8_t* _
     }
 }
 
+// Fixed-width incidence: up to K faces per needed vertex in vslot[v K ..]
+// with its count in vdeg[v], in one pass (no count, scan and fill). A vertex
+// with more than K incident faces sets counters[12]; the host then reruns
+// the call with the CSR lists.
+__global__ void __launch_bounds__(kBlock) k_vf_slots(Problem P, const uint8_t* __restrict__ vneed,
+    uint32_t* __restrict__ vdeg, uint32_t* __restrict__ vslot, uint32_t K, uint32_t* __restrict__ counters)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t v = P.fidx[o + k];
+            if (!vneed[v]) continue;
+            const uint32_t j = atomicAdd(&vdeg[v], 1u);
+            if (j < K) vslot[(size_t)v * K + j] = f;
+            else counters[12] = 1u;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_vf_fill(Problem P, const uint8_t* __restrict__ vneed,
     const uint32_t* __restrict__ voff, uint32_t* __restrict__ vcur, uint32_t* __restrict__ vface, uint64_t cap)
 {
@@ -1568,11 +1587,19 @@ __global__ void k_triplets(Problem P, const uint32_t* __restrict__ poly_list, co
 // cull as kernel.cpp:2074-2177 does.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t other_face(const Problem& P, const uint32_t* __restrict__ voff,
-    const uint32_t* __restrict__ vface, uint32_t F, uint32_t a, uint32_t b, uint32_t& slot_out)
+    const uint32_t* __restrict__ vface, uint32_t K, uint32_t F, uint32_t a, uint32_t b, uint32_t& slot_out)
 {
-    // faces incident to a that hold the halfedge b -> a
-    const uint32_t lo = voff[a], hi = voff[a + 1];
-    for (uint32_t i = lo; i < hi; ++i) {
+    // faces incident to a that hold the halfedge b -> a: CSR lists (K == 0),
+    // or K slots per vertex with voff[a] the count
+    uint64_t lo, hi;
+    if (K) {
+        lo = (uint64_t)a * K;
+        hi = lo + min(voff[a], K);
+    } else {
+        lo = voff[a];
+        hi = voff[a + 1];
+    }
+    for (uint64_t i = lo; i < hi; ++i) {
         const uint32_t G = vface[i];
         if (G == F) continue;
         const uint32_t o = face_o(P, G), n = face_n(P, G);
@@ -1587,8 +1614,9 @@ __device__ __forceinline__ uint32_t other_face(const Problem& P, const uint32_t*
 
 __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* __restrict__ fbox,
     const unsigned long long* __restrict__ pairs, const uint32_t* __restrict__ counters_ro, uint64_t pair_cap,
-    const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vface, Test* __restrict__ tests, uint64_t test_cap,
-    uint32_t* __restrict__ counters, const int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_status)
+    const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vface, uint32_t inc_slots, Test* __restrict__ tests,
+    uint64_t test_cap, uint32_t* __restrict__ counters, const int32_t* __restrict__ pair_bad,
+    uint32_t* __restrict__ pair_status)
 {
     __shared__ uint32_t s_nmax;
     const uint64_t np = min((uint64_t)counters_ro[0], pair_cap);
@@ -1630,7 +1658,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
                 if (emit) {
                     a = P.fidx[o + k];
                     b = P.fidx[o + (k + 1 == n ? 0 : k + 1)];
-                    G = other_face(P, voff, vface, F, a, b, oslot);
+                    G = other_face(P, voff, vface, inc_slots, F, a, b, oslot);
                     if (G != kNone && G < F && box_overlap(load_box(fbox, G), gb)) emit = false;
                 }
                 if (emit) {
@@ -2144,6 +2172,11 @@ void launch_incidence(const Problem& P, Work& W, cudaStream_t s)
     g_launches++;
     k_mark_vertices<<<g, kBlock, 0, s>>>(P, W.cand, W.vneed);
     cudaMemsetAsync(W.voff, 0, sizeof(uint32_t) * ((size_t)P.nv + 1), s);
+    if (W.inc_slots) {
+        g_launches++;
+        k_vf_slots<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff, W.vface, W.inc_slots, W.counters);
+        return;
+    }
     g_launches++;
     k_vf_count<<<g, kBlock, 0, s>>>(P, W.vneed, W.voff);
     exclusive_scan(W.voff, P.nv + 1, nullptr, W.scan_temp, s);
@@ -2162,8 +2195,8 @@ void launch_tests(const Problem& P, Work& W, cudaStream_t s)
 {
     const int g = grid_for(W.pair_cap);
     g_launches++;
-    k_pair_tests<<<g, kBlock, 0, s>>>(P, W.fbox, W.pairs, W.counters, W.pair_cap, W.voff, W.vface, W.tests,
-        W.test_cap, W.counters, W.pair_bad, W.pair_status);
+    k_pair_tests<<<g, kBlock, 0, s>>>(P, W.fbox, W.pairs, W.counters, W.pair_cap, W.voff, W.vface, W.inc_slots,
+        W.tests, W.test_cap, W.counters, W.pair_bad, W.pair_status);
 }
 
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)

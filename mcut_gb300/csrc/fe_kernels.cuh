@@ -90,8 +90,8 @@ struct Work {
     unsigned long long* pairs;        // [pair_cap]
     uint32_t* counters;               // [16]: 0 pairs, 1 tests, 2 records, 3 cand faces, 4 poly faces,
                                       //        5..7 escalations, 8 traversal work cursor, 9 packets, 10 narrow hits,
-                                      //        11 queued projections, 13 top-cut entries, 14 split entries,
-//        15 second-launch work cursor
+                                      //        11 queued projections, 12 incidence slot overflow,
+                                      //        13 top-cut entries, 14 split entries, 15 second-launch work cursor
     uint2* packets;                   // [ns] query packets: sorted source positions [x, y]
     uint8_t* cand;                    // [nf]
     uint32_t* plane_slot;             // [nf]
@@ -118,6 +118,7 @@ struct Work {
     uint64_t tri_scratch_cap;         // entries
     uint64_t tri_stride;              // entries per polygon (largest C(n,3)); 0: no polygons
     uint64_t pair_cap, test_cap, inc_cap, plane_cap;
+    uint32_t inc_slots;               // 0: CSR incidence (voff offsets, vface lists); K: K slots per vertex, voff counts
     // tuning (results do not depend on it)
     uint32_t traversal;               // 0 warp/packet breadth-first, 1 warp/packet depth-first, 2 thread/face
     uint32_t packet_faces;            // source faces per query packet (1..32)

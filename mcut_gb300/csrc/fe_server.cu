@@ -69,10 +69,11 @@ uint64_t mesh_indices(const mcgpu_mesh& m)
 }
 
 // Device bytes one request adds to a batch: the dispatch's per-face and
-// per-vertex buffers (face boxes f64 + f32, keys, values, tree, incidence,
-// pairs, tests and records at their usual sizes, and a plane slot for every
-// face, 104 B, as a repeated dispatch shape sizes them) plus slack.
-uint64_t estimate_bytes(uint64_t faces, uint64_t verts) { return (1ull << 20) + faces * 744 + verts * 64; }
+// per-vertex buffers (face boxes f64 + f32, keys, values, tree, pairs, tests
+// and records at their usual sizes, a plane slot for every face, 104 B, as a
+// repeated dispatch shape sizes them, and 16 incidence slots per vertex,
+// 64 B) plus slack.
+uint64_t estimate_bytes(uint64_t faces, uint64_t verts) { return (1ull << 20) + faces * 744 + verts * 128; }
 
 } // namespace
 

@@ -181,3 +181,41 @@ def test_face_boxes_and_vertices_match_oracle(ctx, name):
     assert G.same_bits(ctx.face_boxes(), want["face_boxes"].reshape(-1, 6))
     v = ctx.vertices()
     assert G.same_bits(v, np.concatenate([want["src_xyz"].reshape(-1, 3), want["cut_xyz"].reshape(-1, 3)]))
+
+
+def _cone(k, apex_z=0.6, base_z=-0.6, r=1.0):
+    """Closed cone: k triangles around the apex and k around the base centre,
+    both vertices of valence k."""
+    ang = np.linspace(0.0, 2.0 * np.pi, k, endpoint=False) + 0.1234
+    ring = np.stack([r * np.cos(ang), r * np.sin(ang), np.full(k, base_z)], 1)
+    v = np.concatenate([ring, [[0.0, 0.0, apex_z], [0.0, 0.0, base_z]]])
+    f = []
+    for i in range(k):
+        j = (i + 1) % k
+        f += [i, j, k, j, i, k + 1]
+    return dict(v=np.ascontiguousarray(v), f=np.asarray(f, np.uint32), fs=None)
+
+
+@pytest.mark.parametrize("k", [40, 200])
+def test_high_valence_vertex_against_oracle(ctx, k):
+    """The apex has more incident faces than the fixed incidence slots (16):
+    the call reruns with CSR incidence, the next (fused) call keeps it, and a
+    context that always uses CSR lists agrees."""
+    import os
+    from mcut_gb300 import Context
+    s = _cone(k)
+    c = meshgen.grid(24, 1.5, lambda X, Y: 0.05 + 0.03 * X + 0.02 * Y)
+    want = oracle.front_end(s, c, impl="port", threads=4)
+    assert int(want["status"]) == 0 and len(want["rec_ids"]) > 0
+    for _ in range(2):
+        r = ctx.dispatch(s, c, keep_tests=True, keep_pairs=True)
+        check_against(r, want, meshgen.num_faces(s))
+    os.environ["MCGPU_INC_SLOTS"] = "0"
+    try:
+        csr = Context(0)
+    finally:
+        del os.environ["MCGPU_INC_SLOTS"]
+    try:
+        check_against(csr.dispatch(s, c, keep_tests=True, keep_pairs=True), want, meshgen.num_faces(s))
+    finally:
+        csr.close()

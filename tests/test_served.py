@@ -102,9 +102,9 @@ def test_served_admission_budget(alone):
     st = srv.stats()
     srv.close()
     assert st["completed"] == len(reqs)
-    # the server's estimate: 1 MiB + 744 B per face + 64 B per vertex
+    # the server's estimate: 1 MiB + 744 B per face + 128 B per vertex
     biggest = max((1 << 20) + 744 * (meshgen.num_faces(s) + meshgen.num_faces(c))
-                  + 64 * (s["v"].shape[0] + c["v"].shape[0]) for s, c in reqs)
+                  + 128 * (s["v"].shape[0] + c["v"].shape[0]) for s, c in reqs)
     assert st["peak_inflight_bytes"] <= max(budget, biggest)
 
 
