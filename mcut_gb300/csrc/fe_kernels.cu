@@ -1797,10 +1797,15 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
 // The triangles that pass 1 queued (a segment meets their plane): unit
 // normal, d, largest component and projection matrix, once per face
 // (polygons got theirs with the plane).
-// Narrow-phase kernels over short lists (hit triangles, hits) run long fp64
-// chains per item: launched in blocks of kSpread threads so that a list of a
-// few thousand items still occupies every SM.
+// Narrow-phase kernels over short lists run long fp64 chains per item: the
+// hit triangles' plane finishing is launched in blocks of kSpread threads so
+// that a list of a few thousand items still occupies every SM (the hit list
+// itself does best in blocks of 256, measured).
 constexpr int kSpread = 64;
+#ifndef MCGPU_NH_BLOCK
+#define MCGPU_NH_BLOCK 256
+#endif
+constexpr int kNarrowHitsBlock = MCGPU_NH_BLOCK;
 __global__ void __launch_bounds__(kSpread) k_finish_planes(Problem P, FacePlane* __restrict__ planes,
     const uint32_t* __restrict__ plane_slot, const uint32_t* __restrict__ proj_list,
     const uint32_t* __restrict__ counters)
@@ -1825,7 +1830,7 @@ __global__ void __launch_bounds__(kSpread) k_finish_planes(Problem P, FacePlane*
 #ifndef MCGPU_NH_MINB
 #define MCGPU_NH_MINB 1
 #endif
-__global__ void __launch_bounds__(kSpread, MCGPU_NH_MINB) k_narrow_hits(Problem P, const Test* __restrict__ tests,
+__global__ void __launch_bounds__(kNarrowHitsBlock, MCGPU_NH_MINB) k_narrow_hits(Problem P, const Test* __restrict__ tests,
     const uint2* __restrict__ hits, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info,
     unsigned long long* __restrict__ rec_key, uint32_t* __restrict__ rec_val, double* __restrict__ rec_pt,
@@ -2209,9 +2214,9 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
         keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
     k_finish_planes<<<grid_spread(W.plane_cap), kSpread, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot,
         W.proj_list, W.counters);
-    k_narrow_hits<<<grid_spread(W.test_cap), kSpread, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot,
-        (const FacePlane*)W.planes,
-        keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
+    const int gh = std::max(1, grid_spread(W.test_cap) * kSpread / kNarrowHitsBlock);
+    k_narrow_hits<<<gh, kNarrowHitsBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot,
+        (const FacePlane*)W.planes, keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
         W.pair_bad);
 }
 
