@@ -64,13 +64,25 @@ typedef enum mcgpu_status {
 #define MCGPU_VERTEX_ARRAY_FLOAT (1u << 0) /* vertices are float[3*V] (MC_DISPATCH_VERTEX_ARRAY_FLOAT) */
 #define MCGPU_RECENTRE (1u << 1)           /* vertices are user coordinates: apply preproc's
                                               recentring (preproc.cpp:2124-2290, 147-181) and
-                                              derive cut_eps = |cut box diagonal| * 1e-4 */
+                                              derive cut_eps = |cut box diagonal| * the context's
+                                              general-position constant (default 1e-4) */
 #define MCGPU_KEEP_TESTS (1u << 2)         /* keep every culled edge-face test and its predicates */
 #define MCGPU_KEEP_PAIRS (1u << 3)         /* keep the candidate face pairs */
 #define MCGPU_PROFILE (1u << 4)            /* time the stages with CUDA events */
 #define MCGPU_DEVICE_POINTERS (1u << 5)    /* mesh arrays are device pointers (recentred, double); a
                                               single pair's and a packed batch's coordinates are read
                                               in place, so keep them alive while results are read */
+#define MCGPU_ENFORCE_GENERAL_POSITION (1u << 6)
+/* mcgpu_dispatch only: on a general-position violation, perturb the cut mesh
+   by uniform(-1, 1) * cut_eps per axis (the reference's mt19937 sequence, one
+   per context) and run the narrow phase again against the unperturbed pairs
+   and face boxes, up to the context's attempts; still violated after the
+   last attempt, the status stays MCGPU_GP_VIOLATION (the reference throws
+   "max perturbation iterations reached"). MC_DISPATCH_ENFORCE_GENERAL_POSITION,
+   preproc.cpp:2590-2699, 2933-2945. */
+#define MCGPU_ENFORCE_GENERAL_POSITION_ABSOLUTE (1u << 7)
+/* the same, with MCGPU_RECENTRE's cut_eps = the context's constant alone
+   instead of constant * |cut box diagonal| (MC_DISPATCH_ENFORCE_GENERAL_POSITION_ABSOLUTE) */
 
 typedef struct mcgpu_mesh {
     const void* vertices;         /* double[3*num_vertices], float with MCGPU_VERTEX_ARRAY_FLOAT */
@@ -103,7 +115,9 @@ typedef struct mcgpu_summary {
     float stage_ms[8];        /* per-stage device time of the call (MCGPU_PROFILE; a batch's
                                  summaries all carry the batch's times) */
     uint32_t kernel_launches; /* CUDA kernels this call launched (whole batch) */
-    uint32_t reserved;
+    uint32_t perturbations;   /* general-position enforcement: cut-mesh perturbations applied */
+    double perturbation[3];   /* the last perturbation applied (recentred units), else 0
+                                 (MC_CONNECTED_COMPONENT_DATA_DISPATCH_PERTURBATION_VECTOR) */
 } mcgpu_summary;
 
 /* mcgpu_get_data queries */
@@ -194,6 +208,14 @@ typedef struct mcgpu_tuning {
 
 int mcgpu_context_set_tuning(mcgpu_context ctx, const mcgpu_tuning* tuning);
 int mcgpu_context_get_tuning(mcgpu_context ctx, mcgpu_tuning* tuning);
+
+/* General-position enforcement of a context: the constant (> 0) scales
+ * MCGPU_RECENTRE's cut_eps and the perturbations, attempts (>= 1) bounds the
+ * perturbations of one dispatch; defaults 1e-4 and 4 (frontend.h:596-597).
+ * Replaces mcBindState / mcGetInfo with MC_CONTEXT_GENERAL_POSITION_
+ * ENFORCEMENT_CONSTANT / _ATTEMPTS (frontend.cpp:390-410, 335-350). */
+int mcgpu_context_set_general_position(mcgpu_context ctx, double constant, uint32_t attempts);
+int mcgpu_context_get_general_position(mcgpu_context ctx, double* constant, uint32_t* attempts);
 
 /* Autotuner: runs `sample` (a packed batch, as mcgpu_dispatch_packed with
  * `flags`) under each candidate tuning -- leaf size {2, 4, 8} x {warp per

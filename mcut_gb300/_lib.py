@@ -25,6 +25,8 @@ KEEP_TESTS = 1 << 2
 KEEP_PAIRS = 1 << 3
 PROFILE = 1 << 4
 DEVICE_POINTERS = 1 << 5
+ENFORCE_GENERAL_POSITION = 1 << 6
+ENFORCE_GENERAL_POSITION_ABSOLUTE = 1 << 7
 
 DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DATA_VERTICES, DATA_FACE_BOXES, \
     DATA_RECORD_OFFSETS = range(1, 9)
@@ -46,7 +48,8 @@ class Summary(C.Structure):
     _fields_ = [("status", C.c_int32), ("bad_face", C.c_int32), ("cut_eps", C.c_double),
                 ("num_pairs", C.c_uint64), ("num_tests", C.c_uint64), ("num_records", C.c_uint64),
                 ("escalations", C.c_uint64 * 3), ("stage_ms", C.c_float * 8),
-                ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
+                ("kernel_launches", C.c_uint32), ("perturbations", C.c_uint32),
+                ("perturbation", C.c_double * 3)]
 
 
 class Tuning(C.Structure):
@@ -102,6 +105,8 @@ def load():
                                            C.c_void_p, C.c_uint64, C.POINTER(Summary)]
     lib.mcgpu_context_set_tuning.argtypes = [ctx, C.POINTER(Tuning)]
     lib.mcgpu_context_get_tuning.argtypes = [ctx, C.POINTER(Tuning)]
+    lib.mcgpu_context_set_general_position.argtypes = [ctx, C.c_double, C.c_uint32]
+    lib.mcgpu_context_get_general_position.argtypes = [ctx, C.POINTER(C.c_double), C.POINTER(C.c_uint32)]
     lib.mcgpu_autotune.argtypes = [ctx, C.c_uint32, C.POINTER(Batch), C.c_uint32, C.POINTER(Tuning),
                                    C.POINTER(C.c_float)]
     srv = C.c_void_p

@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <random>
 #include <atomic>
 #include <chrono>
 #include <string>
@@ -93,7 +94,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -131,6 +132,13 @@ struct mcgpu_context_t {
     bool use_fuse = true;                 // MCGPU_FUSE=0: every call stage by stage
     bool host_reads = false;              // the device reads pageable host memory (MCGPU_HOST_READS=0: never)
     uint32_t inc_slots = 16;              // vertex -> face slots per vertex (MCGPU_INC_SLOTS; 0: CSR lists)
+    // general-position enforcement (frontend.h:596-597) and the perturbation
+    // sequence: the reference's thread_local engines of the context's API
+    // thread (preproc.cpp:2621-2627), one sequence per context
+    double gp_constant = 1e-4;
+    uint32_t gp_attempts = 4;
+    std::mt19937 gp_rng { std::default_random_engine(1)() };
+    std::uniform_real_distribution<double> gp_uniform { -1.0, 1.0 };
     bool csr_incidence = false;           // a vertex of this layout had more faces than slots
     uint64_t split_cap = 0;               // MCGPU_SPLIT_CAP: fixed split-entry capacity (0: by size)
     struct Graph {
@@ -235,19 +243,19 @@ void apply_frame(bool fin, const mcgpu_mesh& m, const double* com, const double*
     }
 }
 
-// |translated cut box diagonal| * 1e-4 (preproc.cpp:2518, 2667-2676)
-double frame_eps(const MeshStats& Cm, const double* t)
+double frame_eps(const MeshStats& Cm, const double* t, double constant, bool absolute)
 {
     double d[3];
     for (int j = 0; j < 3; ++j) d[j] = (Cm.mx[j] + t[j]) - (Cm.mn[j] + t[j]);
-    return std::sqrt(hdot(d, d)) * 1e-4;
+    return (absolute ? 1.0 : std::sqrt(hdot(d, d))) * constant;
 }
 
 } // namespace mcgpu
 
 namespace {
 
-void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out)
+void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out,
+    double gp_constant = 1e-4, bool gp_absolute = false)
 {
     MeshStats ss, cs;
     mesh_stats(S.vertices, fin, S.num_vertices, ss);
@@ -256,7 +264,7 @@ void recentre_pair(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* 
     pair_frame(ss, cs, com, t);
     apply_frame(fin, S, com, t, sx);
     apply_frame(fin, Cm, com, t, cx);
-    *eps_out = frame_eps(cs, t);
+    *eps_out = frame_eps(cs, t, gp_constant, gp_absolute);
 }
 
 // memcpy on several host threads (large staging copies)
@@ -279,7 +287,7 @@ void memcpy_mt(void* dst, const void* src, size_t bytes, unsigned threads)
 // stats run side by side (each centroid is still summed in vertex order, as
 // the reference sums it), then the coordinate maps run in chunks
 void recentre_pair_mt(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, double* sx, double* cx, double* eps_out,
-    unsigned threads)
+    unsigned threads, double gp_constant, bool gp_absolute)
 {
     MeshStats ss, cs;
     std::thread tc([&] { mesh_stats(Cm.vertices, fin, Cm.num_vertices, cs); });
@@ -309,7 +317,7 @@ void recentre_pair_mt(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, doubl
         });
     }
     for (auto& th : ts) th.join();
-    *eps_out = frame_eps(cs, t);
+    *eps_out = frame_eps(cs, t, gp_constant, gp_absolute);
 }
 
 // Host arrays read in place by the device (it walks the host's page tables:
@@ -332,6 +340,18 @@ __global__ void __launch_bounds__(256) k_host_copy(HostSegs g)
             uint32_t* b = static_cast<uint32_t*>(h.dst);
             for (uint64_t i = t0; i < h.bytes / 4; i += st) b[i] = a[i];
         }
+    }
+}
+
+// the cut vertices of one general-position enforcement attempt: the
+// recentred coordinate plus the perturbation, one rounding
+// (preproc.cpp:131-133, 176-180)
+__global__ void k_perturb(const double* __restrict__ in, double* __restrict__ out, uint64_t n3, double p0, double p1,
+    double p2)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n3; k += (uint64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(k % 3);
+        out[k] = in[k] + (j == 0 ? p0 : (j == 1 ? p1 : p2));
     }
 }
 
@@ -511,6 +531,7 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     cudaStream_t s = c->s;
     const bool fin = (flags & MCGPU_VERTEX_ARRAY_FLOAT) != 0;
     const bool dev = (flags & MCGPU_DEVICE_POINTERS) != 0;
+    const bool gp_absolute = (flags & MCGPU_ENFORCE_GENERAL_POSITION_ABSOLUTE) != 0;
     // device inputs are read in place (a packed batch as one array, a single
     // pair as its two arrays); everything else is copied
     const bool split = dev && !pk && n == 1;
@@ -554,12 +575,14 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
                 mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
                 pair_frame(ss, res[p]->st, j.com, j.t);
                 apply_frame(fin, srcs[p], j.com, j.t, sx);
-                L.eps[p] = frame_eps(res[p]->st, j.t);
+                L.eps[p] = frame_eps(res[p]->st, j.t, c->gp_constant, gp_absolute);
             } else if (n == 1 && L.nv > 200000) {
                 const unsigned hw = std::max(2u, std::min(16u, std::thread::hardware_concurrency()));
-                recentre_pair_mt(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p], hw);
+                recentre_pair_mt(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p], hw,
+                    c->gp_constant, gp_absolute);
             } else {
-                recentre_pair(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p]);
+                recentre_pair(fin, srcs[p], cuts[p], sx, st + ((size_t)L.vbase[p] + L.vs[p]) * 3, &L.eps[p],
+                    c->gp_constant, gp_absolute);
             }
             if (ist) {
                 const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
@@ -734,6 +757,9 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     if (flags & MCGPU_DEVICE_POINTERS && flags & (MCGPU_RECENTRE | MCGPU_VERTEX_ARRAY_FLOAT))
         return fail(MCGPU_INVALID_VALUE, "device pointers must hold recentred double coordinates");
     if (!(flags & MCGPU_RECENTRE) && !eps) return fail(MCGPU_INVALID_VALUE, "cut_eps required without RECENTRE");
+    const bool enforce = (flags & (MCGPU_ENFORCE_GENERAL_POSITION | MCGPU_ENFORCE_GENERAL_POSITION_ABSOLUTE)) != 0;
+    if (enforce && (n != 1 || pk || res))
+        return fail(MCGPU_INVALID_VALUE, "general-position enforcement is per pair (mcgpu_dispatch)");
     if ((flags & MCGPU_VERTEX_ARRAY_FLOAT) && !(flags & MCGPU_RECENTRE))
         return fail(MCGPU_INVALID_VALUE, "float vertices need MCGPU_RECENTRE");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
@@ -1013,6 +1039,47 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->fuse_key = key0;
     c->fuse_ok = true;
     c->fuse_nrec = c->n_records;
+
+    // General-position enforcement (preproc.cpp:2590-2699, 2933-2945): each
+    // attempt perturbs the narrow phase's cut vertices by uniform(-1, 1) *
+    // cut_eps per axis and runs stage 3 and the record order again. The pairs,
+    // face boxes and cut tree of the unperturbed meshes stay: the reference
+    // builds the cut BVH only on the first attempt (preproc.cpp:2680) and
+    // traverses only after a rebuild (preproc.cpp:2820-2846); the boxes are
+    // enlarged by cut_eps, so they still hold the perturbed faces.
+    uint32_t perturbations = 0;
+    double pert[3] = { 0.0, 0.0, 0.0 };
+    auto violated = [&]() {
+        if ((hc[16] & ST_INVALID) || (int32_t)hc[17] != kNoBad) return false;
+        // a perturbed pass that meets nothing is a violation (kernel.cpp:3211-3225)
+        return (hc[16] & ST_GP) != 0 || (perturbations > 0 && c->n_records == 0);
+    };
+    if (enforce && violated()) {
+        const uint64_t nc3 = 3ull * (L.nv - L.vs[0]);
+        const double* base = P.xsplit != 0xFFFFFFFFu ? P.Xc : P.X + (size_t)L.vs[0] * 3;
+        double* xp = c->buf[B_XPERT].get<double>(std::max<uint64_t>(nc3, 3));
+        P.Xc = xp; // the cut vertices the narrow phase reads from now on
+        P.xsplit = L.vs[0];
+        while (violated() && perturbations < c->gp_attempts) {
+            for (int j = 0; j < 3; ++j) pert[j] = c->gp_uniform(c->gp_rng) * L.eps[0];
+            ++perturbations;
+            g_launches++;
+            k_perturb<<<grid1(nc3), 256, 0, s>>>(base, xp, nc3, pert[0], pert[1], pert[2]);
+            // stage 3 starts again from its own counters (the pair count and the
+            // traversal's stay), statuses and record ranges
+            ck(cudaMemsetAsync(W.counters + 1, 0, 7 * sizeof(uint32_t), s), "memset");
+            ck(cudaMemsetAsync(W.counters + 10, 0, 3 * sizeof(uint32_t), s), "memset");
+            ck(cudaMemsetAsync(W.pair_status, 0, 4, s), "memset");
+            ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4, s), "memset");
+            ck(cudaMemsetAsync(W.pair_nrec, 0, 8, s), "memset");
+            run_segment(c, 1, seg_key(P, W, n, keep, prof), [&](int*) { seg1(); });
+            read_status(false);
+            ck(cudaStreamSynchronize(s), "sync narrow");
+            c->n_tests = hc[1];
+            c->n_records = hc[2];
+            record_segment();
+        }
+    }
     ck(cudaGetLastError(), "kernel launch");
 
     c->sums.assign(n, mcgpu_summary());
@@ -1032,6 +1099,12 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         m.cut_eps = L.eps[p];
         m.num_records = c->n_records ? hc[16 + 2 * n + p + 1] - hc[16 + 2 * n + p] : 0;
         c->rec_begin[p + 1] = c->rec_begin[p] + m.num_records;
+    }
+    if (perturbations) {
+        mcgpu_summary& m = c->sums[0];
+        if (m.status == MCGPU_OK && c->n_records == 0) m.status = MCGPU_GP_VIOLATION;
+        m.perturbations = perturbations;
+        memcpy(m.perturbation, pert, sizeof pert);
     }
     if (n == 1) {
         c->sums[0].num_pairs = npairs;
@@ -1225,6 +1298,25 @@ int mcgpu_context_get_tuning(mcgpu_context c, mcgpu_tuning* t)
 {
     if (!c || !t) return fail(MCGPU_INVALID_VALUE, "null argument");
     *t = c->tune;
+    return MCGPU_OK;
+}
+
+int mcgpu_context_set_general_position(mcgpu_context c, double constant, uint32_t attempts)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null argument");
+    // the reference rejects a constant <= 0 and fewer than one attempt (frontend.cpp:390-410)
+    if (!(constant > 0.0) || !std::isfinite(constant)) return fail(MCGPU_INVALID_VALUE, "invalid general position constant");
+    if (attempts < 1) return fail(MCGPU_INVALID_VALUE, "invalid general position enforcement attempts");
+    c->gp_constant = constant;
+    c->gp_attempts = attempts;
+    return MCGPU_OK;
+}
+
+int mcgpu_context_get_general_position(mcgpu_context c, double* constant, uint32_t* attempts)
+{
+    if (!c || !constant || !attempts) return fail(MCGPU_INVALID_VALUE, "null argument");
+    *constant = c->gp_constant;
+    *attempts = c->gp_attempts;
     return MCGPU_OK;
 }
 

@@ -18,7 +18,9 @@ struct MeshStats {
 void mesh_stats(const void* v, bool fin, uint32_t n, MeshStats& st);
 void pair_frame(const MeshStats& S, const MeshStats& Cm, double* com, double* t);
 void apply_frame(bool fin, const mcgpu_mesh& m, const double* com, const double* t, double* out);
-double frame_eps(const MeshStats& Cm, const double* t);
+// cut_eps: |translated cut box diagonal|, or 1 (absolute), times the
+// general-position constant (preproc.cpp:2518, 2664-2676)
+double frame_eps(const MeshStats& Cm, const double* t, double constant = 1e-4, bool absolute = false);
 
 // A cut mesh kept on the device: double user coordinates and triangle
 // indices, with its host-side stats (so a pair's frame needs only the source).

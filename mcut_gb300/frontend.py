@@ -40,6 +40,8 @@ class FrontEndResult:
     escalations: tuple
     stage_ms: dict
     kernel_launches: int
+    perturbations: int = 0                           # general-position enforcement attempts applied
+    perturbation: tuple = (0.0, 0.0, 0.0)            # the last perturbation (recentred units)
     record_ids: np.ndarray = field(default=None)     # [R,5] q, r, face, f0, f1
     record_points: np.ndarray = field(default=None)  # [R,3]
     pairs: np.ndarray = field(default=None)          # [P,2]
@@ -77,10 +79,17 @@ class Context:
 
     def dispatch(self, src, cut, cut_eps: float | None = None, recentre: bool = True, float_input: bool = False,
                  keep_tests: bool = False, keep_pairs: bool = False, profile: bool = False,
-                 fetch: bool = True) -> FrontEndResult:
+                 fetch: bool = True, enforce_general_position: bool | str = False) -> FrontEndResult:
+        """One front-end dispatch. enforce_general_position: True perturbs the
+        cut mesh on a general-position violation (MC_DISPATCH_ENFORCE_GENERAL_
+        POSITION), "absolute" with the context's constant as the absolute scale."""
         flags = (L.RECENTRE if recentre else 0) | (L.VERTEX_ARRAY_FLOAT if float_input else 0) \
             | (L.KEEP_TESTS if keep_tests else 0) | (L.KEEP_PAIRS if keep_pairs else 0) \
             | (L.PROFILE if profile else 0)
+        if enforce_general_position == "absolute":
+            flags |= L.ENFORCE_GENERAL_POSITION_ABSOLUTE
+        elif enforce_general_position:
+            flags |= L.ENFORCE_GENERAL_POSITION
         ms, ks = _as_mesh(src, float_input)
         mc, kc = _as_mesh(cut, float_input)
         sm = L.Summary()
@@ -92,7 +101,8 @@ class Context:
             status=sm.status, status_name=L.STATUS_NAMES[sm.status], bad_face=sm.bad_face, cut_eps=sm.cut_eps,
             num_pairs=sm.num_pairs, num_tests=sm.num_tests, num_records=sm.num_records,
             escalations=tuple(sm.escalations), stage_ms=dict(zip(L.STAGES, list(sm.stage_ms))),
-            kernel_launches=sm.kernel_launches)
+            kernel_launches=sm.kernel_launches, perturbations=sm.perturbations,
+            perturbation=tuple(sm.perturbation))
         if fetch:
             r.record_ids = self._get(L.DATA_RECORD_IDS, np.uint32, 5)
             r.record_points = self._get(L.DATA_RECORD_POINTS, np.float64, 3)
@@ -102,6 +112,17 @@ class Context:
                 r.tests = self._get(L.DATA_TESTS, np.uint32, 3)
                 r.test_info = self._get(L.DATA_TEST_INFO, np.int8, 4)
         return r
+
+    def set_general_position(self, constant: float = 1e-4, attempts: int = 4):
+        """Enforcement constant and attempts (mcBindState MC_CONTEXT_GENERAL_POSITION_ENFORCEMENT_*)."""
+        L.check(self._lib.mcgpu_context_set_general_position(self._h, float(constant), int(attempts)),
+                "mcgpu_context_set_general_position")
+
+    def general_position(self):
+        c, a = C.c_double(), C.c_uint32()
+        L.check(self._lib.mcgpu_context_get_general_position(self._h, C.byref(c), C.byref(a)),
+                "mcgpu_context_get_general_position")
+        return c.value, a.value
 
     def set_tuning(self, leaf_size=4, traversal=0, packet_faces=32, stack_depth=64, split_round=2):
         t = L.Tuning(leaf_size, traversal, packet_faces, stack_depth, split_round)

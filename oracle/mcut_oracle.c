@@ -606,9 +606,11 @@ static double input_coord(const mesh_t *m, int fin, size_t k, double c, double t
 }
 
 /* calculate_vertex_parameters + the conversion in client_input_arrays_to_hmesh
- * (preproc.cpp:2124-2290, 147-181); eps = |cut box diagonal| * 1e-4
+ * (preproc.cpp:2124-2290, 147-181); eps = |cut box diagonal| * the general-
+ * position constant, or the constant alone with absolute enforcement
  * (preproc.cpp:2518, 2667-2676) */
-static double recentre(const mesh_t *S, const mesh_t *Cm, int fin, double *sx, double *cx)
+static double recentre(const mesh_t *S, const mesh_t *Cm, int fin, double gp_constant, int gp_absolute, double *sx,
+    double *cx)
 {
     double smn[3], smx[3], scom[3], cmn[3], cmx[3], ccom[3], com[3], gmn[3], tp[3], t[3];
     vertex_bounds(S->v, fin, S->nv, smn, smx, scom);
@@ -626,7 +628,7 @@ static double recentre(const mesh_t *S, const mesh_t *Cm, int fin, double *sx, d
         for (int j = 0; j < 3; ++j) cx[(size_t)i * 3 + j] = input_coord(Cm, fin, (size_t)i * 3 + j, com[j], t[j]);
     double d[3];
     for (int j = 0; j < 3; ++j) d[j] = (cmx[j] + t[j]) - (cmn[j] + t[j]);
-    return sqrt(dot3(d, d)) * 1e-4;
+    return (gp_absolute ? 1.0 : sqrt(dot3(d, d))) * gp_constant;
 }
 
 /* face boxes (bvh.cpp:242-314) */
@@ -832,9 +834,17 @@ static int test_cmp(const void *x, const void *y)
     return a->g < b->g ? -1 : (a->g > b->g);
 }
 
-int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf,
+/* One front-end pass. With a perturbation (general-position enforcement,
+ * preproc.cpp:2590-2699) the cut vertices of the narrow phase are the
+ * recentred ones plus the perturbation (one rounding, preproc.cpp:131-133,
+ * 176-180), while the face boxes and the candidate pairs stay those of the
+ * unperturbed meshes: the reference builds the cut BVH only on the first
+ * attempt (preproc.cpp:2680) and traverses only after a rebuild
+ * (preproc.cpp:2820-2846). A perturbed pass with no record is a general-
+ * position violation (kernel.cpp:3211-3225). */
+int oracle_front_end2(const void *sv, const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf,
     const void *cv, const uint32_t *cf, const uint32_t *cfs, uint32_t ncv, uint32_t ncf, int float_input,
-    int threads, fe_result *out)
+    int threads, double gp_constant, int gp_absolute, const double *perturbation, fe_result *out)
 {
     memset(out, 0, sizeof *out);
     out->bad_face = -1;
@@ -851,7 +861,7 @@ int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, ui
     }
     const uint32_t NV = nsv + ncv, NF = nsf + ncf;
     double *x = (double *)malloc(sizeof(double) * 3 * (size_t)NV); /* ps vertices */
-    const double eps = recentre(&S, &Cm, float_input, x, x + (size_t)nsv * 3);
+    const double eps = recentre(&S, &Cm, float_input, gp_constant, gp_absolute, x, x + (size_t)nsv * 3);
     out->cut_eps = eps;
     out->src_xyz = (double *)malloc(sizeof(double) * 3 * (size_t)nsv);
     out->cut_xyz = (double *)malloc(sizeof(double) * 3 * (size_t)ncv);
@@ -877,6 +887,11 @@ int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, ui
     out->n_pairs = pv.n;
     out->pairs = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)(pv.n ? pv.n : 1));
     for (int64_t i = 0; i < pv.n; ++i) { out->pairs[2 * i] = pv.p[i].s; out->pairs[2 * i + 1] = pv.p[i].c; }
+    if (perturbation) {
+        for (uint32_t i = 0; i < ncv; ++i)
+            for (int j = 0; j < 3; ++j) x[((size_t)nsv + i) * 3 + j] = x[((size_t)nsv + i) * 3 + j] + perturbation[j];
+        memcpy(out->cut_xyz, x + (size_t)nsv * 3, sizeof(double) * 3 * (size_t)ncv);
+    }
 
     /* ps face CSR (sources first, then cut faces with vertex ids offset by Vs) */
     uint64_t *foff = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)NF + 1));
@@ -1061,6 +1076,7 @@ int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, ui
         nr += T[i].rec;
     }
     out->n_records = nr;
+    if (perturbation && out->status == FE_OK && nr == 0) out->status = FE_GP_VIOLATION;
     out->rec_ids = (uint32_t *)malloc(sizeof(uint32_t) * 3 * (size_t)(nr ? nr : 1));
     out->rec_pts = (double *)malloc(sizeof(double) * 3 * (size_t)(nr ? nr : 1));
     int64_t k = 0;
@@ -1074,6 +1090,13 @@ int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, ui
     free(T); free(pl); free(E); free(he_edge); free(plist); free(poff); free(foff); free(fidx);
     free(fb); free(x); free(S.off); free(Cm.off);
     return 0;
+}
+
+int oracle_front_end(const void *sv, const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf,
+    const void *cv, const uint32_t *cf, const uint32_t *cfs, uint32_t ncv, uint32_t ncf, int float_input,
+    int threads, fe_result *out)
+{
+    return oracle_front_end2(sv, sf, sfs, nsv, nsf, cv, cf, cfs, ncv, ncf, float_input, threads, 1e-4, 0, NULL, out);
 }
 
 /* predicate entry points for the predicate-level pin tests */

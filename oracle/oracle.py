@@ -55,11 +55,11 @@ def _lib(impl: str):
     if not os.path.exists(path):
         build(ref=(impl == "ref"))
     lib = C.CDLL(path)
-    fn = lib.oracle_front_end if impl == "port" else lib.ref_front_end
+    fn = lib.oracle_front_end2 if impl == "port" else lib.ref_front_end2
     fn.restype = C.c_int
     fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
-                   C.c_int, C.c_int, C.POINTER(FeResult)]
+                   C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p, C.POINTER(FeResult)]
     fr = lib.oracle_free if impl == "port" else lib.ref_free
     fr.argtypes = [C.POINTER(FeResult)]
     if impl == "ref":
@@ -90,13 +90,22 @@ def _arr(ptr, n, dtype):
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
 
 
-def front_end(src, cut, impl: str = "port", threads: int = 0, float_input: bool = False):
-    """Run one front-end dispatch; canonical-ordered numpy outputs."""
+def front_end(src, cut, impl: str = "port", threads: int = 0, float_input: bool = False,
+              gp_constant: float = 1e-4, gp_absolute: bool = False, perturbation=None):
+    """Run one front-end dispatch; canonical-ordered numpy outputs.
+
+    gp_constant / gp_absolute set the cut-box enlargement (the reference's
+    general-position constant times the cut box diagonal, or the constant
+    alone); `perturbation` (3 doubles) runs the narrow phase of one
+    general-position enforcement attempt: the cut vertices plus the
+    perturbation against the unperturbed pairs and face boxes."""
     lib, fn, fr = _lib(impl)
     ks, sa = _mesh_args(src, float_input)
     kc, ca = _mesh_args(cut, float_input)
     res = FeResult()
-    rc = fn(*sa, *ca, int(bool(float_input)), int(threads), C.byref(res))
+    pert = None if perturbation is None else np.ascontiguousarray(perturbation, dtype=np.float64)
+    rc = fn(*sa, *ca, int(bool(float_input)), int(threads), float(gp_constant), int(bool(gp_absolute)),
+            None if pert is None else pert.ctypes.data, C.byref(res))
     if rc != 0:
         raise RuntimeError(f"oracle front_end failed rc={rc}")
     nsf, ncf = sa[4], ca[4]

@@ -100,9 +100,15 @@ int sgn(double x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
 
 } // namespace
 
-extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
+// With a perturbation (general-position enforcement) the polygon soup's cut
+// vertices are the recentred ones plus the perturbation, as
+// client_input_arrays_to_hmesh adds it (preproc.cpp:131-133, 176-180), while
+// the BVHs, face boxes and candidate pairs stay those of the unperturbed
+// meshes (preproc.cpp:2680, 2820-2846); a perturbed pass with no record is a
+// general-position violation (kernel.cpp:3211-3225).
+extern "C" int ref_front_end2(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
     const void* cv, const uint32_t* cf, const uint32_t* cfs, uint32_t ncv, uint32_t ncf,
-    int float_input, int n_helpers, fe_result* out)
+    int float_input, int n_helpers, double gp_constant, int gp_absolute, const double* perturbation, fe_result* out)
 {
     memset(out, 0, sizeof(*out));
     out->bad_face = -1;
@@ -115,13 +121,18 @@ extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t*
     std::vector<double> sx, cx;
     recentre(S, float_input != 0, com, trans, sx);
     recentre(C, float_input != 0, com, trans, cx);
+    std::vector<double> px = cx; // the narrow phase's cut coordinates
+    if (perturbation)
+        for (uint32_t i = 0; i < ncv; ++i)
+            for (int j = 0; j < 3; ++j) px[i * 3 + j] = cx[i * 3 + j] + perturbation[j];
     out->src_xyz = dup(sx);
-    out->cut_xyz = dup(cx);
+    out->cut_xyz = dup(px);
 
-    // cut-mesh enlargement: diag length of the (translated) cut box times the
-    // default general-position constant (preproc.cpp:2518, 2667-2676; frontend.h:596)
+    // cut-mesh enlargement: diag length of the (translated) cut box, or 1 with
+    // absolute enforcement, times the general-position constant
+    // (preproc.cpp:2518, 2664-2676; frontend.h:596)
     const double cut_diag = length(cmax - cmin, 1);
-    const double eps = cut_diag * 1e-4;
+    const double eps = (gp_absolute ? 1.0 : cut_diag) * gp_constant;
     out->cut_eps = eps;
 
     hmesh_t sm, cm, ps;
@@ -131,7 +142,7 @@ extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t*
     }
     for (uint32_t i = 0; i < ncv; ++i) {
         cm.add_vertex(cx[i * 3], cx[i * 3 + 1], cx[i * 3 + 2]);
-        ps.add_vertex(cx[i * 3], cx[i * 3 + 1], cx[i * 3 + 2]);
+        ps.add_vertex(px[i * 3], px[i * 3 + 1], px[i * 3 + 2]);
     }
     add_faces(sm, S, 0);
     add_faces(cm, C, 0);
@@ -297,7 +308,15 @@ extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t*
     out->n_records = (int64_t)recs.size();
     out->rec_ids = dup(rid);
     out->rec_pts = dup(rpt);
+    if (perturbation && out->status == FE_OK && recs.empty()) out->status = FE_GP_VIOLATION;
     return 0;
+}
+
+extern "C" int ref_front_end(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
+    const void* cv, const uint32_t* cf, const uint32_t* cfs, uint32_t ncv, uint32_t ncf,
+    int float_input, int n_helpers, fe_result* out)
+{
+    return ref_front_end2(sv, sf, sfs, nsv, nsf, cv, cf, cfs, ncv, ncf, float_input, n_helpers, 1e-4, 0, nullptr, out);
 }
 
 extern "C" double ref_orient3d(const double* pa, const double* pb, const double* pc, const double* pd)

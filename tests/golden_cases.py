@@ -45,3 +45,13 @@ def same_bits(a, b):
         return bool(np.array_equal(a.view(np.uint64 if a.itemsize == 8 else np.uint32),
                                    b.astype(a.dtype).view(np.uint64 if a.itemsize == 8 else np.uint32)))
     return bool(np.array_equal(a, b))
+
+
+def perturbation_cube():
+    """The cube of the reference's general-position test
+    (tests/source/perturbationState.cpp:47-68): float vertices, six quads;
+    cut by itself every face is coplanar with a face of the other mesh."""
+    v = np.array([-1, -1, 1, 1, -1, 1, 1, -1, -1, -1, -1, -1,
+                  -1, 1, 1, 1, 1, 1, 1, 1, -1, -1, 1, -1], np.float32).reshape(-1, 3)
+    f = np.array([3, 2, 1, 0, 4, 5, 6, 7, 0, 1, 5, 4, 1, 2, 6, 5, 2, 3, 7, 6, 3, 0, 4, 7], np.uint32)
+    return dict(v=v, f=f, fs=np.full(6, 4, np.uint32))

@@ -71,6 +71,8 @@ def test_null_arguments_are_errors_not_crashes():
     assert lib.mcgpu_recentre(0, None, None, None, None, C.byref(eps)) == L.INVALID_VALUE
     assert "null" in L.last_error()
     assert lib.mcgpu_context_create(None, 0) == L.INVALID_VALUE
+    assert lib.mcgpu_context_set_general_position(None, 1e-4, 4) == L.INVALID_VALUE
+    assert lib.mcgpu_context_get_general_position(None, None, None) == L.INVALID_VALUE
     assert lib.mcgpu_get_data(None, L.DATA_RECORD_IDS, 0, None, None) == L.INVALID_VALUE
     b = L.Batch(0, None, None, None, None, None)
     assert lib.mcgpu_dispatch_packed(None, 0, C.byref(b), None) == L.INVALID_VALUE

@@ -40,3 +40,40 @@ def test_port_equals_reference_on_mid_size_case():
     assert a["status"] == b["status"]
     for k in G.FE_KEYS + ["face_boxes", "src_xyz", "cut_xyz"]:
         assert G.same_bits(a[k], b[k]), k
+
+
+def _same(a, b):
+    assert a["status"] == b["status"] and G.same_bits(a["cut_eps"], b["cut_eps"])
+    for k in ("pairs", "tests", "test_info", "rec_ids", "rec_pts", "cut_xyz", "face_boxes"):
+        assert G.same_bits(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("absolute", [False, True])
+def test_perturbed_pass_matches_reference(absolute):
+    """One general-position enforcement attempt (the cut vertices of the
+    narrow phase plus the perturbation, the unperturbed pairs and boxes):
+    the restatement against the reference's own functions, for the
+    reference's perturbation test case and its first perturbations."""
+    import gp_rng
+    m = G.perturbation_cube()
+    const = 1.5e-5 if absolute else 1e-4
+    base = oracle.front_end(m, m, impl="port", float_input=True, gp_constant=const, gp_absolute=absolute)
+    assert base["status"] == 1  # general position violated
+    for p in gp_rng.perturbations(3, base["cut_eps"]):
+        a = oracle.front_end(m, m, impl="port", float_input=True, gp_constant=const, gp_absolute=absolute,
+                             perturbation=p)
+        b = oracle.front_end(m, m, impl="ref", float_input=True, gp_constant=const, gp_absolute=absolute,
+                             perturbation=p)
+        _same(a, b)
+        assert G.same_bits(a["face_boxes"], base["face_boxes"]) and G.same_bits(a["pairs"], base["pairs"])
+
+
+@pytest.mark.parametrize("name", ["two_spheres", "crack3"])
+def test_perturbed_pass_matches_reference_on_fixtures(name):
+    import gp_rng
+    c = CASES[name]
+    fin = bool(c["float_input"])
+    base = oracle.front_end(c["src"], c["cut"], impl="port", float_input=fin)
+    p = gp_rng.perturbations(1, base["cut_eps"])[0]
+    _same(oracle.front_end(c["src"], c["cut"], impl="port", float_input=fin, perturbation=p),
+          oracle.front_end(c["src"], c["cut"], impl="ref", float_input=fin, perturbation=p))
