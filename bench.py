@@ -624,13 +624,17 @@ def run_gpu(args, world, rank, local):
         algo = BYTES[dom][1] * (Fs + Fc)
         units = f"{BYTES[dom][1]} B x {Fs + Fc} faces"
     achieved = algo / (per[dom] / 1e3) / 1e9
-    traffic = None
+    traffic, fp64 = None, None
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get(dom)
+            tj = json.load(open(prof))
+            traffic = tj.get(dom)
+            # the narrow phase is fp64-pipe-bound: its kernels' fp64 pipe activity (ncu)
+            fp64 = {k: v for k, v in tj.get("fp64_pipe_active_pct", {}).items()
+                    if k.split("<")[0] in STAGE_KERNELS[dom]} or None
         except Exception:
-            traffic = None
+            traffic, fp64 = None, None
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -647,7 +651,8 @@ def run_gpu(args, world, rank, local):
         "latency_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
         "roofline": {"bound": "hbm", "kernel": dom, "stage_kernels": STAGE_KERNELS[dom], "achieved": achieved,
                      "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "algorithmic_bytes": algo,
+                     "frac": achieved / hbm, "traffic": traffic, "fp64_pipe_active_pct": fp64,
+                     "algorithmic_bytes": algo,
                      "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)"},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "front_end": summ,
