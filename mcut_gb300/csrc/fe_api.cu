@@ -421,10 +421,22 @@ __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint3
     }
 }
 
-__global__ void k_init_meshbox(unsigned long long* mb, uint64_t n)
+// a dispatch's starting state in one launch: empty mesh boxes (min at the
+// top, max at the bottom of the ordered-uint64 encoding), zero counters,
+// statuses and record ranges, no degenerate face
+__global__ void k_init_dispatch(unsigned long long* __restrict__ mb, uint32_t n_pairs, uint32_t* __restrict__ counters,
+    uint32_t* __restrict__ pair_status, int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_nrec)
 {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        mb[i] = (i % 6) < 3 ? ~0ull : 0ull;
+    const uint64_t n12 = (uint64_t)n_pairs * 12;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n12 + 16; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < n12) mb[i] = (i % 6) < 3 ? ~0ull : 0ull;
+        else counters[i - n12] = 0u;
+        if (i < n_pairs) {
+            pair_status[i] = 0u;
+            pair_bad[i] = kNoBad;
+        }
+        if (i <= n_pairs) pair_nrec[i] = 0u;
+    }
 }
 
 int grid1(uint64_t n)
@@ -822,15 +834,10 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     int src_buf = 0, cut_buf = 0;
     uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
     auto seg0 = [&](int* aux) {
-        // mesh boxes start empty: min at the top, max at the bottom of the ordered-uint64 encoding
         rec(c, 2 * MCGPU_STAGE_BOUNDS);
         g_launches++;
-        k_init_meshbox<<<grid1((uint64_t)n * 12), 256, 0, s>>>(W.mesh_box, (uint64_t)n * 12);
-        ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
-        ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
-        ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
-        ck(cudaMemsetAsync(W.pair_bad, 0x7F, 4 * (size_t)n, s), "memset");
-        ck(cudaMemsetAsync(W.pair_nrec, 0, 4 * (size_t)(n + 1), s), "memset");
+        k_init_dispatch<<<grid1((uint64_t)n * 12 + 16), 256, 0, s>>>(W.mesh_box, n, W.counters, W.pair_status,
+            W.pair_bad, W.pair_nrec); // the candidate-face flags are cleared by the bounds kernel
         launch_bounds_morton(P, W, wide, key_bits, s);
         rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
         rec(c, 2 * MCGPU_STAGE_SORT);

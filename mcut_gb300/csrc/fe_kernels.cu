@@ -179,9 +179,11 @@ __global__ void k_mesh_frames(const unsigned long long* __restrict__ mesh_box, u
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
     float* __restrict__ fbox32, const float4* __restrict__ frame, K* __restrict__ skey, uint32_t* __restrict__ sval,
-    K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit, uint32_t* __restrict__ pair_status)
+    K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit, uint32_t* __restrict__ pair_status,
+    uint8_t* __restrict__ cand)
 {
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+        cand[f] = 0; // no candidate pair yet (the traversal sets it)
         const uint32_t fp = P.face_pair[f];
         const uint32_t p = fp & ~kCutBit;
         const bool is_cut = (fp & kCutBit) != 0;
@@ -328,9 +330,10 @@ __device__ __forceinline__ void load_key_box(const double* __restrict__ fbox, ui
 // leaf clusters: `leaf_size` consecutive sorted cut faces of one pair
 template <typename K>
 __global__ void __launch_bounds__(kBlock) k_clusters(Problem P, const K* __restrict__ ckey, K* __restrict__ clkey,
-    uint32_t* __restrict__ cl_start, uint8_t* __restrict__ cl_n)
+    uint32_t* __restrict__ cl_start, uint8_t* __restrict__ cl_n, uint32_t* __restrict__ split_far)
 {
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < P.ncl; c += gridDim.x * blockDim.x) {
+        if (c + 1 < P.ncl) split_far[c] = 0xFFFFFFFFu; // no child has reached split c yet (the tree build)
         uint32_t lo = 0, hi = P.n_pairs;
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
@@ -2055,10 +2058,10 @@ void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cu
     if (wide)
         k_face_bounds<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame,
             (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits,
-            W.pair_status);
+            W.pair_status, W.cand);
     else
         k_face_bounds<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame, (uint32_t*)W.skeys[0], W.svals[0],
-            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status);
+            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status, W.cand);
 }
 
 int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)
@@ -2084,12 +2087,11 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
     g_launches++;
     if (wide)
         k_clusters<unsigned long long><<<gc, kBlock, 0, s>>>(P, (const unsigned long long*)W.ckeys[cut_buf],
-            (unsigned long long*)W.cl_key, W.cl_start, W.cl_n);
+            (unsigned long long*)W.cl_key, W.cl_start, W.cl_n, W.split_far);
     else
         k_clusters<uint32_t><<<gc, kBlock, 0, s>>>(P, (const uint32_t*)W.ckeys[cut_buf], (uint32_t*)W.cl_key,
-            W.cl_start, W.cl_n);
+            W.cl_start, W.cl_n, W.split_far);
     if (n < 2) return;
-    cudaMemsetAsync(W.split_far, 0xFF, sizeof(uint32_t) * (size_t)(n - 1), s);
     g_launches++;
     const int g = (n + kRefitWin - 1) / kRefitWin;
     if (wide)
