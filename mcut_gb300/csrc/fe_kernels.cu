@@ -349,27 +349,6 @@ __global__ void __launch_bounds__(kBlock) k_clusters(Problem P, const K* __restr
 
 struct FBox { float lo[3], hi[3]; uint32_t plo, phi; };
 
-__device__ __forceinline__ void put_child(Node* nd, int slot, const FBox& b)
-{
-    float* f0 = reinterpret_cast<float*>(&nd->b0);
-    // 12 floats: left lo3 hi3, right lo3 hi3
-    float* o = f0 + slot * 6;
-    o[0] = b.lo[0]; o[1] = b.lo[1]; o[2] = b.lo[2];
-    o[3] = b.hi[0]; o[4] = b.hi[1]; o[5] = b.hi[2];
-    nd->prange[slot] = b.plo | (b.phi << 16);
-}
-__device__ __forceinline__ FBox get_child(const Node* nd, int slot)
-{
-    const float* o = reinterpret_cast<const float*>(&nd->b0) + slot * 6;
-    FBox b;
-    b.lo[0] = __ldcg(o); b.lo[1] = __ldcg(o + 1); b.lo[2] = __ldcg(o + 2);
-    b.hi[0] = __ldcg(o + 3); b.hi[1] = __ldcg(o + 4); b.hi[2] = __ldcg(o + 5);
-    const uint32_t pr = __ldcg(&nd->prange[slot]);
-    b.plo = pr & 0xFFFFu;
-    b.phi = pr >> 16;
-    return b;
-}
-
 // Bottom-up build of the binary radix tree over the sorted leaf clusters,
 // boxes included (agglomerative LBVH, Apetrei, EG 2014). D(j), the boundary
 // between sorted clusters j and j+1, is the XOR of their keys with the XOR of
