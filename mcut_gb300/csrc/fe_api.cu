@@ -94,7 +94,7 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -121,6 +121,7 @@ struct mcgpu_context_t {
     PinBuf pin_counters, pin_tab, pin_stage, pin_idx;
     Layout L;
     mcgpu::Problem P {};
+    mcgpu::Problem Pin {}; // the bounds kernel's view of the indices
     mcgpu::Work W {};
     std::vector<mcgpu_summary> sums;
     std::vector<uint64_t> rec_begin;  // per pair, +1
@@ -671,10 +672,19 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         ck(cudaMemcpyAsync(foff, off.data(), sizeof(uint32_t) * (L.nf + 1), cudaMemcpyHostToDevice, s), "H2D foff");
         ck(cudaStreamSynchronize(s), "sync foff"); // `off` is a pageable temporary
     }
+    // A batch's indices are made global here, with its face -> pair table.
+    // One pair's are made global by the bounds kernel, which reads the raw
+    // indices (the caller's device arrays or the uploaded copy, left as they
+    // are) and writes the global table and the face -> pair table as it goes.
     uint32_t* face_pair = c->buf[B_FPAIR].get<uint32_t>(L.nf);
-    g_launches++;
-    k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf,
-        split ? srcs[0].face_indices : nullptr, split ? cuts[0].face_indices : nullptr);
+    uint32_t* fidx_glob = fidx;
+    if (n > 1) {
+        g_launches++;
+        k_prep<<<grid1(std::max(L.nidx, L.nf)), 256, 0, s>>>(n, dtab, fidx, L.nidx, face_pair, L.nf, nullptr,
+            nullptr);
+    } else {
+        fidx_glob = c->buf[B_FIDXG].get<uint32_t>(std::max<uint64_t>(L.nidx, 1));
+    }
 
     Problem& P = c->P;
     P.n_pairs = n;
@@ -686,8 +696,10 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.Xc = split ? static_cast<const double*>(cuts[0].vertices) : nullptr;
     P.xsplit = split ? L.vs[0] : 0xFFFFFFFFu;
     P.foff = foff;
-    P.fidx = fidx;
+    P.fidx = fidx_glob;
     P.face_pair = face_pair;
+    P.fidx_cut = nullptr;
+    P.fidx_split = P.cut_vbase = P.face_split = 0u;
     P.pair_fbase = dtab + 4 * (n + 1);
     P.pair_fs = dtab + 5 * (n + 1);
     P.pair_vbase = dtab + 2 * (n + 1);
@@ -699,6 +711,21 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.all_triangles = L.all_tri ? 1 : 0;
     P.leaf_size = L.leaf_size;
     P.ncl = (uint32_t)L.ncl;
+    // the bounds kernel's input view: one pair's raw indices, cut ones
+    // offset by the source vertex count on the fly
+    Problem& Pin = c->Pin;
+    Pin = P;
+    c->W.fidx_out = c->W.face_pair_out = nullptr;
+    if (n == 1) {
+        Pin.fidx = split ? srcs[0].face_indices : fidx;
+        Pin.face_pair = nullptr;
+        Pin.fidx_cut = split ? cuts[0].face_indices : fidx + L.is[0];
+        Pin.fidx_split = L.is[0];
+        Pin.cut_vbase = L.vs[0];
+        Pin.face_split = L.fs[0];
+        c->W.fidx_out = fidx_glob;
+        c->W.face_pair_out = face_pair;
+    }
 }
 
 // stage events: 2k at the start of stage k, 2k+1 at its end; the host
@@ -838,7 +865,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         g_launches++;
         k_init_dispatch<<<grid1((uint64_t)n * 12 + 16), 256, 0, s>>>(W.mesh_box, n, W.counters, W.pair_status,
             W.pair_bad, W.pair_nrec); // the candidate-face flags are cleared by the bounds kernel
-        launch_bounds_morton(P, W, wide, key_bits, s);
+        launch_bounds_morton(P, c->Pin, W, wide, key_bits, s);
         rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
         rec(c, 2 * MCGPU_STAGE_SORT);
         aux[0] = launch_sort(P, W, wide, key_bits, s, aux[1]);
@@ -945,14 +972,14 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         W.inc_slots = 0;
     };
     clear_stage3();
-    if (seg_key(P, W, n, key_bits, prof) != c->fuse_key) c->csr_incidence = false; // a new layout
+    if (seg_key(P, c->Pin, W, n, key_bits, prof) != c->fuse_key) c->csr_incidence = false; // a new layout
     uint64_t npairs = 0;
     std::vector<unsigned char> key0;
     // a vertex with more incident faces than the fixed incidence slots reruns
     // the call with CSR incidence (kept for the layout's later calls)
     for (;;) {
         clear_stage3();
-        key0 = seg_key(P, W, n, key_bits, prof);
+        key0 = seg_key(P, c->Pin, W, n, key_bits, prof);
         bool done = false;
         // Fused call: after a call of the same shape, the three segments run as
         // one graph with one readback. Stage 3 is sized for the pair capacity (a
@@ -970,7 +997,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
                 W.rec_ids = c->buf[B_RIDS].get<uint32_t>((size_t)rec_cap * 5);
                 W.rec_pts = c->buf[B_RPTS].get<double>((size_t)rec_cap * 3);
             }
-            run_segment(c, 3, seg_key(P, W, n, key_bits, keep, dev_rec, rec_cap), [&](int* aux) {
+            run_segment(c, 3, seg_key(P, c->Pin, W, n, key_bits, keep, dev_rec, rec_cap), [&](int* aux) {
                 seg0(aux);
                 seg1();
                 aux[2] = dev_rec ? launch_records_dev(P, W, rec_cap, s) : 0;

@@ -30,6 +30,22 @@ namespace {
 constexpr int kBlock = 256;
 
 // vertex v of the dispatch (two segments when the caller's arrays are read in place)
+// ps face-vertex entry k as the bounds kernel reads it: a single pair's cut
+// entries come from the caller's (or the uploaded) raw cut indices, offset
+// by the source vertex count on the fly (fidx_cut != null); the bounds kernel
+// writes the global table every later kernel reads directly
+__device__ __forceinline__ uint32_t fidx_at(const Problem& P, uint64_t k)
+{
+    if (P.fidx_cut && k >= P.fidx_split) return P.fidx_cut[k - P.fidx_split] + P.cut_vbase;
+    return P.fidx[k];
+}
+// pair id | kCutBit of ps face f (one pair without a table: cut faces from face_split on)
+__device__ __forceinline__ uint32_t face_pair_of(const Problem& P, uint32_t f)
+{
+    if (!P.face_pair) return f >= P.face_split ? kCutBit : 0u;
+    return P.face_pair[f];
+}
+
 __device__ __forceinline__ void load_v(const Problem& P, uint32_t v, double* x)
 {
     if (v < P.xsplit) load_xyz(P.X, v, x);
@@ -180,11 +196,12 @@ template <typename K>
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
     float* __restrict__ fbox32, const float4* __restrict__ frame, K* __restrict__ skey, uint32_t* __restrict__ sval,
     K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit, uint32_t* __restrict__ pair_status,
-    uint8_t* __restrict__ cand)
+    uint8_t* __restrict__ cand, uint32_t* __restrict__ fidx_out, uint32_t* __restrict__ face_pair_out)
 {
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         cand[f] = 0; // no candidate pair yet (the traversal sets it)
-        const uint32_t fp = P.face_pair[f];
+        const uint32_t fp = face_pair_of(P, f);
+        if (face_pair_out) face_pair_out[f] = fp;
         const uint32_t p = fp & ~kCutBit;
         const bool is_cut = (fp & kCutBit) != 0;
         const uint32_t o = face_o(P, f), n = face_n(P, f);
@@ -203,7 +220,8 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         }
         bool bad = false;
         for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t v = P.fidx[o + k];
+            const uint32_t v = fidx_at(P, o + k);
+            if (fidx_out) fidx_out[o + k] = v;
             if (v < vlo || v >= vhi) { bad = true; continue; }
             double x[3];
             load_v(P, v, x);
@@ -2027,7 +2045,7 @@ int grid_spread(uint64_t n)
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s)
+void launch_bounds_morton(const Problem& P, const Problem& Pin, Work& W, bool wide, int key_bits, cudaStream_t s)
 {
     float4* frame = reinterpret_cast<float4*>(W.mesh_frame);
     g_launches += 3;
@@ -2035,12 +2053,12 @@ void launch_bounds_morton(const Problem& P, Work& W, bool wide, int key_bits, cu
     k_mesh_frames<<<(2 * P.n_pairs + 255) / 256, 256, 0, s>>>(W.mesh_box, 2 * P.n_pairs, frame);
     const int g = grid_for(P.nf);
     if (wide)
-        k_face_bounds<unsigned long long><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame,
+        k_face_bounds<unsigned long long><<<g, kBlock, 0, s>>>(Pin, W.fbox, W.fbox32, frame,
             (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits,
-            W.pair_status, W.cand);
+            W.pair_status, W.cand, W.fidx_out, W.face_pair_out);
     else
-        k_face_bounds<uint32_t><<<g, kBlock, 0, s>>>(P, W.fbox, W.fbox32, frame, (uint32_t*)W.skeys[0], W.svals[0],
-            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status, W.cand);
+        k_face_bounds<uint32_t><<<g, kBlock, 0, s>>>(Pin, W.fbox, W.fbox32, frame, (uint32_t*)W.skeys[0], W.svals[0],
+            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status, W.cand, W.fidx_out, W.face_pair_out);
 }
 
 int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)

@@ -50,7 +50,11 @@ struct Problem {
     uint32_t xsplit;            // 0xFFFFFFFF: every vertex in X
     const uint32_t* foff;
     const uint32_t* fidx;
-    const uint32_t* face_pair;
+    const uint32_t* face_pair;  // null for one pair: cut faces are those from face_split on
+    // one pair: entries from fidx_split on are raw cut indices in fidx_cut,
+    // global id = raw + cut_vbase (null: fidx holds global ids)
+    const uint32_t* fidx_cut;
+    uint32_t fidx_split, cut_vbase, face_split;
     // per pair tables [n_pairs (+1)]
     const uint32_t* pair_fbase; // first ps face of the pair
     const uint32_t* pair_fs;    // source faces of the pair
@@ -69,6 +73,8 @@ struct Work {
     double* fbox;                     // [nf*6]
     float* fbox32;                    // [nf*6] the same boxes rounded outward to fp32
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
+    uint32_t* fidx_out;               // one pair: the bounds kernel writes the global ps indices here
+    uint32_t* face_pair_out;          // ... and the face -> pair table (null for a batch: k_prep made them)
     void* mesh_frame;                 // [n_pairs*2*2] float4: fp32 box low corner, 1023 / extent
     // sort buffers (keys u32 for one pair, u64 for batches); the cut keys and
     // values follow the source ones in the same arrays (ckeys[b] = skeys[b] + ns)
@@ -127,7 +133,9 @@ struct Work {
 };
 
 // stage launchers (all asynchronous on `s`)
-void launch_bounds_morton(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s);
+// Pin: the input view the bounds kernel reads the indices through (for one
+// pair the raw source / cut indices); P: the global view of later stages
+void launch_bounds_morton(const Problem& P, const Problem& Pin, Work& W, bool wide_keys, int key_bits, cudaStream_t s);
 int launch_sort(const Problem& P, Work& W, bool wide_keys, int key_bits, cudaStream_t s, int& cut_buf);
 void launch_hierarchy(const Problem& P, Work& W, bool wide_keys, int cut_buf, cudaStream_t s);
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s);

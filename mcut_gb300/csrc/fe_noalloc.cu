@@ -262,7 +262,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
         (uint32_t)nf, reinterpret_cast<uint32_t*>(base + oFidx), reinterpret_cast<uint32_t*>(base + oFpair),
         W.mesh_box);
 
-    launch_bounds_morton(P, W, false, kMortonBits, s);
+    launch_bounds_morton(P, P, W, false, kMortonBits, s);
     int cut_buf = 0;
     const int src_buf = launch_sort(P, W, false, kMortonBits, s, cut_buf);
     launch_hierarchy(P, W, false, cut_buf, s);
