@@ -60,12 +60,13 @@ BYTES = {
 # the kernels each stage's CUDA events bracket (k_src_packets and the incidence
 # kernels run on the second stream inside the hierarchy and adjacency stages)
 STAGE_KERNELS = {
-    "upload": ["k_prep"],
-    "bounds": ["k_init_meshbox", "k_vertex_bounds", "k_mesh_frames", "k_face_bounds"],
+    "upload": ["k_prep"],  # batches only: one pair's indices are made global by k_face_bounds
+    "bounds": ["k_init_dispatch", "k_vertex_bounds", "k_mesh_frames", "k_face_bounds"],
     "sort": ["k_upsweep", "k_digit_scan", "k_downsweep"],
     "hierarchy": ["k_clusters", "k_build", "k_src_packets"],
     "traverse": ["k_top_cut", "k_traverse_wave"],
-    "adjacency": ["k_plane_slots", "k_planes", "k_triplets", "k_mark_vertices", "k_vf_count", "k_vf_fill"],
+    "adjacency": ["k_plane_slots", "k_planes", "k_triplets", "k_mark_vertices", "k_vf_slots", "k_vf_count",
+                  "k_vf_fill"],
     "narrow": ["k_pair_tests", "k_narrow_signs", "k_finish_planes", "k_narrow_hits", "k_rank_records",
                "k_scatter_records"],
 }
