@@ -152,7 +152,7 @@ struct mcgpu_context_t {
     // the fused call (one graph, one readback) follows a call with the same segment-0 key
     std::vector<unsigned char> fuse_key;
     bool fuse_ok = false;
-    uint64_t fuse_nrec = 0;
+    uint64_t fuse_nrec = 0, fuse_npairs = 0;
 };
 
 namespace {
@@ -982,14 +982,15 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         key0 = seg_key(P, c->Pin, W, n, key_bits, prof);
         bool done = false;
         // Fused call: after a call of the same shape, the three segments run as
-        // one graph with one readback. Stage 3 is sized for the pair capacity (a
-        // plane slot for every face, tests for every pair the buffer holds), so
-        // nothing overflows whatever the pair count, and the records are ordered
-        // from the count left on the device. A pair overflow or a traversal stack
-        // overflow reruns the call stage by stage; a record count past the
-        // one-launch ordering reruns only the record segment.
+        // one graph with one readback. Stage 3 is sized before the pair count is
+        // known: a plane slot for every face, and tests for the previous call's
+        // pairs plus a quarter (at most the pair capacity); every kernel guards
+        // its capacity, and the records are ordered from the count left on the
+        // device. A pair, test or traversal-stack overflow reruns the call stage
+        // by stage; a record count past the one-launch ordering reruns only the
+        // record segment.
         if (c->use_graphs && c->use_fuse && !prof && c->fuse_ok && c->fuse_key == key0) {
-            rc = size_stage3(W.pair_cap, true);
+            rc = size_stage3(std::min<uint64_t>(W.pair_cap, c->fuse_npairs + c->fuse_npairs / 4 + 1024), true);
             if (rc != MCGPU_OK) return rc;
             const uint32_t rec_cap = (uint32_t)std::min<uint64_t>(W.test_cap, kRankSortMax);
             const bool dev_rec = c->fuse_nrec <= rec_cap;
@@ -1006,9 +1007,9 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
             cut_buf = c->graphs[3].aux[1];
             read_status(dev_rec && n > 1);
             ck(cudaStreamSynchronize(s), "sync fused");
-            bool stack = false;
-            for (uint32_t p = 0; p < n; ++p) stack |= (hc[16 + p] & ST_STACK) != 0;
-            if (!stack && hc[0] <= W.pair_cap) {
+            bool rerun = false;
+            for (uint32_t p = 0; p < n; ++p) rerun |= (hc[16 + p] & (ST_STACK | ST_OVERFLOW_TESTS)) != 0;
+            if (!rerun && hc[0] <= W.pair_cap) {
                 npairs = hc[0];
                 c->n_pairs_found = npairs;
                 c->n_tests = hc[1];
@@ -1073,6 +1074,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->fuse_key = key0;
     c->fuse_ok = true;
     c->fuse_nrec = c->n_records;
+    c->fuse_npairs = npairs;
 
     // General-position enforcement (preproc.cpp:2590-2699, 2933-2945): each
     // attempt perturbs the narrow phase's cut vertices by uniform(-1, 1) *
