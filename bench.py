@@ -73,6 +73,23 @@ STAGE_KERNELS = {
 }
 
 
+def ncu_figures(stage):
+    """The stage's DRAM traffic and its kernels' ncu pipe / SIMT figures from
+    profiles/traffic.json (one capture of the workload; see that file's
+    sources): (traffic bytes, {figure: {kernel: value}}), or (None, {})."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            tj = json.load(fh)
+    except (OSError, ValueError):
+        return None, {}
+    figs = {}
+    for key in ("fp64_pipe_active_pct", "fp32_pipe_active_pct", "threads_per_warp_instruction", "l2_hit_pct"):
+        sel = {k: v for k, v in tj.get(key, {}).items() if k.split("<")[0] in STAGE_KERNELS[stage]}
+        if sel:
+            figs[key] = sel
+    return tj.get(stage), figs
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -631,17 +648,9 @@ def run_gpu(args, world, rank, local):
         algo = BYTES[dom][1] * (Fs + Fc)
         units = f"{BYTES[dom][1]} B x {Fs + Fc} faces"
     achieved = algo / (per[dom] / 1e3) / 1e9
-    traffic, fp64 = None, None
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        try:
-            tj = json.load(open(prof))
-            traffic = tj.get(dom)
-            # the narrow phase is fp64-pipe-bound: its kernels' fp64 pipe activity (ncu)
-            fp64 = {k: v for k, v in tj.get("fp64_pipe_active_pct", {}).items()
-                    if k.split("<")[0] in STAGE_KERNELS[dom]} or None
-        except Exception:
-            traffic, fp64 = None, None
+    # DRAM traffic and, per kernel of the stage, pipe activity, lanes per warp
+    # instruction and L2 hits (ncu)
+    traffic, figs = ncu_figures(dom)
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -658,7 +667,7 @@ def run_gpu(args, world, rank, local):
         "latency_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
         "roofline": {"bound": "hbm", "kernel": dom, "stage_kernels": STAGE_KERNELS[dom], "achieved": achieved,
                      "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "fp64_pipe_active_pct": fp64,
+                     "frac": achieved / hbm, "traffic": traffic, **figs,
                      "algorithmic_bytes": algo,
                      "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)"},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
