@@ -17,12 +17,11 @@ Skipped on hosts without the reference sources.
 """
 import os
 
-import numpy as np
 import pytest
 
+import fuzz_cases as F
 import golden_cases as G
 import oracle
-from mcut_gb300 import meshgen as M
 
 REF_ROOT = os.environ.get("MCUT_REF_ROOT", "/root/reference")
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "source")),
@@ -47,64 +46,32 @@ def _same(src, cut, **kw):
     return a
 
 
-def _lattice(m, step):
-    return dict(v=np.round(m["v"] / step) * step, f=m["f"], fs=m["fs"])
-
-
-def _quads(n, h, rng, warp):
-    g = M.grid(n, h)
-    i = np.arange(n - 1)
-    I, J = np.meshgrid(i, i, indexing="xy")
-    a = (J * n + I).ravel()
-    f = np.stack([a, a + 1, a + n + 1, a + n], 1).astype(np.uint32)
-    v = g["v"].copy()
-    v[:, 2] += rng.uniform(-warp, warp, len(v))
-    return dict(v=v, f=f.ravel(), fs=np.full(len(f), 4, np.uint32))
-
-
 @pytest.mark.parametrize("seed", range(4))
 def test_random_fracture_pairs(seed):
-    rng = np.random.default_rng(M.SEED_BASE + 100 + seed)
     recs = 0
-    for _ in range(25):
-        s, c = M.crack_pair(rng, level=int(rng.integers(1, 4)), n=int(rng.integers(4, 24)))
-        recs += len(_same(s, c)["rec_ids"])
+    for s, c, kw in F.fracture(seed):
+        recs += len(_same(s, c, **kw)["rec_ids"])
     assert recs > 0
 
 
 @pytest.mark.parametrize("seed", range(4))
 def test_lattice_snapped_pairs(seed):
-    rng = np.random.default_rng(M.SEED_BASE + 200 + seed)
-    statuses = set()
-    for _ in range(25):
-        s, c = M.crack_pair(rng, level=int(rng.integers(1, 3)), n=int(rng.integers(3, 9)))
-        statuses.add(_same(_lattice(s, 0.125), _lattice(c, 0.125))["status"])
+    statuses = {_same(s, c, **kw)["status"] for s, c, kw in F.lattice(seed)}
     assert oracle.FE_GP_VIOLATION in statuses
 
 
 def test_collapsed_faces():
-    rng = np.random.default_rng(M.SEED_BASE + 300)
-    statuses = set()
-    for _ in range(40):
-        s, c = M.crack_pair(rng, level=int(rng.integers(1, 3)), n=int(rng.integers(3, 9)))
-        statuses.add(_same(_lattice(s, 0.5), _lattice(c, 0.5))["status"])
+    statuses = {_same(s, c, **kw)["status"] for s, c, kw in F.collapsed()}
     assert statuses & {oracle.FE_DEGENERATE_SRC_FACE, oracle.FE_DEGENERATE_CUT_FACE}
 
 
 @pytest.mark.parametrize("warp", [0.0, 1e-3, 0.05])
 def test_quad_meshes(warp):
-    rng = np.random.default_rng(M.SEED_BASE + 400)
-    for _ in range(10):
-        s = M.icosphere(int(rng.integers(1, 3)), 1.0)
-        c = _quads(int(rng.integers(3, 10)), 1.5, rng, warp)
-        c["v"] = c["v"] @ M._rotation(rng).T + rng.uniform(-0.3, 0.3, 3)
-        _same(s, c)
+    for s, c, kw in F.quads(warp):
+        _same(s, c, **kw)
 
 
 @pytest.mark.parametrize("absolute", [False, True])
 def test_float_input_and_cut_box_constant(absolute):
-    rng = np.random.default_rng(M.SEED_BASE + 500 + int(absolute))
-    for _ in range(12):
-        s, c = M.crack_pair(rng, level=2, n=int(rng.integers(4, 16)))
-        _same(s, c, float_input=True, gp_absolute=absolute,
-              gp_constant=float(rng.choice([1e-4, 1e-3, 1e-2])))
+    for s, c, kw in F.float32(absolute):
+        _same(s, c, **kw)
