@@ -53,6 +53,36 @@ typedef struct fe_result {
     double *cut_xyz;           /* 3*Vc recentred coordinates */
 } fe_result;
 
+/* Input-mesh conversion and checks (hmesh_oracle.c; ref_hmesh in the
+ * harness): the halfedge mesh MCUT builds from one mesh's arrays and the
+ * outcome of its input checks. */
+enum {
+    HM_OK = 0,
+    HM_FACE_SIZE = 1,       /* a face with fewer than 3 vertices */
+    HM_INDEX_RANGE = 2,     /* a vertex index >= the vertex count */
+    HM_DUPLICATE_INDEX = 3, /* a vertex twice in one face */
+    HM_NON_MANIFOLD = 4,    /* a directed halfedge in two faces */
+    HM_TOO_SMALL = 5,       /* fewer than 3 vertices or no face */
+    HM_COMPONENTS = 6       /* the vertex graph is not one connected component */
+};
+
+typedef struct hm_result {
+    int32_t status;
+    int32_t bad_face;       /* the face a conversion error stopped at, else -1 */
+    uint32_t n_edges;       /* this and the arrays: set once the conversion succeeded */
+    uint32_t n_components;
+    uint32_t *he_target;    /* [2*n_edges] */
+    int32_t *he_face;       /* [2*n_edges], -1 = no face */
+    int32_t *he_next;       /* [2*n_edges], -1 = unlinked */
+    int32_t *he_prev;       /* [2*n_edges] */
+    uint32_t *corner_he;    /* one per face corner: the halfedge v_i -> v_i+1 */
+    uint32_t *v_off;        /* [nv+1] */
+    uint32_t *v_he;         /* the halfedges ending at each vertex, creation order */
+} hm_result;
+
+int oracle_hmesh(const uint32_t *f, const uint32_t *fs, uint32_t nv, uint32_t nf, hm_result *out);
+void oracle_hmesh_free(hm_result *r);
+
 #ifdef __cplusplus
 }
 #endif

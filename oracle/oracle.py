@@ -171,3 +171,46 @@ def dispatch(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: in
                               C.byref(ncc), C.byref(niv))
     del ks, kc
     return dict(result=rc, ccs=info[:ncc.value].copy(), n_ivtx=int(niv.value))
+
+
+HM_OK, HM_FACE_SIZE, HM_INDEX_RANGE, HM_DUPLICATE_INDEX, HM_NON_MANIFOLD, HM_TOO_SMALL, HM_COMPONENTS = range(7)
+
+
+class HmResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("bad_face", C.c_int32), ("n_edges", C.c_uint32), ("n_components", C.c_uint32),
+        ("he_target", C.POINTER(C.c_uint32)), ("he_face", C.POINTER(C.c_int32)),
+        ("he_next", C.POINTER(C.c_int32)), ("he_prev", C.POINTER(C.c_int32)),
+        ("corner_he", C.POINTER(C.c_uint32)), ("v_off", C.POINTER(C.c_uint32)), ("v_he", C.POINTER(C.c_uint32)),
+    ]
+
+
+def hmesh(f, fs, nv: int, impl: str = "port"):
+    """One mesh's halfedge mesh and input checks (the connectivity MCUT builds
+    from the caller's arrays): status, failing face, edges, and per halfedge
+    its target / face / next / prev, per face corner its halfedge, per vertex
+    the halfedges ending there (CSR), the connected-component count."""
+    lib, _, _ = _lib(impl)
+    fn = lib.oracle_hmesh if impl == "port" else lib.ref_hmesh
+    fr = lib.oracle_hmesh_free if impl == "port" else lib.ref_hmesh_free
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(HmResult)]
+    fr.argtypes = [C.POINTER(HmResult)]
+    f = np.ascontiguousarray(f, dtype=np.uint32)
+    fs = None if fs is None else np.ascontiguousarray(fs, dtype=np.uint32)
+    nf = int(len(fs)) if fs is not None else int(len(f) // 3)
+    res = HmResult()
+    rc = fn(f.ctypes.data if len(f) else None, None if fs is None else fs.ctypes.data, int(nv), nf, C.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"{impl} hmesh failed rc={rc}")
+    out = dict(status=int(res.status), bad_face=int(res.bad_face), n_edges=int(res.n_edges),
+               n_components=int(res.n_components))
+    if res.status in (HM_OK, HM_TOO_SMALL, HM_COMPONENTS):
+        nh = 2 * res.n_edges
+        out.update(
+            he_target=_arr(res.he_target, nh, np.uint32), he_face=_arr(res.he_face, nh, np.int32),
+            he_next=_arr(res.he_next, nh, np.int32), he_prev=_arr(res.he_prev, nh, np.int32),
+            corner_he=_arr(res.corner_he, len(f), np.uint32), v_off=_arr(res.v_off, nv + 1, np.uint32),
+            v_he=_arr(res.v_he, nh, np.uint32))
+    fr(C.byref(res))
+    return out

@@ -19,9 +19,16 @@
 //                   returning status and per-CC type / vertex / face counts,
 //                   plus the intersection-point count read back from the
 //                   reference's own verbose dumps (kernel.cpp:1736-1738,3260-3266).
+//   ref_hmesh     : one mesh's halfedge mesh as the reference builds it (its
+//                   own hmesh_t::add_vertex / add_face, preceded by the face
+//                   checks of client_input_arrays_to_hmesh, preproc.cpp:390-460)
+//                   and check_input_mesh's outcome (preproc.cpp:505-579, with
+//                   the reference's find_connected_components), read back
+//                   through hmesh_t's public accessors.
 #include <mcut/mcut.h>
 #include <mcut/internal/bvh.h>
 #include <mcut/internal/hmesh.h>
+#include <mcut/internal/kernel.h>
 #include <mcut/internal/math.h>
 #include <mcut/internal/tpool.h>
 
@@ -411,4 +418,101 @@ extern "C" int ref_dispatch(const void* sv, const uint32_t* sf, const uint32_t* 
     if (workdir && chdir(cwd) != 0)
         return -1002;
     return (int)err;
+}
+
+// One mesh's halfedge mesh and input checks, step for step as the
+// single-threaded branch of client_input_arrays_to_hmesh (preproc.cpp:390-460)
+// and check_input_mesh (preproc.cpp:505-579) run them; the connectivity is the
+// reference's own hmesh_t, read back through its public accessors.
+extern "C" int ref_hmesh(const uint32_t* f, const uint32_t* fs, uint32_t nv, uint32_t nf, hm_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    out->bad_face = -1;
+    hmesh_t m;
+    for (uint32_t v = 0; v < nv; ++v)
+        m.add_vertex(0.0, 0.0, 0.0);
+    uint64_t o = 0;
+    int st = HM_OK;
+    std::vector<vd_t> fv;
+    for (uint32_t i = 0; i < nf && st == HM_OK; ++i) {
+        const uint32_t n = fs ? fs[i] : 3;
+        if (n < 3) { st = HM_FACE_SIZE; out->bad_face = (int32_t)i; break; }
+        fv.clear();
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint32_t idx = f[o + j];
+            if (idx >= nv) { st = HM_INDEX_RANGE; break; }
+            const vd_t d(idx);
+            if (std::find(fv.cbegin(), fv.cend(), d) != fv.cend()) { st = HM_DUPLICATE_INDEX; break; }
+            fv.push_back(d);
+        }
+        if (st == HM_OK && m.add_face(fv) == hmesh_t::null_face())
+            st = HM_NON_MANIFOLD;
+        if (st != HM_OK)
+            out->bad_face = (int32_t)i;
+        o += n;
+    }
+    fflush(stdout); // add_face reports a non-manifold face on stdout
+    out->status = st;
+    if (st != HM_OK)
+        return 0;
+    const uint32_t ne = (uint32_t)m.number_of_edges();
+    out->n_edges = ne;
+    const size_t nh = 2 * (size_t)ne;
+    out->he_target = (uint32_t*)malloc(4 * (nh ? nh : 1));
+    out->he_face = (int32_t*)malloc(4 * (nh ? nh : 1));
+    out->he_next = (int32_t*)malloc(4 * (nh ? nh : 1));
+    out->he_prev = (int32_t*)malloc(4 * (nh ? nh : 1));
+    if ((size_t)m.number_of_halfedges() != nh)
+        return -1;
+    for (uint32_t e = 0; e < ne; ++e)
+        if ((uint32_t)m.halfedge(ed_t(e), 0) != 2 * e || (uint32_t)m.halfedge(ed_t(e), 1) != 2 * e + 1)
+            return -2;
+    for (size_t h = 0; h < nh; ++h) {
+        const hd_t hd((uint32_t)h);
+        out->he_target[h] = (uint32_t)m.target(hd);
+        const fd_t fd = m.face(hd);
+        out->he_face[h] = fd == hmesh_t::null_face() ? -1 : (int32_t)fd;
+        const hd_t nx = m.next(hd), pv = m.prev(hd);
+        out->he_next[h] = nx == hmesh_t::null_halfedge() ? -1 : (int32_t)nx;
+        out->he_prev[h] = pv == hmesh_t::null_halfedge() ? -1 : (int32_t)pv;
+    }
+    out->corner_he = (uint32_t*)malloc(4 * (o ? o : 1));
+    o = 0;
+    for (uint32_t i = 0; i < nf; ++i) {
+        const std::vector<hd_t>& hs = m.get_halfedges_around_face(fd_t(i));
+        for (size_t j = 0; j < hs.size(); ++j)
+            out->corner_he[o + j] = (uint32_t)hs[j];
+        o += hs.size();
+    }
+    out->v_off = (uint32_t*)calloc((size_t)nv + 1, 4);
+    out->v_he = (uint32_t*)malloc(4 * (nh ? nh : 1));
+    for (uint32_t v = 0; v < nv; ++v) {
+        const std::vector<hd_t>& hs = m.get_halfedges_around_vertex(vd_t(v));
+        out->v_off[v + 1] = out->v_off[v] + (uint32_t)hs.size();
+        for (size_t j = 0; j < hs.size(); ++j)
+            out->v_he[out->v_off[v] + j] = (uint32_t)hs[j];
+    }
+    if (nv < 3 || nf < 1) {
+        out->status = HM_TOO_SMALL;
+        return 0;
+    }
+    thread_pool pool(1, 0);
+    std::vector<int> fccmap, ccv, ccf;
+    const int nc = find_connected_components(pool, fccmap, m, ccv, ccf);
+    out->n_components = (uint32_t)nc;
+    if (nc != 1)
+        out->status = HM_COMPONENTS;
+    return 0;
+}
+
+extern "C" void ref_hmesh_free(hm_result* r)
+{
+    free(r->he_target);
+    free(r->he_face);
+    free(r->he_next);
+    free(r->he_prev);
+    free(r->corner_he);
+    free(r->v_off);
+    free(r->v_he);
+    memset(r, 0, sizeof(*r));
 }
