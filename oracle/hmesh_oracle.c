@@ -7,7 +7,8 @@
  * checks of check_input_mesh (preproc.cpp:505-579): at least 3 vertices, at
  * least one face, exactly one connected component of the vertex graph
  * (find_connected_components, kernel.cpp:235-364; a vertex no face uses is a
- * component of its own).
+ * component of its own), and whether the mesh is closed (mesh_is_closed,
+ * preproc.cpp:1957-1994).
  *
  * TEST INFRASTRUCTURE ONLY: the checker for a device edge table and validity
  * pass; the product library never links it. tests/test_hmesh_oracle.py pins
@@ -147,6 +148,10 @@ int oracle_hmesh(const uint32_t *f, const uint32_t *fs, uint32_t nv, uint32_t nf
         }
         free(cur);
     }
+    /* mesh_is_closed (preproc.cpp:1957-1994): no halfedge without a face */
+    out->closed = 1;
+    for (uint32_t h = 0; h < 2 * ne; ++h)
+        if (out->he_face[h] < 0) { out->closed = 0; break; }
     /* check_input_mesh (preproc.cpp:505-579) */
     if (nv < 3 || nf < 1) { out->status = HM_TOO_SMALL; return 0; }
     uint32_t *p = (uint32_t *)malloc(4 * (size_t)nv);

@@ -71,6 +71,7 @@ typedef struct hm_result {
     int32_t bad_face;       /* the face a conversion error stopped at, else -1 */
     uint32_t n_edges;       /* this and the arrays: set once the conversion succeeded */
     uint32_t n_components;
+    int32_t closed;         /* every halfedge has a face (mesh_is_closed, preproc.cpp:1957-1994) */
     uint32_t *he_target;    /* [2*n_edges] */
     int32_t *he_face;       /* [2*n_edges], -1 = no face */
     int32_t *he_next;       /* [2*n_edges], -1 = unlinked */

@@ -179,7 +179,7 @@ HM_OK, HM_FACE_SIZE, HM_INDEX_RANGE, HM_DUPLICATE_INDEX, HM_NON_MANIFOLD, HM_TOO
 class HmResult(C.Structure):
     _fields_ = [
         ("status", C.c_int32), ("bad_face", C.c_int32), ("n_edges", C.c_uint32), ("n_components", C.c_uint32),
-        ("he_target", C.POINTER(C.c_uint32)), ("he_face", C.POINTER(C.c_int32)),
+        ("closed", C.c_int32), ("he_target", C.POINTER(C.c_uint32)), ("he_face", C.POINTER(C.c_int32)),
         ("he_next", C.POINTER(C.c_int32)), ("he_prev", C.POINTER(C.c_int32)),
         ("corner_he", C.POINTER(C.c_uint32)), ("v_off", C.POINTER(C.c_uint32)), ("v_he", C.POINTER(C.c_uint32)),
     ]
@@ -189,7 +189,8 @@ def hmesh(f, fs, nv: int, impl: str = "port"):
     """One mesh's halfedge mesh and input checks (the connectivity MCUT builds
     from the caller's arrays): status, failing face, edges, and per halfedge
     its target / face / next / prev, per face corner its halfedge, per vertex
-    the halfedges ending there (CSR), the connected-component count."""
+    the halfedges ending there (CSR), the connected-component count and
+    whether every halfedge has a face."""
     lib, _, _ = _lib(impl)
     fn = lib.oracle_hmesh if impl == "port" else lib.ref_hmesh
     fr = lib.oracle_hmesh_free if impl == "port" else lib.ref_hmesh_free
@@ -204,7 +205,7 @@ def hmesh(f, fs, nv: int, impl: str = "port"):
     if rc != 0:
         raise RuntimeError(f"{impl} hmesh failed rc={rc}")
     out = dict(status=int(res.status), bad_face=int(res.bad_face), n_edges=int(res.n_edges),
-               n_components=int(res.n_components))
+               n_components=int(res.n_components), closed=bool(res.closed))
     if res.status in (HM_OK, HM_TOO_SMALL, HM_COMPONENTS):
         nh = 2 * res.n_edges
         out.update(

@@ -23,7 +23,8 @@
 //                   own hmesh_t::add_vertex / add_face, preceded by the face
 //                   checks of client_input_arrays_to_hmesh, preproc.cpp:390-460)
 //                   and check_input_mesh's outcome (preproc.cpp:505-579, with
-//                   the reference's find_connected_components), read back
+//                   the reference's find_connected_components) and
+//                   mesh_is_closed (preproc.cpp:1957-1994), read back
 //                   through hmesh_t's public accessors.
 #include <mcut/mcut.h>
 #include <mcut/internal/bvh.h>
@@ -52,6 +53,7 @@ bool calculate_vertex_parameters(double& quantization_multiplier, vec3_<double>&
     vec3_<double>& cutmesh_bboxmin, vec3_<double>& cutmesh_bboxmax, McFlags dispatchFlags,
     const void* pSrcMeshVertices, McUint32 numSrcMeshVertices, const void* pCutMeshVertices,
     McUint32 numCutMeshVertices);
+bool mesh_is_closed(const hmesh_t& mesh);
 bool determine_three_noncollinear_vertices(int& i, int& j, int& k, const std::vector<vec3>& polygon_vertices,
     const vec3& polygon_normal, const int polygon_normal_largest_component, const double multiplier);
 
@@ -492,6 +494,7 @@ extern "C" int ref_hmesh(const uint32_t* f, const uint32_t* fs, uint32_t nv, uin
         for (size_t j = 0; j < hs.size(); ++j)
             out->v_he[out->v_off[v] + j] = (uint32_t)hs[j];
     }
+    out->closed = mesh_is_closed(m) ? 1 : 0;
     if (nv < 3 || nf < 1) {
         out->status = HM_TOO_SMALL;
         return 0;

@@ -8,7 +8,8 @@ rejects (preproc.cpp:505-579). Against the reference's own hmesh_t (harness,
 where the reference checkout exists) it must agree on the status, the face
 a conversion error stops at, the edge count, and per halfedge its target,
 face, next and prev, per face corner its halfedge, per vertex its halfedge
-list and the component count: on every fixture mesh, the polygon soups the
+list, the component count and closedness (mesh_is_closed,
+preproc.cpp:1957-1994): on every fixture mesh, the polygon soups the
 front end numbers its edges in, seeded random meshes, and seeded corruptions
 of each kind MCUT rejects.
 
@@ -108,9 +109,10 @@ def parallel_hmesh(f, fs, nv):
     rep = np.zeros(m, bool)
     rep[oh[1:]] = h[oh][1:] == h[oh][:-1]
     if rep.any():
-        return dict(status=oracle.HM_NON_MANIFOLD, bad_face=int(face[rep].min()), n_edges=0, n_components=0)
+        return dict(status=oracle.HM_NON_MANIFOLD, bad_face=int(face[rep].min()), n_edges=0, n_components=0,
+                    closed=False)
     if bad_code != oracle.HM_OK:
-        return dict(status=bad_code, bad_face=bad_face, n_edges=0, n_components=0)
+        return dict(status=bad_code, bad_face=bad_face, n_edges=0, n_components=0, closed=False)
     ne = int(is_first.sum())
     he_target = np.empty(2 * ne, np.int64)
     he_target[2 * eid_at_slot[first_slot]] = v1[first_slot]
@@ -123,7 +125,8 @@ def parallel_hmesh(f, fs, nv):
     he_prev[h[nxt]] = h
     # each vertex's halfedges in creation order = ascending halfedge id per target
     v_off = np.concatenate([[0], np.cumsum(np.bincount(he_target, minlength=nv))])
-    out = dict(status=oracle.HM_OK, bad_face=-1, n_edges=ne, n_components=0, he_target=he_target,
+    out = dict(status=oracle.HM_OK, bad_face=-1, n_edges=ne, n_components=0, closed=bool(np.all(he_face >= 0)),
+               he_target=he_target,
                he_face=he_face, he_next=he_next, he_prev=he_prev, corner_he=h, v_off=v_off,
                v_he=np.argsort(he_target, kind="stable"))
     if nv < 3 or nf < 1:
@@ -149,7 +152,7 @@ def parallel_hmesh(f, fs, nv):
 
 
 def _same(a, b):
-    for k in ("status", "bad_face", "n_edges", "n_components"):
+    for k in ("status", "bad_face", "n_edges", "n_components", "closed"):
         assert a[k] == b[k], (k, a[k], b[k])
     for k in ARRAYS:
         if k in a or k in b:
@@ -259,3 +262,13 @@ def test_corrupted_inputs(name):
     assert kinds["two_components"] == {oracle.HM_COMPONENTS}
     assert kinds["unused_vertex"] == {oracle.HM_COMPONENTS}
     assert kinds["no_face"] == {oracle.HM_TOO_SMALL}
+
+
+def test_closedness():
+    """A sphere is closed, a height-field grid is not; the soup of the two is
+    not (the grid's border halfedges have no face)."""
+    c = CASES["sphere_hf_small"]
+    for m, want in ((c["src"], True), (c["cut"], False)):
+        f, fs = _faces(m)
+        assert _check(f, fs, len(m["v"]))["closed"] is want
+    assert _check(*soup(c["src"], c["cut"]))["closed"] is False
