@@ -7,6 +7,7 @@ field. This also compiles the public header as plain C99.
 """
 import ctypes as C
 import os
+import re
 import shutil
 import subprocess
 
@@ -25,9 +26,16 @@ STRUCTS = [
 ]
 
 
+def _header_constants():
+    with open(L.HEADER) as fh:
+        return sorted(set(re.findall(r"\bMCGPU_[A-Z0-9_]+\b", fh.read())))
+
+
 def _c_layout():
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "mcut_gb300.h"', '#include "mcut_oracle.h"',
              "int main(void) {"]
+    for name in _header_constants():
+        lines.append(f'  printf("{name} %llu\\n", (unsigned long long)({name}));')
     for cname, cls in STRUCTS:
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
         for field, _ in cls._fields_:
@@ -56,3 +64,20 @@ def test_ctypes_structs_match_the_c_layout():
         for field, _ in cls._fields_:
             d = getattr(cls, field)
             assert lay[f"{cname}.{field}"] == (d.offset, d.size), (cname, field)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_python_constants_match_the_header():
+    """Every status, flag, data query and stage the header names has the same
+    value in the Python host."""
+    lay = _c_layout()
+    checked = 0
+    for name in _header_constants():
+        short = name[len("MCGPU_"):]
+        if short.startswith("STAGE_"):
+            want = L.STAGES.index(short[len("STAGE_"):].lower())
+        else:
+            want = getattr(L, short)
+        assert lay[name] == (want,), name
+        checked += 1
+    assert checked == len(_header_constants()) >= 30
