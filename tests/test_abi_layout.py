@@ -31,10 +31,15 @@ def _header_constants():
         return sorted(set(re.findall(r"\bMCGPU_[A-Z0-9_]+\b", fh.read())))
 
 
+def _oracle_constants():
+    with open(os.path.join(ROOT, "oracle", "mcut_oracle.h")) as fh:
+        return sorted(set(re.findall(r"\b(?:FE|HM)_[A-Z0-9_]+\b", fh.read())))
+
+
 def _c_layout():
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "mcut_gb300.h"', '#include "mcut_oracle.h"',
              "int main(void) {"]
-    for name in _header_constants():
+    for name in _header_constants() + _oracle_constants():
         lines.append(f'  printf("{name} %llu\\n", (unsigned long long)({name}));')
     for cname, cls in STRUCTS:
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
@@ -81,3 +86,12 @@ def test_python_constants_match_the_header():
         assert lay[name] == (want,), name
         checked += 1
     assert checked == len(_header_constants()) >= 30
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="no C compiler")
+def test_oracle_constants_match_its_header():
+    lay = _c_layout()
+    names = _oracle_constants()
+    for name in names:
+        assert lay[name] == (getattr(oracle, name),), name
+    assert len(names) >= 12
