@@ -135,3 +135,41 @@ def test_differences_outside_the_range_escalate():
         a, b, c, d = (scale * rng.standard_normal((2000, 3)) for _ in range(4))
         decided, _, ok = filter_sign(a, b, c, d)
         assert not ok.any() and not decided.any()
+
+
+def _f32_input_bits(d):
+    """f32_filter_input's integer rounding of one fp64 difference (the device
+    forms the fp32 bits from the fp64 bits), restated on Python integers:
+    (in range, fp32 bits)."""
+    b = int(np.float64(d).view(np.uint64))
+    if (b << 1) & ((1 << 64) - 1) == 0:
+        return True, 0
+    e = (b >> 52) & 0x7FF
+    if e < 1023 - 40 or e > 1023 + 40:
+        return False, None
+    m = b & 0xFFFFFFFFFFFFF
+    fb = ((b >> 63) << 31) | ((e - 1023 + 127) << 23) | (m >> 29)
+    r = m & 0x1FFFFFFF
+    if r > 0x10000000 or (r == 0x10000000 and (fb & 1)):
+        fb += 1
+    return True, fb
+
+
+def test_input_rounding_is_ieee_to_nearest_even():
+    """The device's bitwise fp64 -> fp32 rounding equals the IEEE conversion
+    the numpy restatement uses, ties and mantissa carries included."""
+    rng = np.random.default_rng(17)
+    e = rng.integers(1023 - 40, 1023 + 41, size=20000).astype(np.uint64)
+    m = rng.integers(0, 1 << 52, size=20000, dtype=np.uint64)
+    m[:4000] = (m[:4000] & ~np.uint64(0x1FFFFFFF)) | np.uint64(0x10000000)  # exact ties
+    m[4000:6000] = np.uint64((1 << 52) - 1)  # rounds up into the exponent
+    sgn = rng.integers(0, 2, size=20000).astype(np.uint64)
+    d = ((sgn << np.uint64(63)) | (e << np.uint64(52)) | m).view(np.float64)
+    want = d.astype(np.float32).view(np.uint32)
+    for x, w in zip(d, want):
+        ok, bits = _f32_input_bits(x)
+        assert ok and bits == int(w), x
+    for x in (0.0, -0.0):
+        assert _f32_input_bits(x) == (True, 0)
+    for x in (2.0 ** -41, -(2.0 ** 41), 2.0 ** 60, 5e-324):
+        assert _f32_input_bits(x)[0] is False
