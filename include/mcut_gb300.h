@@ -122,7 +122,8 @@ typedef struct mcgpu_summary {
 
 /* mcgpu_get_data queries */
 typedef enum mcgpu_data {
-    MCGPU_DATA_RECORD_IDS = 1,    /* uint32[5*R]: q, r, tested face, f0, f1 (edge creation order, then face) */
+    MCGPU_DATA_RECORD_IDS = 1,    /* uint32[5*R]: q, r, tested face, f0, f1, ordered by the edge's first
+                                     face corner in the source-then-cut face arrays, then face */
     MCGPU_DATA_RECORD_POINTS = 2, /* double[3*R]: intersection points (recentred coordinates) */
     MCGPU_DATA_PAIRS = 3,         /* uint32[2*P]: (source face, cut face); MCGPU_KEEP_PAIRS */
     MCGPU_DATA_TESTS = 4,         /* uint32[3*T]: q, r, face; MCGPU_KEEP_TESTS */

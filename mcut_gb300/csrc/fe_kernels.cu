@@ -2225,8 +2225,9 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
 int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
 {
     if (nrec == 0) return 0;
-    // key = halfedge slot (edge creation order), then face: both global and
-    // monotone in the pair index, so records come out grouped by pair. The
+    // key = halfedge slot (the edge's first face corner in the source-then-cut
+    // face arrays), then face: both global and monotone in the pair index,
+    // so records come out grouped by pair. The
     // key is packed to the bits the ids need, which sets the radix passes.
     const uint32_t nidx = P.all_triangles ? 3u * P.nf : 0xFFFFFFFFu;
     const int sbits = nidx == 0xFFFFFFFFu ? 32 : 32 - __builtin_clz(nidx | 1u);

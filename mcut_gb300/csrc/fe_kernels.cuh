@@ -38,7 +38,7 @@ struct Test {
     uint32_t q, r;    // oriented edge (global vertex ids)
     uint32_t g;       // tested face (global)
     uint32_t f0, f1;  // faces of the edge (f0: lowest, owns the orientation), f1 may be kNone
-    uint32_t slot;    // halfedge slot of q->r in f0 (edge creation order)
+    uint32_t slot;    // halfedge slot of q->r in f0: the edge's first face corner
 };
 
 struct Problem {

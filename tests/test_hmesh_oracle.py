@@ -273,3 +273,33 @@ def test_closedness():
         f, fs = _faces(m)
         assert _check(f, fs, len(m["v"]))["closed"] is want
     assert _check(*soup(c["src"], c["cut"]))["closed"] is False
+
+
+def test_record_order_key_against_the_soup_edge_numbering():
+    """The device orders records by the slot of the edge's first face corner in
+    the source-then-cut face arrays (then face). On source-mesh edges that is
+    MCUT's edge numbering in the soup. Cut faces re-enter the soup rotated by
+    one, so their edges are numbered in a cyclic shift of the corner order.
+    This test checks both statements on every fixture with records."""
+    for name, c in sorted(CASES.items()):
+        if not len(c["rec_ids"]):
+            continue
+        src, cut = c["src"], c["cut"]
+        f, fs, nv = soup(src, cut)
+        r = oracle.hmesh(f, fs, nv, "port")
+        eid = {(int(r["he_target"][2 * e + 1]), int(r["he_target"][2 * e])): e for e in range(r["n_edges"])}
+        nsv = len(src["v"])
+        raw = np.concatenate([np.asarray(src["f"], np.int64), np.asarray(cut["f"], np.int64) + nsv])
+        n = (np.full(len(raw) // 3, 3) if src.get("fs") is None and cut.get("fs") is None else
+             np.concatenate([np.full(len(src["f"]) // 3, 3) if src.get("fs") is None else np.asarray(src["fs"]),
+                             np.full(len(cut["f"]) // 3, 3) if cut.get("fs") is None else np.asarray(cut["fs"])]))
+        first, o = {}, 0
+        for k in n:
+            for j in range(int(k)):
+                a, b = int(raw[o + j]), int(raw[o + (j + 1) % int(k)])
+                first.setdefault((min(a, b), max(a, b)), o + j)
+            o += int(k)
+        src_recs = [(int(q), int(rr), int(g)) for q, rr, g in c["rec_ids"] if int(q) < nsv]
+        by_slot = sorted(src_recs, key=lambda t: (first[(min(t[0], t[1]), max(t[0], t[1]))], t[2]))
+        by_edge = sorted(src_recs, key=lambda t: (eid[(t[0], t[1])], t[2]))
+        assert by_slot == by_edge, name
