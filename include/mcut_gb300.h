@@ -52,7 +52,8 @@ typedef enum mcgpu_status {
     MCGPU_GP_VIOLATION = 1,        /* touching / on-edge / on-vertex configuration */
     MCGPU_DEGENERATE_SRC_FACE = 2, /* a candidate source face has |Newell n|^2 < 1e-9 */
     MCGPU_DEGENERATE_CUT_FACE = 3,
-    MCGPU_INVALID_INPUT = 4,       /* face size < 3, index out of range, non-manifold edge */
+    MCGPU_INVALID_INPUT = 4,       /* a face with fewer than 3 vertices or an index out of range;
+                                      MCUT's other input checks run before the seam */
     MCGPU_CUDA_ERROR = 5,
     MCGPU_OUT_OF_MEMORY = 6,
     MCGPU_INVALID_VALUE = 7,       /* bad argument (null pointer, unknown query, ...) */

@@ -20,7 +20,7 @@ enum : uint32_t {
     ST_OVERFLOW_PAIRS = 2u,   // candidate-pair buffer too small
     ST_OVERFLOW_TESTS = 4u,   // edge-face test buffer too small
     ST_STACK = 8u,            // traversal stack overflow (re-run deep)
-    ST_INVALID = 16u,         // invalid input (index out of range, non-manifold)
+    ST_INVALID = 16u,         // invalid input (a vertex index out of range)
 };
 
 // ---------------------------------------------------------------------------
