@@ -56,11 +56,12 @@ def std_sort_orders(arrays):
 
 # ---- the device's replay (t_std_sort and its helpers), on [value, index] lists ----
 
-def tless(a, b):
+def by_magnitude(a, b):
+    """The device's tless: larger |value| first."""
     return abs(a[0]) > abs(b[0])
 
 
-def ins_sort(f, lo, n):
+def ins_sort(f, lo, n, tless):
     for i in range(lo + 1, lo + n):
         v = f[i]
         if tless(v, f[lo]):
@@ -74,7 +75,7 @@ def ins_sort(f, lo, n):
             f[j] = v
 
 
-def unguarded_ins(f, frm, n):
+def unguarded_ins(f, frm, n, tless):
     for i in range(frm, n):
         v = f[i]
         j = i
@@ -84,7 +85,7 @@ def unguarded_ins(f, frm, n):
         f[j] = v
 
 
-def median(f, r, a, b, c):
+def median(f, r, a, b, c, tless):
     def sw(x, y):
         f[x], f[y] = f[y], f[x]
     if tless(f[a], f[b]):
@@ -102,7 +103,7 @@ def median(f, r, a, b, c):
         sw(r, b)
 
 
-def sift(f, base, hole, length, v):
+def sift(f, base, hole, length, v, tless):
     top = hole
     child = hole
     while child < (length - 1) // 2:
@@ -123,23 +124,23 @@ def sift(f, base, hole, length, v):
     f[base + hole] = v
 
 
-def heap_sort(f, base, n, log):
+def heap_sort(f, base, n, log, tless):
     log.append("heap")
     if n < 2:
         return
     par = (n - 2) // 2
     while True:
-        sift(f, base, par, n, f[base + par])
+        sift(f, base, par, n, f[base + par], tless)
         if par == 0:
             break
         par -= 1
     for last in range(n - 1, 0, -1):
         v = f[base + last]
         f[base + last] = f[base]
-        sift(f, base, 0, last, v)
+        sift(f, base, 0, last, v, tless)
 
 
-def device_sort(values, log=None):
+def device_sort(values, log=None, tless=by_magnitude):
     log = [] if log is None else log
     f = [[float(v), i] for i, v in enumerate(values)]
     n = len(f)
@@ -150,12 +151,12 @@ def device_sort(values, log=None):
     while True:
         while length > 16:
             if depth == 0:
-                heap_sort(f, off, length, log)
+                heap_sort(f, off, length, log, tless)
                 length = 0
                 break
             depth -= 1
             mid = length // 2
-            median(f, off, off + 1, off + mid, off + length - 1)
+            median(f, off, off + 1, off + mid, off + length - 1, tless)
             lo, hi = 1, length
             while True:
                 while tless(f[off + lo], f[off]):
@@ -174,10 +175,10 @@ def device_sort(values, log=None):
             break
         off, length, depth = stack.pop()
     if n > 16:
-        ins_sort(f, 0, 16)
-        unguarded_ins(f, 16, n)
+        ins_sort(f, 0, 16, tless)
+        unguarded_ins(f, 16, n, tless)
     else:
-        ins_sort(f, 0, n)
+        ins_sort(f, 0, n, tless)
     return [x[1] for x in f]
 
 
@@ -207,14 +208,8 @@ def killer(n):
             state["candidate"] = y
         return val[x] < val[y]
 
-    global tless
-    saved = tless
     # descending by |v| sorts larger first: "a before b" == a has the larger key
-    tless = lambda a, b: cmp_less(b, a)  # noqa: E731
-    try:
-        device_sort(list(range(n)))
-    finally:
-        tless = saved
+    device_sort(list(range(n)), tless=lambda a, b: cmp_less(b, a))
     for i in range(n):
         if val[i] == gas:
             freeze(i)
