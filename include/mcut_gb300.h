@@ -238,17 +238,20 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
 
 /* Front-end dispatch that allocates no GPU or pinned memory. No counterpart
  * in the reference (MCUT allocates freely on the host). It is for callers
- * that may not call cudaMalloc when they need the records: a thread that is
- * recording a CUDA graph on its stream, a plugin that must stay inside its
- * host application's own memory arena, a frame loop that cannot wait on the
- * driver's allocator. All scratch sits in one file-scope __device__ array of
- * about 12 MB that every GPU loading this library keeps until exit.
+ * that may not call cudaMalloc when they need the records: a plugin that must
+ * stay inside its host application's own device-memory arena, a process whose
+ * device memory another framework's caching allocator already holds, a frame
+ * loop that cannot wait on the driver's allocator. All scratch sits in one
+ * file-scope __device__ array of about 12 MB that every GPU loading this
+ * library keeps until exit. The call reads counters back into host variables
+ * between its stages, so it waits for `stream` three or four times and
+ * returns when its GPU work is done.
  * Limits: triangles only; at most 16384 vertices and 16384 faces over both
  * meshes, 32768 candidate pairs, 65536 edge-face tests -- anything larger
  * returns MCGPU_TOO_LARGE. Every call shares that array and it keeps the
  * previous call's contents (each call clears what it needs): calls whose GPU
  * work overlaps race, so serialise them. The first call on a device looks up
- * the array's address; make it outside any stream capture.
+ * the array's address; make it before any stream capture begins.
  * src/cut: DEVICE pointers to internal (recentred) double coordinates and
  * uint32 triangle indices (face_sizes NULL). record_ids (uint32[5*capacity])
  * and record_points (double[3*capacity]) are device buffers filled as

@@ -716,6 +716,7 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     Problem& Pin = c->Pin;
     Pin = P;
     c->W.fidx_out = c->W.face_pair_out = nullptr;
+    c->W.fidx_fix = n > 1 ? fidx : nullptr;
     if (n == 1) {
         Pin.fidx = split ? srcs[0].face_indices : fidx;
         Pin.face_pair = nullptr;
@@ -1048,7 +1049,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
                 deep = deep || stack;
                 ck(cudaMemsetAsync(W.counters, 0, 64, s), "memset");
                 ck(cudaMemsetAsync(W.cand, 0, L.nf, s), "memset");
-                ck(cudaMemsetAsync(W.pair_status, 0, 4 * (size_t)n, s), "memset");
+                // the traversal's bits go; the bounds kernel's ST_INVALID stays
+                launch_clear_status(W.pair_status, n, ST_STACK | ST_OVERFLOW_PAIRS, s);
                 launch_packets(P, W, src_buf, s);
                 launch_traverse(P, W, src_buf, cut_buf, deep, s);
                 ck(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s), "D2H counters");

@@ -196,7 +196,8 @@ template <typename K>
 __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __restrict__ fbox,
     float* __restrict__ fbox32, const float4* __restrict__ frame, K* __restrict__ skey, uint32_t* __restrict__ sval,
     K* __restrict__ ckey, uint32_t* __restrict__ cval, int mesh_bit, uint32_t* __restrict__ pair_status,
-    uint8_t* __restrict__ cand, uint32_t* __restrict__ fidx_out, uint32_t* __restrict__ face_pair_out)
+    uint8_t* __restrict__ cand, uint32_t* __restrict__ fidx_out, uint32_t* __restrict__ face_pair_out,
+    uint32_t* fidx_fix)
 {
     for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
         cand[f] = 0; // no candidate pair yet (the traversal sets it)
@@ -205,7 +206,11 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         const uint32_t p = fp & ~kCutBit;
         const bool is_cut = (fp & kCutBit) != 0;
         const uint32_t o = face_o(P, f), n = face_n(P, f);
-        const uint32_t vlo = P.pair_vbase[p], vhi = P.pair_vbase[p + 1];
+        // an index must name a vertex of the face's own mesh (preproc.cpp:390-460
+        // checks each mesh's indices against its own vertex count); a cut index
+        // that wrapped when offset by the source count lands below this range
+        const uint32_t vmid = P.pair_vbase[p] + P.pair_vs[p];
+        const uint32_t vlo = is_cut ? vmid : P.pair_vbase[p], vhi = is_cut ? P.pair_vbase[p + 1] : vmid;
         // std::min / std::max folds from +-DBL_MAX in vertex order: each
         // running extreme is kept with its dkey(), so a step converts only
         // the new coordinate; a strict compare keeps the first of equal keys,
@@ -220,9 +225,16 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         }
         bool bad = false;
         for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t v = fidx_at(P, o + k);
+            uint32_t v = fidx_at(P, o + k);
+            if (v < vlo || v >= vhi) {
+                // the pair's outcome is MCGPU_INVALID_INPUT; every later kernel
+                // reads the index table, so it gets the mesh's first vertex in place
+                // of the bad index and no access leaves the vertex array
+                bad = true;
+                v = vlo;
+                if (fidx_fix) fidx_fix[o + k] = v;
+            }
             if (fidx_out) fidx_out[o + k] = v;
-            if (v < vlo || v >= vhi) { bad = true; continue; }
             double x[3];
             load_v(P, v, x);
             for (int j = 0; j < 3; ++j) {
@@ -2013,6 +2025,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_records(Problem P, const uint
     }
 }
 
+// clear status bits of every pair (a rerun of a stage clears that stage's own
+// bits and keeps the others, e.g. the bounds kernel's ST_INVALID)
+__global__ void k_clear_status(uint32_t* __restrict__ st, uint32_t n, uint32_t mask)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) st[p] &= ~mask;
+}
+
 static int sm_count()
 {
     static int sms = 0;
@@ -2055,10 +2074,11 @@ void launch_bounds_morton(const Problem& P, const Problem& Pin, Work& W, bool wi
     if (wide)
         k_face_bounds<unsigned long long><<<g, kBlock, 0, s>>>(Pin, W.fbox, W.fbox32, frame,
             (unsigned long long*)W.skeys[0], W.svals[0], (unsigned long long*)W.ckeys[0], W.cvals[0], key_bits,
-            W.pair_status, W.cand, W.fidx_out, W.face_pair_out);
+            W.pair_status, W.cand, W.fidx_out, W.face_pair_out, W.fidx_fix);
     else
         k_face_bounds<uint32_t><<<g, kBlock, 0, s>>>(Pin, W.fbox, W.fbox32, frame, (uint32_t*)W.skeys[0], W.svals[0],
-            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status, W.cand, W.fidx_out, W.face_pair_out);
+            (uint32_t*)W.ckeys[0], W.cvals[0], key_bits, W.pair_status, W.cand, W.fidx_out, W.face_pair_out,
+            W.fidx_fix);
 }
 
 int launch_sort(const Problem& P, Work& W, bool wide, int key_bits, cudaStream_t s, int& cut_buf)
@@ -2217,6 +2237,12 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     k_narrow_hits<<<gh, kNarrowHitsBlock, 0, s>>>(P, W.tests, hits, W.test_cap, W.plane_slot,
         (const FacePlane*)W.planes, keep_tests ? 1 : 0, W.test_info, W.rec_key[0], W.rec_val[0], W.rec_pt_raw, W.counters, W.pair_status,
         W.pair_bad);
+}
+
+void launch_clear_status(uint32_t* pair_status, uint32_t n_pairs, uint32_t mask, cudaStream_t s)
+{
+    g_launches++;
+    k_clear_status<<<grid_for(n_pairs), kBlock, 0, s>>>(pair_status, n_pairs, mask);
 }
 
 // Records up to kRankSortMax are ordered by k_rank_records (one launch). With

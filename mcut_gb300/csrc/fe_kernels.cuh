@@ -75,6 +75,8 @@ struct Work {
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
     uint32_t* fidx_out;               // one pair: the bounds kernel writes the global ps indices here
     uint32_t* face_pair_out;          // ... and the face -> pair table (null for a batch: k_prep made them)
+    uint32_t* fidx_fix;               // a batch: the global table the bounds kernel reads, where it replaces an
+                                      // index outside its mesh (null for one pair: fidx_out gets the fix)
     void* mesh_frame;                 // [n_pairs*2*2] float4: fp32 box low corner, 1023 / extent
     // sort buffers (keys u32 for one pair, u64 for batches); the cut keys and
     // values follow the source ones in the same arrays (ckeys[b] = skeys[b] + ns)
@@ -146,6 +148,8 @@ void launch_incidence(const Problem& P, Work& W, cudaStream_t s);        // vert
 void launch_tests(const Problem& P, Work& W, cudaStream_t s);
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s);
 int launch_records(const Problem& P, Work& W, uint32_t n_records, cudaStream_t s);
+// clears `mask` in every pair's status bits
+void launch_clear_status(uint32_t* pair_status, uint32_t n_pairs, uint32_t mask, cudaStream_t s);
 // record ordering from the device's record count (at most cap = kRankSortMax
 // records; above cap nothing is written); returns the sorted-key buffer
 int launch_records_dev(const Problem& P, Work& W, uint32_t cap, cudaStream_t s);

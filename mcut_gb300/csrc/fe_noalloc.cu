@@ -2,11 +2,12 @@
 // allocate GPU memory.
 //
 // Who needs it: code that may not call cudaMalloc at the moment it wants the
-// intersection records -- a host thread that is recording a CUDA graph on its
-// stream (allocation calls are not allowed while a capture is open), a plugin
-// living inside an application that hands out device memory only through its
-// own arena and treats any other allocation as a leak, or a frame loop with a
-// hard latency budget that must never wait on the driver's allocator.
+// intersection records -- a plugin living inside an application that hands
+// out device memory only through its own arena and treats any other
+// allocation as a leak, a process whose device memory another framework's
+// caching allocator has already reserved (a fresh cudaMalloc would fail
+// there), or a frame loop with a hard latency budget that must never wait on
+// the driver's allocator (cudaMalloc and cudaFree can wait for the device).
 //
 // What it does instead: every scratch buffer of the front end (face boxes,
 // sort keys, tree nodes, candidate pairs, planes, incidence, edge-face tests,
@@ -16,7 +17,8 @@
 // pointers to the internal, recentred coordinates and triangle indices) and
 // the outputs (device buffers for the records). No cudaMalloc, cudaFree,
 // cudaMallocHost or allocating library call is made; status readbacks copy
-// into host stack variables.
+// into host stack variables, so the call waits for its stream three or four
+// times and returns when its GPU work is done.
 //
 // Limits (anything larger is rejected with MCGPU_TOO_LARGE before any GPU
 // work): triangles only, at most kMaxVerts vertices and kMaxFaces faces over
@@ -31,8 +33,8 @@
 //
 // Set-up: the device address of the array is looked up with
 // cudaGetSymbolAddress the first time the entry point runs on a device (with
-// that device current) and cached. Make that first call outside any stream
-// capture.
+// that device current) and cached. Make that first call before any stream
+// capture begins.
 #include <cstring>
 #include <mutex>
 
@@ -141,9 +143,11 @@ int na_fail(mcgpu_summary* out, int code)
 extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
     uint32_t* record_ids, double* record_points, uint64_t record_capacity, mcgpu_summary* out)
 {
-    if (!src || !cut || !src->vertices || !src->face_indices || !cut->vertices || !cut->face_indices)
-        return MCGPU_INVALID_VALUE;
     if (out) memset(out, 0, sizeof(*out));
+    if (!src || !cut || !src->vertices || !src->face_indices || !cut->vertices || !cut->face_indices)
+        return na_fail(out, MCGPU_INVALID_VALUE);
+    // an error left by the caller's earlier, unrelated work is not this call's
+    (void)cudaGetLastError();
     if (src->face_sizes || cut->face_sizes) return na_fail(out, MCGPU_TOO_LARGE); // triangles only
     const uint64_t nv = (uint64_t)src->num_vertices + cut->num_vertices;
     const uint64_t nf = (uint64_t)src->num_faces + cut->num_faces;
@@ -246,6 +250,8 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.tri_scratch = nullptr;
     W.tri_scratch_cap = 0;
     W.tri_stride = 0;
+    // the bounds kernel replaces an index outside its mesh in the table it reads
+    W.fidx_fix = reinterpret_cast<uint32_t*>(base + oFidx);
 
     auto ok = [](cudaError_t e) { return e == cudaSuccess; };
     // inputs and the per-pair table into scratch; clear what must start at zero
@@ -274,11 +280,18 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
         || !ok(cudaStreamSynchronize(s)))
         return na_fail(out, MCGPU_CUDA_ERROR);
     if (hc[16] & ST_STACK) {
+        // the walk again with 512-entry stacks; its own bits are cleared first and
+        // the bounds kernel's ST_INVALID stays
         if (!ok(cudaMemsetAsync(W.counters, 0, 64, s)) || !ok(cudaMemsetAsync(W.cand, 0, nf, s)))
             return na_fail(out, MCGPU_CUDA_ERROR);
+        launch_clear_status(W.pair_status, 1, ST_STACK | ST_OVERFLOW_PAIRS, s);
         launch_traverse(P, W, src_buf, cut_buf, true, s);
-        if (!ok(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s)) || !ok(cudaStreamSynchronize(s)))
+        if (!ok(cudaMemcpyAsync(hc, W.counters, 64, cudaMemcpyDeviceToHost, s))
+            || !ok(cudaMemcpyAsync(hc + 16, W.pair_status, 4, cudaMemcpyDeviceToHost, s))
+            || !ok(cudaStreamSynchronize(s)))
             return na_fail(out, MCGPU_CUDA_ERROR);
+        // a tree deeper than the long stacks: the pair list would be incomplete
+        if (hc[16] & ST_STACK) return na_fail(out, MCGPU_TOO_LARGE);
     }
     if (out) out->num_pairs = hc[0];
     if (hc[0] > kMaxPairs) return na_fail(out, MCGPU_TOO_LARGE);

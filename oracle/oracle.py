@@ -40,10 +40,32 @@ class FeResult(C.Structure):
 _libs = {}
 
 
+# The reference checkout the harness is compiled from: named by MCUT_REF_ROOT
+# (no default). Once built, oracle/_ref/ serves without the checkout.
+REF_ROOT = os.environ.get("MCUT_REF_ROOT") or None
+
+
+def ref_checkout() -> bool:
+    """True when MCUT_REF_ROOT names a reference checkout."""
+    return bool(REF_ROOT) and os.path.isdir(os.path.join(REF_ROOT, "source"))
+
+
+def ref_available() -> bool:
+    """True when the reference harness is built or can be built here."""
+    return os.path.exists(REF_LIB) or ref_checkout()
+
+
 def build(ref: bool = False, ref_root: str | None = None) -> None:
-    """Compile liboracle.so (and, with ref=True, the reference harness) via the Makefile."""
+    """Compile liboracle.so (and, with ref=True, the reference harness) via the Makefile.
+    The harness needs the reference checkout (ref_root, else MCUT_REF_ROOT);
+    without one an already built harness is kept as it is."""
+    ref_root = ref_root or REF_ROOT
+    if ref and not ref_root:
+        if os.path.exists(REF_LIB):
+            return
+        raise RuntimeError("the reference harness needs MCUT_REF_ROOT (a reference checkout)")
     cmd = ["make", "-s", "-C", HERE] + (["ref"] if ref else ["liboracle.so"])
-    if ref_root:
+    if ref:
         cmd.append(f"REF_ROOT={ref_root}")
     subprocess.run(cmd, check=True)
 

@@ -3,7 +3,7 @@
 Run where the reference checkout exists (it compiles the reference sources in
 place into oracle/_ref via oracle/Makefile):
 
-    python tests/golden/make_golden.py [--ref-root /path/to/mcut]
+    python tests/golden/make_golden.py --ref-root /path/to/mcut   (or MCUT_REF_ROOT=...)
 
 Every fixture stores the inputs (so hosts without the reference can replay
 them) and the reference's own outputs:
@@ -179,8 +179,11 @@ def predicate_cases(rng, n=6000):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default=os.environ.get("MCUT_REF_ROOT", "/root/reference"))
+    ap.add_argument("--ref-root", default=os.environ.get("MCUT_REF_ROOT"),
+                    help="reference checkout (default: $MCUT_REF_ROOT)")
     args = ap.parse_args()
+    if not args.ref_root:
+        ap.error("name the reference checkout with --ref-root or MCUT_REF_ROOT")
     import oracle  # noqa: E402
     oracle.build(ref=True, ref_root=args.ref_root)
 

@@ -125,6 +125,42 @@ def test_batch_equals_single(ctx):
         assert G.same_bits(b, want["rec_pts"]), k
 
 
+@pytest.mark.parametrize("kind", ["cross_mesh", "wrapping", "far"])
+def test_index_outside_its_mesh(ctx, kind):
+    """Each mesh's indices are checked against its own vertex count, as the
+    reference's input conversion does (preproc.cpp:390-460): a source index
+    naming a cut vertex, a cut index that wraps when offset by the source
+    vertex count and an index past every vertex give MCGPU_INVALID_INPUT, as
+    the oracle does; in a batch only that pair's status changes and the other
+    pairs keep their records."""
+    from mcut_gb300 import _lib as L
+    c = CASES["two_spheres"]
+    src = dict(c["src"], f=c["src"]["f"].copy())
+    cut = dict(c["cut"], f=c["cut"]["f"].copy())
+    vs = src["v"].shape[0]
+    if kind == "cross_mesh":
+        src["f"][7] = vs + 1
+    elif kind == "wrapping":
+        cut["f"][4] = 0xFFFFFFFF - vs + 2
+    else:
+        src["f"][5] = 1_000_000_000
+    assert oracle.front_end(src, cut, impl="port")["status"] == oracle.FE_INVALID_INPUT
+    assert ctx.dispatch(src, cut).status == L.INVALID_INPUT
+    names = ["crack1", "two_spheres"]
+    pairs = [(CASES["crack1"]["src"], CASES["crack1"]["cut"]), (src, cut),
+             (CASES["two_spheres"]["src"], CASES["two_spheres"]["cut"])]
+    out = ctx.dispatch_batch(pairs)
+    assert out[1][0]["status"] == L.INVALID_INPUT
+    for k, (summ, ids, pts) in zip(names, [out[0], out[2]]):
+        assert summ["status"] == int(CASES[k]["status"]), k
+        a, b = canonical_records(ids, pts)
+        assert G.same_bits(a, CASES[k]["rec_ids"]), k
+        assert G.same_bits(b, CASES[k]["rec_pts"]), k
+    # the context is unaffected afterwards
+    r = ctx.dispatch(c["src"], c["cut"])
+    assert r.status == 0 and r.num_records == 169
+
+
 def _packed_records(ids, pts, off, i):
     a, b = int(off[i]), int(off[i + 1])
     return canonical_records(ids[a:b], pts[a:b])

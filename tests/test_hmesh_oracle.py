@@ -27,15 +27,14 @@ import fuzz_cases as F
 import golden_cases as G
 import oracle
 
-REF_ROOT = os.environ.get("MCUT_REF_ROOT", "/root/reference")
-HAVE_REF = os.path.isdir(os.path.join(REF_ROOT, "source"))
+HAVE_REF = oracle.ref_available()
 CASES = G.all_cases()
 ARRAYS = ["he_target", "he_face", "he_next", "he_prev", "corner_he", "v_off", "v_he"]
 
 
 @pytest.fixture(scope="module", autouse=True)
 def _build():
-    oracle.build(ref=HAVE_REF, ref_root=REF_ROOT if HAVE_REF else None)
+    oracle.build(ref=HAVE_REF)
 
 
 def _faces(m):

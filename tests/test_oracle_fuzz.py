@@ -23,16 +23,15 @@ import fuzz_cases as F
 import golden_cases as G
 import oracle
 
-REF_ROOT = os.environ.get("MCUT_REF_ROOT", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "source")),
-                                reason="reference checkout not present")
+pytestmark = pytest.mark.skipif(not oracle.ref_available(),
+                                reason="reference harness not built and MCUT_REF_ROOT unset")
 
 KEYS = G.FE_KEYS + ["face_boxes", "cut_xyz"]
 
 
 @pytest.fixture(scope="module", autouse=True)
 def _build():
-    oracle.build(ref=True, ref_root=REF_ROOT)
+    oracle.build(ref=True)
 
 
 def _same(src, cut, **kw):

@@ -11,16 +11,15 @@ import pytest
 import golden_cases as G
 import oracle
 
-REF_ROOT = os.environ.get("MCUT_REF_ROOT", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "source")),
-                                reason="reference checkout not present")
+pytestmark = pytest.mark.skipif(not oracle.ref_available(),
+                                reason="reference harness not built and MCUT_REF_ROOT unset")
 
 CASES = G.all_cases()
 
 
 @pytest.fixture(scope="module", autouse=True)
 def _build():
-    oracle.build(ref=True, ref_root=REF_ROOT)
+    oracle.build(ref=True)
 
 
 @pytest.mark.parametrize("name", sorted(CASES))

@@ -18,8 +18,7 @@ import pytest
 import oracle
 from expansions import fast_expansion_sum_zeroelim, two_product, two_two_diff
 
-REF_ROOT = os.environ.get("MCUT_REF_ROOT", "/root/reference")
-HAVE_REF = os.path.isdir(os.path.join(REF_ROOT, "source"))
+HAVE_REF = oracle.ref_available()
 EPS = 1.1102230246251565e-16
 CCW_A = 3.3306690738754716e-16
 
@@ -112,9 +111,9 @@ def _bits(x):
 @pytest.mark.parametrize("impl", ["port", "ref"])
 def test_value_matches(impl):
     if impl == "ref" and not HAVE_REF:
-        pytest.skip("reference checkout not present")
+        pytest.skip("reference harness not built and MCUT_REF_ROOT unset")
     if impl == "ref":
-        oracle.build(ref=True, ref_root=REF_ROOT)
+        oracle.build(ref=True)
     fn = oracle.ref_orient2d if impl == "ref" else oracle.port_orient2d
     rng = np.random.default_rng(41)
     adaptive = 0
