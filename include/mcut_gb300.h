@@ -131,8 +131,26 @@ typedef enum mcgpu_data {
     MCGPU_DATA_TEST_INFO = 5,     /* int8[4*T]: sign(orient3d q), sign(orient3d r), type char, pip char */
     MCGPU_DATA_VERTICES = 6,      /* double[3*(Vs+Vc)]: the ps coordinates used */
     MCGPU_DATA_FACE_BOXES = 7,    /* double[6*(Fs+Fc)]: min xyz, max xyz (cut boxes enlarged) */
-    MCGPU_DATA_RECORD_OFFSETS = 8 /* uint64[n_pairs+1]: first record of each pair of the last
+    MCGPU_DATA_RECORD_OFFSETS = 8, /* uint64[n_pairs+1]: first record of each pair of the last
                                      dispatch (records of a batch are grouped by pair), then R */
+    /* The record hand-over of a single dispatch: the maps dispatch()'s host
+     * stages read (kernel.cpp:2599-2655, merged at 2673-2714), built on the
+     * device from the records at the first such query. Record i is MCUT's
+     * intersection vertex Vs + Vc + i of m0 (the "m0 ids" below); keys
+     * ascend and each key's vertices ascend. */
+    MCGPU_DATA_EDGE_RECORD_OFFSETS = 9,  /* uint32[E+1]: records [o[e], o[e+1]) share the e-th intersected
+                                            ps edge, their (q, r) (ps_intersecting_edges) */
+    MCGPU_DATA_CUTPATH_PAIRS = 10,       /* uint32[2*K]: (source face, cut face) of every face pair an
+                                            intersection vertex lies on (cutpath_edge_creation_info keys) */
+    MCGPU_DATA_CUTPATH_OFFSETS = 11,     /* uint32[K+1]: pair k's vertices are [o[k], o[k+1]) of ... */
+    MCGPU_DATA_CUTPATH_VERTICES = 12,    /* uint32[o[K]]: m0 ids */
+    MCGPU_DATA_FACE_KEYS = 13,           /* uint32[M]: ps faces an intersection vertex lies on: the tested
+                                            face and the edge's faces (ps_iface_to_ivtx_list keys) */
+    MCGPU_DATA_FACE_OFFSETS = 14,        /* uint32[M+1] */
+    MCGPU_DATA_FACE_VERTICES = 15,       /* uint32[o[M]]: m0 ids */
+    MCGPU_DATA_BORDER_VERTICES = 16,     /* uint32[B]: m0 ids of records on cut-mesh border edges
+                                            (cm_border_reentrant_ivtx_list) */
+    MCGPU_DATA_PARTIAL_CUT = 17          /* uint32[1]: 1 if B > 0 (partial_cut_detected), else 0 */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.

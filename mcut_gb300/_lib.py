@@ -30,6 +30,9 @@ ENFORCE_GENERAL_POSITION_ABSOLUTE = 1 << 7
 
 DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DATA_VERTICES, DATA_FACE_BOXES, \
     DATA_RECORD_OFFSETS = range(1, 9)
+# the record hand-over of a single dispatch (the maps dispatch()'s host stages read)
+DATA_EDGE_RECORD_OFFSETS, DATA_CUTPATH_PAIRS, DATA_CUTPATH_OFFSETS, DATA_CUTPATH_VERTICES, DATA_FACE_KEYS, \
+    DATA_FACE_OFFSETS, DATA_FACE_VERTICES, DATA_BORDER_VERTICES, DATA_PARTIAL_CUT = range(9, 18)
 
 STAGES = ["upload", "bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow", "download"]
 

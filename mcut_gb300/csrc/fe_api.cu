@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "fe_common.cuh"
+#include "fe_derived.cuh"
 #include "fe_host.h"
 #include "fe_kernels.cuh"
 #include "fe_sort.cuh"
@@ -94,7 +95,9 @@ enum BufId {
     B_X, B_FOFF, B_FIDX, B_FPAIR, B_PTAB, B_EPS, B_FBOX, B_MESHBOX, B_SK0, B_SK1, B_SV0, B_SV1, B_CK0, B_CK1, B_CV0,
     B_CV1, B_SORTTMP, B_NODES, B_PARENT, B_PAIRS, B_COUNTERS, B_CAND, B_PSLOT, B_PLANES, B_POLY, B_VNEED,
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
-    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG, B_COUNT
+    B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
+    // the record hand-over (built at the first query for it)
+    B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -153,6 +156,10 @@ struct mcgpu_context_t {
     std::vector<unsigned char> fuse_key;
     bool fuse_ok = false;
     uint64_t fuse_nrec = 0, fuse_npairs = 0;
+    // the record hand-over of the last single dispatch (built on demand)
+    bool derived_ready = false;
+    mcgpu::DerivedOut derived {};
+    uint32_t derived_counts[mcgpu::kDerivedCounts] = {};
 };
 
 namespace {
@@ -804,6 +811,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         return fail(MCGPU_INVALID_VALUE, "float vertices need MCGPU_RECENTRE");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     c->flags = flags;
+    c->derived_ready = false;
     const unsigned long long launches0 = g_launches;
     int rc = build_layout(c, flags, n, srcs, cuts, eps);
     if (rc != MCGPU_OK) return rc;
@@ -1170,6 +1178,54 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     return MCGPU_OK;
 }
 
+// The record hand-over of the last dispatch (one pair), built once per
+// dispatch on the context stream; the counts are read back with it.
+int ensure_derived(mcgpu_context_t* c)
+{
+    if (c->derived_ready) return MCGPU_OK;
+    if (c->L.n_pairs != 1) return fail(MCGPU_INVALID_VALUE, "the record hand-over is built for a single dispatch");
+    const uint64_t R64 = c->n_records;
+    if (7 * R64 + 1 > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "too many records for the hand-over maps");
+    const uint32_t R = (uint32_t)R64;
+    const size_t r = std::max<size_t>(R, 1);
+    DerivedScratch w {};
+    w.ck[0] = c->buf[B_DCK0].get<unsigned long long>(2 * r);
+    w.ck[1] = c->buf[B_DCK1].get<unsigned long long>(2 * r);
+    w.cv[0] = c->buf[B_DCV0].get<uint32_t>(2 * r);
+    w.cv[1] = c->buf[B_DCV1].get<uint32_t>(2 * r);
+    w.fk[0] = c->buf[B_DFK0].get<uint32_t>(3 * r);
+    w.fk[1] = c->buf[B_DFK1].get<uint32_t>(3 * r);
+    w.fv[0] = c->buf[B_DFV0].get<uint32_t>(3 * r);
+    w.fv[1] = c->buf[B_DFV1].get<uint32_t>(3 * r);
+    w.flags = c->buf[B_DFLAGS].get<uint32_t>(7 * r + 1);
+    w.sort_temp = c->buf[B_DSORT].get<uint32_t>(derived_sort_temp_bytes(R) / 4 + 64);
+    w.scan_temp = c->buf[B_DSCAN].get<uint32_t>(derived_scan_temp_bytes(R) / 4 + 64);
+    // outputs back to back: edge_off R+1 | border R | cp_pairs 4R | cp_off 2R+1 | face_keys 3R | face_off 3R+1 | counts
+    uint32_t* o = c->buf[B_DOUT].get<uint32_t>(13 * r + 3 + kDerivedCounts);
+    DerivedOut& d = c->derived;
+    d.edge_off = o;
+    d.border = d.edge_off + r + 1;
+    d.cp_pairs = d.border + r;
+    d.cp_off = d.cp_pairs + 4 * r;
+    d.face_keys = d.cp_off + 2 * r + 1;
+    d.face_off = d.face_keys + 3 * r;
+    d.counts = d.face_off + 3 * r + 1;
+    d.cp_vtx = d.face_vtx = nullptr;
+    const Layout& L = c->L;
+    launch_derived(c->W.rec_ids, R, L.vs[0], (uint32_t)L.nv, L.fs[0], (uint32_t)L.nf, w, d, c->s);
+    if (R == 0) { // no records: one edge offset (0), every list empty
+        ck(cudaMemsetAsync(d.edge_off, 0, 4, c->s), "memset");
+        ck(cudaMemsetAsync(d.cp_off, 0, 4, c->s), "memset");
+        ck(cudaMemsetAsync(d.face_off, 0, 4, c->s), "memset");
+    }
+    ck(cudaMemcpyAsync(c->derived_counts, d.counts, sizeof(c->derived_counts), cudaMemcpyDeviceToHost, c->s),
+        "D2H counts");
+    ck(cudaStreamSynchronize(c->s), "sync hand-over");
+    ck(cudaGetLastError(), "hand-over launch");
+    c->derived_ready = true;
+    return MCGPU_OK;
+}
+
 int copy_out(mcgpu_context_t* c, const void* dptr, uint64_t need, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (bytes_out) *bytes_out = need;
@@ -1467,6 +1523,46 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
         }
         case MCGPU_DATA_FACE_BOXES:
             return copy_out(c, W.fbox, c->L.nf * 48, bytes, mem, bytes_out);
+        case MCGPU_DATA_EDGE_RECORD_OFFSETS:
+        case MCGPU_DATA_CUTPATH_PAIRS:
+        case MCGPU_DATA_CUTPATH_OFFSETS:
+        case MCGPU_DATA_CUTPATH_VERTICES:
+        case MCGPU_DATA_FACE_KEYS:
+        case MCGPU_DATA_FACE_OFFSETS:
+        case MCGPU_DATA_FACE_VERTICES:
+        case MCGPU_DATA_BORDER_VERTICES:
+        case MCGPU_DATA_PARTIAL_CUT: {
+            const int rc = ensure_derived(c);
+            if (rc != MCGPU_OK) return rc;
+            const DerivedOut& d = c->derived;
+            const uint32_t* n = c->derived_counts;
+            switch (query) {
+            case MCGPU_DATA_EDGE_RECORD_OFFSETS:
+                return copy_out(c, d.edge_off, 4ull * (n[kDerivedEdges] + 1), bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_PAIRS:
+                return copy_out(c, d.cp_pairs, 8ull * n[kDerivedCutpath], bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_OFFSETS:
+                return copy_out(c, d.cp_off, 4ull * (n[kDerivedCutpath] + 1), bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_VERTICES:
+                return copy_out(c, d.cp_vtx, 4ull * n[kDerivedCutpathEntries], bytes, mem, bytes_out);
+            case MCGPU_DATA_FACE_KEYS:
+                return copy_out(c, d.face_keys, 4ull * n[kDerivedFaces], bytes, mem, bytes_out);
+            case MCGPU_DATA_FACE_OFFSETS:
+                return copy_out(c, d.face_off, 4ull * (n[kDerivedFaces] + 1), bytes, mem, bytes_out);
+            case MCGPU_DATA_FACE_VERTICES:
+                return copy_out(c, d.face_vtx, 4ull * n[kDerivedFaceEntries], bytes, mem, bytes_out);
+            case MCGPU_DATA_BORDER_VERTICES:
+                return copy_out(c, d.border, 4ull * n[kDerivedBorder], bytes, mem, bytes_out);
+            default: {
+                if (bytes_out) *bytes_out = 4;
+                if (!mem && bytes == 0) return MCGPU_OK;
+                if (!mem || bytes < 4) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+                const uint32_t partial = n[kDerivedBorder] > 0 ? 1u : 0u;
+                memcpy(mem, &partial, 4);
+                return MCGPU_OK;
+            }
+            }
+        }
         case MCGPU_DATA_RECORD_OFFSETS: {
             const uint64_t need = c->rec_begin.size() * 8;
             if (bytes_out) *bytes_out = need;

@@ -113,6 +113,20 @@ class Context:
                 r.test_info = self._get(L.DATA_TEST_INFO, np.int8, 4)
         return r
 
+    def hand_over(self) -> dict:
+        """The record hand-over of the last (single) dispatch: what dispatch()'s
+        host stages read from the narrow phase (kernel.cpp:2599-2655), built on
+        the device. Keys as oracle.seam: edge_off, cp_pairs [K,2], cp_off,
+        cp_vtx, face_keys, face_off, face_vtx, border (m0 vertex ids), plus
+        partial_cut."""
+        g = lambda q, cols=1: self._get(q, np.uint32, cols)  # noqa: E731
+        d = dict(edge_off=g(L.DATA_EDGE_RECORD_OFFSETS).reshape(-1), cp_pairs=g(L.DATA_CUTPATH_PAIRS, 2),
+                 cp_off=g(L.DATA_CUTPATH_OFFSETS).reshape(-1), cp_vtx=g(L.DATA_CUTPATH_VERTICES).reshape(-1),
+                 face_keys=g(L.DATA_FACE_KEYS).reshape(-1), face_off=g(L.DATA_FACE_OFFSETS).reshape(-1),
+                 face_vtx=g(L.DATA_FACE_VERTICES).reshape(-1), border=g(L.DATA_BORDER_VERTICES).reshape(-1))
+        d["partial_cut"] = bool(g(L.DATA_PARTIAL_CUT).reshape(-1)[0])
+        return d
+
     def set_general_position(self, constant: float = 1e-4, attempts: int = 4):
         """Enforcement constant and attempts (mcBindState MC_CONTEXT_GENERAL_POSITION_ENFORCEMENT_*)."""
         L.check(self._lib.mcgpu_context_set_general_position(self._h, float(constant), int(attempts)),

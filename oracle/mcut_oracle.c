@@ -1112,3 +1112,154 @@ void oracle_free(fe_result *r)
     free(r->face_boxes); free(r->src_xyz); free(r->cut_xyz);
     memset(r, 0, sizeof *r);
 }
+
+/* ------------------------------------------------------------------------- */
+/* the record hand-over (kernel.cpp:2599-2655, 2673-2714)                    */
+/* ------------------------------------------------------------------------- */
+
+typedef struct { uint64_t key; uint32_t vtx; } kv_t;
+static int kv_cmp(const void *x, const void *y)
+{
+    const kv_t *a = (const kv_t *)x, *b = (const kv_t *)y;
+    if (a->key != b->key) return a->key < b->key ? -1 : 1;
+    return a->vtx < b->vtx ? -1 : (a->vtx > b->vtx);
+}
+typedef struct { uint32_t edge, g, k; } rord_t; /* edge creation index, tested face, input position */
+static int rord_cmp(const void *x, const void *y)
+{
+    const rord_t *a = (const rord_t *)x, *b = (const rord_t *)y;
+    if (a->edge != b->edge) return a->edge < b->edge ? -1 : 1;
+    return a->g < b->g ? -1 : (a->g > b->g);
+}
+
+/* runs of equal keys in sorted kv: keys, offsets and the vertex column */
+static uint32_t kv_runs(const kv_t *kv, uint64_t n, uint32_t **keys, int pairs, uint32_t **off, uint32_t **vtx)
+{
+    uint32_t nk = 0;
+    for (uint64_t i = 0; i < n; ++i) nk += (i == 0 || kv[i].key != kv[i - 1].key);
+    *keys = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(pairs ? 2 : 1) * (nk ? nk : 1));
+    *off = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)nk + 1));
+    *vtx = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(n ? n : 1));
+    uint32_t j = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        if (i == 0 || kv[i].key != kv[i - 1].key) {
+            if (pairs) {
+                (*keys)[2 * j] = (uint32_t)(kv[i].key >> 32);
+                (*keys)[2 * j + 1] = (uint32_t)kv[i].key;
+            } else {
+                (*keys)[j] = (uint32_t)kv[i].key;
+            }
+            (*off)[j++] = (uint32_t)i;
+        }
+        (*vtx)[i] = kv[i].vtx;
+    }
+    (*off)[nk] = (uint32_t)n;
+    return nk;
+}
+
+int oracle_seam(const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf, const uint32_t *cf,
+    const uint32_t *cfs, uint32_t ncv, uint32_t ncf, const uint32_t *rec3, const double *pts, int64_t nr,
+    fe_seam *out)
+{
+    memset(out, 0, sizeof *out);
+    mesh_t S = { NULL, sf, sfs, nsv, nsf, NULL }, Cm = { NULL, cf, cfs, ncv, ncf, NULL };
+    if (mesh_offsets(&S) || mesh_offsets(&Cm)) { free(S.off); free(Cm.off); return -1; }
+    const uint32_t NV = nsv + ncv, NF = nsf + ncf;
+    /* the ps edges in creation order (hmesh_t::add_face over the source faces,
+     * then the cut faces, hmesh.cpp:406-651): the first face corner fixes q -> r
+     * and f0, the second face is f1 */
+    const uint64_t sidx = S.off[nsf], cidx = Cm.off[ncf], nhe = sidx + cidx;
+    hash_t h;
+    uint64_t cap = 16;
+    while (cap < 2 * nhe) cap <<= 1;
+    h.key = (uint64_t *)malloc(sizeof(uint64_t) * cap);
+    h.val = (uint32_t *)malloc(sizeof(uint32_t) * cap);
+    h.mask = cap - 1;
+    memset(h.key, 0xff, sizeof(uint64_t) * cap);
+    edge_t *E = (edge_t *)malloc(sizeof(edge_t) * (size_t)(nhe ? nhe : 1));
+    uint32_t ne = 0;
+    for (uint32_t f = 0; f < NF; ++f) {
+        const mesh_t *m = f < nsf ? &S : &Cm;
+        const uint32_t lf = f < nsf ? f : f - nsf, vo = f < nsf ? 0 : nsv;
+        const uint64_t o = m->off[lf], n = m->off[lf + 1] - o;
+        for (uint64_t k = 0; k < n; ++k) {
+            const uint32_t a = m->f[o + k] + vo, b = m->f[o + (k + 1) % n] + vo;
+            const uint64_t key = ((uint64_t)(a < b ? a : b) << 32) | (a < b ? b : a);
+            uint64_t s = mix64(key) & h.mask;
+            while (h.key[s] != UINT64_MAX && h.key[s] != key) s = (s + 1) & h.mask;
+            if (h.key[s] == UINT64_MAX) {
+                h.key[s] = key;
+                h.val[s] = ne;
+                E[ne].q = a; E[ne].r = b; E[ne].f0 = f; E[ne].f1 = UINT32_MAX;
+                ++ne;
+            } else if (E[h.val[s]].f1 == UINT32_MAX && E[h.val[s]].f0 != f) {
+                E[h.val[s]].f1 = f;
+            }
+        }
+    }
+    /* records in canonical order */
+    rord_t *ord = (rord_t *)malloc(sizeof(rord_t) * (size_t)(nr ? nr : 1));
+    int bad = 0;
+    for (int64_t i = 0; i < nr; ++i) {
+        const uint32_t a = rec3[3 * i], b = rec3[3 * i + 1];
+        const uint64_t key = ((uint64_t)(a < b ? a : b) << 32) | (a < b ? b : a);
+        uint64_t s = mix64(key) & h.mask;
+        while (h.key[s] != UINT64_MAX && h.key[s] != key) s = (s + 1) & h.mask;
+        if (h.key[s] == UINT64_MAX) { bad = 1; ord[i].edge = 0; }
+        else ord[i].edge = h.val[s];
+        ord[i].g = rec3[3 * i + 2];
+        ord[i].k = (uint32_t)i;
+    }
+    free(h.key); free(h.val);
+    if (bad) { free(ord); free(E); free(S.off); free(Cm.off); return -1; }
+    if (nr) qsort(ord, (size_t)nr, sizeof(rord_t), rord_cmp);
+
+    out->n_records = nr;
+    out->rec_ids = (uint32_t *)malloc(sizeof(uint32_t) * 5 * (size_t)(nr ? nr : 1));
+    out->rec_pts = (double *)malloc(sizeof(double) * 3 * (size_t)(nr ? nr : 1));
+    out->edge_off = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)nr + 1));
+    out->border = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nr ? nr : 1));
+    kv_t *cp = (kv_t *)malloc(sizeof(kv_t) * 2 * (size_t)(nr ? nr : 1));
+    kv_t *fc = (kv_t *)malloc(sizeof(kv_t) * 3 * (size_t)(nr ? nr : 1));
+    uint64_t ncp = 0, nfc = 0;
+    for (int64_t i = 0; i < nr; ++i) {
+        const edge_t *e = &E[ord[i].edge];
+        const uint32_t g = ord[i].g, vtx = NV + (uint32_t)i;
+        uint32_t *r5 = out->rec_ids + 5 * i;
+        r5[0] = e->q; r5[1] = e->r; r5[2] = g; r5[3] = e->f0; r5[4] = e->f1;
+        memcpy(out->rec_pts + 3 * i, pts + 3 * (size_t)ord[i].k, sizeof(double) * 3);
+        /* ps_intersecting_edges[tested_edge] (kernel.cpp:2609) */
+        if (i == 0 || ord[i].edge != ord[i - 1].edge) out->edge_off[out->n_edges++] = (uint32_t)i;
+        /* cutpath_edge_creation_info: {source face, cut face} for the tested face
+         * and each face of the tested edge (kernel.cpp:2614-2627; utils.h pair
+         * orders its two faces, and source faces come first) */
+        const int cut_edge = e->q >= nsv; /* the edge's vertices are cut-mesh vertices */
+        const uint32_t ef[2] = { e->f0, e->f1 };
+        for (int k = 0; k < 2; ++k) {
+            if (ef[k] == UINT32_MAX) continue;
+            const uint32_t sface = cut_edge ? g : ef[k], cface = cut_edge ? ef[k] : g;
+            cp[ncp].key = ((uint64_t)sface << 32) | cface;
+            cp[ncp++].vtx = vtx;
+        }
+        /* ps_iface_to_ivtx_list (kernel.cpp:2638-2644) */
+        fc[nfc].key = g; fc[nfc++].vtx = vtx;
+        for (int k = 0; k < 2; ++k)
+            if (ef[k] != UINT32_MAX) { fc[nfc].key = ef[k]; fc[nfc++].vtx = vtx; }
+        /* cm_border_reentrant_ivtx_list / partial_cut_detected (kernel.cpp:2629-2650) */
+        if (cut_edge && e->f1 == UINT32_MAX) out->border[out->n_border++] = vtx;
+    }
+    out->edge_off[out->n_edges] = (uint32_t)nr;
+    qsort(cp, (size_t)ncp, sizeof(kv_t), kv_cmp);
+    qsort(fc, (size_t)nfc, sizeof(kv_t), kv_cmp);
+    out->n_cutpath = kv_runs(cp, ncp, &out->cp_pairs, 1, &out->cp_off, &out->cp_vtx);
+    out->n_faces = kv_runs(fc, nfc, &out->face_keys, 0, &out->face_off, &out->face_vtx);
+    free(cp); free(fc); free(ord); free(E); free(S.off); free(Cm.off);
+    return 0;
+}
+
+void oracle_seam_free(fe_seam *s)
+{
+    free(s->rec_ids); free(s->rec_pts); free(s->edge_off); free(s->cp_pairs); free(s->cp_off); free(s->cp_vtx);
+    free(s->face_keys); free(s->face_off); free(s->face_vtx); free(s->border);
+    memset(s, 0, sizeof *s);
+}

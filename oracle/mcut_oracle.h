@@ -53,6 +53,47 @@ typedef struct fe_result {
     double *cut_xyz;           /* 3*Vc recentred coordinates */
 } fe_result;
 
+/* The record hand-over of one front-end pass (kernel.cpp:2599-2655 and the
+ * merge at kernel.cpp:2673-2714): what dispatch()'s host stages read from the
+ * narrow phase. Every record becomes an intersection vertex of m0 with id
+ * Vs + Vc + its position in the record order, which here is canonical: by
+ * the tested edge's first face corner in the source-then-cut face arrays (the
+ * edge's creation order in MCUT's halfedge mesh), then the tested face. The
+ * reference numbers them in its threads' merge order instead.
+ * Maps (vertex lists ascending, keys ascending as the reference's std::map
+ * keeps them):
+ *   edges     ps_intersecting_edges: records [edge_off[e], edge_off[e+1]) share
+ *             the e-th intersected edge (their q, r)
+ *   cutpath   cutpath_edge_creation_info: key (source face, cut face) of the
+ *             tested face and each face of the tested edge
+ *   faces     ps_iface_to_ivtx_list: the tested face and the edge's faces
+ *   border    cm_border_reentrant_ivtx_list: records whose edge is a cut-mesh
+ *             border edge; n_border > 0 is partial_cut_detected */
+typedef struct fe_seam {
+    int64_t n_records;
+    uint32_t *rec_ids;         /* 5*R: q, r, tested face, f0 (the edge's first face), f1 (other or ~0u) */
+    double *rec_pts;           /* 3*R */
+    uint32_t n_edges;
+    uint32_t *edge_off;        /* [n_edges+1] */
+    uint32_t n_cutpath;
+    uint32_t *cp_pairs;        /* [2*n_cutpath] */
+    uint32_t *cp_off;          /* [n_cutpath+1] */
+    uint32_t *cp_vtx;          /* [cp_off[n_cutpath]] m0 ids */
+    uint32_t n_faces;
+    uint32_t *face_keys;       /* [n_faces] */
+    uint32_t *face_off;        /* [n_faces+1] */
+    uint32_t *face_vtx;        /* [face_off[n_faces]] m0 ids */
+    uint32_t n_border;
+    uint32_t *border;          /* [n_border] m0 ids */
+} fe_seam;
+
+/* From a pass's records (rec3: q, r, face per record, any order; pts) and the
+ * two meshes' faces. Returns 0, or -1 if a record's edge is not in the meshes. */
+int oracle_seam(const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf, const uint32_t *cf,
+    const uint32_t *cfs, uint32_t ncv, uint32_t ncf, const uint32_t *rec3, const double *pts, int64_t nr,
+    fe_seam *out);
+void oracle_seam_free(fe_seam *s);
+
 /* Input-mesh conversion and checks (hmesh_oracle.c; ref_hmesh in the
  * harness): the halfedge mesh MCUT builds from one mesh's arrays and the
  * outcome of its input checks. */

@@ -107,7 +107,7 @@ def _mesh_args(m, float_input=False):
 
 
 def _arr(ptr, n, dtype):
-    if n == 0:
+    if n == 0 or not ptr:  # an array the producer did not fill (e.g. after invalid input)
         return np.zeros(0, dtype=dtype)
     return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
 
@@ -145,6 +145,58 @@ def front_end(src, cut, impl: str = "port", threads: int = 0, float_input: bool 
     fr(C.byref(res))
     del ks, kc
     return out
+
+
+class FeSeam(C.Structure):
+    _fields_ = [("n_records", C.c_int64), ("rec_ids", C.POINTER(C.c_uint32)), ("rec_pts", C.POINTER(C.c_double)),
+                ("n_edges", C.c_uint32), ("edge_off", C.POINTER(C.c_uint32)),
+                ("n_cutpath", C.c_uint32), ("cp_pairs", C.POINTER(C.c_uint32)), ("cp_off", C.POINTER(C.c_uint32)),
+                ("cp_vtx", C.POINTER(C.c_uint32)),
+                ("n_faces", C.c_uint32), ("face_keys", C.POINTER(C.c_uint32)), ("face_off", C.POINTER(C.c_uint32)),
+                ("face_vtx", C.POINTER(C.c_uint32)),
+                ("n_border", C.c_uint32), ("border", C.POINTER(C.c_uint32))]
+
+
+SEAM_KEYS = ["rec_ids", "rec_pts", "edge_off", "cp_pairs", "cp_off", "cp_vtx", "face_keys", "face_off", "face_vtx",
+             "border"]
+
+
+def seam(src, cut, rec_ids, rec_pts):
+    """The record hand-over of one pass (kernel.cpp:2599-2655, oracle_seam):
+    records in canonical order with their edges' faces, and the derived maps
+    dispatch()'s host stages read, as flat arrays (see mcut_oracle.h)."""
+    lib, _, _ = _lib("port")
+    if not hasattr(lib, "_seam_ready"):
+        lib.oracle_seam.restype = C.c_int
+        lib.oracle_seam.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                    C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(FeSeam)]
+        lib.oracle_seam_free.argtypes = [C.POINTER(FeSeam)]
+        lib._seam_ready = True
+    ks, sa = _mesh_args(src)
+    kc, ca = _mesh_args(cut)
+    r3 = np.ascontiguousarray(np.asarray(rec_ids, dtype=np.uint32)[:, :3])
+    p3 = np.ascontiguousarray(rec_pts, dtype=np.float64)
+    out = FeSeam()
+    rc = lib.oracle_seam(sa[1], sa[2], sa[3], sa[4], ca[1], ca[2], ca[3], ca[4], r3.ctypes.data, p3.ctypes.data,
+                         len(r3), C.byref(out))
+    if rc != 0:
+        raise RuntimeError("oracle_seam: a record's edge is not in the meshes")
+    nr = int(out.n_records)
+    d = dict(
+        rec_ids=_arr(out.rec_ids, 5 * nr, np.uint32).reshape(-1, 5),
+        rec_pts=_arr(out.rec_pts, 3 * nr, np.float64).reshape(-1, 3),
+        edge_off=_arr(out.edge_off, out.n_edges + 1, np.uint32),
+        cp_pairs=_arr(out.cp_pairs, 2 * out.n_cutpath, np.uint32).reshape(-1, 2),
+        cp_off=_arr(out.cp_off, out.n_cutpath + 1, np.uint32),
+        face_keys=_arr(out.face_keys, out.n_faces, np.uint32),
+        face_off=_arr(out.face_off, out.n_faces + 1, np.uint32),
+        border=_arr(out.border, out.n_border, np.uint32),
+    )
+    d["cp_vtx"] = _arr(out.cp_vtx, int(d["cp_off"][-1]), np.uint32)
+    d["face_vtx"] = _arr(out.face_vtx, int(d["face_off"][-1]), np.uint32)
+    lib.oracle_seam_free(C.byref(out))
+    del ks, kc
+    return d
 
 
 def _pts(*ps):
