@@ -1320,13 +1320,21 @@ __global__ void __launch_bounds__(kBlock) k_vf_fill(Problem P, const uint8_t* __
     }
 }
 
-// vertex k of the face's list as the reference sees it: hmesh_t's
-// get_vertices_around_face returns the TARGETS of the face's halfedges, i.e.
-// the input order rotated by one (hmesh.cpp:722-733)
-__device__ __forceinline__ uint32_t face_vertex(const Problem& P, uint32_t o, uint32_t n, uint32_t k)
+// vertex k of the face's list as the reference's narrow phase sees it: the
+// polygon soup's get_vertices_around_face returns the TARGETS of the face's
+// halfedges (hmesh.cpp:722-733). The soup copies the source mesh, so a
+// source face lists its input corners rotated by one; it adds each cut face
+// as the cut mesh's own get_vertices_around_face lists it (kernel.cpp:
+// 1650-1700), so a cut face lists them rotated by two. rot = face_rot(P, f).
+__device__ __forceinline__ uint32_t face_rot(const Problem& P, uint32_t f)
 {
-    const uint32_t j = k + 1;
-    return P.fidx[o + (j == n ? 0 : j)];
+    return (face_pair_of(P, f) & kCutBit) ? 2u : 1u;
+}
+__device__ __forceinline__ uint32_t face_vertex(const Problem& P, uint32_t o, uint32_t n, uint32_t k, uint32_t rot)
+{
+    uint32_t j = k + rot; // k < n and rot <= 2 < n + 1: one wrap at most
+    if (j >= n) j -= n;
+    return P.fidx[o + j];
 }
 
 // unit normal, d and the largest component from the raw Newell normal in
@@ -1374,14 +1382,14 @@ __global__ void __launch_bounds__(kBlock, MCGPU_PL_MINB) k_planes(Problem P, con
     const uint32_t nslots = (uint32_t)min((uint64_t)counters[3], plane_cap);
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslots; slot += gridDim.x * blockDim.x) {
         const uint32_t f = slot_face[slot];
-        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        const uint32_t o = face_o(P, f), n = face_n(P, f), rot = face_rot(P, f);
         // Newell's normal over the rotated vertex list
         double nx = 0.0, ny = 0.0, nz = 0.0;
         double cur[3], nxt[3], first[3];
-        load_v(P, face_vertex(P, o, n, 0), first);
+        load_v(P, face_vertex(P, o, n, 0, rot), first);
         cur[0] = first[0]; cur[1] = first[1]; cur[2] = first[2];
         for (uint32_t k = 0; k < n; ++k) {
-            if (k + 1 < n) load_v(P, face_vertex(P, o, n, k + 1), nxt);
+            if (k + 1 < n) load_v(P, face_vertex(P, o, n, k + 1, rot), nxt);
             else { nxt[0] = first[0]; nxt[1] = first[1]; nxt[2] = first[2]; }
             nx = nx + (cur[1] - nxt[1]) * (cur[2] + nxt[2]);
             ny = ny + (cur[2] - nxt[2]) * (cur[0] + nxt[0]);
@@ -1553,7 +1561,7 @@ __global__ void k_triplets(Problem P, const uint32_t* __restrict__ poly_list, co
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < npoly; t += gridDim.x * blockDim.x) {
         const uint32_t f = poly_list[t];
         FacePlane& pl = planes[plane_slot[f]];
-        const uint32_t o = face_o(P, f), n = face_n(P, f);
+        const uint32_t o = face_o(P, f), n = face_n(P, f), rot = face_rot(P, f);
         // scratch: one region of `stride` triplets (the largest polygon's count) per polygon
         const uint64_t per = (uint64_t)n * (n - 1) * (n - 2) / 6;
         const uint64_t base = (uint64_t)t * stride;
@@ -1566,15 +1574,15 @@ __global__ void k_triplets(Problem P, const uint32_t* __restrict__ poly_list, co
         long m = 0;
         for (uint32_t i = 0; i < n; ++i) {
             double vi[3], xi[2];
-            load_v(P, face_vertex(P, o, n, i), vi);
+            load_v(P, face_vertex(P, o, n, i, rot), vi);
             project2(pl.P, vi, xi);
             for (uint32_t j = i + 1; j < n; ++j) {
                 double vj[3], xj[2];
-                load_v(P, face_vertex(P, o, n, j), vj);
+                load_v(P, face_vertex(P, o, n, j, rot), vj);
                 project2(pl.P, vj, xj);
                 for (uint32_t k = j + 1; k < n; ++k) {
                     double vk[3], xk[2];
-                    load_v(P, face_vertex(P, o, n, k), vk);
+                    load_v(P, face_vertex(P, o, n, k, rot), vk);
                     project2(pl.P, vk, xk);
                     const double r = orient2d(xi, xj, xk);
                     if (!(r == 0.0)) tr[m++] = Trip { r, (int)i, (int)j, (int)k, 0 };
@@ -1703,7 +1711,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
 // ---------------------------------------------------------------------------
 // narrow phase (kernel.cpp:2456-2658; math.cpp:249-287, 391-427, 643-703, 851-902)
 // ---------------------------------------------------------------------------
-__device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_t n, const double* pt)
+__device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_t n, uint32_t rot, const double* pt)
 {
     double q[2];
     project2(Pm, pt, q);
@@ -1711,12 +1719,12 @@ __device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_
     double prv[2];
     {
         double v[3];
-        load_v(P, face_vertex(P, o, n, n - 1), v);
+        load_v(P, face_vertex(P, o, n, n - 1, rot), v);
         project2(Pm, v, prv);
     }
     for (uint32_t i = 0; i < n; ++i) {
         double v[3], c[2];
-        load_v(P, face_vertex(P, o, n, i), v);
+        load_v(P, face_vertex(P, o, n, i, rot), v);
         project2(Pm, v, c);
         const double xi = c[0] - q[0], yi = c[1] - q[1];
         if (xi == 0.0 && yi == 0.0) return 'v';
@@ -1771,9 +1779,9 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
                 double q[3], r[3], a[3], b[3], c[3];
                 load_v(P, t.q, q);
                 load_v(P, t.r, r);
-                load_v(P, face_vertex(P, o, n, t0), a);
-                load_v(P, face_vertex(P, o, n, t1), b);
-                load_v(P, face_vertex(P, o, n, t2), c);
+                load_v(P, face_vertex(P, o, n, t0, face_rot(P, t.g)), a);
+                load_v(P, face_vertex(P, o, n, t1, face_rot(P, t.g)), b);
+                load_v(P, face_vertex(P, o, n, t2, face_rot(P, t.g)), c);
                 int st0, st1;
                 sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
                 sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
@@ -1828,7 +1836,7 @@ __global__ void __launch_bounds__(kSpread) k_finish_planes(Problem P, FacePlane*
         FacePlane& plr = planes[plane_slot[f]];
         FacePlane pl = plr;
         double first[3];
-        load_v(P, face_vertex(P, face_o(P, f), 3, 0), first);
+        load_v(P, face_vertex(P, face_o(P, f), 3, 0, face_rot(P, f)), first);
         finish_plane(pl, first);
         projection_matrix(pl.n, pl.mc, pl.P);
         plr = pl;
@@ -1862,17 +1870,17 @@ __global__ void __launch_bounds__(kNarrowHitsBlock, MCGPU_NH_MINB) k_narrow_hits
             const char type = (char)((hv.y >> 16) & 0xFFu);
             t = tests[i];
             const FacePlane pl = planes[plane_slot[t.g]];
-            const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
+            const uint32_t o = face_o(P, t.g), n = face_n(P, t.g), rot = face_rot(P, t.g);
             const double* Pm = pl.P;
             double q[3], r[3];
             load_v(P, t.q, q);
             load_v(P, t.r, r);
             char pip = 0;
             if (type == 'q' || type == 'r') {
-                pip = pip_face(P, Pm, o, n, type == 'q' ? q : r);
+                pip = pip_face(P, Pm, o, n, rot, type == 'q' ? q : r);
             } else if (type == 'p') {
-                pip = pip_face(P, Pm, o, n, q);
-                if (!(pip == 'i' || pip == 'v' || pip == 'e')) pip = pip_face(P, Pm, o, n, r);
+                pip = pip_face(P, Pm, o, n, rot, q);
+                if (!(pip == 'i' || pip == 'v' || pip == 'e')) pip = pip_face(P, Pm, o, n, rot, r);
             } else {
                 const double num = pl.d - dot3(q, pl.n);
                 const double rq[3] = { r[0] - q[0], r[1] - q[1], r[2] - q[2] };
@@ -1881,7 +1889,7 @@ __global__ void __launch_bounds__(kNarrowHitsBlock, MCGPU_NH_MINB) k_narrow_hits
                     const double tt = num / den;
                     for (int k = 0; k < 3; ++k) pt[k] = q[k] + tt * (r[k] - q[k]);
                 }
-                pip = pip_face(P, Pm, o, n, pt);
+                pip = pip_face(P, Pm, o, n, rot, pt);
                 rec = pip == 'i';
             }
             const uint32_t p = P.face_pair[t.g] & ~kCutBit;

@@ -834,6 +834,9 @@ static int test_cmp(const void *x, const void *y)
     return a->g < b->g ? -1 : (a->g > b->g);
 }
 
+static int front_end_core(mesh_t *Sp, mesh_t *Cp, double *x, double eps, const double *perturbation,
+    fe_result *out);
+
 /* One front-end pass. With a perturbation (general-position enforcement,
  * preproc.cpp:2590-2699) the cut vertices of the narrow phase are the
  * recentred ones plus the perturbation (one rounding, preproc.cpp:131-133,
@@ -859,9 +862,45 @@ int oracle_front_end2(const void *sv, const uint32_t *sf, const uint32_t *sfs, u
         out->status = FE_INVALID_INPUT;
         return 0;
     }
-    const uint32_t NV = nsv + ncv, NF = nsf + ncf;
-    double *x = (double *)malloc(sizeof(double) * 3 * (size_t)NV); /* ps vertices */
+    double *x = (double *)malloc(sizeof(double) * 3 * ((size_t)nsv + ncv)); /* ps vertices */
     const double eps = recentre(&S, &Cm, float_input, gp_constant, gp_absolute, x, x + (size_t)nsv * 3);
+    return front_end_core(&S, &Cm, x, eps, perturbation, out);
+}
+
+/* The same pass over internal (already recentred) coordinates and a given
+ * cut-box enlargement: the form the front end has inside dispatch(), where
+ * the halfedge meshes hold recentred coordinates (kernel.h:122-170). */
+int oracle_front_end_internal(const double *xs, const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf,
+    const double *xc, const uint32_t *cf, const uint32_t *cfs, uint32_t ncv, uint32_t ncf, double eps, int threads,
+    fe_result *out)
+{
+    memset(out, 0, sizeof *out);
+    out->bad_face = -1;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    mesh_t S = { xs, sf, sfs, nsv, nsf, NULL }, Cm = { xc, cf, cfs, ncv, ncf, NULL };
+    if (nsv < 3 || ncv < 3 || nsf < 1 || ncf < 1 || mesh_offsets(&S) || mesh_offsets(&Cm)) {
+        free(S.off); free(Cm.off);
+        out->status = FE_INVALID_INPUT;
+        return 0;
+    }
+    double *x = (double *)malloc(sizeof(double) * 3 * ((size_t)nsv + ncv));
+    memcpy(x, xs, sizeof(double) * 3 * (size_t)nsv);
+    memcpy(x + (size_t)nsv * 3, xc, sizeof(double) * 3 * (size_t)ncv);
+    return front_end_core(&S, &Cm, x, eps, NULL, out);
+}
+
+/* everything after the recentring: x (ps coordinates, taken over and freed)
+ * and the cut-box enlargement eps */
+static int front_end_core(mesh_t *Sp, mesh_t *Cp, double *x, double eps, const double *perturbation, fe_result *out)
+{
+    mesh_t S = *Sp, Cm = *Cp;
+    const uint32_t nsv = S.nv, nsf = S.nf, ncv = Cm.nv, ncf = Cm.nf;
+    const uint32_t *sf = S.f, *cf = Cm.f;
+    const uint32_t NV = nsv + ncv, NF = nsf + ncf;
     out->cut_eps = eps;
     out->src_xyz = (double *)malloc(sizeof(double) * 3 * (size_t)nsv);
     out->cut_xyz = (double *)malloc(sizeof(double) * 3 * (size_t)ncv);
@@ -951,10 +990,14 @@ int oracle_front_end2(const void *sv, const uint32_t *sf, const uint32_t *sfs, u
 
     /* face properties of every candidate face; a degenerate one aborts
      * before the narrow phase (kernel.cpp:2184-2356). The face's vertex list
-     * is the one hmesh_t::get_vertices_around_face returns: the TARGETS of its
-     * halfedges, i.e. the input order rotated by one (v1, v2, ..., v0),
-     * hmesh.cpp:722-733. Newell's sum, d = <v_first, n>, the plane triplet
-     * and the 2-D polygon all use that order. */
+     * is the one the polygon soup's get_vertices_around_face returns: the
+     * TARGETS of its halfedges (hmesh.cpp:722-733). The soup copies the
+     * source mesh, so a source face lists its input corners rotated by one
+     * (v1, v2, ..., v0); it adds each cut face as the cut mesh's own
+     * get_vertices_around_face lists it (kernel.cpp:1650-1700), so a cut face
+     * lists them rotated by two (v2, ..., v0, v1). Newell's sum,
+     * d = <v_first, n>, the plane triplet and the 2-D polygon all use that
+     * order. */
     plane_t *pl = (plane_t *)calloc(NF, sizeof(plane_t));
     int bad = -1;
 #pragma omp parallel for schedule(dynamic, 256)
@@ -962,7 +1005,8 @@ int oracle_front_end2(const void *sv, const uint32_t *sf, const uint32_t *sfs, u
         if (poff[f + 1] == poff[f]) continue;
         const int n = (int)(foff[f + 1] - foff[f]);
         const double **fv = (const double **)malloc(sizeof(double *) * (size_t)n);
-        for (int k = 0; k < n; ++k) fv[k] = x + (size_t)fidx[foff[f] + (k + 1) % n] * 3;
+        const int rot = (uint32_t)f < nsf ? 1 : 2;
+        for (int k = 0; k < n; ++k) fv[k] = x + (size_t)fidx[foff[f] + (k + rot) % n] * 3;
         face_plane(fv, n, &pl[f]);
         if (pl[f].degenerate) {
 #pragma omp critical
@@ -1017,7 +1061,8 @@ int oracle_front_end2(const void *sv, const uint32_t *sf, const uint32_t *sfs, u
             const int n = (int)(foff[t->g + 1] - foff[t->g]);
             const double *fvb[8];
             const double **fv = n <= 8 ? fvb : (const double **)malloc(sizeof(double *) * (size_t)n);
-            for (int k = 0; k < n; ++k) fv[k] = x + (size_t)fidx[foff[t->g] + (k + 1) % n] * 3;
+            const int rot = t->g < nsf ? 1 : 2;
+            for (int k = 0; k < n; ++k) fv[k] = x + (size_t)fidx[foff[t->g] + (k + rot) % n] * 3;
             const double *q = x + (size_t)t->q * 3, *r = x + (size_t)t->r * 3;
             memset(t->info, 0, 4);
             t->rec = 0;

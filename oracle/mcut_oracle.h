@@ -53,6 +53,14 @@ typedef struct fe_result {
     double *cut_xyz;           /* 3*Vc recentred coordinates */
 } fe_result;
 
+/* One front-end pass over internal (recentred) double coordinates with a
+ * given cut-box enlargement (no recentring): what the front end computes
+ * inside dispatch(). */
+int oracle_front_end_internal(const double *xs, const uint32_t *sf, const uint32_t *sfs, uint32_t nsv, uint32_t nsf,
+    const double *xc, const uint32_t *cf, const uint32_t *cfs, uint32_t ncv, uint32_t ncf, double eps, int threads,
+    fe_result *out);
+void oracle_free(fe_result *r);
+
 /* The record hand-over of one front-end pass (kernel.cpp:2599-2655 and the
  * merge at kernel.cpp:2673-2714): what dispatch()'s host stages read from the
  * narrow phase. Every record becomes an intersection vertex of m0 with id

@@ -199,6 +199,182 @@ def seam(src, cut, rec_ids, rec_pts):
     return d
 
 
+SEAM_LIB = os.path.join(HERE, "_ref", "libseam_harness.so")
+
+
+def seam_available() -> bool:
+    """True when the seam harness (the reference with its front-end seam
+    opened, make_seam.py) is built or can be built here."""
+    return os.path.exists(SEAM_LIB) or ref_checkout()
+
+
+def _seam_lib():
+    if "seam" in _libs:
+        return _libs["seam"]
+    if not os.path.exists(SEAM_LIB) or ref_checkout():
+        if not ref_checkout() and not os.path.exists(SEAM_LIB):
+            raise RuntimeError("the seam harness needs MCUT_REF_ROOT (a reference checkout)")
+        if ref_checkout():
+            subprocess.run(["make", "-s", "-C", HERE, "seam", f"REF_ROOT={REF_ROOT}"], check=True)
+    _lib("port")
+    lib = C.CDLL(SEAM_LIB)
+    lib.seam_dispatch.restype = C.c_int
+    lib.seam_dispatch.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(FeSeam), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                  C.c_uint32, C.c_int, C.c_char_p, C.c_void_p, C.c_void_p, C.c_int,
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_char_p, C.c_int]
+    lib.seam_observe_reference.restype = C.c_int
+    lib.seam_observe_reference.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                           C.c_uint32, C.c_int, C.c_char_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+    lib.seam_pass_input.restype = C.c_int
+    lib.seam_pass_input.argtypes = [C.c_int, C.c_void_p, C.POINTER(C.c_double)] + [C.c_void_p] * 5
+    lib.seam_coordinate_hash.restype = C.c_uint64
+    lib.seam_coordinate_hash.argtypes = [C.c_void_p, C.c_uint64]
+    _libs["seam"] = lib
+    return lib
+
+
+def coordinate_hash(xyz) -> int:
+    """FNV-1a of ps coordinates (source then cut vertices), as a replay checks them."""
+    a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+    return int(_seam_lib().seam_coordinate_hash(a.ctypes.data, a.size))
+
+
+def observe_reference(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: int = 0,
+                      cap: int = 1 << 22):
+    """The unmodified reference's mcDispatch, observed at the seam: the records
+    of its last front-end pass in its own numbering. -> dict(result, rec_ids
+    [n,3] (q, r, tested face), rec_pts [n,3], calls)."""
+    import tempfile
+    lib = _seam_lib()
+    fin = bool(flags & MC_DISPATCH_VERTEX_ARRAY_FLOAT)
+    ks, sa = _mesh_args(src, fin)
+    kc, ca = _mesh_args(cut, fin)
+    rec = np.zeros((cap, 3), np.uint32)
+    pts = np.zeros((cap, 3), np.float64)
+    n, calls = C.c_int64(0), C.c_int(0)
+    with tempfile.TemporaryDirectory() as wd:
+        res = lib.seam_observe_reference(*sa, *ca, int(flags), int(helpers), wd.encode(), rec.ctypes.data,
+                                         pts.ctypes.data, cap, C.byref(n), C.byref(calls))
+    del ks, kc
+    m = min(n.value, cap)
+    return dict(result=int(res), rec_ids=rec[:m].copy(), rec_pts=pts[:m].copy(), calls=calls.value)
+
+
+def _fe_seam(h, keep):
+    """An FeSeam view of a hand-over dict (oracle.seam's keys); None: empty."""
+    if h is None:
+        return FeSeam()
+    def u32(a):
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.uint32).reshape(-1))
+        keep.append(a)
+        return a.ctypes.data_as(C.POINTER(C.c_uint32))
+    pts = np.ascontiguousarray(np.asarray(h["rec_pts"], dtype=np.float64).reshape(-1))
+    keep.append(pts)
+    return FeSeam(n_records=len(h["rec_ids"]), rec_ids=u32(h["rec_ids"]),
+                  rec_pts=pts.ctypes.data_as(C.POINTER(C.c_double)),
+                  n_edges=len(h["edge_off"]) - 1, edge_off=u32(h["edge_off"]),
+                  n_cutpath=len(h["cp_off"]) - 1, cp_pairs=u32(h["cp_pairs"]), cp_off=u32(h["cp_off"]),
+                  cp_vtx=u32(h["cp_vtx"]),
+                  n_faces=len(h["face_off"]) - 1, face_keys=u32(h["face_keys"]), face_off=u32(h["face_off"]),
+                  face_vtx=u32(h["face_vtx"]),
+                  n_border=len(h["border"]), border=u32(h["border"]))
+
+
+def seam_dispatch(src, cut, passes=None, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: int = 0,
+                  max_cc: int = 4096, reference_numbering: bool = False, want_inputs: bool = False):
+    """mcDispatch of the reference with its front end replaced at the seam
+    (kernel.cpp:2415-3206) and its host stages unchanged.
+
+    passes=None: the oracle computes every front-end pass (live). Otherwise a
+    list, one entry per front-end pass in order, of dict(hand_over=<dict as
+    oracle.seam or the GPU's records + Context.hand_over>, coord_hash=<int,
+    0 unchecked>, gp_violation=<bool>) replayed in turn.
+    reference_numbering renumbers each hand-over's intersection vertices in
+    the order the reference's own narrow phase gives them (its edge map's
+    iteration order, in parallel_for blocks); otherwise the hand-over's
+    canonical order is kept.
+    -> dict(result, ccs [n,3] (type, vertices, faces), used_vertices [n]
+    (vertices the CC's faces reference), calls, error, msg[, inputs: each
+    pass's soup as the hook saw it])."""
+    import tempfile
+    lib = _seam_lib()
+    fin = bool(flags & MC_DISPATCH_VERTEX_ARRAY_FLOAT)
+    ks, sa = _mesh_args(src, fin)
+    kc, ca = _mesh_args(cut, fin)
+    keep = []
+    n_rep = 0 if passes is None else len(passes)
+    arr = hashes = stats = None
+    if n_rep:
+        arr = (FeSeam * n_rep)(*[_fe_seam(p["hand_over"], keep) for p in passes])
+        hashes = np.array([int(p.get("coord_hash", 0)) for p in passes], np.uint64)
+        stats = np.array([int(bool(p.get("gp_violation", False))) for p in passes], np.int32)
+    cc = np.zeros((max_cc, 3), np.int32)
+    used = np.zeros(max_cc, np.int32)
+    n_cc, calls, err = C.c_int(0), C.c_int(0), C.c_int(0)
+    msg = C.create_string_buffer(256)
+    with tempfile.TemporaryDirectory() as wd:
+        res = lib.seam_dispatch(0 if passes is None else 1, int(bool(reference_numbering)), n_rep, arr,
+                                None if hashes is None else hashes.ctypes.data,
+                                None if stats is None else stats.ctypes.data,
+                                *sa, *ca, int(flags), int(helpers), wd.encode(), cc.ctypes.data, used.ctypes.data,
+                                max_cc, C.byref(n_cc), C.byref(calls), C.byref(err), msg, 256)
+    del ks, kc, keep
+    n = min(n_cc.value, max_cc)
+    out = dict(result=int(res), ccs=cc[:n].copy(), used_vertices=used[:n].copy(), calls=calls.value,
+               error=err.value, msg=msg.value.decode())
+    if want_inputs:
+        out["inputs"] = [_pass_input(lib, k) for k in range(calls.value)]
+    return out
+
+
+def _pass_input(lib, k):
+    cnt = np.zeros(6, np.uint32)
+    eps = C.c_double(0.0)
+    lib.seam_pass_input(k, cnt.ctypes.data, C.byref(eps), None, None, None, None, None)
+    vs, vc, fs, fc, ns, nc = (int(x) for x in cnt)
+    x = np.zeros((vs + vc, 3), np.float64)
+    si, ss = np.zeros(ns, np.uint32), np.zeros(fs, np.uint32)
+    ci, cs = np.zeros(nc, np.uint32), np.zeros(fc, np.uint32)
+    lib.seam_pass_input(k, cnt.ctypes.data, C.byref(eps), x.ctypes.data, si.ctypes.data, ss.ctypes.data,
+                        ci.ctypes.data, cs.ctypes.data)
+    tri = lambda sz: None if np.all(sz == 3) else sz  # noqa: E731
+    return dict(src=dict(v=x[:vs].copy(), f=si, fs=tri(ss)), cut=dict(v=x[vs:].copy(), f=ci, fs=tri(cs)),
+                cut_eps=float(eps.value))
+
+
+def front_end_internal(src, cut, cut_eps: float, threads: int = 0):
+    """One front-end pass of the oracle over internal (recentred) double
+    coordinates with the given cut-box enlargement (oracle_front_end_internal).
+    Same outputs as front_end."""
+    lib, _, fr = _lib("port")
+    if not hasattr(lib, "_internal_ready"):
+        lib.oracle_front_end_internal.restype = C.c_int
+        lib.oracle_front_end_internal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                                  C.c_double, C.c_int, C.POINTER(FeResult)]
+        lib._internal_ready = True
+    ks, sa = _mesh_args(src)
+    kc, ca = _mesh_args(cut)
+    res = FeResult()
+    if lib.oracle_front_end_internal(*sa, *ca, float(cut_eps), int(threads), C.byref(res)) != 0:
+        raise RuntimeError("oracle front_end_internal failed")
+    out = dict(
+        status=int(res.status), bad_face=int(res.bad_face), cut_eps=float(res.cut_eps),
+        pairs=_arr(res.pairs, 2 * res.n_pairs, np.uint32).reshape(-1, 2),
+        tests=_arr(res.tests, 3 * res.n_tests, np.uint32).reshape(-1, 3),
+        test_info=_arr(res.test_info, 4 * res.n_tests, np.int8).reshape(-1, 4),
+        rec_ids=_arr(res.rec_ids, 3 * res.n_records, np.uint32).reshape(-1, 3),
+        rec_pts=_arr(res.rec_pts, 3 * res.n_records, np.float64).reshape(-1, 3),
+    )
+    fr(C.byref(res))
+    del ks, kc
+    return out
+
+
 def _pts(*ps):
     return [np.ascontiguousarray(p, dtype=np.float64) for p in ps]
 

@@ -155,8 +155,18 @@ extern "C" int ref_front_end2(const void* sv, const uint32_t* sf, const uint32_t
     }
     add_faces(sm, S, 0);
     add_faces(cm, C, 0);
+    // the polygon soup as kernel.cpp:1593-1700 builds it: a copy of the
+    // source mesh, then each cut-mesh face as cs.get_vertices_around_face
+    // lists it (its corners from the second one on), offset by Vs
     add_faces(ps, S, 0);
-    add_faces(ps, C, nsv);
+    {
+        std::vector<vd_t> fv;
+        for (uint32_t f = 0; f < ncf; ++f) {
+            fv.clear();
+            cm.get_vertices_around_face(fv, fd_t(f), nsv);
+            ps.add_face(fv);
+        }
+    }
 
     thread_pool pool((uint32_t)n_helpers, 0);
     std::vector<bounding_box_t<vec3_<double>>> sAABB, cAABB, sFB, cFB;

@@ -9,6 +9,8 @@ cm_border_reentrant_ivtx_list and partial_cut_detected. The oracle
 device builds the same arrays with sorts and scans. Order, ids and point bits
 must all be equal.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -70,3 +72,26 @@ def test_hand_over_empty_and_batch(ctx):
     ctx.dispatch_batch([(CASES["crack1"]["src"], CASES["crack1"]["cut"])] * 2)
     with pytest.raises(RuntimeError):
         ctx._get(L.DATA_CUTPATH_PAIRS, np.uint32, 2)
+
+
+PASSES = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seam_passes.npz"))
+REENTRY = sorted((k[: -len("/passes")], p) for k in PASSES.files if k.endswith("/passes")
+                 for p in range(1, int(PASSES[k])))
+
+
+@pytest.mark.parametrize("name,k", REENTRY)
+def test_hand_over_reentry_pass(ctx, name, k):
+    """The meshes MCUT's host stages send back through the front end after a
+    first pass (floating polygons, kernel.cpp:4078-4200 / preproc.cpp
+    re-dispatch), recorded at the seam: the device's hand-over equals the
+    oracle's on them too."""
+    def mesh(side):
+        fs = PASSES[f"{name}/p{k}/{side}_fs"]
+        return dict(v=PASSES[f"{name}/p{k}/{side}_v"], f=PASSES[f"{name}/p{k}/{side}_f"], fs=fs if fs.size else None)
+    s, c = mesh("src"), mesh("cut")
+    eps = float(PASSES[f"{name}/p{k}/eps"])
+    want = oracle.front_end_internal(s, c, eps)
+    r = ctx.dispatch(s, c, cut_eps=eps, recentre=False)
+    assert r.status == want["status"]
+    if r.status in (0, 1):
+        check(ctx, r, oracle.seam(s, c, want["rec_ids"], want["rec_pts"]))
