@@ -152,3 +152,19 @@ def test_gpu_fixture_covers_every_pass(gpu_z):
     for name in sorted(k[: -len("/passes")] for k in PASSES.files if k.endswith("/passes")):
         for k in range(int(PASSES[name + "/passes"])):
             assert int(gpu_z[f"{name}/p{k}/hash"]) == int(PASSES[f"{name}/p{k}/hash"]), (name, k)
+
+
+@pytest.mark.parametrize("name", [k for k in WITH_CCS if int(CASES[k]["status"]) == 0])
+def test_fixture_records_are_mcdispatch_records(name):
+    """The unmodified reference's own narrow phase inside mcDispatch, read at
+    the seam (observer): its records and point bits equal the fixture's,
+    which the oracle and the device are compared with. Dispatches with a
+    re-entry pass are left out (the observer sees the last pass)."""
+    c = CASES[name]
+    src, cut, flags = _user_meshes(c)
+    o = oracle.observe_reference(src, cut, flags=flags)
+    if o["calls"] != 1:
+        pytest.skip("the dispatch ran more than one front-end pass")
+    key = lambda ids, pts: sorted((tuple(sorted(r[:2])) + (r[2],), p.tobytes())  # noqa: E731
+                                  for r, p in zip(np.asarray(ids).tolist(), np.asarray(pts, np.float64)))
+    assert key(o["rec_ids"], o["rec_pts"]) == key(c["rec_ids"], c["rec_pts"])
