@@ -97,7 +97,8 @@ enum BufId {
     B_VOFF, B_VCUR, B_VFACE, B_SCANTMP, B_TESTS, B_TINFO, B_RK0, B_RK1, B_RV0, B_RV1, B_RPTRAW, B_RIDS, B_RPTS,
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
-    B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT, B_COUNT
+    B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
+    B_X32, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -828,6 +829,10 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     const int key_bits = kMortonBits + pbits;
     // stage-1 buffers
     W.fbox = c->buf[B_FBOX].get<double>(L.nf * 6);
+    // fp32 vertex copies for orient3d's first filter (written by the bounds kernel)
+    W.x32 = c->buf[B_X32].get<float4>(std::max<uint64_t>(L.nv, 1));
+    P.X32 = W.x32;
+    c->Pin.X32 = W.x32;
     W.fbox32 = c->buf[B_LKB].get<float>(L.nf * 6);
     W.mesh_box = c->buf[B_MESHBOX].get<unsigned long long>((size_t)n * 12);
     W.mesh_frame = c->buf[B_FRAME].get<uint8_t>((size_t)n * 64);
@@ -1106,6 +1111,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         double* xp = c->buf[B_XPERT].get<double>(std::max<uint64_t>(nc3, 3));
         P.Xc = xp; // the cut vertices the narrow phase reads from now on
         P.xsplit = L.vs[0];
+        P.X32 = nullptr; // the fp32 copies are of the unperturbed vertices
         while (violated() && perturbations < c->gp_attempts) {
             for (int j = 0; j < 3; ++j) pert[j] = c->gp_uniform(c->gp_rng) * L.eps[0];
             ++perturbations;
@@ -1200,8 +1206,9 @@ int ensure_derived(mcgpu_context_t* c)
     w.flags = c->buf[B_DFLAGS].get<uint32_t>(7 * r + 1);
     w.sort_temp = c->buf[B_DSORT].get<uint32_t>(derived_sort_temp_bytes(R) / 4 + 64);
     w.scan_temp = c->buf[B_DSCAN].get<uint32_t>(derived_scan_temp_bytes(R) / 4 + 64);
-    // outputs back to back: edge_off R+1 | border R | cp_pairs 4R | cp_off 2R+1 | face_keys 3R | face_off 3R+1 | counts
-    uint32_t* o = c->buf[B_DOUT].get<uint32_t>(13 * r + 3 + kDerivedCounts);
+    // outputs back to back: edge_off R+1 | border R | cp_pairs 4R | cp_off 2R+1 | face_keys 3R | face_off 3R+1 |
+    // counts: 14R + 3 + kDerivedCounts words
+    uint32_t* o = c->buf[B_DOUT].get<uint32_t>(14 * r + 3 + kDerivedCounts);
     DerivedOut& d = c->derived;
     d.edge_off = o;
     d.border = d.edge_off + r + 1;
@@ -1209,7 +1216,7 @@ int ensure_derived(mcgpu_context_t* c)
     d.cp_off = d.cp_pairs + 4 * r;
     d.face_keys = d.cp_off + 2 * r + 1;
     d.face_off = d.face_keys + 3 * r;
-    d.counts = d.face_off + 3 * r + 1;
+    d.counts = d.face_off + 3 * r + 1; // == o + 14 r + 3
     d.cp_vtx = d.face_vtx = nullptr;
     const Layout& L = c->L;
     launch_derived(c->W.rec_ids, R, L.vs[0], (uint32_t)L.nv, L.fs[0], (uint32_t)L.nf, w, d, c->s);

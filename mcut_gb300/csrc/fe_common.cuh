@@ -308,6 +308,71 @@ __device__ __forceinline__ bool f32_filter_input(double d, float& f)
     f = __uint_as_float(fb);
     return true;
 }
+// A coordinate's fp32 copy for the fp32-vertex filter below: zero stays zero,
+// a magnitude in [2^-100, 2^40) is rounded to nearest (ties to even) with
+// integer operations (normal in fp32 either way), anything else becomes NaN,
+// which sends every test touching the vertex to the next stage.
+__device__ __forceinline__ float f32_vertex_coord(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if ((b << 1) == 0ull) return 0.0f;
+    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    if (e < 1023u - 100u || e > 1023u + 39u) return __uint_as_float(0x7FC00000u);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    unsigned fb = ((unsigned)(b >> 63) << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
+    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+    if (r > 0x10000000u || (r == 0x10000000u && (fb & 1u))) fb += 1u; // a carry moves into the exponent
+    return __uint_as_float(fb);
+}
+
+// Stage 0: orient3d's sign from the fp32 vertex copies, or 0 to escalate.
+// Differences s = fl(P~ - D~) of the rounded coordinates miss the true ones
+// by at most E = c (|s| + |P~| + |D~|) (c = 2^-24 (1 + 2^-20) covers the
+// coordinate rounding, the difference's rounding and E's own evaluation);
+// with M = |s| + E each monomial t_a t_b t_c of the determinant lies within
+// E_a M_b M_c + M_a E_b M_c + M_a M_b E_c of s_a s_b s_c (delta, summed over
+// the six monomials), and Shewchuk's stage-A bound covers the fp32
+// evaluation, 8u times the permanent of the M values. The bound's own
+// evaluation (products and sums of non-negative values) is covered by the
+// factor 1 + 2^-20, underflow by 2^-140; coordinates below 2^40 keep every
+// product below 2^128. tests/test_fp32_vertex_filter.py restates this
+// operation for operation and checks it against exact signs.
+__device__ __forceinline__ int orient3d_sign_f32v(float4 pa, float4 pb, float4 pc, float4 pd)
+{
+    const float kC = 0x1.00001p-24f;    // 2^-24 (1 + 2^-20)
+    const float kU8 = 0x1p-21f;         // 8 * 2^-24
+    const float kGrow = 0x1.00001p0f;   // 1 + 2^-20
+    const float kTiny = 0x1p-140f;      // 2^-140 (subnormal)
+    const float ax = pa.x - pd.x, ay = pa.y - pd.y, az = pa.z - pd.z;
+    const float bx = pb.x - pd.x, by = pb.y - pd.y, bz = pb.z - pd.z;
+    const float cx = pc.x - pd.x, cy = pc.y - pd.y, cz = pc.z - pd.z;
+    const float det = az * (bx * cy - cx * by) + bz * (cx * ay - ax * cy) + cz * (ax * by - bx * ay);
+    const float Eax = kC * ((fabsf(ax) + fabsf(pa.x)) + fabsf(pd.x));
+    const float Eay = kC * ((fabsf(ay) + fabsf(pa.y)) + fabsf(pd.y));
+    const float Eaz = kC * ((fabsf(az) + fabsf(pa.z)) + fabsf(pd.z));
+    const float Ebx = kC * ((fabsf(bx) + fabsf(pb.x)) + fabsf(pd.x));
+    const float Eby = kC * ((fabsf(by) + fabsf(pb.y)) + fabsf(pd.y));
+    const float Ebz = kC * ((fabsf(bz) + fabsf(pb.z)) + fabsf(pd.z));
+    const float Ecx = kC * ((fabsf(cx) + fabsf(pc.x)) + fabsf(pd.x));
+    const float Ecy = kC * ((fabsf(cy) + fabsf(pc.y)) + fabsf(pd.y));
+    const float Ecz = kC * ((fabsf(cz) + fabsf(pc.z)) + fabsf(pd.z));
+    const float Max = fabsf(ax) + Eax, May = fabsf(ay) + Eay, Maz = fabsf(az) + Eaz;
+    const float Mbx = fabsf(bx) + Ebx, Mby = fabsf(by) + Eby, Mbz = fabsf(bz) + Ebz;
+    const float Mcx = fabsf(cx) + Ecx, Mcy = fabsf(cy) + Ecy, Mcz = fabsf(cz) + Ecz;
+    const float P1 = Mbx * Mcy + Mcx * Mby;
+    const float Q1 = (Ebx * Mcy + Mbx * Ecy) + (Ecx * Mby + Mcx * Eby);
+    const float P2 = Mcx * May + Max * Mcy;
+    const float Q2 = (Ecx * May + Mcx * Eay) + (Eax * Mcy + Max * Ecy);
+    const float P3 = Max * Mby + Mbx * May;
+    const float Q3 = (Eax * Mby + Max * Eby) + (Ebx * May + Mbx * Eay);
+    const float permM = Maz * P1 + Mbz * P2 + Mcz * P3;
+    const float delta = (Eaz * P1 + Maz * Q1) + (Ebz * P2 + Mbz * Q2) + (Ecz * P3 + Mcz * Q3);
+    const float bound = (kU8 * permM + delta) * kGrow + kTiny;
+    if (det > bound) return 1;
+    if (-det > bound) return -1;
+    return 0;
+}
+
 __device__ __forceinline__ int orient3d_sign_filtered(const double* pa, const double* pb, const double* pc,
     const double* pd, int& stage)
 {

@@ -104,7 +104,8 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v)
 // of consecutive vertices, almost always of one mesh: each thread folds in
 // registers, the block folds in shared memory, one thread issues the
 // atomics; a tile that straddles meshes falls back to per-thread atomics.
-__global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned long long* __restrict__ mesh_box)
+__global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned long long* __restrict__ mesh_box,
+    float4* __restrict__ x32)
 {
     __shared__ unsigned long long red[kBlock / 32][6];
     __shared__ uint32_t skey;
@@ -128,6 +129,8 @@ __global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned lo
             const uint32_t k = p * 2 + ((v - P.pair_vbase[p]) >= P.pair_vs[p] ? 1u : 0u);
             double x[3];
             load_v(P, v, x);
+            // the vertex's fp32 copy for orient3d's first filter
+            if (x32) x32[v] = make_float4(f32_vertex_coord(x[0]), f32_vertex_coord(x[1]), f32_vertex_coord(x[2]), 0.0f);
             if (key != kNone && k != key) {
                 mesh_box_flush(mesh_box, key, lo, hi);
                 for (int j = 0; j < 3; ++j) { lo[j] = ~0ull; hi[j] = 0ull; }
@@ -1776,17 +1779,37 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
             int8_t sq = 0, sr = 0;
             char type = '0';
             if (t0 >= 0) {
-                double q[3], r[3], a[3], b[3], c[3];
-                load_v(P, t.q, q);
-                load_v(P, t.r, r);
-                load_v(P, face_vertex(P, o, n, t0, face_rot(P, t.g)), a);
-                load_v(P, face_vertex(P, o, n, t1, face_rot(P, t.g)), b);
-                load_v(P, face_vertex(P, o, n, t2, face_rot(P, t.g)), c);
-                int st0, st1;
-                sq = (int8_t)orient3d_sign_filtered(a, b, c, q, st0);
-                sr = (int8_t)orient3d_sign_filtered(a, b, c, r, st1);
-                esc[st0]++;
-                esc[st1]++;
+                const uint32_t rot = face_rot(P, t.g);
+                const uint32_t va = face_vertex(P, o, n, t0, rot), vb = face_vertex(P, o, n, t1, rot),
+                               vc = face_vertex(P, o, n, t2, rot);
+                // the fp32-vertex filter first; the fp64 coordinates only for
+                // the signs it leaves undecided
+                int dq = 0, dr = 0;
+                if (P.X32) {
+                    const float4 fa = P.X32[va], fb = P.X32[vb], fc = P.X32[vc];
+                    dq = orient3d_sign_f32v(fa, fb, fc, P.X32[t.q]);
+                    dr = orient3d_sign_f32v(fa, fb, fc, P.X32[t.r]);
+                    esc[ESC_F32] += (dq != 0) + (dr != 0);
+                }
+                sq = (int8_t)dq;
+                sr = (int8_t)dr;
+                if (dq == 0 || dr == 0) {
+                    double a[3], b[3], c[3], x[3];
+                    load_v(P, va, a);
+                    load_v(P, vb, b);
+                    load_v(P, vc, c);
+                    int st;
+                    if (dq == 0) {
+                        load_v(P, t.q, x);
+                        sq = (int8_t)orient3d_sign_filtered(a, b, c, x, st);
+                        esc[st]++;
+                    }
+                    if (dr == 0) {
+                        load_v(P, t.r, x);
+                        sr = (int8_t)orient3d_sign_filtered(a, b, c, x, st);
+                        esc[st]++;
+                    }
+                }
                 if (sq == 0 && sr == 0) type = 'p';
                 else if (sq == 0) type = 'q';
                 else if (sr == 0) type = 'r';
@@ -1951,15 +1974,56 @@ __global__ void __launch_bounds__(kBlock) k_pair_record_ranges(Problem P, const 
     }
 }
 
-// Rank of every record key among all keys (keys are unique: one record per
-// (edge, face)). Block (x, y) compares its 256 records with key slice y,
-// staged in shared memory, and adds its counts into rank[] -- n^2 compares
-// spread over the whole GPU in one launch, cheaper than a multi-pass radix
-// sort for the few thousand records of a dispatch.
+// Record order in two steps. k_sort_slices sorts each slice of kRankChunk
+// (key, value) pairs in place, in shared memory (bitonic network; padding
+// keys are all ones and sort last). k_rank_records then gives every record
+// its rank among all keys (unique: one record per (edge, face)): block (x, y)
+// stages sorted slice y in shared memory and each of its 256 records counts
+// the slice's smaller keys by binary search, adding the count into rank[].
+// The scatter that follows moves each record to its rank.
 #ifndef MCGPU_RANK_CHUNK
 #define MCGPU_RANK_CHUNK 512
 #endif
 constexpr int kRankChunk = MCGPU_RANK_CHUNK;
+static_assert((kRankChunk & (kRankChunk - 1)) == 0 && kRankChunk == 2 * kBlock, "one compare-exchange per thread");
+__global__ void __launch_bounds__(kBlock) k_sort_slices(unsigned long long* __restrict__ key, uint32_t* __restrict__ val,
+    uint32_t n_host, const uint32_t* __restrict__ ndev, uint32_t cap)
+{
+    __shared__ unsigned long long sk[kRankChunk];
+    __shared__ uint32_t sv[kRankChunk];
+    const uint32_t n = record_count(n_host, ndev, cap);
+    const uint32_t lo = blockIdx.x * kRankChunk;
+    if (lo >= n) return; // grids sized for a capacity
+    const uint32_t m = min(n - lo, (uint32_t)kRankChunk);
+    for (uint32_t j = threadIdx.x; j < kRankChunk; j += kBlock) {
+        sk[j] = j < m ? key[lo + j] : ~0ull;
+        sv[j] = j < m ? val[lo + j] : 0u;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= (uint32_t)kRankChunk; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            // thread t compares element a with its partner a + stride
+            const uint32_t t = threadIdx.x;
+            const uint32_t a = 2 * t - (t & (stride - 1));
+            const uint32_t b = a + stride;
+            const bool up = (a & size) == 0;
+            const unsigned long long ka = sk[a], kb = sk[b];
+            if ((ka > kb) == up) {
+                sk[a] = kb;
+                sk[b] = ka;
+                const uint32_t v = sv[a];
+                sv[a] = sv[b];
+                sv[b] = v;
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t j = threadIdx.x; j < m; j += kBlock) {
+        key[lo + j] = sk[j];
+        val[lo + j] = sv[j];
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long long* __restrict__ key, uint32_t n_host,
     const uint32_t* __restrict__ ndev, uint32_t cap, uint32_t* __restrict__ rank)
 {
@@ -1967,24 +2031,18 @@ __global__ void __launch_bounds__(kBlock) k_rank_records(const unsigned long lon
     const uint32_t n = record_count(n_host, ndev, cap);
     const uint32_t lo = blockIdx.y * kRankChunk;
     if (lo >= n || blockIdx.x * kBlock >= n) return; // grids sized for a capacity
-    const uint32_t hi = min(n, lo + kRankChunk);
-    for (uint32_t j = lo + threadIdx.x; j < hi; j += kBlock) sk[j - lo] = key[j];
+    const uint32_t m = min(n, lo + kRankChunk) - lo;
+    for (uint32_t j = threadIdx.x; j < m; j += kBlock) sk[j] = key[lo + j];
     __syncthreads();
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i >= n) return;
     const unsigned long long k = key[i];
-    const int m = (int)(hi - lo);
-    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-    int j = 0;
-    for (; j + 4 <= m; j += 4) {
-        c0 += sk[j] < k;
-        c1 += sk[j + 1] < k;
-        c2 += sk[j + 2] < k;
-        c3 += sk[j + 3] < k;
+    uint32_t a = 0, b = m; // the slice's keys below k: lower bound in the sorted slice
+    while (a < b) {
+        const uint32_t mid = (a + b) >> 1;
+        if (sk[mid] < k) a = mid + 1; else b = mid;
     }
-    for (; j < m; ++j) c0 += sk[j] < k;
-    const uint32_t c = c0 + c1 + c2 + c3;
-    if (c) atomicAdd(&rank[i], c);
+    if (a) atomicAdd(&rank[i], a);
 }
 
 // records in rank order -> sorted keys and output arrays with per-pair local ids
@@ -2076,7 +2134,7 @@ void launch_bounds_morton(const Problem& P, const Problem& Pin, Work& W, bool wi
 {
     float4* frame = reinterpret_cast<float4*>(W.mesh_frame);
     g_launches += 3;
-    k_vertex_bounds<<<grid_for(P.nv / kBoundsItems + 1), kBlock, 0, s>>>(P, W.mesh_box);
+    k_vertex_bounds<<<grid_for(P.nv / kBoundsItems + 1), kBlock, 0, s>>>(P, W.mesh_box, W.x32);
     k_mesh_frames<<<(2 * P.n_pairs + 255) / 256, 256, 0, s>>>(W.mesh_box, 2 * P.n_pairs, frame);
     const int g = grid_for(P.nf);
     if (wide)
@@ -2271,7 +2329,9 @@ int launch_records(const Problem& P, Work& W, uint32_t nrec, cudaStream_t s)
         // raw keys (slot << 32 | face) order like the packed ones
         uint32_t* rank = W.rec_val[1];
         cudaMemsetAsync(rank, 0, sizeof(uint32_t) * nrec, s);
-        g_launches += 2;
+        g_launches += 3;
+        k_sort_slices<<<(nrec + kRankChunk - 1) / kRankChunk, kBlock, 0, s>>>(W.rec_key[0], W.rec_val[0], nrec,
+            nullptr, 0);
         k_rank_records<<<dim3((nrec + kBlock - 1) / kBlock, (nrec + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
             W.rec_key[0], nrec, nullptr, 0, rank);
         k_scatter_records<<<g, kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, nrec, nullptr, 0, W.tests,
@@ -2305,7 +2365,8 @@ int launch_records_dev(const Problem& P, Work& W, uint32_t cap, cudaStream_t s)
     const uint32_t* nd = W.counters + 2;
     uint32_t* rank = W.rec_val[1];
     cudaMemsetAsync(rank, 0, sizeof(uint32_t) * cap, s);
-    g_launches += 2;
+    g_launches += 3;
+    k_sort_slices<<<(cap + kRankChunk - 1) / kRankChunk, kBlock, 0, s>>>(W.rec_key[0], W.rec_val[0], 0, nd, cap);
     k_rank_records<<<dim3((cap + kBlock - 1) / kBlock, (cap + kRankChunk - 1) / kRankChunk), kBlock, 0, s>>>(
         W.rec_key[0], 0, nd, cap, rank);
     k_scatter_records<<<grid_for(cap), kBlock, 0, s>>>(P, W.rec_key[0], W.rec_val[0], rank, 0, nd, cap, W.tests,

@@ -64,6 +64,7 @@ struct Problem {
     const uint32_t* pair_cbase; // first position of the pair in the cut-face list
     const double* pair_eps;     // cut-box enlargement
     const uint32_t* pair_clbase;// first leaf cluster of the pair
+    const float4* X32;          // fp32 copies of the vertices (orient3d's first filter); null: not used
     int all_triangles;          // foff[f] == 3f
     uint32_t leaf_size;         // cut faces per tree leaf (consecutive in Morton order, one pair)
     uint32_t ncl;               // total leaf clusters
@@ -75,6 +76,7 @@ struct Work {
     unsigned long long* mesh_box;     // [n_pairs*2*6] ordered-uint64 min/max
     uint32_t* fidx_out;               // one pair: the bounds kernel writes the global ps indices here
     uint32_t* face_pair_out;          // ... and the face -> pair table (null for a batch: k_prep made them)
+    float4* x32;                      // [nv] the bounds kernel writes each vertex's fp32 copy here (null: none)
     uint32_t* fidx_fix;               // a batch: the global table the bounds kernel reads, where it replaces an
                                       // index outside its mesh (null for one pair: fidx_out gets the fix)
     void* mesh_frame;                 // [n_pairs*2*2] float4: fp32 box low corner, 1023 / extent

@@ -96,7 +96,8 @@ constexpr size_t kSplitCap = 2048;
 constexpr size_t oSplit = oTop + al(64 * 32);
 constexpr size_t oNrange = oSplit + al(kSplitCap * 144ull);
 constexpr size_t oFrame = oNrange + al(kMaxFaces * 64ull); // split_box
-constexpr size_t kScratchBytes = oFrame + al(64);
+constexpr size_t oX32 = oFrame + al(64);
+constexpr size_t kScratchBytes = oX32 + al(kMaxVerts * 16ull);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -183,6 +184,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     P.pair_cbase = tab + 10;
     P.pair_eps = reinterpret_cast<double*>(base + oEps);
     P.pair_clbase = tab + 12;
+    P.X32 = reinterpret_cast<float4*>(base + oX32);
     P.all_triangles = 1;
     P.leaf_size = kLeafSize;
     P.ncl = ncl;
@@ -193,6 +195,7 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
     W.stack_depth = 64;
     W.split_round = 2;
     W.fbox = reinterpret_cast<double*>(base + oFbox);
+    W.x32 = reinterpret_cast<float4*>(base + oX32);
     W.mesh_box = reinterpret_cast<unsigned long long*>(base + oMbox);
     uint32_t* keys = reinterpret_cast<uint32_t*>(base + oKeys);
     // source then cut keys in one array per buffer (one sort orders both meshes)

@@ -2,7 +2,7 @@
 
 The device keeps one fp32 copy of every vertex (each coordinate rounded to
 nearest; a coordinate that is neither zero nor of magnitude in
-[2^-100, 2^40] is stored as NaN, which sends every test touching it to the
+[2^-100, 2^40) is stored as NaN, which sends every test touching it to the
 next stage). For a test it forms the nine coordinate differences in fp32
 from those copies, evaluates Shewchuk's orient3d expression in fp32, and
 decides the sign only when |det| exceeds a bound that covers
@@ -22,8 +22,8 @@ decides the sign only when |det| exceeds a bound that covers
     and sums of non-negative fp32 values: a factor 1 + 2^-20) and underflow
     (2^-140 absolute, far above the few 2^-149 ulps underflow can lose).
 
-bound = (8u permM + delta)(1 + 2^-20) + 2^-140. Coordinates of magnitude at
-most 2^40 keep every product below 2^128 (no overflow).
+bound = (8u permM + delta)(1 + 2^-20) + 2^-140. Coordinates of magnitude
+below 2^40 keep every product below 2^128 (no overflow).
 
 This module restates that arithmetic operation for operation in numpy float32
 (IEEE round to nearest, no fused multiply-add, as the device build with
@@ -49,7 +49,7 @@ def to_f32(x):
     """The device's fp32 vertex copy: nearest, NaN outside the admitted range."""
     x = np.asarray(x, np.float64)
     m = np.abs(x)
-    ok = (x == 0) | ((m >= LO) & (m <= HI))
+    ok = (x == 0) | ((m >= LO) & (m < HI))
     with np.errstate(over="ignore"):
         return np.where(ok, x.astype(np.float32), F(np.nan))
 
@@ -161,7 +161,7 @@ def test_mixed_scale_axes():
 def test_coordinates_outside_the_range_escalate():
     rng = np.random.default_rng(12)
     a, b, c, d = (rng.standard_normal((500, 3)) for _ in range(4))
-    for bad in (2.0 ** 41, 2.0 ** -110, np.inf):
+    for bad in (2.0 ** 40, 2.0 ** 41, 2.0 ** -110, np.inf, np.nan):
         a2 = a.copy()
         a2[:, 1] = bad
         decided, _ = filter_sign(a2, b, c, d)
