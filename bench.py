@@ -425,7 +425,41 @@ def run_configs(ctx, lib, world, cpu=True):
                  "ms_per_dispatch_e2e": float(np.median(te)),
                  "escalations": {"fp32_filter": esc[0], "fp64_filter": esc[1], "exact": esc[2],
                                  "rates": [e / tot for e in esc]}}
+    out["hmesh"] = run_hmesh(ctx, cpu)
     return out
+
+
+def run_hmesh(ctx, cpu=True):
+    """The halfedge mesh and input checks of the headline pair's two meshes
+    (client_input_arrays_to_hmesh + check_input_mesh + mesh_is_closed) on the
+    device, from device-resident indices, wall time per call (the call reads
+    its counts back); beside it the CPU restatement of MCUT's face-by-face
+    loop (oracle/hmesh_oracle.c, one thread) on the same meshes."""
+    import torch
+    from mcut_gb300 import meshgen
+    s, c = meshgen.sphere_heightfield(16.0)
+    res = {"workload": "halfedge mesh + input checks of the C2x16 meshes (327,680 and 2,093,058 tris)"}
+    for name, m in (("source", s), ("cut", c)):
+        f = torch.from_numpy(np.ascontiguousarray(m["f"], np.uint32).view(np.int32)).cuda()
+        mesh = dict(f=f, fs=None, nv=len(m["v"]))
+        for _ in range(3):
+            r = ctx.halfedge_mesh(mesh, device=True, fetch=False)
+        ts = []
+        for _ in range(10):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = ctx.halfedge_mesh(mesh, device=True, fetch=False)
+            ts.append(1e3 * (time.perf_counter() - t0))
+        row = {"faces": int(len(m["f"]) // 3), "edges": int(r["n_edges"]), "status": int(r["status"]),
+               "closed": bool(r["closed"]), "gpu_ms": float(np.median(ts)), "kernel_launches": int(r["kernel_launches"])}
+        if cpu:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            t0 = time.perf_counter()
+            oracle.hmesh(m["f"], None, len(m["v"]), "port")
+            row["cpu_port_1_thread_ms"] = 1e3 * (time.perf_counter() - t0)
+        res[name] = row
+    return res
 
 
 SERVED_WORKLOAD = ("served: open-loop Poisson arrivals; each request one fracture pair with total triangles "

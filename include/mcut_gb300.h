@@ -150,7 +150,16 @@ typedef enum mcgpu_data {
     MCGPU_DATA_FACE_VERTICES = 15,       /* uint32[o[M]]: m0 ids */
     MCGPU_DATA_BORDER_VERTICES = 16,     /* uint32[B]: m0 ids of records on cut-mesh border edges
                                             (cm_border_reentrant_ivtx_list) */
-    MCGPU_DATA_PARTIAL_CUT = 17          /* uint32[1]: 1 if B > 0 (partial_cut_detected), else 0 */
+    MCGPU_DATA_PARTIAL_CUT = 17,         /* uint32[1]: 1 if B > 0 (partial_cut_detected), else 0 */
+    /* The halfedge mesh of the last mcgpu_halfedge_mesh call (E edges, halfedge 2e runs the way the
+     * face corner that created edge e runs, 2e + 1 the other way; hmesh.cpp:406-651) */
+    MCGPU_DATA_HE_TARGET = 18,           /* uint32[2E]: vertex each halfedge ends at */
+    MCGPU_DATA_HE_FACE = 19,             /* int32[2E]: its face, -1 on a border */
+    MCGPU_DATA_HE_NEXT = 20,             /* int32[2E]: next halfedge around its face, -1 on a border */
+    MCGPU_DATA_HE_PREV = 21,             /* int32[2E] */
+    MCGPU_DATA_CORNER_HE = 22,           /* uint32[corners]: the halfedge of face corner i (v_i -> v_i+1) */
+    MCGPU_DATA_VERTEX_HE_OFFSETS = 23,   /* uint32[V+1]: vertex v's halfedges are [o[v], o[v+1]) of ... */
+    MCGPU_DATA_VERTEX_HE = 24            /* uint32[2E]: the halfedges ending at each vertex, in creation order */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.
@@ -278,6 +287,39 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
  * end's outcome is out->status. */
 int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const mcgpu_mesh* cut, double cut_eps,
     uint32_t* record_ids, double* record_points, uint64_t record_capacity, mcgpu_summary* out);
+
+/* Outcome of mcgpu_halfedge_mesh, in the order MCUT checks a mesh. */
+typedef enum mcgpu_hmesh_status {
+    MCGPU_HMESH_OK = 0,
+    MCGPU_HMESH_FACE_SIZE = 1,       /* a face with fewer than 3 vertices */
+    MCGPU_HMESH_INDEX_RANGE = 2,     /* an index >= the mesh's vertex count */
+    MCGPU_HMESH_DUPLICATE_INDEX = 3, /* a vertex twice in one face */
+    MCGPU_HMESH_NON_MANIFOLD = 4,    /* a directed halfedge in two faces */
+    MCGPU_HMESH_TOO_SMALL = 5,       /* fewer than 3 vertices or no face */
+    MCGPU_HMESH_COMPONENTS = 6       /* the vertex graph is not one connected component */
+} mcgpu_hmesh_status;
+
+typedef struct mcgpu_hmesh_report {
+    int32_t status;           /* mcgpu_hmesh_status */
+    int32_t bad_face;         /* the face a conversion error (codes 1-4) stopped at, else -1 */
+    uint32_t num_edges;       /* set once the conversion succeeded (codes 0, 5, 6) */
+    uint32_t num_components;  /* connected components of the vertex graph (codes 0, 6) */
+    int32_t closed;           /* every halfedge has a face (mesh_is_closed); set with num_edges */
+    uint32_t kernel_launches; /* CUDA kernels this call launched */
+} mcgpu_hmesh_report;
+
+/* MCUT's halfedge mesh of one input mesh and its input checks, on the
+ * device. Replaces client_input_arrays_to_hmesh (preproc.cpp:57-468, face by
+ * face through hmesh_t::add_face / add_edge, hmesh.cpp:406-651),
+ * check_input_mesh (preproc.cpp:505-579) and mesh_is_closed
+ * (preproc.cpp:1957-1994): the same status and failing face as that
+ * face-by-face loop, the same edge and halfedge numbering, next / prev links
+ * and per-vertex halfedge lists. Only the indices and face sizes are read
+ * (vertices may be NULL); with MCGPU_DEVICE_POINTERS they are device arrays.
+ * The arrays stay in the context until its next mcgpu_halfedge_mesh call
+ * (mcgpu_get_data queries 18-24). Returns MCGPU_OK when it ran; the
+ * mesh's outcome is out->status. */
+int mcgpu_halfedge_mesh(mcgpu_context ctx, uint32_t flags, const mcgpu_mesh* mesh, mcgpu_hmesh_report* out);
 
 /* ---- Request server: continuous batching on one GPU ------------------------
  * Replaces MCUT's per-context task queue for the front end (mcEnqueueDispatch,

@@ -34,6 +34,13 @@ DATA_RECORD_IDS, DATA_RECORD_POINTS, DATA_PAIRS, DATA_TESTS, DATA_TEST_INFO, DAT
 DATA_EDGE_RECORD_OFFSETS, DATA_CUTPATH_PAIRS, DATA_CUTPATH_OFFSETS, DATA_CUTPATH_VERTICES, DATA_FACE_KEYS, \
     DATA_FACE_OFFSETS, DATA_FACE_VERTICES, DATA_BORDER_VERTICES, DATA_PARTIAL_CUT = range(9, 18)
 
+# the halfedge mesh of the last mcgpu_halfedge_mesh call
+DATA_HE_TARGET, DATA_HE_FACE, DATA_HE_NEXT, DATA_HE_PREV, DATA_CORNER_HE, DATA_VERTEX_HE_OFFSETS, \
+    DATA_VERTEX_HE = range(18, 25)
+# mcgpu_hmesh_status (the oracle's HM_* values)
+HMESH_OK, HMESH_FACE_SIZE, HMESH_INDEX_RANGE, HMESH_DUPLICATE_INDEX, HMESH_NON_MANIFOLD, HMESH_TOO_SMALL, \
+    HMESH_COMPONENTS = range(7)
+
 STAGES = ["upload", "bounds", "sort", "hierarchy", "traverse", "adjacency", "narrow", "download"]
 
 
@@ -69,6 +76,11 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "batches", "pending", "inflight_bytes",
                                           "peak_inflight_bytes", "resident_bytes", "resident_meshes")]
+
+
+class HmeshReport(C.Structure):
+    _fields_ = [("status", C.c_int32), ("bad_face", C.c_int32), ("num_edges", C.c_uint32),
+                ("num_components", C.c_uint32), ("closed", C.c_int32), ("kernel_launches", C.c_uint32)]
 
 
 class LibraryNotBuilt(RuntimeError):

@@ -15,6 +15,7 @@
 
 #include "fe_common.cuh"
 #include "fe_derived.cuh"
+#include "fe_hmesh.cuh"
 #include "fe_host.h"
 #include "fe_kernels.cuh"
 #include "fe_sort.cuh"
@@ -98,7 +99,11 @@ enum BufId {
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
-    B_X32, B_COUNT
+    B_X32,
+    // the halfedge mesh (mcgpu_halfedge_mesh)
+    B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
+    B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
+    B_HM_VHE, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -161,6 +166,11 @@ struct mcgpu_context_t {
     bool derived_ready = false;
     mcgpu::DerivedOut derived {};
     uint32_t derived_counts[mcgpu::kDerivedCounts] = {};
+    // the last halfedge mesh (mcgpu_halfedge_mesh); valid when hm_ready
+    bool hm_ready = false;
+    uint32_t hm_ne = 0, hm_nv = 0;
+    uint64_t hm_nidx = 0;
+    mcgpu::HmeshOut hm {};
 };
 
 namespace {
@@ -1570,6 +1580,26 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
             }
             }
         }
+        case MCGPU_DATA_HE_TARGET:
+        case MCGPU_DATA_HE_FACE:
+        case MCGPU_DATA_HE_NEXT:
+        case MCGPU_DATA_HE_PREV:
+        case MCGPU_DATA_CORNER_HE:
+        case MCGPU_DATA_VERTEX_HE_OFFSETS:
+        case MCGPU_DATA_VERTEX_HE: {
+            if (!c->hm_ready) return fail(MCGPU_INVALID_VALUE, "no halfedge mesh (mcgpu_halfedge_mesh) built");
+            const uint64_t nhe = 2ull * c->hm_ne;
+            switch (query) {
+            case MCGPU_DATA_HE_TARGET: return copy_out(c, c->hm.he_target, 4 * nhe, bytes, mem, bytes_out);
+            case MCGPU_DATA_HE_FACE: return copy_out(c, c->hm.he_face, 4 * nhe, bytes, mem, bytes_out);
+            case MCGPU_DATA_HE_NEXT: return copy_out(c, c->hm.he_next, 4 * nhe, bytes, mem, bytes_out);
+            case MCGPU_DATA_HE_PREV: return copy_out(c, c->hm.he_prev, 4 * nhe, bytes, mem, bytes_out);
+            case MCGPU_DATA_CORNER_HE: return copy_out(c, c->hm.corner_he, 4 * c->hm_nidx, bytes, mem, bytes_out);
+            case MCGPU_DATA_VERTEX_HE_OFFSETS:
+                return copy_out(c, c->hm.v_off, 4ull * (c->hm_nv + 1), bytes, mem, bytes_out);
+            default: return copy_out(c, c->hm.v_he, 4 * nhe, bytes, mem, bytes_out);
+            }
+        }
         case MCGPU_DATA_RECORD_OFFSETS: {
             const uint64_t need = c->rec_begin.size() * 8;
             if (bytes_out) *bytes_out = need;
@@ -1603,6 +1633,138 @@ int mcgpu_get_batch_data(mcgpu_context c, uint32_t pair, uint32_t query, uint64_
         }
     } catch (const CudaError& e) {
         return fail(MCGPU_CUDA_ERROR, e.where + ": " + cudaGetErrorString(e.e));
+    }
+}
+
+int mcgpu_halfedge_mesh(mcgpu_context c, uint32_t flags, const mcgpu_mesh* m, mcgpu_hmesh_report* out)
+{
+    if (out) memset(out, 0, sizeof *out);
+    if (!c || !m || !out) return fail(MCGPU_INVALID_VALUE, "null argument");
+    out->bad_face = -1;
+    if (m->num_faces && !m->face_indices) return fail(MCGPU_INVALID_VALUE, "null face indices");
+    const bool dev = (flags & MCGPU_DEVICE_POINTERS) != 0;
+    try {
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        cudaStream_t s = c->s;
+        c->hm_ready = false;
+        const unsigned long long launches0 = g_launches;
+        const uint32_t nf = m->num_faces, nv = m->num_vertices;
+        uint32_t* foff = nullptr;
+        uint64_t nidx = 3ull * nf;
+        uint32_t* scan_temp = nullptr;
+        auto scan_space = [&](uint64_t n) {
+            scan_temp = c->buf[B_HM_SCAN].get<uint32_t>(scan_temp_bytes((uint32_t)std::min<uint64_t>(n, 0xFFFFFFFFull)) / 4 + 64);
+        };
+        if (m->face_sizes) {
+            foff = c->buf[B_HM_FOFF].get<uint32_t>((size_t)nf + 1);
+            if (dev) {
+                // face offsets on the device: exclusive scan of the sizes, the corner count after them
+                ck(cudaMemcpyAsync(foff, m->face_sizes, 4ull * nf, cudaMemcpyDeviceToDevice, s), "D2D sizes");
+                ck(cudaMemsetAsync(foff + nf, 0, 4, s), "memset");
+                scan_space((uint64_t)nf + 1);
+                exclusive_scan(foff, nf + 1, nullptr, scan_temp, s);
+                uint32_t tot = 0;
+                ck(cudaMemcpyAsync(&tot, foff + nf, 4, cudaMemcpyDeviceToHost, s), "D2H corners");
+                ck(cudaStreamSynchronize(s), "sync corners");
+                nidx = tot;
+            } else {
+                std::vector<uint32_t> off((size_t)nf + 1);
+                uint64_t o = 0;
+                for (uint32_t f = 0; f < nf; ++f) {
+                    off[f] = (uint32_t)o;
+                    o += m->face_sizes[f];
+                    if (o > 0x7FFFFFFFull) return fail(MCGPU_TOO_LARGE, "more than 2^31 face corners");
+                }
+                off[nf] = (uint32_t)o;
+                nidx = o;
+                ck(cudaMemcpyAsync(foff, off.data(), 4ull * (nf + 1), cudaMemcpyHostToDevice, s), "H2D offsets");
+                ck(cudaStreamSynchronize(s), "sync offsets"); // `off` is a pageable temporary
+            }
+        }
+        if (nidx > 0x7FFFFFFFull || nv >= 0x7FFFFFFFu) return fail(MCGPU_TOO_LARGE, "more than 2^31 corners or vertices");
+        const uint32_t* idx = m->face_indices;
+        if (!dev && nidx) {
+            uint32_t* d = c->buf[B_HM_IDX].get<uint32_t>(nidx);
+            ck(cudaMemcpyAsync(d, m->face_indices, 4 * nidx, cudaMemcpyHostToDevice, s), "H2D indices");
+            idx = d;
+        }
+        HmeshInput in { idx, foff, nv, nf, nidx };
+        uint64_t buckets = 64;
+        while (buckets < 2 * nidx) buckets <<= 1;
+        HmeshTable t {};
+        t.key = c->buf[B_HM_KEY].get<unsigned long long>(buckets);
+        t.first = c->buf[B_HM_FIRST].get<uint32_t>(buckets);
+        t.dir_first = c->buf[B_HM_DIR].get<uint32_t>(2 * buckets);
+        t.mask = buckets - 1;
+        HmeshScratch w {};
+        const size_t ni = std::max<uint64_t>(nidx, 1);
+        w.slot_face = foff ? c->buf[B_HM_SLOTFACE].get<uint32_t>(ni) : nullptr;
+        w.slot_bucket = c->buf[B_HM_BUCKET].get<uint32_t>(ni);
+        w.eid = c->buf[B_HM_EID].get<uint32_t>(ni);
+        w.vcur = c->buf[B_HM_VCUR].get<uint32_t>(std::max<uint32_t>(nv, 1));
+        w.parent = c->buf[B_HM_PARENT].get<uint32_t>(std::max<uint32_t>(nv, 1));
+        scan_space(std::max<uint64_t>(nidx, (uint64_t)nv + 1));
+        w.scan_temp = scan_temp;
+        uint32_t* small = c->buf[B_HM_SMALL].get<uint32_t>(16);
+        w.err = reinterpret_cast<unsigned long long*>(small);
+        w.counts = small + 2;
+        ck(cudaMemsetAsync(t.key, 0, 8 * buckets, s), "memset");
+        ck(cudaMemsetAsync(t.first, 0xFF, 4 * buckets, s), "memset");
+        ck(cudaMemsetAsync(t.dir_first, 0xFF, 8 * buckets, s), "memset");
+        ck(cudaMemsetAsync(small, 0, 64, s), "memset");
+        ck(cudaMemsetAsync(w.err, 0xFF, 8, s), "memset");
+        launch_hmesh_edges(in, t, w, s);
+        uint32_t hs[16];
+        ck(cudaMemcpyAsync(hs, small, 64, cudaMemcpyDeviceToHost, s), "D2H hmesh");
+        ck(cudaStreamSynchronize(s), "sync hmesh");
+        unsigned long long err;
+        memcpy(&err, hs, 8);
+        out->kernel_launches = (uint32_t)(g_launches - launches0);
+        if (err == ~0ull - 1) return fail(MCGPU_CUDA_ERROR, "halfedge mesh: edge table probe bound reached");
+        if (err != ~0ull) {
+            out->status = (int32_t)(err & 7u);
+            out->bad_face = (int32_t)(err >> 3);
+            return MCGPU_OK;
+        }
+        const uint32_t ne = hs[2 + kHmEdges];
+        const size_t nhe = std::max<uint64_t>(2ull * ne, 1);
+        HmeshOut& o = c->hm;
+        o.he_target = c->buf[B_HM_TGT].get<uint32_t>(nhe);
+        o.he_face = c->buf[B_HM_FACE].get<int32_t>(nhe);
+        o.he_next = c->buf[B_HM_NEXT].get<int32_t>(nhe);
+        o.he_prev = c->buf[B_HM_PREV].get<int32_t>(nhe);
+        o.corner_he = c->buf[B_HM_CORNER].get<uint32_t>(ni);
+        o.v_off = c->buf[B_HM_VOFF].get<uint32_t>((size_t)nv + 1);
+        o.v_he = c->buf[B_HM_VHE].get<uint32_t>(nhe);
+        ck(cudaMemsetAsync(o.he_face, 0xFF, 4 * nhe, s), "memset");
+        ck(cudaMemsetAsync(o.he_next, 0xFF, 4 * nhe, s), "memset");
+        ck(cudaMemsetAsync(o.he_prev, 0xFF, 4 * nhe, s), "memset");
+        ck(cudaMemsetAsync(o.v_off, 0, 4 * ((size_t)nv + 1), s), "memset");
+        ck(cudaMemsetAsync(w.vcur, 0, 4ull * std::max<uint32_t>(nv, 1), s), "memset");
+        launch_hmesh_build(in, t, w, o, ne, s);
+        ck(cudaMemcpyAsync(hs, small, 64, cudaMemcpyDeviceToHost, s), "D2H hmesh");
+        ck(cudaStreamSynchronize(s), "sync hmesh");
+        ck(cudaGetLastError(), "hmesh launch");
+        memcpy(&err, hs, 8);
+        out->kernel_launches = (uint32_t)(g_launches - launches0);
+        if (err != ~0ull) return fail(MCGPU_CUDA_ERROR, "halfedge mesh: union-find retry bound reached");
+        c->hm_ready = true;
+        c->hm_ne = ne;
+        c->hm_nv = nv;
+        c->hm_nidx = nidx;
+        out->num_edges = ne;
+        out->closed = hs[2 + kHmBorder] ? 0 : 1;
+        // check_input_mesh (preproc.cpp:505-579): after the conversion
+        if (nv < 3 || nf < 1) {
+            out->status = MCGPU_HMESH_TOO_SMALL;
+            return MCGPU_OK;
+        }
+        out->num_components = hs[2 + kHmComponents];
+        out->status = out->num_components == 1 ? MCGPU_HMESH_OK : MCGPU_HMESH_COMPONENTS;
+        return MCGPU_OK;
+    } catch (const CudaError& e) {
+        return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
+            e.where + ": " + cudaGetErrorString(e.e));
     }
 }
 

@@ -314,13 +314,13 @@ __device__ __forceinline__ bool f32_filter_input(double d, float& f)
 // which sends every test touching the vertex to the next stage.
 __device__ __forceinline__ float f32_vertex_coord(double x)
 {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    if ((b << 1) == 0ull) return 0.0f;
-    const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+    // on the two 32-bit halves: sign | exponent (11) | mantissa high (20) and mantissa low (32)
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    if (((hi << 1) | lo) == 0u) return 0.0f;
+    const unsigned e = (hi >> 20) & 0x7FFu;
     if (e < 1023u - 100u || e > 1023u + 39u) return __uint_as_float(0x7FC00000u);
-    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-    unsigned fb = ((unsigned)(b >> 63) << 31) | ((e - 1023u + 127u) << 23) | (unsigned)(m >> 29);
-    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);
+    unsigned fb = (hi & 0x80000000u) | ((e - 1023u + 127u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned r = lo & 0x1FFFFFFFu;
     if (r > 0x10000000u || (r == 0x10000000u && (fb & 1u))) fb += 1u; // a carry moves into the exponent
     return __uint_as_float(fb);
 }

@@ -127,6 +127,34 @@ class Context:
         d["partial_cut"] = bool(g(L.DATA_PARTIAL_CUT).reshape(-1)[0])
         return d
 
+    def halfedge_mesh(self, mesh, device: bool = False, fetch: bool = True) -> dict:
+        """MCUT's halfedge mesh of one mesh and its input checks on the device
+        (mcgpu_halfedge_mesh). mesh: dict(f=indices, fs=sizes or None,
+        v or nv=vertex count); with ``device`` f (and fs) are torch CUDA
+        tensors. -> dict(status, bad_face, n_edges, n_components, closed,
+        kernel_launches[, he_target, he_face, he_next, he_prev, corner_he,
+        v_off, v_he])."""
+        ptr = (lambda a: a.data_ptr()) if device else (lambda a: a.ctypes.data)
+        f = mesh["f"] if device else np.ascontiguousarray(mesh["f"], dtype=np.uint32)
+        fs = mesh.get("fs")
+        if fs is not None and not device:
+            fs = np.ascontiguousarray(fs, dtype=np.uint32)
+        nv = int(mesh["nv"]) if "nv" in mesh else int(len(mesh["v"]))
+        nf = int(fs.shape[0]) if fs is not None else int(f.shape[0] // 3)
+        cm = L.Mesh(None, ptr(f) if nf else None, None if fs is None else ptr(fs), nv, nf)
+        rep = L.HmeshReport()
+        L.check(self._lib.mcgpu_halfedge_mesh(self._h, L.DEVICE_POINTERS if device else 0, C.byref(cm),
+                                              C.byref(rep)), "mcgpu_halfedge_mesh")
+        out = dict(status=rep.status, bad_face=rep.bad_face, n_edges=rep.num_edges,
+                   n_components=rep.num_components, closed=bool(rep.closed), kernel_launches=rep.kernel_launches)
+        if fetch and rep.status in (L.HMESH_OK, L.HMESH_TOO_SMALL, L.HMESH_COMPONENTS):
+            g = lambda q, dt: self._get(q, dt, 1).reshape(-1)  # noqa: E731
+            out.update(he_target=g(L.DATA_HE_TARGET, np.uint32), he_face=g(L.DATA_HE_FACE, np.int32),
+                       he_next=g(L.DATA_HE_NEXT, np.int32), he_prev=g(L.DATA_HE_PREV, np.int32),
+                       corner_he=g(L.DATA_CORNER_HE, np.uint32), v_off=g(L.DATA_VERTEX_HE_OFFSETS, np.uint32),
+                       v_he=g(L.DATA_VERTEX_HE, np.uint32))
+        return out
+
     def set_general_position(self, constant: float = 1e-4, attempts: int = 4):
         """Enforcement constant and attempts (mcBindState MC_CONTEXT_GENERAL_POSITION_ENFORCEMENT_*)."""
         L.check(self._lib.mcgpu_context_set_general_position(self._h, float(constant), int(attempts)),

@@ -22,6 +22,7 @@ BUILD = os.path.join(ROOT, "tests", "_build")
 STRUCTS = [
     ("mcgpu_mesh", L.Mesh), ("mcgpu_batch", L.Batch), ("mcgpu_summary", L.Summary),
     ("mcgpu_tuning", L.Tuning), ("mcgpu_server_config", L.ServerConfig), ("mcgpu_server_stats", L.ServerStats),
+    ("mcgpu_hmesh_report", L.HmeshReport),
     ("fe_result", oracle.FeResult), ("hm_result", oracle.HmResult),
 ]
 

@@ -133,3 +133,41 @@ def test_directed_rounding_is_the_nearest_float_on_each_side():
                                     else (-math.inf, -float(np.finfo(np.float32).max))), x
             else:
                 assert rd == want_rd and ru == want_ru, (x, rd, want_rd, ru, want_ru)
+
+
+def f32_vertex_coord(x):
+    """f32_vertex_coord (fe_common.cuh) on the double's two 32-bit halves:
+    zero stays zero, a magnitude in [2^-100, 2^40) rounds to nearest (ties to
+    even), anything else is NaN."""
+    u = _bits(x)
+    hi, lo = u >> 32, u & 0xFFFFFFFF
+    if ((hi << 1) & 0xFFFFFFFF) | lo == 0:
+        return 0.0
+    e = (hi >> 20) & 0x7FF
+    if e < 1023 - 100 or e > 1023 + 39:
+        return float("nan")
+    fb = (hi & 0x80000000) | ((e - 1023 + 127) << 23) | ((hi & 0xFFFFF) << 3) | (lo >> 29)
+    r = lo & 0x1FFFFFFF
+    if r > 0x10000000 or (r == 0x10000000 and (fb & 1)):
+        fb += 1
+    return float(np.frombuffer(np.uint32(fb).tobytes(), np.float32)[0])
+
+
+def test_vertex_copy_rounding_is_ieee_nearest():
+    rng = np.random.default_rng(21)
+    xs = list(_samples(rng, 20000))
+    # exact ties, carries into the exponent, the range edges
+    for e in (-100, -99, -1, 0, 1, 20, 39):
+        b = 2.0 ** e
+        xs += [b, -b, b * (1 + 2.0 ** -24), b * (1 + 3 * 2.0 ** -24), b * (2 - 2.0 ** -30), b * (1 - 2.0 ** -40)]
+    xs += [2.0 ** 40, 2.0 ** -101, 0.0, -0.0, math.inf, -math.inf, math.nan]
+    for x in xs:
+        got = f32_vertex_coord(x)
+        m = abs(x)
+        if x == 0:
+            assert got == 0.0
+        elif not (2.0 ** -100 <= m < 2.0 ** 40):
+            assert math.isnan(got), x
+        else:
+            want = float(np.float32(x))
+            assert got == want, (x, got, want)
