@@ -58,7 +58,8 @@ typedef enum mcgpu_status {
     MCGPU_OUT_OF_MEMORY = 6,
     MCGPU_INVALID_VALUE = 7,       /* bad argument (null pointer, unknown query, ...) */
     MCGPU_TOO_LARGE = 8,           /* exceeds a fixed capacity of the entry point */
-    MCGPU_NOT_READY = 9            /* a served request has not completed yet */
+    MCGPU_NOT_READY = 9,           /* a served request has not completed yet */
+    MCGPU_CANCELLED = 10           /* a served request was cancelled before it ran */
 } mcgpu_status;
 
 /* dispatch flags */
@@ -112,7 +113,8 @@ typedef struct mcgpu_summary {
     uint64_t num_pairs;       /* candidate (source face, cut face) pairs */
     uint64_t num_tests;       /* culled edge-face tests */
     uint64_t num_records;     /* intersection records (type '1', point inside) */
-    uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, exact stage */
+    uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, exact stage
+                                 (in a batch, these four counts are the pair's own) */
     float stage_ms[8];        /* per-stage device time of the call (MCGPU_PROFILE; a batch's
                                  summaries all carry the batch's times) */
     uint32_t kernel_launches; /* CUDA kernels this call launched (whole batch) */
@@ -333,10 +335,15 @@ int mcgpu_halfedge_mesh(mcgpu_context ctx, uint32_t flags, const mcgpu_mesh* mes
  * the caller's arrays must stay valid until the request completes
  * (frontend.cpp:690-711). Cut meshes added with mcgpu_server_add_cut_mesh
  * stay resident on the device: a request naming one uploads only its
- * source mesh. Admission: the estimated device bytes of the requests in
- * flight plus the resident meshes stay within hbm_budget_bytes (a request
- * that alone exceeds it returns MCGPU_TOO_LARGE; one request on an idle
- * device is always admitted). */
+ * source mesh. Device memory: the resident meshes plus what every worker
+ * may hold -- its pool while idle, its batch's cap while it runs one --
+ * stay within hbm_budget_bytes. A batch's cap is its requests' estimated
+ * bytes with slack; its context cannot grow past it
+ * (mcgpu_context_set_memory_limit). Idle workers' pools are freed when a
+ * batch does not fit beside them; a batch that meets its cap runs again
+ * with all the free budget, then in halves, and a request that still does
+ * not fit completes with MCGPU_TOO_LARGE (as does one whose estimate alone
+ * exceeds the budget, at submission). */
 typedef struct mcgpu_server_t* mcgpu_server;
 
 typedef struct mcgpu_server_config {
@@ -352,7 +359,13 @@ typedef struct mcgpu_server_config {
 
 typedef struct mcgpu_server_stats {
     uint64_t submitted, completed, batches, pending;
-    uint64_t inflight_bytes, peak_inflight_bytes, resident_bytes, resident_meshes;
+    uint64_t inflight_bytes, peak_inflight_bytes; /* estimated bytes of the requests in batches */
+    uint64_t resident_bytes, resident_meshes;
+    uint64_t pool_bytes;          /* device bytes the workers' pools hold now */
+    uint64_t peak_reserved_bytes; /* peak of resident bytes + every worker's allowance: the bound
+                                     on the device memory the server held */
+    uint64_t pool_trims;          /* pools freed to make room */
+    uint64_t cancelled;           /* requests cancelled before they ran */
 } mcgpu_server_stats;
 
 int mcgpu_server_create(mcgpu_server* server, const mcgpu_server_config* config);
@@ -363,6 +376,10 @@ int mcgpu_server_add_cut_mesh(mcgpu_server server, const mcgpu_mesh* cut, uint32
 /* Queue one request: `cut`, or NULL and a resident `cut_id`. */
 int mcgpu_server_submit(mcgpu_server server, const mcgpu_mesh* src, const mcgpu_mesh* cut, uint32_t cut_id,
     uint64_t* ticket);
+/* Take a queued request out of the queue before a batch takes it: it
+ * completes with MCGPU_CANCELLED (MCGPU_NOT_READY: it is in a running batch;
+ * MCGPU_INVALID_VALUE: it has completed). Its ticket stays until released. */
+int mcgpu_server_cancel(mcgpu_server server, uint64_t ticket);
 /* Wait for a request (timeout_ms < 0: no limit; MCGPU_NOT_READY on timeout).
  * latency_ms: submission to records on the host. */
 int mcgpu_server_wait(mcgpu_server server, uint64_t ticket, int timeout_ms, mcgpu_summary* out,
@@ -372,6 +389,18 @@ int mcgpu_server_get_data(mcgpu_server server, uint64_t ticket, uint32_t query, 
     uint64_t* bytes_out);
 int mcgpu_server_release_request(mcgpu_server server, uint64_t ticket);
 int mcgpu_server_get_stats(mcgpu_server server, mcgpu_server_stats* out);
+
+/* ---- Device memory of a context ------------------------------------------
+ * A context keeps its device buffers between calls (a grow-only pool).
+ * mcgpu_context_get_memory: the bytes the pool holds now and its cap.
+ * mcgpu_context_set_memory_limit: a call that would grow the pool past
+ * limit_bytes fails with MCGPU_OUT_OF_MEMORY before that buffer is freed
+ * (0: no cap). mcgpu_context_trim: waits for the context's streams, then
+ * frees the whole pool and the captured launch graphs; the record, pair,
+ * hand-over and halfedge-mesh queries of earlier calls are gone. */
+int mcgpu_context_get_memory(mcgpu_context ctx, uint64_t* device_bytes, uint64_t* limit_bytes);
+int mcgpu_context_set_memory_limit(mcgpu_context ctx, uint64_t limit_bytes);
+int mcgpu_context_trim(mcgpu_context ctx);
 
 /* Human-readable description of the last failure on this thread. */
 const char* mcgpu_last_error(void);

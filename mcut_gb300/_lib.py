@@ -14,9 +14,9 @@ LIB_PATH = os.path.join(HERE, "libmcut_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "mcut_gb300.h")
 
 OK, GP_VIOLATION, DEGENERATE_SRC_FACE, DEGENERATE_CUT_FACE, INVALID_INPUT, CUDA_ERROR, OUT_OF_MEMORY, \
-    INVALID_VALUE, TOO_LARGE, NOT_READY = range(10)
+    INVALID_VALUE, TOO_LARGE, NOT_READY, CANCELLED = range(11)
 STATUS_NAMES = ["OK", "GP_VIOLATION", "DEGENERATE_SRC_FACE", "DEGENERATE_CUT_FACE", "INVALID_INPUT",
-                "CUDA_ERROR", "OUT_OF_MEMORY", "INVALID_VALUE", "TOO_LARGE", "NOT_READY"]
+                "CUDA_ERROR", "OUT_OF_MEMORY", "INVALID_VALUE", "TOO_LARGE", "NOT_READY", "CANCELLED"]
 NO_CUT = 0xFFFFFFFF
 
 VERTEX_ARRAY_FLOAT = 1 << 0
@@ -75,7 +75,8 @@ class ServerConfig(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "batches", "pending", "inflight_bytes",
-                                          "peak_inflight_bytes", "resident_bytes", "resident_meshes")]
+                                          "peak_inflight_bytes", "resident_bytes", "resident_meshes",
+                                          "pool_bytes", "peak_reserved_bytes", "pool_trims", "cancelled")]
 
 
 class HmeshReport(C.Structure):
@@ -124,6 +125,9 @@ def load():
     lib.mcgpu_context_get_general_position.argtypes = [ctx, C.POINTER(C.c_double), C.POINTER(C.c_uint32)]
     lib.mcgpu_autotune.argtypes = [ctx, C.c_uint32, C.POINTER(Batch), C.c_uint32, C.POINTER(Tuning),
                                    C.POINTER(C.c_float)]
+    lib.mcgpu_context_get_memory.argtypes = [ctx, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.mcgpu_context_set_memory_limit.argtypes = [ctx, C.c_uint64]
+    lib.mcgpu_context_trim.argtypes = [ctx]
     srv = C.c_void_p
     lib.mcgpu_server_create.argtypes = [C.POINTER(srv), C.POINTER(ServerConfig)]
     lib.mcgpu_server_release.argtypes = [srv]
@@ -132,6 +136,7 @@ def load():
     lib.mcgpu_server_wait.argtypes = [srv, C.c_uint64, C.c_int, C.POINTER(Summary), C.POINTER(C.c_double)]
     lib.mcgpu_server_get_data.argtypes = [srv, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, C.POINTER(C.c_uint64)]
     lib.mcgpu_server_release_request.argtypes = [srv, C.c_uint64]
+    lib.mcgpu_server_cancel.argtypes = [srv, C.c_uint64]
     lib.mcgpu_server_get_stats.argtypes = [srv, C.POINTER(ServerStats)]
     lib.mcgpu_last_error.restype = C.c_char_p
     for name in exported_names_in_header():

@@ -41,27 +41,33 @@ inline void ck(cudaError_t e, const char* where)
     if (e != cudaSuccess) throw CudaError { e, where };
 }
 
-// grow-only device buffer
+// grow-only device buffer of a context's pool; `held` sums the pool's bytes,
+// and a growth that would take it past a nonzero `limit` fails as an
+// allocation failure before anything is freed
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+    uint64_t* held = nullptr;
+    const uint64_t* limit = nullptr;
     template <typename T>
     T* get(size_t count)
     {
         const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
         if (bytes > cap) {
-            if (p) cudaFree(p);
-            p = nullptr;
-            cap = 0;
-            size_t want = bytes + bytes / 4;
+            const size_t want = bytes + bytes / 4;
+            if (limit && *limit && *held - cap + want > *limit)
+                throw CudaError { cudaErrorMemoryAllocation, "context memory limit" };
+            release();
             ck(cudaMalloc(&p, want), "cudaMalloc");
             cap = want;
+            *held += want;
         }
         return reinterpret_cast<T*>(p);
     }
     void release()
     {
         if (p) cudaFree(p);
+        if (held) *held -= cap;
         p = nullptr;
         cap = 0;
     }
@@ -99,7 +105,7 @@ enum BufId {
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
-    B_X32,
+    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES,
     // the halfedge mesh (mcgpu_halfedge_mesh)
     B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
     B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
@@ -127,7 +133,9 @@ struct mcgpu_context_t {
     cudaEvent_t fork[2] = {}, join[2] = {};
     cudaEvent_t ev[16] = {};  // begin / end of each stage (MCGPU_PROFILE)
     DevBuf buf[B_COUNT];
-    PinBuf pin_counters, pin_tab, pin_stage, pin_idx;
+    uint64_t dev_held = 0;   // bytes the pool holds (every buf)
+    uint64_t dev_limit = 0;  // 0: no cap (mcgpu_context_set_memory_limit)
+    PinBuf pin_counters, pin_tab, pin_stage, pin_idx, pin_seg, pin_frames;
     Layout L;
     mcgpu::Problem P {};
     mcgpu::Problem Pin {}; // the bounds kernel's view of the indices
@@ -162,6 +170,7 @@ struct mcgpu_context_t {
     std::vector<unsigned char> fuse_key;
     bool fuse_ok = false;
     uint64_t fuse_nrec = 0, fuse_npairs = 0;
+    bool have_results = false; // a dispatch completed since the last trim (queries 1-17 read it)
     // the record hand-over of the last single dispatch (built on demand)
     bool derived_ready = false;
     mcgpu::DerivedOut derived {};
@@ -339,29 +348,6 @@ void recentre_pair_mt(bool fin, const mcgpu_mesh& S, const mcgpu_mesh& Cm, doubl
     *eps_out = frame_eps(cs, t, gp_constant, gp_absolute);
 }
 
-// Host arrays read in place by the device (it walks the host's page tables:
-// cudaDevAttrPageableMemoryAccess): one launch moves every segment at the
-// host link's bandwidth, with no staging copy by the driver. 8-byte words
-// where both ends and the size allow, else 4-byte words.
-struct HostSeg { const void* src; void* dst; uint64_t bytes; };
-struct HostSegs { HostSeg s[4]; int n; };
-__global__ void __launch_bounds__(256) k_host_copy(HostSegs g)
-{
-    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, st = (uint64_t)gridDim.x * blockDim.x;
-    for (int k = 0; k < g.n; ++k) {
-        const HostSeg h = g.s[k];
-        if ((((uintptr_t)h.src | (uintptr_t)h.dst | h.bytes) & 7u) == 0) {
-            const uint2* a = static_cast<const uint2*>(h.src);
-            uint2* b = static_cast<uint2*>(h.dst);
-            for (uint64_t i = t0; i < h.bytes / 8; i += st) b[i] = a[i];
-        } else {
-            const uint32_t* a = static_cast<const uint32_t*>(h.src);
-            uint32_t* b = static_cast<uint32_t*>(h.dst);
-            for (uint64_t i = t0; i < h.bytes / 4; i += st) b[i] = a[i];
-        }
-    }
-}
-
 // the cut vertices of one general-position enforcement attempt: the
 // recentred coordinate plus the perturbation, one rounding
 // (preproc.cpp:131-133, 176-180)
@@ -371,6 +357,33 @@ __global__ void k_perturb(const double* __restrict__ in, double* __restrict__ ou
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n3; k += (uint64_t)gridDim.x * blockDim.x) {
         const int j = (int)(k % 3);
         out[k] = in[k] + (j == 0 ? p0 : (j == 1 ? p1 : p2));
+    }
+}
+
+// Gathers segments of 4-byte words (host arrays the device reads over the
+// link, or device arrays) into device buffers, one launch for every pair's
+// arrays. segs[k].begin is the first word of segment k in the concatenation,
+// segs[nseg].begin the total.
+struct GatherSeg {
+    const uint32_t* src;
+    uint32_t* dst;
+    uint64_t begin;
+};
+__global__ void __launch_bounds__(256) k_gather(const GatherSeg* __restrict__ segs, uint32_t nseg)
+{
+    const uint64_t total = segs[nseg].begin, stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    uint32_t lo = 0, hi = nseg; // the last segment starting at or before i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (segs[mid].begin <= i) lo = mid; else hi = mid;
+    }
+    uint32_t k = lo;
+    for (; i < total; i += stride) {
+        while (i >= segs[k + 1].begin) ++k;
+        const uint64_t o = i - segs[k].begin;
+        segs[k].dst[o] = segs[k].src[o];
     }
 }
 
@@ -444,7 +457,8 @@ __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint3
 // top, max at the bottom of the ordered-uint64 encoding), zero counters,
 // statuses and record ranges, no degenerate face
 __global__ void k_init_dispatch(unsigned long long* __restrict__ mb, uint32_t n_pairs, uint32_t* __restrict__ counters,
-    uint32_t* __restrict__ pair_status, int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_nrec)
+    uint32_t* __restrict__ pair_status, int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_nrec,
+    uint32_t* __restrict__ pair_cnt)
 {
     const uint64_t n12 = (uint64_t)n_pairs * 12;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n12 + 16; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -455,6 +469,7 @@ __global__ void k_init_dispatch(unsigned long long* __restrict__ mb, uint32_t n_
             pair_bad[i] = kNoBad;
         }
         if (i <= n_pairs) pair_nrec[i] = 0u;
+        if (pair_cnt && i < (uint64_t)n_pairs * 5) pair_cnt[i] = 0u;
     }
 }
 
@@ -571,22 +586,78 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     uint32_t* fidx = c->buf[B_FIDX].get<uint32_t>(L.nidx);
     // a single pair from host arrays, copied by the device reading them
     const bool host_read = c->host_reads && !dev && !pk && !res && n == 1 && !(flags & MCGPU_RECENTRE)
-        && ((uintptr_t)srcs[0].vertices & 3) == 0 && ((uintptr_t)cuts[0].vertices & 3) == 0
+        && ((uintptr_t)srcs[0].vertices & 7) == 0 && ((uintptr_t)cuts[0].vertices & 7) == 0
         && ((uintptr_t)srcs[0].face_indices & 3) == 0 && ((uintptr_t)cuts[0].face_indices & 3) == 0;
-    if (host_read) {
-        HostSegs g {};
-        const uint64_t ic = (uint64_t)L.ibase[1] - L.is[0];
-        g.s[0] = HostSeg { srcs[0].vertices, const_cast<double*>(X), (uint64_t)L.vs[0] * 24 };
-        g.s[1] = HostSeg { cuts[0].vertices, const_cast<double*>(X) + (size_t)L.vs[0] * 3,
-            (uint64_t)cuts[0].num_vertices * 24 };
-        g.s[2] = HostSeg { srcs[0].face_indices, fidx, (uint64_t)L.is[0] * 4 };
-        g.s[3] = HostSeg { cuts[0].face_indices, fidx + L.is[0], ic * 4 };
-        g.n = 4;
-        g_launches++;
-        k_host_copy<<<grid1((L.nv * 24 + L.nidx * 4) / 8), 256, 0, s>>>(g);
+    // With host_read the bounds kernels read the caller's arrays over the host
+    // link themselves -- the vertex kernel the coordinates (writing the device
+    // copy X), the face kernel the indices (writing the global table) -- so
+    // the upload runs at the link's rate with their work hidden under it.
+    c->W.hx_src = host_read ? static_cast<const double*>(srcs[0].vertices) : nullptr;
+    c->W.hx_cut = host_read ? static_cast<const double*>(cuts[0].vertices) : nullptr;
+    c->W.hx_out = host_read ? const_cast<double*>(X) : nullptr;
+    c->W.x_raw = nullptr;
+    c->W.raw_float = 0;
+    c->W.frames = nullptr;
+    // user coordinates from host arrays: gathered raw to the device by one
+    // launch while the host sums the centroids, mapped by the bounds kernel
+    bool gathered = c->host_reads && !dev && !pk && (flags & MCGPU_RECENTRE) && !(fin && res);
+    for (uint32_t p = 0; gathered && p < n; ++p) {
+        const uintptr_t a = (uintptr_t)srcs[p].vertices | (uintptr_t)srcs[p].face_indices
+            | ((res && res[p]) ? 0 : ((uintptr_t)cuts[p].vertices | (uintptr_t)cuts[p].face_indices));
+        gathered = (a & 3) == 0;
     }
     if ((pk && dev) || split || host_read) {
-        // read in place, or copied above
+        // read in place
+    } else if (gathered) {
+        const size_t vsz = fin ? 12 : 24;
+        uint8_t* xraw = c->buf[B_XRAW].get<uint8_t>(L.nv * vsz);
+        GatherSeg* gs = c->pin_seg.get<GatherSeg>(4 * (size_t)n + 1);
+        uint64_t words = 0;
+        uint32_t k = 0;
+        auto add = [&](const void* src, void* dst, uint64_t bytes) {
+            gs[k++] = GatherSeg { static_cast<const uint32_t*>(src), static_cast<uint32_t*>(dst), words };
+            words += bytes / 4;
+        };
+        for (uint32_t p = 0; p < n; ++p) {
+            const bool r = res && res[p];
+            const uint64_t nvc = (uint64_t)L.vbase[p + 1] - L.vbase[p] - L.vs[p];
+            const uint64_t ic = (uint64_t)L.ibase[p + 1] - L.ibase[p] - L.is[p];
+            add(srcs[p].vertices, xraw + (size_t)L.vbase[p] * vsz, (uint64_t)L.vs[p] * vsz);
+            add(r ? static_cast<const void*>(res[p]->X) : cuts[p].vertices,
+                xraw + ((size_t)L.vbase[p] + L.vs[p]) * vsz, nvc * vsz);
+            add(srcs[p].face_indices, fidx + L.ibase[p], (uint64_t)L.is[p] * 4);
+            add(r ? static_cast<const void*>(res[p]->idx) : cuts[p].face_indices, fidx + L.ibase[p] + L.is[p],
+                ic * 4);
+        }
+        gs[k] = GatherSeg { nullptr, nullptr, words };
+        GatherSeg* dseg = c->buf[B_GSEG].get<GatherSeg>((size_t)k + 1);
+        ck(cudaMemcpyAsync(dseg, gs, sizeof(GatherSeg) * (k + 1), cudaMemcpyHostToDevice, s), "H2D segments");
+        g_launches++;
+        k_gather<<<grid1(words), 256, 0, s>>>(dseg, k);
+        // meanwhile: each pair's frame from its meshes' bounds and centroids
+        // (summed in vertex order; a large pair's two meshes side by side)
+        double* fr = c->pin_frames.get<double>(6 * (size_t)n);
+        parallel_pairs(n, L.nv, [&](uint32_t p) {
+            MeshStats ss, cs;
+            const bool r = res && res[p];
+            if (!r && n == 1 && L.nv > 200000) {
+                std::thread tc([&] { mesh_stats(cuts[p].vertices, fin, cuts[p].num_vertices, cs); });
+                mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
+                tc.join();
+            } else {
+                mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
+                if (r) cs = res[p]->st;
+                else mesh_stats(cuts[p].vertices, fin, cuts[p].num_vertices, cs);
+            }
+            pair_frame(ss, cs, fr + 6 * (size_t)p, fr + 6 * (size_t)p + 3);
+            L.eps[p] = frame_eps(cs, fr + 6 * (size_t)p + 3, c->gp_constant, gp_absolute);
+        });
+        double* dfr = c->buf[B_FRAMES].get<double>(6 * (size_t)n);
+        ck(cudaMemcpyAsync(dfr, fr, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s), "H2D frames");
+        c->W.x_raw = xraw;
+        c->W.raw_float = fin ? 1 : 0;
+        c->W.frames = dfr;
+        c->W.hx_out = const_cast<double*>(X);
     } else if (pk && !(flags & MCGPU_RECENTRE)) {
         ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
             "H2D X");
@@ -645,8 +716,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     }
     const cudaMemcpyKind ikind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const bool staged = (flags & MCGPU_RECENTRE) != 0; // indices went up with the recentred coordinates
-    if (split || host_read) {
-        // k_prep reads the caller's index arrays, or they were copied above
+    if (split || host_read || gathered) {
+        // the bounds kernel reads the caller's index arrays, or they were gathered above
     } else if (pk && !staged)
         ck(cudaMemcpyAsync(fidx, pk->idx, (size_t)L.nidx * 4, ikind, s), "H2D idx");
     else for (uint32_t p = 0; p < n; ++p) {
@@ -736,9 +807,9 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     c->W.fidx_out = c->W.face_pair_out = nullptr;
     c->W.fidx_fix = n > 1 ? fidx : nullptr;
     if (n == 1) {
-        Pin.fidx = split ? srcs[0].face_indices : fidx;
+        Pin.fidx = (split || host_read) ? srcs[0].face_indices : fidx;
         Pin.face_pair = nullptr;
-        Pin.fidx_cut = split ? cuts[0].face_indices : fidx + L.is[0];
+        Pin.fidx_cut = (split || host_read) ? cuts[0].face_indices : fidx + L.is[0];
         Pin.fidx_split = L.is[0];
         Pin.cut_vbase = L.vs[0];
         Pin.face_split = L.fs[0];
@@ -823,6 +894,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     c->flags = flags;
     c->derived_ready = false;
+    c->have_results = false;
     const unsigned long long launches0 = g_launches;
     int rc = build_layout(c, flags, n, srcs, cuts, eps);
     if (rc != MCGPU_OK) return rc;
@@ -871,6 +943,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.pair_status = c->buf[B_PSTAT].get<uint32_t>(n);
     W.pair_bad = c->buf[B_PBAD].get<int32_t>(n);
     W.pair_nrec = c->buf[B_PNREC].get<uint32_t>(n + 1);
+    W.pair_cnt = n > 1 ? c->buf[B_PCNT].get<uint32_t>((size_t)n * 5) : nullptr;
     W.scan_temp = c->buf[B_SCANTMP].get<uint32_t>(scan_temp_bytes((uint32_t)L.nv + 1) / 4 + 64);
     if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
@@ -883,12 +956,15 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     const uint32_t prof = flags & MCGPU_PROFILE;
     const uint32_t keep = flags & MCGPU_KEEP_TESTS;
     int src_buf = 0, cut_buf = 0;
-    uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 3 * (size_t)n + 8);
+    // host readback block: counters [0, 16), per-pair status, degenerate face,
+    // record ranges (n + 1), then from hcnt a batch's per-pair counts (5 n)
+    uint32_t* hc = c->pin_counters.get<uint32_t>(16 + 8 * (size_t)n + 8);
+    uint32_t* const hcnt = hc + 16 + 3 * (size_t)n + 8;
     auto seg0 = [&](int* aux) {
         rec(c, 2 * MCGPU_STAGE_BOUNDS);
         g_launches++;
         k_init_dispatch<<<grid1((uint64_t)n * 12 + 16), 256, 0, s>>>(W.mesh_box, n, W.counters, W.pair_status,
-            W.pair_bad, W.pair_nrec); // the candidate-face flags are cleared by the bounds kernel
+            W.pair_bad, W.pair_nrec, W.pair_cnt); // the candidate-face flags are cleared by the bounds kernel
         launch_bounds_morton(P, c->Pin, W, wide, key_bits, s);
         rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
         rec(c, 2 * MCGPU_STAGE_SORT);
@@ -980,6 +1056,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         if (ranges)
             ck(cudaMemcpyAsync(hc + 16 + 2 * (size_t)n, W.pair_nrec, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s),
                 "D2H ranges");
+        if (W.pair_cnt)
+            ck(cudaMemcpyAsync(hcnt, W.pair_cnt, 20 * (size_t)n, cudaMemcpyDeviceToHost, s), "D2H pair counts");
     };
     // the stage-3 buffers of the previous call stay out of the segment keys
     auto clear_stage3 = [&]() {
@@ -1174,6 +1252,14 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         c->sums[0].escalations[0] = hc[5];
         c->sums[0].escalations[1] = hc[6];
         c->sums[0].escalations[2] = hc[7];
+    } else {
+        for (uint32_t p = 0; p < n; ++p) {
+            mcgpu_summary& m = c->sums[p];
+            const uint32_t* k = hcnt + 5 * (size_t)p;
+            m.num_pairs = k[0];
+            m.num_tests = k[1];
+            for (int j = 0; j < 3; ++j) m.escalations[j] = k[2 + j];
+        }
     }
     if (flags & MCGPU_PROFILE) {
         // stage times of the whole call (every summary of a batch carries them)
@@ -1187,6 +1273,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         for (auto& m : c->sums) memcpy(m.stage_ms, st, sizeof st);
     }
     for (auto& m : c->sums) m.kernel_launches = (uint32_t)(g_launches - launches0);
+    c->have_results = true;
     if (out) {
         if (n == 1) *out = c->sums[0];
         else memcpy(out, c->sums.data(), sizeof(mcgpu_summary) * n);
@@ -1271,6 +1358,10 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         mcgpu_context_t* c = new (std::nothrow) mcgpu_context_t();
         if (!c) return fail(MCGPU_OUT_OF_MEMORY, "host allocation");
         c->device = device;
+        for (auto& b : c->buf) {
+            b.held = &c->dev_held;
+            b.limit = &c->dev_limit;
+        }
         if (const char* e = getenv("MCGPU_LEAF_SIZE")) {
             const int v = atoi(e);
             if (v >= 1 && v <= 16) c->tune.leaf_size = (uint32_t)v;
@@ -1305,6 +1396,44 @@ int mcgpu_context_create(mcgpu_context* out, int device)
     }
 }
 
+int mcgpu_context_get_memory(mcgpu_context c, uint64_t* device_bytes, uint64_t* limit_bytes)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    if (device_bytes) *device_bytes = c->dev_held;
+    if (limit_bytes) *limit_bytes = c->dev_limit;
+    return MCGPU_OK;
+}
+
+int mcgpu_context_set_memory_limit(mcgpu_context c, uint64_t limit_bytes)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    c->dev_limit = limit_bytes;
+    return MCGPU_OK;
+}
+
+int mcgpu_context_trim(mcgpu_context c)
+{
+    if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    cudaSetDevice(c->device);
+    if (cudaStreamSynchronize(c->s) != cudaSuccess || cudaStreamSynchronize(c->s2) != cudaSuccess)
+        return fail(MCGPU_CUDA_ERROR, "stream synchronize before trim");
+    // the captured launch graphs hold the pool's addresses
+    for (auto& g : c->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key.clear();
+        g.seen = 0;
+    }
+    c->fuse_key.clear();
+    c->fuse_ok = false;
+    c->derived_ready = false;
+    c->hm_ready = false;
+    c->have_results = false;
+    c->W = mcgpu::Work {};
+    for (auto& b : c->buf) b.release();
+    return MCGPU_OK;
+}
+
 int mcgpu_context_release(mcgpu_context c)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
@@ -1315,6 +1444,8 @@ int mcgpu_context_release(mcgpu_context c)
     c->pin_tab.release();
     c->pin_stage.release();
     c->pin_idx.release();
+    c->pin_seg.release();
+    c->pin_frames.release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto& g : c->graphs)
@@ -1480,6 +1611,8 @@ int mcgpu_autotune(mcgpu_context c, uint32_t flags, const mcgpu_batch* sample, u
 int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    if (query < MCGPU_DATA_HE_TARGET && !c->have_results)
+        return fail(MCGPU_INVALID_VALUE, "no dispatch results (none completed, or the pool was trimmed)");
     try {
         const Work& W = c->W;
         switch (query) {
@@ -1620,6 +1753,7 @@ int mcgpu_get_batch_data(mcgpu_context c, uint32_t pair, uint32_t query, uint64_
     uint64_t* bytes_out)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
+    if (!c->have_results) return fail(MCGPU_INVALID_VALUE, "no dispatch results (none completed, or the pool was trimmed)");
     if (pair >= c->L.n_pairs) return fail(MCGPU_INVALID_VALUE, "pair index out of range");
     try {
         const uint64_t b = c->rec_begin[pair], n = c->rec_begin[pair + 1] - b;

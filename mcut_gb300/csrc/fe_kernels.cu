@@ -75,6 +75,28 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool want)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// Adds v[k] to cnt[5 p + f0 + k] for each distinct pair id p among the warp's
+// lanes, one atomic per pair and value (lanes with p == kNone add nothing).
+// All 32 lanes call it.
+template <int K>
+__device__ __forceinline__ void pair_add(uint32_t* cnt, uint32_t p, int f0, const uint32_t (&v)[K])
+{
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    unsigned todo = __ballot_sync(full, p != kNone);
+    while (todo) {
+        const int leader = __ffs(todo) - 1;
+        const uint32_t lp = __shfl_sync(full, p, leader);
+        const bool mine = p == lp;
+        todo &= ~__ballot_sync(full, mine);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const uint32_t x = __reduce_add_sync(full, mine ? v[k] : 0u);
+            if (lane == leader && x) atomicAdd(&cnt[(size_t)lp * 5 + f0 + k], x);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // face boxes + per-mesh boxes (bvh.cpp:242-368)
 // ---------------------------------------------------------------------------
@@ -105,7 +127,8 @@ __device__ __forceinline__ uint32_t expand_bits(uint32_t v)
 // registers, the block folds in shared memory, one thread issues the
 // atomics; a tile that straddles meshes falls back to per-thread atomics.
 __global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned long long* __restrict__ mesh_box,
-    float4* __restrict__ x32)
+    float4* __restrict__ x32, const double* __restrict__ hx_src, const double* __restrict__ hx_cut,
+    double* __restrict__ hx_out, const void* __restrict__ x_raw, int raw_float, const double* __restrict__ frames)
 {
     __shared__ unsigned long long red[kBlock / 32][6];
     __shared__ uint32_t skey;
@@ -128,7 +151,34 @@ __global__ void __launch_bounds__(kBlock) k_vertex_bounds(Problem P, unsigned lo
             while (v >= P.pair_vbase[p + 1]) ++p;
             const uint32_t k = p * 2 + ((v - P.pair_vbase[p]) >= P.pair_vs[p] ? 1u : 0u);
             double x[3];
-            load_v(P, v, x);
+            if (hx_src) {
+                // one pair from host arrays: read over the host link, kept on the device
+                const uint32_t vs = P.pair_vs[0];
+                const double* h = v < vs ? hx_src + 3 * (size_t)v : hx_cut + 3 * (size_t)(v - vs);
+                x[0] = h[0];
+                x[1] = h[1];
+                x[2] = h[2];
+                hx_out[3 * (size_t)v] = x[0];
+                hx_out[3 * (size_t)v + 1] = x[1];
+                hx_out[3 * (size_t)v + 2] = x[2];
+            } else if (x_raw) {
+                // user coordinates into the pair's frame, x' = (x - com) + t per
+                // coordinate, in the input's precision (preproc.cpp:147-181)
+                const double* fr = frames + 6 * (size_t)p;
+                if (raw_float) {
+                    const float* r = static_cast<const float*>(x_raw) + 3 * (size_t)v;
+                    for (int j = 0; j < 3; ++j)
+                        x[j] = (double)__fadd_rn(__fsub_rn(r[j], __double2float_rn(fr[j])), __double2float_rn(fr[3 + j]));
+                } else {
+                    const double* r = static_cast<const double*>(x_raw) + 3 * (size_t)v;
+                    for (int j = 0; j < 3; ++j) x[j] = __dadd_rn(__dsub_rn(r[j], fr[j]), fr[3 + j]);
+                }
+                hx_out[3 * (size_t)v] = x[0];
+                hx_out[3 * (size_t)v + 1] = x[1];
+                hx_out[3 * (size_t)v + 2] = x[2];
+            } else {
+                load_v(P, v, x);
+            }
             // the vertex's fp32 copy for orient3d's first filter
             if (x32) x32[v] = make_float4(f32_vertex_coord(x[0]), f32_vertex_coord(x[1]), f32_vertex_coord(x[2]), 0.0f);
             if (key != kNone && k != key) {
@@ -1639,7 +1689,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
     const unsigned long long* __restrict__ pairs, const uint32_t* __restrict__ counters_ro, uint64_t pair_cap,
     const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vface, uint32_t inc_slots, Test* __restrict__ tests,
     uint64_t test_cap, uint32_t* __restrict__ counters, const int32_t* __restrict__ pair_bad,
-    uint32_t* __restrict__ pair_status)
+    uint32_t* __restrict__ pair_status, uint32_t* __restrict__ pair_cnt)
 {
     __shared__ uint32_t s_nmax;
     const uint64_t np = min((uint64_t)counters_ro[0], pair_cap);
@@ -1652,8 +1702,12 @@ __global__ void __launch_bounds__(kBlock) k_pair_tests(Problem P, const double* 
             sface = (uint32_t)(pr >> 32);
             cface = (uint32_t)pr;
             p = P.face_pair[sface] & ~kCutBit;
-            live = pair_bad[p] == kNoBad; // the reference stops before the narrow phase
         }
+        if (pair_cnt) {
+            const uint32_t one[1] = { 1u };
+            pair_add<1>(pair_cnt, live ? p : kNone, 0, one);
+        }
+        if (live) live = pair_bad[p] == kNoBad; // the reference stops before the narrow phase
         // edges of the source face against the cut face, then the reverse;
         // the loop runs to the block's longest face so every thread reaches
         // each block_append
@@ -1755,7 +1809,8 @@ __device__ char pip_face(const Problem& P, const double* Pm, uint32_t o, uint32_
 __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem P, const Test* __restrict__ tests,
     const uint32_t* __restrict__ counters_ro, uint64_t test_cap, const uint32_t* __restrict__ plane_slot,
     const FacePlane* __restrict__ planes, int keep_tests, int8_t* __restrict__ test_info, uint2* __restrict__ hits,
-    uint32_t* __restrict__ proj_flag, uint32_t* __restrict__ proj_list, uint32_t* __restrict__ counters)
+    uint32_t* __restrict__ proj_flag, uint32_t* __restrict__ proj_list, uint32_t* __restrict__ counters,
+    uint32_t* __restrict__ pair_cnt)
 {
     const uint64_t nt = min((uint64_t)counters_ro[1], test_cap);
     uint32_t esc[3] = { 0, 0, 0 };
@@ -1763,8 +1818,11 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
         const uint64_t i = i0 + threadIdx.x;
         bool hit = false, first_hit = false;
         uint32_t code = 0, slot = 0;
+        uint32_t e[3] = { 0, 0, 0 }; // this test's signs by deciding stage
+        uint32_t pid = kNone;
         if (i < nt) {
             const Test t = tests[i];
+            if (pair_cnt) pid = P.face_pair[t.g] & ~kCutBit;
             const uint32_t o = face_o(P, t.g), n = face_n(P, t.g);
             // a triangle's plane-defining vertices are its own three (a
             // degenerate triangle makes its whole pair degenerate, and the hit
@@ -1789,7 +1847,7 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
                     const float4 fa = P.X32[va], fb = P.X32[vb], fc = P.X32[vc];
                     dq = orient3d_sign_f32v(fa, fb, fc, P.X32[t.q]);
                     dr = orient3d_sign_f32v(fa, fb, fc, P.X32[t.r]);
-                    esc[ESC_F32] += (dq != 0) + (dr != 0);
+                    e[ESC_F32] += (dq != 0) + (dr != 0);
                 }
                 sq = (int8_t)dq;
                 sr = (int8_t)dr;
@@ -1802,12 +1860,12 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
                     if (dq == 0) {
                         load_v(P, t.q, x);
                         sq = (int8_t)orient3d_sign_filtered(a, b, c, x, st);
-                        esc[st]++;
+                        e[st]++;
                     }
                     if (dr == 0) {
                         load_v(P, t.r, x);
                         sr = (int8_t)orient3d_sign_filtered(a, b, c, x, st);
-                        esc[st]++;
+                        e[st]++;
                     }
                 }
                 if (sq == 0 && sr == 0) type = 'p';
@@ -1829,6 +1887,11 @@ __global__ void __launch_bounds__(kBlock, MCGPU_NS_MINB) k_narrow_signs(Problem 
         if (hit && pos < test_cap) hits[pos] = make_uint2((uint32_t)i, code);
         const uint32_t k = warp_append(&counters[11], first_hit);
         if (first_hit) proj_list[k] = slot;
+        for (int j = 0; j < 3; ++j) esc[j] += e[j];
+        if (pair_cnt) {
+            const uint32_t v[4] = { 1u, e[0], e[1], e[2] };
+            pair_add<4>(pair_cnt, pid, 1, v);
+        }
     }
     for (int k = 0; k < 3; ++k) {
         uint32_t v = esc[k];
@@ -2134,7 +2197,8 @@ void launch_bounds_morton(const Problem& P, const Problem& Pin, Work& W, bool wi
 {
     float4* frame = reinterpret_cast<float4*>(W.mesh_frame);
     g_launches += 3;
-    k_vertex_bounds<<<grid_for(P.nv / kBoundsItems + 1), kBlock, 0, s>>>(P, W.mesh_box, W.x32);
+    k_vertex_bounds<<<grid_for(P.nv / kBoundsItems + 1), kBlock, 0, s>>>(P, W.mesh_box, W.x32, W.hx_src, W.hx_cut,
+        W.hx_out, W.x_raw, W.raw_float, W.frames);
     k_mesh_frames<<<(2 * P.n_pairs + 255) / 256, 256, 0, s>>>(W.mesh_box, 2 * P.n_pairs, frame);
     const int g = grid_for(P.nf);
     if (wide)
@@ -2286,7 +2350,7 @@ void launch_tests(const Problem& P, Work& W, cudaStream_t s)
     const int g = grid_for(W.pair_cap);
     g_launches++;
     k_pair_tests<<<g, kBlock, 0, s>>>(P, W.fbox, W.pairs, W.counters, W.pair_cap, W.voff, W.vface, W.inc_slots,
-        W.tests, W.test_cap, W.counters, W.pair_bad, W.pair_status);
+        W.tests, W.test_cap, W.counters, W.pair_bad, W.pair_status, W.pair_cnt);
 }
 
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
@@ -2296,7 +2360,7 @@ void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s)
     uint2* hits = reinterpret_cast<uint2*>(W.rec_key[1]);
     g_launches += 3;
     k_narrow_signs<<<g, kBlock, 0, s>>>(P, W.tests, W.counters, W.test_cap, W.plane_slot, (const FacePlane*)W.planes,
-        keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters);
+        keep_tests ? 1 : 0, W.test_info, hits, W.proj_flag, W.proj_list, W.counters, W.pair_cnt);
     k_finish_planes<<<grid_spread(W.plane_cap), kSpread, 0, s>>>(P, (FacePlane*)W.planes, W.plane_slot,
         W.proj_list, W.counters);
     const int gh = std::max(1, grid_spread(W.test_cap) * kSpread / kNarrowHitsBlock);

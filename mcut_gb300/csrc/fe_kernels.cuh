@@ -77,6 +77,19 @@ struct Work {
     uint32_t* fidx_out;               // one pair: the bounds kernel writes the global ps indices here
     uint32_t* face_pair_out;          // ... and the face -> pair table (null for a batch: k_prep made them)
     float4* x32;                      // [nv] the bounds kernel writes each vertex's fp32 copy here (null: none)
+    // one pair from the caller's host arrays (the device reads pageable
+    // memory): the vertex bounds kernel reads the vertices there, source then
+    // cut (hx_src null: from P.X), and writes the device copy hx_out
+    const double* hx_src;
+    const double* hx_cut;
+    double* hx_out;
+    // user coordinates (MCGPU_RECENTRE): the raw vertices gathered to the
+    // device (float or double, the internal layout) and each pair's frame
+    // (com xyz, t xyz); the vertex bounds kernel writes x' = (x - com) + t to
+    // hx_out (x_raw null: not used)
+    const void* x_raw;
+    int raw_float;
+    const double* frames;
     uint32_t* fidx_fix;               // a batch: the global table the bounds kernel reads, where it replaces an
                                       // index outside its mesh (null for one pair: fidx_out gets the fix)
     void* mesh_frame;                 // [n_pairs*2*2] float4: fp32 box low corner, 1023 / extent
@@ -124,6 +137,8 @@ struct Work {
     uint32_t* pair_status;            // [n_pairs] ST_* bits
     int32_t* pair_bad;                // [n_pairs] lowest degenerate ps face (local), INT_MAX if none
     uint32_t* pair_nrec;              // [n_pairs+1] first sorted record of each pair (+ total)
+    uint32_t* pair_cnt;               // [n_pairs*5] a batch's per-pair counts: candidate pairs, tests,
+                                      //   escalations (fp32 / fp64 / exact); null: one pair (counters only)
     double* tri_scratch;              // polygon triplet scratch (24-byte entries)
     uint64_t tri_scratch_cap;         // entries
     uint64_t tri_stride;              // entries per polygon (largest C(n,3)); 0: no polygons

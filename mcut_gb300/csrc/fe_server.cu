@@ -14,6 +14,17 @@
 // indices) with their bounds and centroid; a request naming one uploads
 // only its source mesh, and the cut is mapped into the pair's frame on the
 // device.
+//
+// Device memory: each worker may hold an allowance of device bytes -- its
+// context's pool while idle, its batch's cap while it runs one -- and the
+// resident meshes plus every allowance stay within hbm_budget_bytes. A batch
+// is formed from the requests whose estimated bytes fit what the other
+// workers' allowances leave; its context cannot grow past the cap
+// (mcgpu_context_set_memory_limit). Idle workers' pools are freed when a
+// batch does not fit beside them. A batch that meets its cap runs again
+// with the pool freed and the cap widened to all that is free, then in
+// halves; a request that still does not fit fails with MCGPU_TOO_LARGE.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -46,6 +57,7 @@ struct Request {
     bool done = false;
     int rc = MCGPU_OK;
     std::string err;
+    bool cancelled = false;
     mcgpu_summary sum {};
     std::vector<uint32_t> ids;
     std::vector<double> pts;
@@ -74,6 +86,10 @@ uint64_t mesh_indices(const mcgpu_mesh& m)
 // repeated dispatch shape sizes them, and 16 incidence slots per vertex,
 // 64 B) plus slack.
 uint64_t estimate_bytes(uint64_t faces, uint64_t verts) { return (1ull << 20) + faces * 744 + verts * 128; }
+// the cap a batch of estimated bytes e runs under: the pool grows each
+// buffer by a quarter beyond its need, its smallest buffers have fixed
+// minimum sizes, and the estimate is not a bound
+uint64_t batch_cap(uint64_t e) { return 2 * e + (64ull << 20); }
 
 } // namespace
 
@@ -88,14 +104,56 @@ struct mcgpu_server_t {
     std::vector<mcgpu_context> ctxs;
     uint64_t next_id = 1, inflight = 0, peak_inflight = 0, resident_bytes = 0, pending_faces = 0;
     uint32_t busy = 0; // workers with a batch on the device
-    uint64_t submitted = 0, completed = 0, batches = 0, batched_pairs = 0;
+    uint64_t submitted = 0, completed = 0, batches = 0, batched_pairs = 0, cancelled = 0;
+    // per worker: bytes its pool holds (read after each batch), the bytes it
+    // may hold (its pool while idle, its batch's cap while running), running
+    std::vector<uint64_t> pool, allow;
+    std::vector<uint8_t> running;
+    uint64_t peak_reserved = 0, trims = 0;
     bool stop = false;
 };
 
 namespace {
 
-void run_batch(mcgpu_server_t* S, mcgpu_context ctx, const std::vector<Request*>& batch,
-    const std::vector<const mcgpu::ResidentCut*>& res)
+// the bytes every worker but w may hold (caller holds S->m)
+uint64_t others_allowance(const mcgpu_server_t* S, size_t w)
+{
+    uint64_t a = 0;
+    for (size_t k = 0; k < S->allow.size(); ++k)
+        if (k != w) a += S->allow[k];
+    return a;
+}
+
+uint64_t free_bytes(const mcgpu_server_t* S, size_t w)
+{
+    const uint64_t used = S->resident_bytes + others_allowance(S, w);
+    return S->cfg.hbm_budget_bytes > used ? S->cfg.hbm_budget_bytes - used : 0;
+}
+
+void note_reserved(mcgpu_server_t* S)
+{
+    uint64_t r = S->resident_bytes;
+    for (uint64_t a : S->allow) r += a;
+    if (r > S->peak_reserved) S->peak_reserved = r;
+}
+
+// frees the pools of the idle workers other than w (caller holds S->m; an
+// idle worker touches its context only after taking S->m to form a batch)
+bool trim_idle(mcgpu_server_t* S, size_t w)
+{
+    bool any = false;
+    for (size_t k = 0; k < S->ctxs.size(); ++k) {
+        if (k == w || S->running[k] || S->pool[k] == 0) continue;
+        mcgpu_context_trim(S->ctxs[k]);
+        S->pool[k] = S->allow[k] = 0;
+        S->trims++;
+        any = true;
+    }
+    return any;
+}
+
+// one batched dispatch; on success each request gets its summary and records
+int run_batch(mcgpu_context ctx, const std::vector<Request*>& batch, const std::vector<const mcgpu::ResidentCut*>& res)
 {
     const uint32_t n = (uint32_t)batch.size();
     std::vector<mcgpu_mesh> srcs(n), cuts(n);
@@ -105,34 +163,37 @@ void run_batch(mcgpu_server_t* S, mcgpu_context ctx, const std::vector<Request*>
     }
     std::vector<mcgpu_summary> sums(n);
     int rc = mcgpu::dispatch_with_resident(ctx, MCGPU_RECENTRE, n, srcs.data(), cuts.data(), res.data(), sums.data());
-    std::vector<uint64_t> off;
+    if (rc != MCGPU_OK) return rc;
+    std::vector<uint64_t> off(n + 1);
     std::vector<uint32_t> ids;
     std::vector<double> pts;
-    if (rc == MCGPU_OK) {
-        uint64_t b = 0;
-        off.resize(n + 1);
-        rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_OFFSETS, (n + 1) * 8, off.data(), &b);
-        if (rc == MCGPU_OK) {
-            ids.resize(off[n] * 5 + 1);
-            pts.resize(off[n] * 3 + 1);
-            rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_IDS, ids.size() * 4, ids.data(), &b);
-            if (rc == MCGPU_OK) rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_POINTS, pts.size() * 8, pts.data(), &b);
-        }
-    }
-    const std::string err = rc == MCGPU_OK ? std::string() : std::string(mcgpu_last_error());
+    uint64_t b = 0;
+    rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_OFFSETS, (n + 1) * 8, off.data(), &b);
+    if (rc != MCGPU_OK) return rc;
+    ids.resize(off[n] * 5 + 1);
+    pts.resize(off[n] * 3 + 1);
+    rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_IDS, ids.size() * 4, ids.data(), &b);
+    if (rc == MCGPU_OK) rc = mcgpu_get_data(ctx, MCGPU_DATA_RECORD_POINTS, pts.size() * 8, pts.data(), &b);
+    if (rc != MCGPU_OK) return rc;
     for (uint32_t i = 0; i < n; ++i) {
         Request* r = batch[i];
-        r->rc = rc;
-        if (rc != MCGPU_OK) {
-            r->err = err;
-            continue;
-        }
+        r->rc = MCGPU_OK;
         r->sum = sums[i];
-        r->sum.num_pairs = 0; // batch totals are not split per pair
-        r->sum.num_tests = 0;
         r->ids.assign(ids.begin() + off[i] * 5, ids.begin() + off[i + 1] * 5);
         r->pts.assign(pts.begin() + off[i] * 3, pts.begin() + off[i + 1] * 3);
     }
+    return MCGPU_OK;
+}
+
+// marks requests done and wakes their waiters (caller holds S->m)
+void complete(mcgpu_server_t* S, const std::vector<Request*>& done)
+{
+    const Clock::time_point now = Clock::now();
+    for (Request* r : done) {
+        r->done = true;
+        r->t_done = now;
+    }
+    S->completed += done.size();
 }
 
 void worker(mcgpu_server_t* S, int w)
@@ -160,23 +221,34 @@ void worker(mcgpu_server_t* S, int w)
                 res.clear();
                 uint64_t faces = 0;
                 bytes = 0;
+                uint64_t avail = free_bytes(S, w);
+                bool alone = false; // the first request runs with every byte the budget has
                 while (!S->pending.empty() && batch.size() < S->cfg.max_batch_pairs) {
                     Request* r = S->pending.front();
                     if (!batch.empty() && faces + r->faces > S->cfg.max_batch_faces) break;
-                    // admission: in-flight estimates + resident meshes stay within the budget
-                    // (a request alone on an idle device is always admitted: it passed the
-                    // size check at submission)
-                    const bool idle = S->inflight == 0 && batch.empty();
-                    if (!idle && S->resident_bytes + S->inflight + bytes + r->est_bytes > S->cfg.hbm_budget_bytes) break;
+                    if (batch_cap(bytes + r->est_bytes) > avail) {
+                        if (!batch.empty()) break;
+                        // the first request does not fit beside the other workers' pools:
+                        // free the idle ones, else wait for a running batch to end
+                        if (trim_idle(S, w)) avail = free_bytes(S, w);
+                        if (batch_cap(r->est_bytes) > avail) {
+                            if (S->busy > 0) break;
+                            alone = true;
+                        }
+                    }
                     S->pending.pop_front();
                     S->pending_faces -= r->faces;
                     batch.push_back(r);
                     res.push_back(r->cut_id == kNoCut ? nullptr : &S->cuts[r->cut_id]->rc);
                     faces += r->faces;
                     bytes += r->est_bytes;
+                    if (alone) break;
                 }
                 if (!batch.empty()) {
                     S->busy++;
+                    S->running[w] = 1;
+                    S->allow[w] = std::max(S->pool[w], alone ? avail : std::min(avail, batch_cap(bytes)));
+                    note_reserved(S);
                     S->inflight += bytes;
                     if (S->inflight > S->peak_inflight) S->peak_inflight = S->inflight;
                     break;
@@ -184,17 +256,56 @@ void worker(mcgpu_server_t* S, int w)
                 S->cv_work.wait(lk);
             }
         }
-        run_batch(S, ctx, batch, res);
+        mcgpu_context_set_memory_limit(ctx, S->allow[w]);
+        int rc = run_batch(ctx, batch, res);
+        std::string err = rc == MCGPU_OK ? std::string() : std::string(mcgpu_last_error());
+        // a batch that met its cap runs again with the cap widened to all that
+        // is free (the pool keeps what it grew), then with this pool and the
+        // idle ones freed, then in halves (the later half goes back to the
+        // front of the queue)
+        for (int attempt = 0; rc == MCGPU_OUT_OF_MEMORY; ++attempt) {
+            if (attempt >= 1) mcgpu_context_trim(ctx);
+            {
+                std::lock_guard<std::mutex> lk(S->m);
+                if (attempt >= 1) {
+                    S->pool[w] = 0;
+                    S->trims++;
+                    trim_idle(S, (size_t)w);
+                }
+                if (attempt >= 2) {
+                    if (batch.size() < 2) break; // one request that does not fit the budget
+                    const size_t half = batch.size() / 2;
+                    for (size_t k = batch.size(); k-- > half;) {
+                        S->pending.push_front(batch[k]);
+                        S->pending_faces += batch[k]->faces;
+                        S->inflight -= batch[k]->est_bytes;
+                        bytes -= batch[k]->est_bytes;
+                    }
+                    batch.resize(half);
+                    res.resize(half);
+                }
+                S->allow[w] = free_bytes(S, w);
+                note_reserved(S);
+            }
+            S->cv_work.notify_all();
+            mcgpu_context_set_memory_limit(ctx, S->allow[w]);
+            rc = run_batch(ctx, batch, res);
+            err = rc == MCGPU_OK ? std::string() : std::string(mcgpu_last_error());
+        }
+        uint64_t held = 0;
+        mcgpu_context_get_memory(ctx, &held, nullptr);
         {
             std::lock_guard<std::mutex> lk(S->m);
             S->busy--;
+            S->running[w] = 0;
+            S->pool[w] = S->allow[w] = held;
             S->inflight -= bytes;
-            const Clock::time_point now = Clock::now();
             for (Request* r : batch) {
-                r->done = true;
-                r->t_done = now;
+                if (rc == MCGPU_OK) continue;
+                r->rc = rc == MCGPU_OUT_OF_MEMORY ? MCGPU_TOO_LARGE : rc;
+                r->err = rc == MCGPU_OUT_OF_MEMORY ? "the request does not fit the device memory budget: " + err : err;
             }
-            S->completed += batch.size();
+            complete(S, batch);
             S->batches++;
             S->batched_pairs += batch.size();
         }
@@ -240,6 +351,9 @@ int mcgpu_server_create(mcgpu_server* out, const mcgpu_server_config* cfg)
         }
         S->ctxs.push_back(c);
     }
+    S->pool.assign(S->cfg.workers, 0);
+    S->allow.assign(S->cfg.workers, 0);
+    S->running.assign(S->cfg.workers, 0);
     for (uint32_t w = 0; w < S->cfg.workers; ++w) S->workers.emplace_back(worker, S, (int)w);
     *out = S;
     return MCGPU_OK;
@@ -272,17 +386,32 @@ int mcgpu_server_add_cut_mesh(mcgpu_server S, const mcgpu_mesh* cut, uint32_t* c
     if (cut->num_vertices < 3 || cut->num_faces < 1) return sfail(MCGPU_INVALID_INPUT, "empty cut mesh");
     std::unique_ptr<Resident> r(new Resident());
     const size_t xb = (size_t)cut->num_vertices * 24, ib = (size_t)cut->num_faces * 12;
+    {
+        // the resident bytes join the budget: free idle pools if they do not fit
+        std::lock_guard<std::mutex> lk(S->m);
+        const uint64_t size = (uint64_t)xb + ib;
+        if (free_bytes(S, S->allow.size()) < size) trim_idle(S, S->allow.size());
+        if (free_bytes(S, S->allow.size()) < size)
+            return sfail(MCGPU_OUT_OF_MEMORY, "resident cut mesh exceeds the device memory budget");
+        S->resident_bytes += size; // reserved now, so no batch takes these bytes meanwhile
+    }
+    auto unreserve = [&] {
+        std::lock_guard<std::mutex> lk(S->m);
+        S->resident_bytes -= (uint64_t)xb + ib;
+    };
     mcgpu::mesh_stats(cut->vertices, false, cut->num_vertices, r->rc.st);
     cudaSetDevice(S->cfg.device);
     if (cudaMalloc(&r->dX, xb) != cudaSuccess || cudaMalloc(&r->dI, ib) != cudaSuccess) {
         cudaFree(r->dX);
         cudaGetLastError();
+        unreserve();
         return sfail(MCGPU_OUT_OF_MEMORY, "resident cut mesh");
     }
     if (cudaMemcpy(r->dX, cut->vertices, xb, cudaMemcpyHostToDevice) != cudaSuccess
         || cudaMemcpy(r->dI, cut->face_indices, ib, cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(r->dX);
         cudaFree(r->dI);
+        unreserve();
         return sfail(MCGPU_CUDA_ERROR, "resident cut upload");
     }
     r->rc.X = static_cast<const double*>(r->dX);
@@ -291,7 +420,6 @@ int mcgpu_server_add_cut_mesh(mcgpu_server S, const mcgpu_mesh* cut, uint32_t* c
     r->rc.nf = cut->num_faces;
     r->bytes = xb + ib;
     std::lock_guard<std::mutex> lk(S->m);
-    S->resident_bytes += r->bytes;
     *cut_id = (uint32_t)S->cuts.size();
     S->cuts.push_back(std::move(r));
     return MCGPU_OK;
@@ -346,6 +474,30 @@ int mcgpu_server_submit(mcgpu_server S, const mcgpu_mesh* src, const mcgpu_mesh*
     return MCGPU_OK;
 }
 
+int mcgpu_server_cancel(mcgpu_server S, uint64_t ticket)
+{
+    if (!S) return sfail(MCGPU_INVALID_VALUE, "null server");
+    {
+        std::lock_guard<std::mutex> lk(S->m);
+        Request* r = find(S, ticket);
+        if (!r) return sfail(MCGPU_INVALID_VALUE, "unknown ticket");
+        if (r->done) return sfail(MCGPU_INVALID_VALUE, "request already completed");
+        auto it = std::find(S->pending.begin(), S->pending.end(), r);
+        if (it == S->pending.end()) return sfail(MCGPU_NOT_READY, "request is in a running batch");
+        S->pending.erase(it);
+        S->pending_faces -= r->faces;
+        r->cancelled = true;
+        r->rc = MCGPU_CANCELLED;
+        r->err = "request was cancelled";
+        r->done = true;
+        r->t_done = Clock::now();
+        S->cancelled++;
+    }
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+    return MCGPU_OK;
+}
+
 int mcgpu_server_wait(mcgpu_server S, uint64_t ticket, int timeout_ms, mcgpu_summary* out, double* latency_ms)
 {
     if (!S) return sfail(MCGPU_INVALID_VALUE, "null server");
@@ -358,6 +510,7 @@ int mcgpu_server_wait(mcgpu_server S, uint64_t ticket, int timeout_ms, mcgpu_sum
         return sfail(MCGPU_NOT_READY, "request still running");
     if (out) *out = r->sum;
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    if (r->cancelled) return sfail(MCGPU_CANCELLED, r->err);
     if (r->rc != MCGPU_OK) return sfail(r->rc, "the batch holding this request failed: " + r->err);
     return MCGPU_OK;
 }
@@ -370,6 +523,7 @@ int mcgpu_server_get_data(mcgpu_server S, uint64_t ticket, uint32_t query, uint6
     Request* r = find(S, ticket);
     if (!r) return sfail(MCGPU_INVALID_VALUE, "unknown ticket");
     if (!r->done) return sfail(MCGPU_NOT_READY, "request still running");
+    if (r->rc != MCGPU_OK) return sfail(r->rc, "the request has no records: " + r->err);
     const void* src = nullptr;
     uint64_t need = 0;
     if (query == MCGPU_DATA_RECORD_IDS) {
@@ -410,6 +564,11 @@ int mcgpu_server_get_stats(mcgpu_server S, mcgpu_server_stats* out)
     out->peak_inflight_bytes = S->peak_inflight;
     out->resident_bytes = S->resident_bytes;
     out->resident_meshes = S->cuts.size();
+    out->pool_bytes = 0;
+    for (uint64_t b : S->pool) out->pool_bytes += b;
+    out->peak_reserved_bytes = S->peak_reserved;
+    out->pool_trims = S->trims;
+    out->cancelled = S->cancelled;
     return MCGPU_OK;
 }
 

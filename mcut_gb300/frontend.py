@@ -155,6 +155,18 @@ class Context:
                        v_he=g(L.DATA_VERTEX_HE, np.uint32))
         return out
 
+    def memory(self) -> dict:
+        """Device bytes the context's pool holds and its cap (0: none)."""
+        held, cap = C.c_uint64(0), C.c_uint64(0)
+        L.check(self._lib.mcgpu_context_get_memory(self._h, C.byref(held), C.byref(cap)), "mcgpu_context_get_memory")
+        return {"device_bytes": held.value, "limit_bytes": cap.value}
+
+    def set_memory_limit(self, limit_bytes: int = 0):
+        L.check(self._lib.mcgpu_context_set_memory_limit(self._h, int(limit_bytes)), "mcgpu_context_set_memory_limit")
+
+    def trim(self):
+        L.check(self._lib.mcgpu_context_trim(self._h), "mcgpu_context_trim")
+
     def set_general_position(self, constant: float = 1e-4, attempts: int = 4):
         """Enforcement constant and attempts (mcBindState MC_CONTEXT_GENERAL_POSITION_ENFORCEMENT_*)."""
         L.check(self._lib.mcgpu_context_set_general_position(self._h, float(constant), int(attempts)),
@@ -219,7 +231,8 @@ class Context:
             if fetch:
                 ids = self._batch_get(i, L.DATA_RECORD_IDS, np.uint32, 5)
                 pts = self._batch_get(i, L.DATA_RECORD_POINTS, np.float64, 3)
-            out.append((dict(status=s.status, bad_face=s.bad_face, cut_eps=s.cut_eps, num_records=s.num_records),
+            out.append((dict(status=s.status, bad_face=s.bad_face, cut_eps=s.cut_eps, num_records=s.num_records,
+                             num_pairs=s.num_pairs, num_tests=s.num_tests, escalations=tuple(s.escalations)),
                         ids, pts))
         return out
 
@@ -331,6 +344,11 @@ class Server:
     def release(self, ticket: int):
         L.check(self._lib.mcgpu_server_release_request(self._h, ticket), "mcgpu_server_release_request")
         self._keep.pop(ticket, None)
+
+    def cancel(self, ticket: int) -> int:
+        """Takes a queued request out of the queue; returns the status code
+        (OK, or NOT_READY when a batch already holds it)."""
+        return self._lib.mcgpu_server_cancel(self._h, ticket)
 
     def stats(self) -> dict:
         st = L.ServerStats()

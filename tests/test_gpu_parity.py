@@ -125,6 +125,21 @@ def test_batch_equals_single(ctx):
         assert G.same_bits(b, want["rec_pts"]), k
 
 
+def test_batch_counts_per_pair(ctx):
+    """A batch's summaries carry each pair's own candidate-pair, test and
+    escalation counts: equal to the pair dispatched alone."""
+    names = [k for k in sorted(CASES) if k.startswith("crack")] + ["two_spheres", "bm014", "bunny_plane"]
+    pairs = [(CASES[k]["src"], CASES[k]["cut"]) for k in names]
+    rng = np.random.default_rng(meshgen.SEED_BASE + 77)
+    pairs += [meshgen.crack_pair(rng, target_tris=t) for t in (2000, 30000, 120000)]
+    out = ctx.dispatch_batch(pairs, fetch=False)
+    for (s, c), (summ, _, _) in zip(pairs, out):
+        r = ctx.dispatch(s, c, fetch=False)
+        assert (summ["num_pairs"], summ["num_tests"], summ["escalations"]) == \
+            (r.num_pairs, r.num_tests, tuple(r.escalations))
+        assert summ["num_records"] == r.num_records
+
+
 @pytest.mark.parametrize("kind", ["cross_mesh", "wrapping", "far"])
 def test_index_outside_its_mesh(ctx, kind):
     """Each mesh's indices are checked against its own vertex count, as the

@@ -27,21 +27,31 @@ def test_server_without_gpu_is_an_error_not_a_crash():
     assert lib.mcgpu_server_create(C.byref(h), C.byref(cfg)) != L.OK
     assert lib.mcgpu_server_submit(None, None, None, L.NO_CUT, None) == L.INVALID_VALUE
     assert lib.mcgpu_server_wait(None, 1, 0, None, None) == L.INVALID_VALUE
+    assert lib.mcgpu_server_cancel(None, 1) == L.INVALID_VALUE
 
 
 @pytest.fixture(scope="module")
 def alone():
-    """Each request dispatched alone on a plain context."""
+    """Each request dispatched alone on a plain context (its pool freed
+    before each, so that the device bytes it holds after are the request's
+    own need)."""
     from mcut_gb300 import Context
     reqs = _requests(24, meshgen.SEED_BASE + 50)
     ctx = Context(0)
-    out = [ctx.dispatch(s, c) for s, c in reqs]
+    out, needs = [], []
+    for s, c in reqs:
+        ctx.trim()
+        out.append(ctx.dispatch(s, c))
+        needs.append(ctx.memory()["device_bytes"])
     ctx.close()
-    return reqs, out
+    return reqs, out, needs
 
 
 def _same(a_sum, a_ids, a_pts, b):
     assert a_sum.status == b.status
+    # per-request counters: the request's own pairs, tests and escalations
+    assert (a_sum.num_pairs, a_sum.num_tests, tuple(a_sum.escalations)) == \
+        (b.num_pairs, b.num_tests, tuple(b.escalations))
     assert G.same_bits(a_sum.cut_eps, b.cut_eps)
     assert a_ids.shape == b.record_ids.shape
     assert np.array_equal(a_ids, b.record_ids)
@@ -51,7 +61,7 @@ def _same(a_sum, a_ids, a_pts, b):
 @pytest.mark.gpu
 def test_served_same_alone_and_in_the_mix(alone):
     from mcut_gb300 import Server
-    reqs, want = alone
+    reqs, want, needs = alone
     srv = Server(0, workers=3, max_batch_pairs=7)
     tickets = [srv.submit(s, c) for s, c in reqs]
     for t, w in zip(tickets, want):
@@ -69,7 +79,7 @@ def test_served_same_alone_and_in_the_mix(alone):
 @pytest.mark.gpu
 def test_served_resident_cut_meshes(alone):
     from mcut_gb300 import Server
-    reqs, want = alone
+    reqs, want, needs = alone
     srv = Server(0, workers=2)
     ids_ = [srv.add_cut(c) for _, c in reqs[:6]]
     tickets = []
@@ -85,33 +95,109 @@ def test_served_resident_cut_meshes(alone):
     assert st["resident_meshes"] == 6 and st["resident_bytes"] > 0
 
 
+def _estimate(s, c):
+    """The server's per-request estimate: 1 MiB + 744 B per face + 128 B per vertex."""
+    return (1 << 20) + 744 * (meshgen.num_faces(s) + meshgen.num_faces(c)) + 128 * (s["v"].shape[0] + c["v"].shape[0])
+
+
 @pytest.mark.gpu
-def test_served_admission_budget(alone):
-    """A budget that fits about one request at a time: still every result,
-    and the in-flight estimate never passes the budget except for one
-    request running alone."""
+@pytest.mark.parametrize("mult", [1.2, 3.0])
+def test_served_admission_budget(alone, mult):
+    """Budgets that fit one to a few requests at a time: every result is
+    still the request's own, and the device bytes the server reserved (the
+    resident meshes plus every worker's pool or batch cap, which the pools
+    cannot pass) never exceed the budget; idle pools are freed to make room."""
     from mcut_gb300 import Server
-    reqs, want = alone
-    budget = 48 << 20
+    reqs, want, needs = alone
+    # the largest request's own pool and estimate (a request whose estimate
+    # exceeds the budget is refused at submission) plus the resident mesh fit,
+    # a few requests at most beside each other
+    budget = max(int(max(needs) * mult), max(_estimate(s, c) for s, c in reqs)) \
+        + 24 * reqs[0][1]["v"].shape[0] + 12 * meshgen.num_faces(reqs[0][1])
     srv = Server(0, workers=3, hbm_budget_bytes=budget)
-    tickets = [srv.submit(s, c) for s, c in reqs]
-    for t, w in zip(tickets, want):
+    cid = srv.add_cut(reqs[0][1])
+    tickets = [srv.submit(s, c) for s, c in reqs] + [srv.submit(reqs[0][0], cut_id=cid)]
+    for t, w in zip(tickets, want + [want[0]]):
         sm, _ = srv.wait(t)
         ids, pts = srv.records(t)
         _same(sm, ids, pts, w)
     st = srv.stats()
     srv.close()
-    assert st["completed"] == len(reqs)
-    # the server's estimate: 1 MiB + 744 B per face + 128 B per vertex
-    biggest = max((1 << 20) + 744 * (meshgen.num_faces(s) + meshgen.num_faces(c))
-                  + 128 * (s["v"].shape[0] + c["v"].shape[0]) for s, c in reqs)
-    assert st["peak_inflight_bytes"] <= max(budget, biggest)
+    assert st["completed"] == len(reqs) + 1
+    assert 0 < st["peak_reserved_bytes"] <= budget
+    assert st["pool_bytes"] + st["resident_bytes"] <= budget
+
+
+def _ngon(n, axis):
+    """One flat n-gon of radius 1 through the origin, normal along `axis`."""
+    t = np.linspace(0.0, 2.0 * np.pi, n, endpoint=False)
+    p = np.zeros((n, 3))
+    a, b = [k for k in range(3) if k != axis]
+    p[:, a], p[:, b] = np.cos(t), np.sin(t)
+    return {"v": p, "f": np.arange(n, dtype=np.uint32), "fs": np.array([n], np.uint32)}
+
+
+@pytest.mark.gpu
+def test_served_request_larger_than_the_budget(alone):
+    """A request whose estimate passes admission (two 300-gons: 1 MiB + 744 B
+    per face + 128 B per vertex) but whose dispatch needs far more device
+    memory than the budget (the narrow phase's plane triplets, C(n, 3) per
+    polygon) completes with MCGPU_TOO_LARGE after its retries; requests
+    around it keep their own results and the budget holds."""
+    from mcut_gb300 import Server
+    reqs, want, needs = alone
+    big = (_ngon(300, 2), _ngon(300, 0))
+    assert _estimate(*big) < (2 << 20)
+    small = sorted(range(len(reqs)), key=lambda i: needs[i])[:3]
+    budget = max(8 << 20, int(max(needs[i] for i in small) * 1.5), max(_estimate(*reqs[i]) for i in small))
+    assert budget < 2 * 24 * (300 * 299 * 298 // 6)  # below the two polygons' triplet scratch
+    srv = Server(0, workers=2, hbm_budget_bytes=budget)
+    ts = [srv.submit(*reqs[small[0]])]
+    tb = srv.submit(*big)
+    ts += [srv.submit(*reqs[i]) for i in small[1:]]
+    with pytest.raises(RuntimeError, match="TOO_LARGE"):
+        srv.wait(tb)
+    for t, i in zip(ts, small):
+        sm, _ = srv.wait(t)
+        ids, pts = srv.records(t)
+        _same(sm, ids, pts, want[i])
+    st = srv.stats()
+    srv.close()
+    assert st["peak_reserved_bytes"] <= budget and st["pool_trims"] > 0
+
+
+@pytest.mark.gpu
+def test_served_cancel(alone):
+    """A queued request can be taken out before a batch holds it; waiting on
+    it reports MCGPU_CANCELLED; a completed one cannot be cancelled; the rest
+    complete with their own results."""
+    from mcut_gb300 import Server
+    from mcut_gb300 import _lib as L
+    reqs, want, needs = alone
+    srv = Server(0, workers=1, max_batch_pairs=1, linger_us=2_000_000)
+    tickets = [srv.submit(s, c) for s, c in reqs[:10]]
+    rcs = {t: srv.cancel(t) for t in tickets[5:]}
+    assert all(rc in (L.OK, L.NOT_READY) for rc in rcs.values())
+    assert any(rc == L.OK for rc in rcs.values())
+    for i, t in enumerate(tickets):
+        if rcs.get(t) == L.OK:
+            with pytest.raises(RuntimeError, match="CANCELLED"):
+                srv.wait(t)
+            continue
+        sm, _ = srv.wait(t)
+        ids, pts = srv.records(t)
+        _same(sm, ids, pts, want[i])
+    assert srv.cancel(tickets[0]) == L.INVALID_VALUE
+    st = srv.stats()
+    srv.close()
+    assert st["cancelled"] == sum(rc == L.OK for rc in rcs.values())
+    assert st["completed"] == 10 - st["cancelled"]
 
 
 @pytest.mark.gpu
 def test_served_records_match_oracle(alone):
     from mcut_gb300 import Server
-    reqs, _ = alone
+    reqs, _, _ = alone
     srv = Server(0)
     tickets = [srv.submit(s, c) for s, c in reqs[:8]]
     for t, (s, c) in zip(tickets, reqs[:8]):
