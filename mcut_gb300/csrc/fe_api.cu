@@ -105,7 +105,7 @@ enum BufId {
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
-    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES,
+    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB,
     // the halfedge mesh (mcgpu_halfedge_mesh)
     B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
     B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
@@ -135,7 +135,8 @@ struct mcgpu_context_t {
     DevBuf buf[B_COUNT];
     uint64_t dev_held = 0;   // bytes the pool holds (every buf)
     uint64_t dev_limit = 0;  // 0: no cap (mcgpu_context_set_memory_limit)
-    PinBuf pin_counters, pin_tab, pin_stage, pin_idx, pin_seg, pin_frames;
+    PinBuf pin_counters, pin_tab, pin_stage, pin_idx, pin_seg, pin_frames, pin_eps;
+    bool eps_on_device = false; // the last upload's cut-box enlargements come from the device (pin_eps)
     Layout L;
     mcgpu::Problem P {};
     mcgpu::Problem Pin {}; // the bounds kernel's view of the indices
@@ -195,8 +196,11 @@ double dminr(double a, double b) { return (b < a) ? b : a; }
 float fmaxr(float a, float b) { return (a < b) ? b : a; }
 float fminr(float a, float b) { return (b < a) ? b : a; }
 
-void vertex_bounds(const void* v, bool fin, uint32_t n, double* mn, double* mx, double* com)
+// the accumulators are locals: the compiler cannot keep values it must
+// assume the vertex array aliases in registers
+void vertex_bounds(const void* v, bool fin, uint32_t n, double* mn_out, double* mx_out, double* com_out)
 {
+    double mn[3], mx[3], com[3];
     for (int j = 0; j < 3; ++j) {
         mn[j] = 1.7976931348623157e308;
         mx[j] = -1.7976931348623157e308;
@@ -221,7 +225,37 @@ void vertex_bounds(const void* v, bool fin, uint32_t n, double* mn, double* mx, 
                 com[j] += x;
             }
     }
-    for (int j = 0; j < 3; ++j) com[j] = com[j] / (double)n;
+    for (int j = 0; j < 3; ++j) {
+        mn_out[j] = mn[j];
+        mx_out[j] = mx[j];
+        com_out[j] = com[j] / (double)n;
+    }
+}
+
+// a mesh's centroid sums, each coordinate summed in vertex order (the
+// reference's accumulation; the bounds are taken on the device): one pass,
+// three independent chains
+void mesh_sums(const void* v, bool fin, uint32_t n, double* out)
+{
+    double a = 0.0, b = 0.0, c = 0.0;
+    if (fin) {
+        const float* p = (const float*)v;
+        for (uint32_t i = 0; i < n; ++i) {
+            a += (double)p[3 * (size_t)i];
+            b += (double)p[3 * (size_t)i + 1];
+            c += (double)p[3 * (size_t)i + 2];
+        }
+    } else {
+        const double* p = (const double*)v;
+        for (uint32_t i = 0; i < n; ++i) {
+            a += p[3 * (size_t)i];
+            b += p[3 * (size_t)i + 1];
+            c += p[3 * (size_t)i + 2];
+        }
+    }
+    out[0] = a;
+    out[1] = b;
+    out[2] = c;
 }
 
 double hdot(const double* a, const double* b)
@@ -384,6 +418,110 @@ __global__ void __launch_bounds__(256) k_gather(const GatherSeg* __restrict__ se
         while (i >= segs[k + 1].begin) ++k;
         const uint64_t o = i - segs[k].begin;
         segs[k].dst[o] = segs[k].src[o];
+    }
+}
+
+// Bounds of every mesh's raw user coordinates, per (pair, mesh, axis), with
+// the reference's sequential rule: max = (m < x) ? x : m and min =
+// (x < m) ? x : m from +-DBL_MAX (+-inf for float input, the float cast of
+// DBL_MAX), so NaNs never enter and of equal values the first in vertex
+// order stays -- which only shows for zeros of either sign. Keys order the
+// values with -0 and +0 equal; the first zero of each (pair, mesh, axis)
+// (vertex << 1 | sign) gives the sign when a bound is zero.
+__device__ __forceinline__ unsigned long long raw_key(double x)
+{
+    const long long b = __double_as_longlong(x == 0.0 ? 0.0 : x);
+    return b < 0 ? ~(unsigned long long)b : ((unsigned long long)b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double raw_value(unsigned long long k)
+{
+    return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+constexpr int kRawChunk = 16; // consecutive vertices per thread
+__global__ void __launch_bounds__(256) k_raw_bounds(const void* __restrict__ xraw, int fin, uint32_t nv,
+    uint32_t n_pairs, const uint32_t* __restrict__ vbase, const uint32_t* __restrict__ vs,
+    unsigned long long* __restrict__ lo, unsigned long long* __restrict__ hi, unsigned long long* __restrict__ zero)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kRawChunk;
+    for (uint64_t v0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) * kRawChunk; v0 < nv; v0 += stride) {
+        uint32_t l = 0, h = n_pairs; // the pair of v0
+        while (h - l > 1) {
+            const uint32_t mid = (l + h) >> 1;
+            if (vbase[mid] <= v0) l = mid; else h = mid;
+        }
+        uint32_t p = l, seg = kNone;
+        unsigned long long a[3], b[3], z[3];
+        auto flush = [&]() {
+            if (seg == kNone) return;
+            for (int j = 0; j < 3; ++j) {
+                if (a[j] != ~0ull) atomicMin(&lo[3 * (size_t)seg + j], a[j]);
+                if (b[j] != 0ull) atomicMax(&hi[3 * (size_t)seg + j], b[j]);
+                if (z[j] != ~0ull) atomicMin(&zero[3 * (size_t)seg + j], z[j]);
+            }
+        };
+        const uint64_t v1 = v0 + kRawChunk < nv ? v0 + kRawChunk : (uint64_t)nv;
+        for (uint64_t v = v0; v < v1; ++v) {
+            while (v >= vbase[p + 1]) ++p;
+            const uint32_t sg = 2 * p + ((v - vbase[p]) >= vs[p] ? 1u : 0u);
+            if (sg != seg) {
+                flush();
+                seg = sg;
+                for (int j = 0; j < 3; ++j) { a[j] = ~0ull; b[j] = 0ull; z[j] = ~0ull; }
+            }
+            for (int j = 0; j < 3; ++j) {
+                const double x = fin ? (double)static_cast<const float*>(xraw)[3 * v + j]
+                                     : static_cast<const double*>(xraw)[3 * v + j];
+                if (x != x) continue;
+                const unsigned long long k = raw_key(x);
+                a[j] = min(a[j], k);
+                b[j] = max(b[j], k);
+                if (x == 0.0) z[j] = min(z[j], (v << 1) | (__double_as_longlong(x) < 0 ? 1ull : 0ull));
+            }
+        }
+        flush();
+    }
+}
+
+// Each pair's frame from its centroid (summed on the host) and the device's
+// bounds (pair_frame and frame_eps of the host path, operation for
+// operation: preproc.cpp:2124-2290, 2518, 2664-2676): frames[6p..] = com,
+// t; eps[p] the cut-box enlargement.
+__global__ void k_frames(uint32_t n_pairs, const double* __restrict__ com, const unsigned long long* __restrict__ lo,
+    const unsigned long long* __restrict__ hi, const unsigned long long* __restrict__ zero, int fin,
+    double constant, int absolute, double* __restrict__ frames, double* __restrict__ eps)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs) return;
+    const double top = fin ? __longlong_as_double(0x7FF0000000000000ll) : 1.7976931348623157e308;
+    double mn[2][3], mx[2][3];
+    for (int m = 0; m < 2; ++m)
+        for (int j = 0; j < 3; ++j) {
+            const size_t k = 3 * (2 * (size_t)p + m) + j;
+            const double zs = (zero[k] != ~0ull && (zero[k] & 1ull)) ? -0.0 : 0.0;
+            double a = lo[k] == ~0ull ? top : raw_value(lo[k]);
+            double b = hi[k] == 0ull ? -top : raw_value(hi[k]);
+            if (a == 0.0) a = zs;
+            if (b == 0.0) b = zs;
+            mn[m][j] = (a < top) ? a : top;   // the start value stays unless passed
+            mx[m][j] = (-top < b) ? b : -top;
+        }
+    double tp[3], t[3], d[3];
+    const double* c = com + 3 * (size_t)p;
+    for (int j = 0; j < 3; ++j) {
+        const double g = (mn[1][j] < mn[0][j]) ? mn[1][j] : mn[0][j];
+        tp[j] = __dsub_rn(c[j], g);
+    }
+    double o = 0.0;
+    for (int j = 0; j < 3; ++j) o = __dadd_rn(o, __dmul_rn(tp[j], tp[j]));
+    const double len = __dsqrt_rn(o);
+    for (int j = 0; j < 3; ++j) t[j] = __dadd_rn(tp[j], __ddiv_rn(tp[j], len));
+    for (int j = 0; j < 3; ++j) d[j] = __dsub_rn(__dadd_rn(mx[1][j], t[j]), __dadd_rn(mn[1][j], t[j]));
+    double q = 0.0;
+    for (int j = 0; j < 3; ++j) q = __dadd_rn(q, __dmul_rn(d[j], d[j]));
+    eps[p] = __dmul_rn(absolute ? 1.0 : __dsqrt_rn(q), constant);
+    for (int j = 0; j < 3; ++j) {
+        frames[6 * (size_t)p + j] = c[j];
+        frames[6 * (size_t)p + 3 + j] = t[j];
     }
 }
 
@@ -634,29 +772,32 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         ck(cudaMemcpyAsync(dseg, gs, sizeof(GatherSeg) * (k + 1), cudaMemcpyHostToDevice, s), "H2D segments");
         g_launches++;
         k_gather<<<grid1(words), 256, 0, s>>>(dseg, k);
-        // meanwhile: each pair's frame from its meshes' bounds and centroids
-        // (summed in vertex order; a large pair's two meshes side by side)
-        double* fr = c->pin_frames.get<double>(6 * (size_t)n);
+        // meanwhile: each pair's centroid, summed in vertex order on the host
+        // (a large pair: one thread per mesh and axis); the bounds and the
+        // frame follow on the device once the tables are up
+        double* hcom = c->pin_frames.get<double>(3 * (size_t)n);
         parallel_pairs(n, L.nv, [&](uint32_t p) {
-            MeshStats ss, cs;
             const bool r = res && res[p];
+            const mcgpu_mesh* m[2] = { &srcs[p], &cuts[p] };
+            double sum[2][3];
             if (!r && n == 1 && L.nv > 200000) {
-                std::thread tc([&] { mesh_stats(cuts[p].vertices, fin, cuts[p].num_vertices, cs); });
-                mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
+                // the meshes side by side (each pass is bound by one core's reads)
+                std::thread tc([&] { mesh_sums(m[1]->vertices, fin, m[1]->num_vertices, sum[1]); });
+                mesh_sums(m[0]->vertices, fin, m[0]->num_vertices, sum[0]);
                 tc.join();
             } else {
-                mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
-                if (r) cs = res[p]->st;
-                else mesh_stats(cuts[p].vertices, fin, cuts[p].num_vertices, cs);
+                mesh_sums(m[0]->vertices, fin, m[0]->num_vertices, sum[0]);
+                if (!r) mesh_sums(m[1]->vertices, fin, m[1]->num_vertices, sum[1]);
             }
-            pair_frame(ss, cs, fr + 6 * (size_t)p, fr + 6 * (size_t)p + 3);
-            L.eps[p] = frame_eps(cs, fr + 6 * (size_t)p + 3, c->gp_constant, gp_absolute);
+            for (int j = 0; j < 3; ++j) {
+                const double cs = sum[0][j] / (double)srcs[p].num_vertices;
+                const double cc = r ? res[p]->st.com[j] : sum[1][j] / (double)cuts[p].num_vertices;
+                hcom[3 * (size_t)p + j] = (cs + cc) / 2.0;
+            }
         });
-        double* dfr = c->buf[B_FRAMES].get<double>(6 * (size_t)n);
-        ck(cudaMemcpyAsync(dfr, fr, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, s), "H2D frames");
         c->W.x_raw = xraw;
         c->W.raw_float = fin ? 1 : 0;
-        c->W.frames = dfr;
+        c->W.frames = c->buf[B_FRAMES].get<double>(6 * (size_t)n);
         c->W.hx_out = const_cast<double*>(X);
     } else if (pk && !(flags & MCGPU_RECENTRE)) {
         ck(cudaMemcpyAsync(const_cast<double*>(X), pk->X, L.nv * 3 * sizeof(double), cudaMemcpyHostToDevice, s),
@@ -743,7 +884,27 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     uint32_t* dtab = c->buf[B_PTAB].get<uint32_t>(rows_u32);
     double* deps = c->buf[B_EPS].get<double>(n);
     ck(cudaMemcpyAsync(dtab, tab, sizeof(uint32_t) * rows_u32, cudaMemcpyHostToDevice, s), "H2D tab");
-    ck(cudaMemcpyAsync(deps, teps, sizeof(double) * n, cudaMemcpyHostToDevice, s), "H2D eps");
+    c->eps_on_device = gathered;
+    if (gathered) {
+        // bounds of the gathered raw coordinates, then each pair's frame and
+        // cut-box enlargement on the device; the enlargements come back with
+        // the first readback
+        double* dcom = c->buf[B_COM].get<double>(3 * (size_t)n);
+        unsigned long long* rb = c->buf[B_RAWB].get<unsigned long long>(18 * (size_t)n);
+        ck(cudaMemcpyAsync(dcom, c->pin_frames.get<double>(3 * (size_t)n), sizeof(double) * 3 * n,
+               cudaMemcpyHostToDevice, s), "H2D centroids");
+        ck(cudaMemsetAsync(rb, 0xFF, sizeof(unsigned long long) * 12 * n, s), "memset");
+        ck(cudaMemsetAsync(rb + 12 * (size_t)n, 0, sizeof(unsigned long long) * 6 * n, s), "memset");
+        g_launches += 2;
+        k_raw_bounds<<<grid1((L.nv + kRawChunk - 1) / kRawChunk), 256, 0, s>>>(c->W.x_raw, fin ? 1 : 0,
+            (uint32_t)L.nv, n, dtab + 2 * (n + 1), dtab + 3 * (n + 1), rb, rb + 12 * (size_t)n, rb + 6 * (size_t)n);
+        k_frames<<<(n + 127) / 128, 128, 0, s>>>(n, dcom, rb, rb + 12 * (size_t)n, rb + 6 * (size_t)n, fin ? 1 : 0,
+            c->gp_constant, gp_absolute ? 1 : 0, const_cast<double*>(c->W.frames), deps);
+        ck(cudaMemcpyAsync(c->pin_eps.get<double>(n), deps, sizeof(double) * n, cudaMemcpyDeviceToHost, s),
+            "D2H eps");
+    } else {
+        ck(cudaMemcpyAsync(deps, teps, sizeof(double) * n, cudaMemcpyHostToDevice, s), "H2D eps");
+    }
     uint32_t* foff = nullptr;
     if (!L.all_tri) {
         std::vector<uint32_t> off(L.nf + 1);
@@ -1174,6 +1335,8 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         if (hc[12] == 0 || W.inc_slots == 0) break;
         c->csr_incidence = true;
     }
+    // the enlargements the device computed (the first readback has them on the host)
+    if (c->eps_on_device) memcpy(L.eps.data(), c->pin_eps.get<double>(n), sizeof(double) * n);
     c->fuse_key = key0;
     c->fuse_ok = true;
     c->fuse_nrec = c->n_records;
@@ -1446,6 +1609,7 @@ int mcgpu_context_release(mcgpu_context c)
     c->pin_idx.release();
     c->pin_seg.release();
     c->pin_frames.release();
+    c->pin_eps.release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto& g : c->graphs)

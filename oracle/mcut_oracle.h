@@ -133,6 +133,29 @@ typedef struct hm_result {
 int oracle_hmesh(const uint32_t *f, const uint32_t *fs, uint32_t nv, uint32_t nf, hm_result *out);
 void oracle_hmesh_free(hm_result *r);
 
+/* MCUT's cut-path edge creation from the record hand-over (kernel.cpp:
+ * 3332-3632; cutpath_oracle.c). Inputs: the ps vertex count nv and
+ * coordinates x; the ps faces with their corners in the polygon soup's order
+ * (soup_off / soup_idx, ps vertex ids); per intersection vertex (m0 id nv + i)
+ * its registry (tested face, the tested edge's two faces, UINT32_MAX for
+ * none) and coordinates; cutpath_edge_creation_info in key order (key_pairs:
+ * source face, cut face; key_off / key_vtx: its vertices in list order). */
+typedef struct cp_result {
+    int32_t status;         /* 0; 1: a key with fewer than two vertices (dispatch stops) */
+    uint32_t bad_key;       /* that key */
+    uint32_t n_edges;       /* m0_cutpath_edges: edge e runs edge_src[e] -> edge_tgt[e] (halfedge 2e) */
+    uint32_t *edge_src, *edge_tgt;
+    uint32_t n_faces;       /* ps_iface_to_m0_edge_list: faces ascending, each edge list in append order */
+    uint32_t *face_keys, *face_off, *face_edges;
+    uint32_t n_ivtx;        /* ivtx_to_incoming_hlist, per intersection vertex in creation order */
+    uint32_t *ivtx_off, *ivtx_he;
+} cp_result;
+
+int oracle_cutpath(uint32_t nv, const double *x, uint32_t nf, const uint32_t *soup_off, const uint32_t *soup_idx,
+    uint32_t n_ivtx, const uint32_t *reg, const double *ivtx_xyz, uint32_t n_keys, const uint32_t *key_pairs,
+    const uint32_t *key_off, const uint32_t *key_vtx, cp_result *out);
+void oracle_cutpath_free(cp_result *r);
+
 #ifdef __cplusplus
 }
 #endif

@@ -465,3 +465,81 @@ def hmesh(f, fs, nv: int, impl: str = "port"):
             v_he=_arr(res.v_he, nh, np.uint32))
     fr(C.byref(res))
     return out
+
+
+class CpResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("bad_key", C.c_uint32), ("n_edges", C.c_uint32),
+                ("edge_src", C.POINTER(C.c_uint32)), ("edge_tgt", C.POINTER(C.c_uint32)),
+                ("n_faces", C.c_uint32), ("face_keys", C.POINTER(C.c_uint32)), ("face_off", C.POINTER(C.c_uint32)),
+                ("face_edges", C.POINTER(C.c_uint32)),
+                ("n_ivtx", C.c_uint32), ("ivtx_off", C.POINTER(C.c_uint32)), ("ivtx_he", C.POINTER(C.c_uint32))]
+
+
+def soup_faces(src, cut):
+    """The polygon soup's faces with their corners in the soup's order: a
+    source face starts at its second corner (the targets of its halfedges),
+    a cut face at its third (cs.get_vertices_around_face of the soup's
+    edge-created face); cut vertex ids offset by the source vertex count.
+    -> (offsets, indices) as the ps numbers faces (source, then cut)."""
+    off, idx = [0], []
+    vs = len(src["v"])
+    for m, rot, vo in ((src, 1, 0), (cut, 2, vs)):
+        f = np.asarray(m["f"], dtype=np.int64)
+        fs = np.full(len(f) // 3, 3) if m.get("fs") is None else np.asarray(m["fs"], dtype=np.int64)
+        o = np.concatenate([[0], np.cumsum(fs)])
+        for k in range(len(fs)):
+            face = f[o[k]:o[k + 1]] + vo
+            r = rot % len(face)
+            idx.extend(np.concatenate([face[r:], face[:r]]).tolist())
+            off.append(off[-1] + len(face))
+    return np.asarray(off, np.uint32), np.asarray(idx, np.uint32)
+
+
+def cutpath(nv, x, soup_off, soup_idx, registry, ivtx_xyz, cp_pairs, cp_off, cp_vtx):
+    """MCUT's cut-path edge creation from a record hand-over (kernel.cpp:
+    3332-3632, oracle_cutpath). registry: per intersection vertex (m0 id nv +
+    i) its tested face and the tested edge's two faces (UINT32_MAX: none).
+    -> dict(status, bad_key, edges [E,2] (src, tgt; halfedge 2e runs src ->
+    tgt), face_keys, face_off, face_edges, ivtx_off, ivtx_he)."""
+    lib, _, _ = _lib("port")
+    if not hasattr(lib, "_cutpath_ready"):
+        lib.oracle_cutpath.restype = C.c_int
+        lib.oracle_cutpath.argtypes = [C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                       C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(CpResult)]
+        lib.oracle_cutpath_free.argtypes = [C.POINTER(CpResult)]
+        lib._cutpath_ready = True
+    keep = []
+
+    def arr(a, dt):
+        a = np.ascontiguousarray(np.asarray(a, dtype=dt).reshape(-1))
+        keep.append(a)
+        return a.ctypes.data if a.size else None
+    reg = np.asarray(registry, np.uint32).reshape(-1, 3)
+    nf = len(soup_off) - 1
+    res = CpResult()
+    rc = lib.oracle_cutpath(int(nv), arr(x, np.float64), nf, arr(soup_off, np.uint32), arr(soup_idx, np.uint32),
+                            len(reg), arr(reg, np.uint32), arr(ivtx_xyz, np.float64),
+                            len(cp_off) - 1, arr(cp_pairs, np.uint32), arr(cp_off, np.uint32),
+                            arr(cp_vtx, np.uint32), C.byref(res))
+    if rc != 0:
+        raise RuntimeError("oracle_cutpath failed")
+    ne = int(res.n_edges)
+    out = dict(status=int(res.status), bad_key=int(res.bad_key),
+               edges=np.stack([_arr(res.edge_src, ne, np.uint32), _arr(res.edge_tgt, ne, np.uint32)], 1),
+               face_keys=_arr(res.face_keys, res.n_faces, np.uint32),
+               face_off=_arr(res.face_off, res.n_faces + 1, np.uint32),
+               ivtx_off=_arr(res.ivtx_off, res.n_ivtx + 1, np.uint32))
+    out["face_edges"] = _arr(res.face_edges, int(out["face_off"][-1]) if res.n_faces else 0, np.uint32)
+    out["ivtx_he"] = _arr(res.ivtx_he, int(out["ivtx_off"][-1]) if res.n_ivtx else 0, np.uint32)
+    lib.oracle_cutpath_free(C.byref(res))
+    return out
+
+
+def cutpath_of(src, cut, xyz, hand):
+    """The cut path of a pass from its internal coordinates (source then cut
+    vertices) and its record hand-over (oracle.seam's keys)."""
+    off, idx = soup_faces(src, cut)
+    rid = np.asarray(hand["rec_ids"], np.uint32).reshape(-1, 5)
+    return cutpath(len(xyz), xyz, off, idx, rid[:, 2:5], hand["rec_pts"], hand["cp_pairs"], hand["cp_off"],
+                   hand["cp_vtx"])
