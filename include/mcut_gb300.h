@@ -161,7 +161,22 @@ typedef enum mcgpu_data {
     MCGPU_DATA_HE_PREV = 21,             /* int32[2E] */
     MCGPU_DATA_CORNER_HE = 22,           /* uint32[corners]: the halfedge of face corner i (v_i -> v_i+1) */
     MCGPU_DATA_VERTEX_HE_OFFSETS = 23,   /* uint32[V+1]: vertex v's halfedges are [o[v], o[v+1]) of ... */
-    MCGPU_DATA_VERTEX_HE = 24            /* uint32[2E]: the halfedges ending at each vertex, in creation order */
+    MCGPU_DATA_VERTEX_HE = 24,           /* uint32[2E]: the halfedges ending at each vertex, in creation order */
+    /* The cut path of a single dispatch (kernel.cpp:3332-3632): the edges MCUT's m0 gets from the
+     * hand-over's cutpath_edge_creation_info, built on the device at the first such query. Edge e is
+     * m0's e-th edge; its halfedge 2e runs from its first vertex to its second, 2e + 1 back. */
+    MCGPU_DATA_CUTPATH_STATUS = 25,      /* uint32[2]: 0, or 1 when a key holds fewer than two intersection
+                                            vertices (MCUT stops the dispatch there: the arrays below are
+                                            then not used); that key's index, else 0xFFFFFFFF */
+    MCGPU_DATA_CUTPATH_EDGES = 26,       /* uint32[2E]: m0 ids of each edge's first and second vertex
+                                            (m0_cutpath_edges in creation order) */
+    MCGPU_DATA_CUTPATH_FACE_KEYS = 27,   /* uint32[F]: ps faces with cut-path edges, ascending
+                                            (ps_iface_to_m0_edge_list keys) */
+    MCGPU_DATA_CUTPATH_FACE_OFFSETS = 28, /* uint32[F+1] */
+    MCGPU_DATA_CUTPATH_FACE_EDGES = 29,  /* uint32[o[F]]: each face's edges in the order MCUT appends them */
+    MCGPU_DATA_CUTPATH_VERTEX_OFFSETS = 30, /* uint32[R+1]: per intersection vertex (record order) ... */
+    MCGPU_DATA_CUTPATH_VERTEX_HALFEDGES = 31 /* uint32[2E]: ... the halfedges entering it in creation order
+                                            (ivtx_to_incoming_hlist) */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.

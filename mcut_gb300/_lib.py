@@ -37,6 +37,9 @@ DATA_EDGE_RECORD_OFFSETS, DATA_CUTPATH_PAIRS, DATA_CUTPATH_OFFSETS, DATA_CUTPATH
 # the halfedge mesh of the last mcgpu_halfedge_mesh call
 DATA_HE_TARGET, DATA_HE_FACE, DATA_HE_NEXT, DATA_HE_PREV, DATA_CORNER_HE, DATA_VERTEX_HE_OFFSETS, \
     DATA_VERTEX_HE = range(18, 25)
+# the cut path of a single dispatch (m0's edges from the hand-over)
+DATA_CUTPATH_STATUS, DATA_CUTPATH_EDGES, DATA_CUTPATH_FACE_KEYS, DATA_CUTPATH_FACE_OFFSETS, \
+    DATA_CUTPATH_FACE_EDGES, DATA_CUTPATH_VERTEX_OFFSETS, DATA_CUTPATH_VERTEX_HALFEDGES = range(25, 32)
 # mcgpu_hmesh_status (the oracle's HM_* values)
 HMESH_OK, HMESH_FACE_SIZE, HMESH_INDEX_RANGE, HMESH_DUPLICATE_INDEX, HMESH_NON_MANIFOLD, HMESH_TOO_SMALL, \
     HMESH_COMPONENTS = range(7)

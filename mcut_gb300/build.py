@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libmcut_gb300.so")
 OBJ = os.path.join(HERE, "_build")
-SOURCES = ["fe_sort.cu", "fe_kernels.cu", "fe_derived.cu", "fe_hmesh.cu", "fe_api.cu", "fe_noalloc.cu", "fe_server.cu"]
+SOURCES = ["fe_sort.cu", "fe_kernels.cu", "fe_derived.cu", "fe_cutpath.cu", "fe_hmesh.cu", "fe_api.cu", "fe_noalloc.cu", "fe_server.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 # --fmad=false keeps device a*b+c as two roundings; -ffp-contract=off does the
 # same for the host code (aarch64 g++ would otherwise fuse them, which changes

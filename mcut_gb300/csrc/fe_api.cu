@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "fe_common.cuh"
+#include "fe_cutpath.cuh"
 #include "fe_derived.cuh"
 #include "fe_hmesh.cuh"
 #include "fe_host.h"
@@ -106,6 +107,9 @@ enum BufId {
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
     B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB,
+    // the cut path (built at the first query for it)
+    B_CP_CAND, B_CP_INSIDE, B_CP_SORTED, B_CP_PROJ, B_CP_PK0, B_CP_PK1, B_CP_PV0, B_CP_PV1, B_CP_MADE, B_CP_FK0,
+    B_CP_FK1, B_CP_FV0, B_CP_FV1, B_CP_HK0, B_CP_HK1, B_CP_HV0, B_CP_HV1, B_CP_FLAGS, B_CP_SORT, B_CP_SCAN, B_CP_OUT,
     // the halfedge mesh (mcgpu_halfedge_mesh)
     B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
     B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
@@ -172,6 +176,10 @@ struct mcgpu_context_t {
     bool fuse_ok = false;
     uint64_t fuse_nrec = 0, fuse_npairs = 0;
     bool have_results = false; // a dispatch completed since the last trim (queries 1-17 read it)
+    // the cut path of the last single dispatch (built on demand)
+    bool cutpath_ready = false;
+    mcgpu::CutpathOut cutpath {};
+    uint32_t cutpath_counts[mcgpu::kCpCounts] = {};
     // the record hand-over of the last single dispatch (built on demand)
     bool derived_ready = false;
     mcgpu::DerivedOut derived {};
@@ -1055,6 +1063,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     c->flags = flags;
     c->derived_ready = false;
+    c->cutpath_ready = false;
     c->have_results = false;
     const unsigned long long launches0 = g_launches;
     int rc = build_layout(c, flags, n, srcs, cuts, eps);
@@ -1493,6 +1502,77 @@ int ensure_derived(mcgpu_context_t* c)
     return MCGPU_OK;
 }
 
+// The cut path of the last dispatch (one pair), from its record hand-over.
+int ensure_cutpath(mcgpu_context_t* c)
+{
+    if (c->cutpath_ready) return MCGPU_OK;
+    const int rc = ensure_derived(c);
+    if (rc != MCGPU_OK) return rc;
+    const uint32_t K = c->derived_counts[kDerivedCutpath], N = c->derived_counts[kDerivedCutpathEntries];
+    const uint32_t R = (uint32_t)c->n_records;
+    if (5ull * N + 1 > 0xFFFFFFFFull) return fail(MCGPU_TOO_LARGE, "too many intersection vertices for the cut path");
+    const size_t cc = std::max<size_t>(N - K, 1), ne = std::max<size_t>(N, 1);
+    CutpathScratch w {};
+    w.cand = c->buf[B_CP_CAND].get<uint32_t>(4 * cc);
+    w.inside = c->buf[B_CP_INSIDE].get<uint32_t>(2 * cc);
+    w.sorted = c->buf[B_CP_SORTED].get<uint32_t>(ne);
+    w.proj = c->buf[B_CP_PROJ].get<double>(ne);
+    w.pk[0] = c->buf[B_CP_PK0].get<unsigned long long>(cc);
+    w.pk[1] = c->buf[B_CP_PK1].get<unsigned long long>(cc);
+    w.pv[0] = c->buf[B_CP_PV0].get<uint32_t>(cc);
+    w.pv[1] = c->buf[B_CP_PV1].get<uint32_t>(cc);
+    w.made = c->buf[B_CP_MADE].get<uint32_t>(cc + 1);
+    w.fk[0] = c->buf[B_CP_FK0].get<unsigned long long>(5 * cc);
+    w.fk[1] = c->buf[B_CP_FK1].get<unsigned long long>(5 * cc);
+    w.fv[0] = c->buf[B_CP_FV0].get<uint32_t>(5 * cc);
+    w.fv[1] = c->buf[B_CP_FV1].get<uint32_t>(5 * cc);
+    w.hk[0] = c->buf[B_CP_HK0].get<unsigned long long>(2 * cc);
+    w.hk[1] = c->buf[B_CP_HK1].get<unsigned long long>(2 * cc);
+    w.hv[0] = c->buf[B_CP_HV0].get<uint32_t>(2 * cc);
+    w.hv[1] = c->buf[B_CP_HV1].get<uint32_t>(2 * cc);
+    w.flags = c->buf[B_CP_FLAGS].get<uint32_t>(5 * cc + 1);
+    w.sort_temp = c->buf[B_CP_SORT].get<uint32_t>(cutpath_sort_temp_bytes((uint32_t)cc) / 4 + 64);
+    w.scan_temp = c->buf[B_CP_SCAN].get<uint32_t>(cutpath_scan_temp_bytes((uint32_t)cc) / 4 + 64);
+    // outputs back to back: edges 2C | face_keys 5C | face_off 5C+1 | face_edges 5C | ivtx_off R+1 | ivtx_he 2C |
+    // counts
+    const size_t r = (size_t)R;
+    uint32_t* o = c->buf[B_CP_OUT].get<uint32_t>(19 * cc + r + 2 + kCpCounts);
+    CutpathOut& d = c->cutpath;
+    d.edges = o;
+    d.face_keys = d.edges + 2 * cc;
+    d.face_off = d.face_keys + 5 * cc;
+    d.face_edges = d.face_off + 5 * cc + 1;
+    d.ivtx_off = d.face_edges + 5 * cc;
+    d.ivtx_he = d.ivtx_off + r + 1;
+    d.counts = d.ivtx_he + 2 * cc; // == o + 19 cc + r + 2
+    const Layout& L = c->L;
+    const Problem& P = c->P;
+    CutpathInput in {};
+    in.X = P.X;
+    in.Xc = P.Xc;
+    in.xsplit = P.xsplit;
+    in.fidx = P.fidx;
+    in.foff = P.foff;
+    in.nv = (uint32_t)L.nv;
+    in.nf = (uint32_t)L.nf;
+    in.fs = L.fs[0];
+    in.rec_ids = c->W.rec_ids;
+    in.rec_pts = c->W.rec_pts;
+    in.nrec = R;
+    in.cp_pairs = c->derived.cp_pairs;
+    in.cp_off = c->derived.cp_off;
+    in.cp_vtx = c->derived.cp_vtx;
+    in.n_keys = K;
+    in.n_entries = N;
+    launch_cutpath(in, w, d, c->s);
+    ck(cudaMemcpyAsync(c->cutpath_counts, d.counts, sizeof(c->cutpath_counts), cudaMemcpyDeviceToHost, c->s),
+        "D2H cut-path counts");
+    ck(cudaStreamSynchronize(c->s), "sync cut path");
+    ck(cudaGetLastError(), "cut-path launch");
+    c->cutpath_ready = true;
+    return MCGPU_OK;
+}
+
 int copy_out(mcgpu_context_t* c, const void* dptr, uint64_t need, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (bytes_out) *bytes_out = need;
@@ -1590,6 +1670,7 @@ int mcgpu_context_trim(mcgpu_context c)
     c->fuse_key.clear();
     c->fuse_ok = false;
     c->derived_ready = false;
+    c->cutpath_ready = false;
     c->hm_ready = false;
     c->have_results = false;
     c->W = mcgpu::Work {};
@@ -1775,7 +1856,7 @@ int mcgpu_autotune(mcgpu_context c, uint32_t flags, const mcgpu_batch* sample, u
 int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
-    if (query < MCGPU_DATA_HE_TARGET && !c->have_results)
+    if ((query < MCGPU_DATA_HE_TARGET || query >= MCGPU_DATA_CUTPATH_STATUS) && !c->have_results)
         return fail(MCGPU_INVALID_VALUE, "no dispatch results (none completed, or the pool was trimmed)");
     try {
         const Work& W = c->W;
@@ -1875,6 +1956,39 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
                 memcpy(mem, &partial, 4);
                 return MCGPU_OK;
             }
+            }
+        }
+        case MCGPU_DATA_CUTPATH_STATUS:
+        case MCGPU_DATA_CUTPATH_EDGES:
+        case MCGPU_DATA_CUTPATH_FACE_KEYS:
+        case MCGPU_DATA_CUTPATH_FACE_OFFSETS:
+        case MCGPU_DATA_CUTPATH_FACE_EDGES:
+        case MCGPU_DATA_CUTPATH_VERTEX_OFFSETS:
+        case MCGPU_DATA_CUTPATH_VERTEX_HALFEDGES: {
+            const int rc = ensure_cutpath(c);
+            if (rc != MCGPU_OK) return rc;
+            const CutpathOut& d = c->cutpath;
+            const uint32_t* n = c->cutpath_counts;
+            switch (query) {
+            case MCGPU_DATA_CUTPATH_STATUS: {
+                if (bytes_out) *bytes_out = 8;
+                if (!mem && bytes == 0) return MCGPU_OK;
+                if (!mem || bytes < 8) return fail(MCGPU_INVALID_VALUE, "output buffer too small");
+                const uint32_t st[2] = { n[kCpBadKey] != 0xFFFFFFFFu ? 1u : 0u, n[kCpBadKey] };
+                memcpy(mem, st, 8);
+                return MCGPU_OK;
+            }
+            case MCGPU_DATA_CUTPATH_EDGES: return copy_out(c, d.edges, 8ull * n[kCpEdges], bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_FACE_KEYS:
+                return copy_out(c, d.face_keys, 4ull * n[kCpFaces], bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_FACE_OFFSETS:
+                return copy_out(c, d.face_off, 4ull * (n[kCpFaces] + 1), bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_FACE_EDGES:
+                return copy_out(c, d.face_edges, 4ull * n[kCpFaceEntries], bytes, mem, bytes_out);
+            case MCGPU_DATA_CUTPATH_VERTEX_OFFSETS:
+                return copy_out(c, d.ivtx_off, 4ull * (c->n_records + 1), bytes, mem, bytes_out);
+            default:
+                return copy_out(c, d.ivtx_he, 4ull * n[kCpHalfedges], bytes, mem, bytes_out);
             }
         }
         case MCGPU_DATA_HE_TARGET:

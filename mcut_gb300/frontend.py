@@ -127,6 +127,21 @@ class Context:
         d["partial_cut"] = bool(g(L.DATA_PARTIAL_CUT).reshape(-1)[0])
         return d
 
+    def cut_path(self) -> dict:
+        """The cut path of the last (single) dispatch: the edges MCUT's m0 gets
+        from the hand-over (kernel.cpp:3332-3632), built on the device. Keys as
+        oracle.cutpath: status, bad_key, edges [E,2] (first, second vertex;
+        halfedge 2e runs first -> second), face_keys, face_off, face_edges,
+        ivtx_off, ivtx_he."""
+        g = lambda q, cols=1: self._get(q, np.uint32, cols)  # noqa: E731
+        st = g(L.DATA_CUTPATH_STATUS).reshape(-1)
+        return dict(status=int(st[0]), bad_key=int(st[1]) if st[0] else 0, edges=g(L.DATA_CUTPATH_EDGES, 2),
+                    face_keys=g(L.DATA_CUTPATH_FACE_KEYS).reshape(-1),
+                    face_off=g(L.DATA_CUTPATH_FACE_OFFSETS).reshape(-1),
+                    face_edges=g(L.DATA_CUTPATH_FACE_EDGES).reshape(-1),
+                    ivtx_off=g(L.DATA_CUTPATH_VERTEX_OFFSETS).reshape(-1),
+                    ivtx_he=g(L.DATA_CUTPATH_VERTEX_HALFEDGES).reshape(-1))
+
     def halfedge_mesh(self, mesh, device: bool = False, fetch: bool = True) -> dict:
         """MCUT's halfedge mesh of one mesh and its input checks on the device
         (mcgpu_halfedge_mesh). mesh: dict(f=indices, fs=sizes or None,

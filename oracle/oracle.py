@@ -543,3 +543,35 @@ def cutpath_of(src, cut, xyz, hand):
     rid = np.asarray(hand["rec_ids"], np.uint32).reshape(-1, 5)
     return cutpath(len(xyz), xyz, off, idx, rid[:, 2:5], hand["rec_pts"], hand["cp_pairs"], hand["cp_off"],
                    hand["cp_vtx"])
+
+
+def observe_cutpath(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: int = 0):
+    """The unmodified reference's mcDispatch with its cut-path edge creation
+    (kernel.cpp:3332-3632) observed, once per front-end pass: its inputs in
+    the form cutpath() takes them and its outputs (edges in creation order,
+    ps_iface_to_m0_edge_list by face, ivtx_to_incoming_hlist per intersection
+    vertex). -> (mcDispatch result, [dict(inputs..., want=dict(edges,
+    face_keys, face_off, face_edges, ivtx_off, ivtx_he), bad)])."""
+    lib = _seam_lib()
+    if not hasattr(lib, "_cutpath_obs"):
+        lib.seam_cutpath_count.restype = C.c_int
+        lib.seam_cutpath_observation.restype = C.c_int
+        lib.seam_cutpath_observation.argtypes = [C.c_int, C.c_void_p] + [C.c_void_p] * 14
+        lib._cutpath_obs = True
+    res = observe_reference(src, cut, flags=flags, helpers=helpers)
+    obs = []
+    for k in range(lib.seam_cutpath_count()):
+        sz = np.zeros(16, np.uint64)
+        lib.seam_cutpath_observation(k, sz.ctypes.data, *([None] * 14))
+        n = [int(v) for v in sz]
+        x, ix = np.zeros(n[1]), np.zeros(n[5])
+        u = [np.zeros(n[i], np.uint32) for i in (2, 3, 4, 6, 7, 8, 9, 10, 11, 12, 13, 14)]
+        lib.seam_cutpath_observation(k, sz.ctypes.data, x.ctypes.data, ix.ctypes.data, *[a.ctypes.data for a in u])
+        soup_off, soup_idx, reg, key_pairs, key_off, key_vtx, edges, face_keys, face_off, face_edges, ivtx_off, \
+            ivtx_he = u
+        obs.append(dict(nv=n[0], x=x.reshape(-1, 3), soup_off=soup_off, soup_idx=soup_idx, reg=reg.reshape(-1, 3),
+                        ivtx_xyz=ix.reshape(-1, 3), cp_pairs=key_pairs.reshape(-1, 2), cp_off=key_off,
+                        cp_vtx=key_vtx, bad=n[15],
+                        want=dict(edges=edges.reshape(-1, 2), face_keys=face_keys, face_off=face_off,
+                                  face_edges=face_edges, ivtx_off=ivtx_off, ivtx_he=ivtx_he)))
+    return res["result"], obs

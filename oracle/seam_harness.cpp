@@ -322,7 +322,105 @@ void observer(const hmesh_t& ps, const hmesh_t& m0, const std::vector<std::pair<
     }
 }
 
+// The reference's cut-path edge creation, observed (each pass): its inputs in
+// the form oracle_cutpath takes them and its outputs.
+struct CutpathObs {
+    uint32_t nv = 0;
+    std::vector<double> x, ivtx_xyz;
+    std::vector<uint32_t> soup_off, soup_idx, reg, key_pairs, key_off, key_vtx;
+    std::vector<uint32_t> edges, face_keys, face_off, face_edges, ivtx_off, ivtx_he;
+    int bad = 0; // an output the arrays cannot hold (an edge id out of creation order)
+};
+std::vector<CutpathObs> g_cutpath;
+
+void cutpath_observer(const hmesh_t& ps, const hmesh_t& m0, const std::vector<std::pair<ed_t, fd_t>>& registry,
+    const std::map<pair<fd_t>, std::vector<vd_t>>& info, const std::vector<ed_t>& edges,
+    const std::unordered_map<fd_t, std::vector<ed_t>>& face_edges,
+    const std::unordered_map<vd_t, std::vector<hd_t>>& incoming)
+{
+    g_cutpath.emplace_back();
+    CutpathObs& o = g_cutpath.back();
+    const uint32_t nv = o.nv = (uint32_t)ps.number_of_vertices();
+    for (uint32_t v = 0; v < nv; ++v) {
+        const vec3& p = ps.vertex(vd_t(v));
+        o.x.insert(o.x.end(), { p.x(), p.y(), p.z() });
+    }
+    o.soup_off.push_back(0);
+    for (uint32_t f = 0; f < (uint32_t)ps.number_of_faces(); ++f) {
+        for (const vd_t v : ps.get_vertices_around_face(fd_t(f))) o.soup_idx.push_back((uint32_t)v);
+        o.soup_off.push_back((uint32_t)o.soup_idx.size());
+    }
+    auto face_or_none = [](fd_t f) { return f == hmesh_t::null_face() ? 0xFFFFFFFFu : (uint32_t)f; };
+    for (size_t i = 0; i < registry.size(); ++i) {
+        o.reg.push_back((uint32_t)registry[i].second);
+        o.reg.push_back(face_or_none(ps.face(ps.halfedge(registry[i].first, 0))));
+        o.reg.push_back(face_or_none(ps.face(ps.halfedge(registry[i].first, 1))));
+        const vec3& p = m0.vertex(vd_t(nv + (uint32_t)i));
+        o.ivtx_xyz.insert(o.ivtx_xyz.end(), { p.x(), p.y(), p.z() });
+    }
+    o.key_off.push_back(0);
+    for (const auto& kv : info) {
+        o.key_pairs.push_back((uint32_t)kv.first.first);
+        o.key_pairs.push_back((uint32_t)kv.first.second);
+        for (const vd_t v : kv.second) o.key_vtx.push_back((uint32_t)v);
+        o.key_off.push_back((uint32_t)o.key_vtx.size());
+    }
+    for (size_t e = 0; e < edges.size(); ++e) {
+        if ((size_t)edges[e] != e) o.bad = 1;
+        const hd_t h = m0.halfedge(edges[e], 0);
+        o.edges.push_back((uint32_t)m0.source(h));
+        o.edges.push_back((uint32_t)m0.target(h));
+        if ((size_t)h != 2 * e) o.bad = 1;
+    }
+    std::vector<uint32_t> fk;
+    for (const auto& kv : face_edges) fk.push_back((uint32_t)kv.first);
+    std::sort(fk.begin(), fk.end());
+    o.face_off.push_back(0);
+    for (const uint32_t f : fk) {
+        o.face_keys.push_back(f);
+        for (const ed_t e : face_edges.at(fd_t(f))) o.face_edges.push_back((uint32_t)e);
+        o.face_off.push_back((uint32_t)o.face_edges.size());
+    }
+    o.ivtx_off.assign(registry.size() + 1, 0);
+    for (size_t i = 0; i < registry.size(); ++i) {
+        auto it = incoming.find(vd_t(nv + (uint32_t)i));
+        if (it != incoming.end())
+            for (const hd_t h : it->second) o.ivtx_he.push_back((uint32_t)h);
+        o.ivtx_off[i + 1] = (uint32_t)o.ivtx_he.size();
+    }
+    if (incoming.size() > 0)
+        for (const auto& kv : incoming)
+            if ((uint32_t)kv.first < nv || (uint32_t)kv.first >= nv + registry.size()) o.bad = 1;
+}
+
 } // namespace
+
+// The cut-path observations of the last seam_observe_reference call: how many.
+extern "C" int seam_cutpath_count() { return (int)g_cutpath.size(); }
+
+// Observation k: sizes[14] = nv, |x|, |soup_off|, |soup_idx|, |reg|, |ivtx_xyz|,
+// |key_pairs|, |key_off|, |key_vtx|, |edges|, |face_keys|, |face_off|,
+// |face_edges|, |ivtx_off|; then (arrays non-null) the arrays in that order
+// (doubles: x, ivtx_xyz) with |ivtx_he| in sizes[14] and bad in sizes[15].
+extern "C" int seam_cutpath_observation(int k, uint64_t* sizes, double* x, double* ivtx_xyz, uint32_t* soup_off,
+    uint32_t* soup_idx, uint32_t* reg, uint32_t* key_pairs, uint32_t* key_off, uint32_t* key_vtx, uint32_t* edges,
+    uint32_t* face_keys, uint32_t* face_off, uint32_t* face_edges, uint32_t* ivtx_off, uint32_t* ivtx_he)
+{
+    if (k < 0 || k >= (int)g_cutpath.size()) return -1;
+    const CutpathObs& o = g_cutpath[k];
+    const uint64_t sz[16] = { o.nv, o.x.size(), o.soup_off.size(), o.soup_idx.size(), o.reg.size(), o.ivtx_xyz.size(),
+        o.key_pairs.size(), o.key_off.size(), o.key_vtx.size(), o.edges.size(), o.face_keys.size(), o.face_off.size(),
+        o.face_edges.size(), o.ivtx_off.size(), o.ivtx_he.size(), (uint64_t)o.bad };
+    memcpy(sizes, sz, sizeof sz);
+    auto cp = [](auto* dst, const auto& v) {
+        if (dst && !v.empty()) memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+    };
+    cp(x, o.x); cp(ivtx_xyz, o.ivtx_xyz); cp(soup_off, o.soup_off); cp(soup_idx, o.soup_idx); cp(reg, o.reg);
+    cp(key_pairs, o.key_pairs); cp(key_off, o.key_off); cp(key_vtx, o.key_vtx); cp(edges, o.edges);
+    cp(face_keys, o.face_keys); cp(face_off, o.face_off); cp(face_edges, o.face_edges); cp(ivtx_off, o.ivtx_off);
+    cp(ivtx_he, o.ivtx_he);
+    return 0;
+}
 
 // The unmodified reference's dispatch, observed: its records of the last
 // front-end pass in its own numbering (q, r, tested face; up to cap).
@@ -333,8 +431,10 @@ extern "C" int seam_observe_reference(const void* sv, const uint32_t* sf, const 
 {
     g_calls = 0;
     g_observed.clear();
+    g_cutpath.clear();
     mcut_seam_install(nullptr);
     mcut_seam_observe(&observer);
+    mcut_seam_observe_cutpath(&cutpath_observer);
     char cwd[4096];
     if (!getcwd(cwd, sizeof cwd)) return -1000;
     if (workdir && chdir(workdir) != 0) return -1001;
@@ -344,6 +444,7 @@ extern "C" int seam_observe_reference(const void* sv, const uint32_t* sf, const 
     if (err == MC_NO_ERROR) err = mcDispatch(ctx, flags, sv, sf, sfs, nsv, nsf, cv, cf, cfs, ncv, ncf);
     if (ctx != MC_NULL_HANDLE) mcReleaseContext(ctx);
     mcut_seam_observe(nullptr);
+    mcut_seam_observe_cutpath(nullptr);
     if (workdir && chdir(cwd) != 0) return -1002;
     *n = (int64_t)(g_observed.size() / 3);
     for (int64_t i = 0; i < *n && i < cap; ++i) {

@@ -41,3 +41,15 @@ typedef void (*mcut_seam_observer_fn)(const hmesh_t& ps, const hmesh_t& m0,
     const std::vector<std::pair<ed_t, fd_t>>& registry);
 extern mcut_seam_observer_fn g_mcut_seam_observer;
 extern "C" void mcut_seam_observe(mcut_seam_observer_fn fn);
+
+// Observer of the cut-path edge creation (kernel.cpp:3332-3632): called after
+// it with its inputs (the soup, m0's intersection vertices and their
+// registry, cutpath_edge_creation_info) and outputs (m0_cutpath_edges, in
+// creation order, ps_iface_to_m0_edge_list, ivtx_to_incoming_hlist).
+typedef void (*mcut_seam_cutpath_fn)(const hmesh_t& ps, const hmesh_t& m0,
+    const std::vector<std::pair<ed_t, fd_t>>& registry,
+    const std::map<pair<fd_t>, std::vector<vd_t>>& cutpath_edge_creation_info,
+    const std::vector<ed_t>& m0_cutpath_edges, const std::unordered_map<fd_t, std::vector<ed_t>>& ps_iface_to_m0_edge_list,
+    const std::unordered_map<vd_t, std::vector<hd_t>>& ivtx_to_incoming_hlist);
+extern mcut_seam_cutpath_fn g_mcut_seam_cutpath_observer;
+extern "C" void mcut_seam_observe_cutpath(mcut_seam_cutpath_fn fn);
