@@ -426,6 +426,7 @@ def run_configs(ctx, lib, world, cpu=True):
                  "escalations": {"fp32_filter": esc[0], "fp64_filter": esc[1], "exact": esc[2],
                                  "rates": [e / tot for e in esc]}}
     out["hmesh"] = run_hmesh(ctx, cpu)
+    out["cutpath"] = run_cutpath(ctx, cpu)
     return out
 
 
@@ -460,6 +461,50 @@ def run_hmesh(ctx, cpu=True):
             row["cpu_port_1_thread_ms"] = 1e3 * (time.perf_counter() - t0)
         res[name] = row
     return res
+
+
+def run_cutpath(ctx, cpu=True):
+    """The cut-path edges of the headline dispatch (kernel.cpp:3332-3632) on
+    the device: wall time of the first cut-path query after a dispatch whose
+    hand-over is already built (the build, its count readback and one small
+    query); beside it the CPU restatement (oracle/cutpath_oracle.c, one
+    thread) on the same hand-over."""
+    import ctypes as C
+    import torch
+    from mcut_gb300 import meshgen, recentre
+    from mcut_gb300 import _lib as L
+    s, c = meshgen.sphere_heightfield(16.0)
+    sx, cx, eps = recentre(s, c)
+    d = [torch.from_numpy(a).cuda() for a in (sx, cx, s["f"].astype(np.int32), c["f"].astype(np.int32))]
+    ms = L.Mesh(d[0].data_ptr(), d[2].data_ptr(), None, sx.shape[0], s["f"].shape[0] // 3)
+    mc = L.Mesh(d[1].data_ptr(), d[3].data_ptr(), None, cx.shape[0], c["f"].shape[0] // 3)
+    lib, sm, nb = L.load(), L.Summary(), C.c_uint64(0)
+    st = np.zeros(2, np.uint32)
+    ts = []
+    for rep in range(13):
+        L.check(lib.mcgpu_dispatch(ctx._h, L.DEVICE_POINTERS, C.byref(ms), C.byref(mc), eps, C.byref(sm)), "dispatch")
+        L.check(lib.mcgpu_get_data(ctx._h, L.DATA_CUTPATH_PAIRS, 0, None, C.byref(nb)), "hand-over")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L.check(lib.mcgpu_get_data(ctx._h, L.DATA_CUTPATH_STATUS, 8, st.ctypes.data, C.byref(nb)), "cut path")
+        if rep >= 3:
+            ts.append(1e3 * (time.perf_counter() - t0))
+    cp = ctx.cut_path()
+    row = {"workload": "cut-path edges of the C2x16 dispatch (10,974 intersection vertices)",
+           "edges": int(len(cp["edges"])), "faces": int(len(cp["face_keys"])), "status": int(cp["status"]),
+           "gpu_ms": float(np.median(ts))}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        hand = ctx.hand_over()
+        hand["rec_ids"] = ctx._get(L.DATA_RECORD_IDS, np.uint32, 5)
+        hand["rec_pts"] = ctx._get(L.DATA_RECORD_POINTS, np.float64, 3)
+        xyz = ctx.vertices()
+        soup = oracle.soup_faces(s, c)
+        t0 = time.perf_counter()
+        oracle.cutpath_of(s, c, xyz, hand, soup)
+        row["cpu_port_1_thread_ms"] = 1e3 * (time.perf_counter() - t0)
+    return row
 
 
 SERVED_WORKLOAD = ("served: open-loop Poisson arrivals; each request one fracture pair with total triangles "
@@ -692,6 +737,17 @@ def run_gpu(args, world, rank, local):
     # DRAM traffic and, per kernel of the stage, pipe activity, lanes per warp
     # instruction and L2 hits (ncu)
     traffic, figs = ncu_figures(dom)
+    # the fp64-bound kernels against the device's fp64 rate, measured here:
+    # a kernel's fp64 operations per second = its fp64 pipe's active share
+    # (ncu, traffic.json) x that rate
+    g = C.c_double(0.0)
+    fp64 = None
+    if lib.mcgpu_measure_fp64_rate(local, C.byref(g)) == L.OK and g.value > 0:
+        pct = figs.get("fp64_pipe_active_pct", {})
+        fp64 = {"peak_gops": g.value, "peak_source": "measured (mcgpu_measure_fp64_rate: separately rounded "
+                                                     "fp64 multiply + add chains on every SM, CUDA events)",
+                "achieved_gops": {k: g.value * v / 100.0 for k, v in pct.items()},
+                "frac": {k: v / 100.0 for k, v in pct.items()}}
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -711,7 +767,8 @@ def run_gpu(args, world, rank, local):
                      "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, **figs,
                      "algorithmic_bytes": algo,
-                     "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "algorithmic_bytes_rule": units, "peak_source": f"{src_peak} (MEASURED_PEAKS.json hbm_gbs)",
+                     "fp64": fp64},
         "stage_ms": {k: round(v, 4) for k, v in per.items()},
         "front_end": summ,
         "cpu_baseline": cpu,

@@ -417,6 +417,12 @@ int mcgpu_context_get_memory(mcgpu_context ctx, uint64_t* device_bytes, uint64_t
 int mcgpu_context_set_memory_limit(mcgpu_context ctx, uint64_t limit_bytes);
 int mcgpu_context_trim(mcgpu_context ctx);
 
+/* The device's fp64 arithmetic rate in G operations/s: independent chains of
+ * separately rounded multiplies and adds (the form the library's fp64 code
+ * takes), timed with CUDA events over a fixed loop on every SM. The
+ * denominator of the fp64-bound kernels' roofline. */
+int mcgpu_measure_fp64_rate(int device, double* gops);
+
 /* Human-readable description of the last failure on this thread. */
 const char* mcgpu_last_error(void);
 

@@ -131,6 +131,7 @@ def load():
     lib.mcgpu_context_get_memory.argtypes = [ctx, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.mcgpu_context_set_memory_limit.argtypes = [ctx, C.c_uint64]
     lib.mcgpu_context_trim.argtypes = [ctx]
+    lib.mcgpu_measure_fp64_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
     srv = C.c_void_p
     lib.mcgpu_server_create.argtypes = [C.POINTER(srv), C.POINTER(ServerConfig)]
     lib.mcgpu_server_release.argtypes = [srv]

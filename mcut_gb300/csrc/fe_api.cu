@@ -533,6 +533,22 @@ __global__ void k_frames(uint32_t n_pairs, const double* __restrict__ com, const
     }
 }
 
+// the fp64 arithmetic rate: independent chains of a separately rounded
+// multiply and add (as the library's fp64 code runs, --fmad=false)
+constexpr int kFp64Chains = 8;
+__global__ void __launch_bounds__(256) k_fp64_rate(double* __restrict__ out, int iters, double a, double b)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    double x[kFp64Chains];
+    for (int k = 0; k < kFp64Chains; ++k) x[k] = 1.0 + 1e-3 * (double)(t + k);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < kFp64Chains; ++k) x[k] = __dadd_rn(__dmul_rn(x[k], a), b);
+    double s = 0.0;
+    for (int k = 0; k < kFp64Chains; ++k) s += x[k];
+    out[t] = s;
+}
+
 // resident cut mesh: its stored user coordinates mapped into the pair's frame
 __global__ void k_apply_frame(const double* __restrict__ in, double* __restrict__ out, uint64_t n3, double c0,
     double c1, double c2, double t0, double t1, double t2)
@@ -1637,6 +1653,41 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         return fail(e.e == cudaErrorMemoryAllocation ? MCGPU_OUT_OF_MEMORY : MCGPU_CUDA_ERROR,
             e.where + ": " + cudaGetErrorString(e.e));
     }
+}
+
+int mcgpu_measure_fp64_rate(int device, double* gops)
+{
+    if (!gops) return fail(MCGPU_INVALID_VALUE, "null output");
+    *gops = 0.0;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+        return fail(MCGPU_INVALID_VALUE, "no such CUDA device");
+    cudaSetDevice(device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int blocks = std::max(1, sms) * 8, threads = 256, iters = 2048;
+    double* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return fail(MCGPU_OUT_OF_MEMORY, "fp64 probe");
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) { // the first run warms up
+        cudaEventRecord(e0);
+        k_fp64_rate<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) return fail(MCGPU_CUDA_ERROR, std::string("fp64 probe: ") + cudaGetErrorString(err));
+    *gops = (double)blocks * threads * iters * kFp64Chains * 2.0 / (best * 1e6);
+    return MCGPU_OK;
 }
 
 int mcgpu_context_get_memory(mcgpu_context c, uint64_t* device_bytes, uint64_t* limit_bytes)

@@ -481,18 +481,24 @@ def soup_faces(src, cut):
     a cut face at its third (cs.get_vertices_around_face of the soup's
     edge-created face); cut vertex ids offset by the source vertex count.
     -> (offsets, indices) as the ps numbers faces (source, then cut)."""
-    off, idx = [0], []
+    offs, idxs, base = [np.zeros(1, np.int64)], [], 0
     vs = len(src["v"])
     for m, rot, vo in ((src, 1, 0), (cut, 2, vs)):
-        f = np.asarray(m["f"], dtype=np.int64)
-        fs = np.full(len(f) // 3, 3) if m.get("fs") is None else np.asarray(m["fs"], dtype=np.int64)
+        f = np.asarray(m["f"], dtype=np.int64) + vo
+        if m.get("fs") is None:  # triangles: one roll of every row
+            idxs.append(np.roll(f.reshape(-1, 3), -rot, axis=1).reshape(-1))
+            offs.append(base + 3 * np.arange(1, len(f) // 3 + 1, dtype=np.int64))
+            base += len(f)
+            continue
+        fs = np.asarray(m["fs"], dtype=np.int64)
         o = np.concatenate([[0], np.cumsum(fs)])
         for k in range(len(fs)):
-            face = f[o[k]:o[k + 1]] + vo
+            face = f[o[k]:o[k + 1]]
             r = rot % len(face)
-            idx.extend(np.concatenate([face[r:], face[:r]]).tolist())
-            off.append(off[-1] + len(face))
-    return np.asarray(off, np.uint32), np.asarray(idx, np.uint32)
+            idxs.append(np.concatenate([face[r:], face[:r]]))
+        offs.append(base + o[1:])
+        base += int(o[-1])
+    return np.concatenate(offs).astype(np.uint32), np.concatenate(idxs).astype(np.uint32)
 
 
 def cutpath(nv, x, soup_off, soup_idx, registry, ivtx_xyz, cp_pairs, cp_off, cp_vtx):
@@ -536,10 +542,11 @@ def cutpath(nv, x, soup_off, soup_idx, registry, ivtx_xyz, cp_pairs, cp_off, cp_
     return out
 
 
-def cutpath_of(src, cut, xyz, hand):
+def cutpath_of(src, cut, xyz, hand, soup=None):
     """The cut path of a pass from its internal coordinates (source then cut
-    vertices) and its record hand-over (oracle.seam's keys)."""
-    off, idx = soup_faces(src, cut)
+    vertices) and its record hand-over (oracle.seam's keys); soup: the
+    (offsets, indices) of soup_faces when already made."""
+    off, idx = soup if soup is not None else soup_faces(src, cut)
     rid = np.asarray(hand["rec_ids"], np.uint32).reshape(-1, 5)
     return cutpath(len(xyz), xyz, off, idx, rid[:, 2:5], hand["rec_pts"], hand["cp_pairs"], hand["cp_off"],
                    hand["cp_vtx"])
