@@ -175,8 +175,17 @@ typedef enum mcgpu_data {
     MCGPU_DATA_CUTPATH_FACE_OFFSETS = 28, /* uint32[F+1] */
     MCGPU_DATA_CUTPATH_FACE_EDGES = 29,  /* uint32[o[F]]: each face's edges in the order MCUT appends them */
     MCGPU_DATA_CUTPATH_VERTEX_OFFSETS = 30, /* uint32[R+1]: per intersection vertex (record order) ... */
-    MCGPU_DATA_CUTPATH_VERTEX_HALFEDGES = 31 /* uint32[2E]: ... the halfedges entering it in creation order
+    MCGPU_DATA_CUTPATH_VERTEX_HALFEDGES = 31, /* uint32[2E]: ... the halfedges entering it in creation order
                                             (ivtx_to_incoming_hlist) */
+    /* Floating polygons of a single dispatch (kernel.cpp:4078-4200), from its cut path: a circular cut
+     * path (every vertex on two of its edges, none on a border edge of the soup) whose vertices all
+     * pierce the same face. MCUT stops the dispatch on them (DETECTED_FLOATING_POLYGON), partitions
+     * each such face and runs the front end again. P polygons, by face, then smallest vertex. */
+    MCGPU_DATA_FLOATING_FACES = 32,      /* uint32[P]: the ps face holding each polygon */
+    MCGPU_DATA_FLOATING_OFFSETS = 33,    /* uint32[P+1] */
+    MCGPU_DATA_FLOATING_VERTICES = 34,   /* uint32[o[P]]: m0 ids around each polygon, from its smallest */
+    MCGPU_DATA_FLOATING_NORMALS = 35,    /* double[3P]: the face's unit normal (floating_polygon_info_t) */
+    MCGPU_DATA_FLOATING_NORMAL_COMPONENTS = 36 /* int32[P]: its largest component */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.

@@ -40,6 +40,9 @@ DATA_HE_TARGET, DATA_HE_FACE, DATA_HE_NEXT, DATA_HE_PREV, DATA_CORNER_HE, DATA_V
 # the cut path of a single dispatch (m0's edges from the hand-over)
 DATA_CUTPATH_STATUS, DATA_CUTPATH_EDGES, DATA_CUTPATH_FACE_KEYS, DATA_CUTPATH_FACE_OFFSETS, \
     DATA_CUTPATH_FACE_EDGES, DATA_CUTPATH_VERTEX_OFFSETS, DATA_CUTPATH_VERTEX_HALFEDGES = range(25, 32)
+# its floating polygons
+DATA_FLOATING_FACES, DATA_FLOATING_OFFSETS, DATA_FLOATING_VERTICES, DATA_FLOATING_NORMALS, \
+    DATA_FLOATING_NORMAL_COMPONENTS = range(32, 37)
 # mcgpu_hmesh_status (the oracle's HM_* values)
 HMESH_OK, HMESH_FACE_SIZE, HMESH_INDEX_RANGE, HMESH_DUPLICATE_INDEX, HMESH_NON_MANIFOLD, HMESH_TOO_SMALL, \
     HMESH_COMPONENTS = range(7)

@@ -110,6 +110,7 @@ enum BufId {
     // the cut path (built at the first query for it)
     B_CP_CAND, B_CP_INSIDE, B_CP_SORTED, B_CP_PROJ, B_CP_PK0, B_CP_PK1, B_CP_PV0, B_CP_PV1, B_CP_MADE, B_CP_FK0,
     B_CP_FK1, B_CP_FV0, B_CP_FV1, B_CP_HK0, B_CP_HK1, B_CP_HV0, B_CP_HV1, B_CP_FLAGS, B_CP_SORT, B_CP_SCAN, B_CP_OUT,
+    B_FP_PARENT, B_FP_FLAGS, B_FP_SIZE, B_FP_K0, B_FP_K1, B_FP_V0, B_FP_V1, B_FP_SORT, B_FP_SCAN, B_FP_OUT, B_FP_NRM,
     // the halfedge mesh (mcgpu_halfedge_mesh)
     B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
     B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
@@ -176,6 +177,11 @@ struct mcgpu_context_t {
     bool fuse_ok = false;
     uint64_t fuse_nrec = 0, fuse_npairs = 0;
     bool have_results = false; // a dispatch completed since the last trim (queries 1-17 read it)
+    // the floating polygons of the last single dispatch (built on demand)
+    bool floating_ready = false;
+    mcgpu::FloatingOut floating {};
+    uint32_t floating_counts[mcgpu::kFpCounts] = {};
+    mcgpu::CutpathInput cutpath_in {};
     // the cut path of the last single dispatch (built on demand)
     bool cutpath_ready = false;
     mcgpu::CutpathOut cutpath {};
@@ -1080,6 +1086,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->flags = flags;
     c->derived_ready = false;
     c->cutpath_ready = false;
+    c->floating_ready = false;
     c->have_results = false;
     const unsigned long long launches0 = g_launches;
     int rc = build_layout(c, flags, n, srcs, cuts, eps);
@@ -1580,12 +1587,50 @@ int ensure_cutpath(mcgpu_context_t* c)
     in.cp_vtx = c->derived.cp_vtx;
     in.n_keys = K;
     in.n_entries = N;
+    c->cutpath_in = in;
     launch_cutpath(in, w, d, c->s);
     ck(cudaMemcpyAsync(c->cutpath_counts, d.counts, sizeof(c->cutpath_counts), cudaMemcpyDeviceToHost, c->s),
         "D2H cut-path counts");
     ck(cudaStreamSynchronize(c->s), "sync cut path");
     ck(cudaGetLastError(), "cut-path launch");
     c->cutpath_ready = true;
+    return MCGPU_OK;
+}
+
+// The floating polygons of the last dispatch (one pair), from its cut path.
+int ensure_floating(mcgpu_context_t* c)
+{
+    if (c->floating_ready) return MCGPU_OK;
+    const int rc = ensure_cutpath(c);
+    if (rc != MCGPU_OK) return rc;
+    const uint32_t R = (uint32_t)c->n_records;
+    const size_t r = std::max<size_t>(R, 1);
+    FloatingScratch w {};
+    w.parent = c->buf[B_FP_PARENT].get<uint32_t>(r);
+    w.flags = c->buf[B_FP_FLAGS].get<uint32_t>(r);
+    w.size = c->buf[B_FP_SIZE].get<uint32_t>(r);
+    w.k[0] = c->buf[B_FP_K0].get<unsigned long long>(r);
+    w.k[1] = c->buf[B_FP_K1].get<unsigned long long>(r);
+    w.v[0] = c->buf[B_FP_V0].get<uint32_t>(r);
+    w.v[1] = c->buf[B_FP_V1].get<uint32_t>(r);
+    w.sort_temp = c->buf[B_FP_SORT].get<uint32_t>(floating_sort_temp_bytes(R) / 4 + 64);
+    w.scan_temp = c->buf[B_FP_SCAN].get<uint32_t>(floating_scan_temp_bytes(R) / 4 + 64);
+    // outputs: faces R | off R+1 | vtx R | mc R | counts; normals apart (doubles)
+    uint32_t* o = c->buf[B_FP_OUT].get<uint32_t>(4 * r + 1 + kFpCounts);
+    FloatingOut& d = c->floating;
+    d.faces = o;
+    d.off = d.faces + r;
+    d.vtx = d.off + r + 1;
+    d.mc = reinterpret_cast<int32_t*>(d.vtx + r);
+    d.counts = reinterpret_cast<uint32_t*>(d.mc + r);
+    d.normals = c->buf[B_FP_NRM].get<double>(3 * r);
+    launch_floating(c->cutpath_in, c->cutpath, w, d, c->s);
+    ck(cudaMemcpyAsync(c->floating_counts, d.counts, sizeof(c->floating_counts), cudaMemcpyDeviceToHost, c->s),
+        "D2H floating counts");
+    ck(cudaStreamSynchronize(c->s), "sync floating polygons");
+    ck(cudaGetLastError(), "floating-polygon launch");
+    if (c->floating_counts[kFpError]) return fail(MCGPU_CUDA_ERROR, "floating polygons: union-find retry cap");
+    c->floating_ready = true;
     return MCGPU_OK;
 }
 
@@ -1722,6 +1767,7 @@ int mcgpu_context_trim(mcgpu_context c)
     c->fuse_ok = false;
     c->derived_ready = false;
     c->cutpath_ready = false;
+    c->floating_ready = false;
     c->hm_ready = false;
     c->have_results = false;
     c->W = mcgpu::Work {};
@@ -2040,6 +2086,24 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
                 return copy_out(c, d.ivtx_off, 4ull * (c->n_records + 1), bytes, mem, bytes_out);
             default:
                 return copy_out(c, d.ivtx_he, 4ull * n[kCpHalfedges], bytes, mem, bytes_out);
+            }
+        }
+        case MCGPU_DATA_FLOATING_FACES:
+        case MCGPU_DATA_FLOATING_OFFSETS:
+        case MCGPU_DATA_FLOATING_VERTICES:
+        case MCGPU_DATA_FLOATING_NORMALS:
+        case MCGPU_DATA_FLOATING_NORMAL_COMPONENTS: {
+            const int rc = ensure_floating(c);
+            if (rc != MCGPU_OK) return rc;
+            const FloatingOut& d = c->floating;
+            const uint64_t np = c->floating_counts[kFpPolygons];
+            switch (query) {
+            case MCGPU_DATA_FLOATING_FACES: return copy_out(c, d.faces, 4 * np, bytes, mem, bytes_out);
+            case MCGPU_DATA_FLOATING_OFFSETS: return copy_out(c, d.off, 4 * (np + 1), bytes, mem, bytes_out);
+            case MCGPU_DATA_FLOATING_VERTICES:
+                return copy_out(c, d.vtx, 4ull * c->floating_counts[kFpVertices], bytes, mem, bytes_out);
+            case MCGPU_DATA_FLOATING_NORMALS: return copy_out(c, d.normals, 24 * np, bytes, mem, bytes_out);
+            default: return copy_out(c, d.mc, 4 * np, bytes, mem, bytes_out);
             }
         }
         case MCGPU_DATA_HE_TARGET:

@@ -65,6 +65,36 @@ __device__ __forceinline__ uint32_t cp_corner(const CutpathInput& in, uint32_t f
     return in.fidx[o + j];
 }
 
+// face f's unit normal and largest component from its soup corners
+// (compute_polygon_plane_coefficients, math.cpp:130-239); false: no plane
+__device__ bool cp_plane(const CutpathInput& in, uint32_t f, double* nrm, int& mc)
+{
+    const uint32_t o = cp_face_o(in, f), n = cp_face_n(in, f);
+    double nx = 0.0, ny = 0.0, nz = 0.0, c[3], d[3], first[3];
+    cp_vertex(in, cp_corner(in, f, o, n, 0), first);
+    c[0] = first[0]; c[1] = first[1]; c[2] = first[2];
+    for (uint32_t k = 0; k < n; ++k) {
+        if (k + 1 < n) cp_vertex(in, cp_corner(in, f, o, n, k + 1), d);
+        else { d[0] = first[0]; d[1] = first[1]; d[2] = first[2]; }
+        nx = nx + (c[1] - d[1]) * (c[2] + d[2]);
+        ny = ny + (c[2] - d[2]) * (c[0] + d[0]);
+        nz = nz + (c[0] - d[0]) * (c[1] + d[1]);
+        c[0] = d[0]; c[1] = d[1]; c[2] = d[2];
+    }
+    const double nn[3] = { nx, ny, nz };
+    const double sq = dot3(nn, nn);
+    if (isnan(nx) || isnan(ny) || isnan(nz) || sq < 1e-9 || sq == 0.0) return false;
+    const double len = sqrt(sq);
+    nrm[0] = nx / len; nrm[1] = ny / len; nrm[2] = nz / len;
+    mc = 0;
+    double big = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        const double t = fabs(nrm[i]);
+        if (t > big) { big = t; mc = i; }
+    }
+    return true;
+}
+
 // compute_point_in_polygon_test (math.cpp:643-703, 851-902) against face f,
 // with the face's plane from its soup corners (compute_polygon_plane_
 // coefficients, math.cpp:130-239) and calculate_projection_matrix
@@ -260,7 +290,7 @@ __device__ void pj_sort(PjArr f, long n)
     }
 }
 
-__device__ __forceinline__ unsigned long long sentinel(int bits) { return bits >= 64 ? ~0ull : ((1ull << bits) - 1); }
+__host__ __device__ __forceinline__ unsigned long long sentinel(int bits) { return bits >= 64 ? ~0ull : ((1ull << bits) - 1); }
 
 // one thread per key: its candidate edges (a long key's vertices sorted along their line)
 __global__ void __launch_bounds__(kCB) k_cp_candidates(CutpathInput in, CutpathScratch w, uint32_t* __restrict__ counts)
@@ -449,11 +479,158 @@ __global__ void k_cp_edges_count(const uint32_t* __restrict__ made, uint32_t n, 
     if (threadIdx.x == 0 && blockIdx.x == 0) counts[kCpEdges] = made[n];
 }
 
+// ---- floating polygons ----
+__global__ void __launch_bounds__(kCB) k_fp_init(uint32_t R, FloatingScratch w, unsigned long long none)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < R; v += gridDim.x * blockDim.x) {
+        w.parent[v] = v;
+        w.flags[v] = 0;
+        w.size[v] = 0;
+        w.k[0][v] = none;
+        w.v[0][v] = v;
+    }
+}
+
+// parents only ever point to smaller ids, so a find walks down to its root
+__device__ __forceinline__ uint32_t fp_find(const uint32_t* parent, uint32_t x)
+{
+    for (;;) {
+        const uint32_t p = *(volatile const uint32_t*)&parent[x];
+        if (p == x) return x;
+        x = p;
+    }
+}
+
+// union of each cut-path edge's two vertices: a larger root is hooked under a
+// smaller one by compare-and-swap; every failed exchange means another hook
+// happened, so the retries are bounded; the cap only guards the loop
+__global__ void __launch_bounds__(kCB) k_fp_union(const uint32_t* __restrict__ edges, const uint32_t* __restrict__ counts,
+    uint32_t nv, uint32_t* parent, uint32_t* __restrict__ fcounts)
+{
+    const uint32_t ne = counts[kCpEdges];
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+        uint32_t u = fp_find(parent, edges[2 * e] - nv), v = fp_find(parent, edges[2 * e + 1] - nv);
+        for (uint32_t tries = 0;; ++tries) {
+            if (u == v) break;
+            if (tries > 1u << 24) { atomicExch(&fcounts[kFpError], 1u); break; }
+            if (u < v) { const uint32_t t = u; u = v; v = t; }
+            const uint32_t old = atomicCAS(&parent[u], u, v);
+            if (old == u) break;
+            u = fp_find(parent, old);
+            v = fp_find(parent, v);
+        }
+    }
+}
+
+// every vertex's root; component sizes; a component is not a floating polygon
+// when a vertex has other than two edges, lies on a border edge or pierces
+// another face than its root
+__global__ void __launch_bounds__(kCB) k_fp_flags(CutpathInput in, const uint32_t* __restrict__ ivtx_off,
+    FloatingScratch w)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < in.nrec; v += gridDim.x * blockDim.x) {
+        const uint32_t deg = ivtx_off[v + 1] - ivtx_off[v];
+        if (deg == 0) continue;
+        const uint32_t r = fp_find(w.parent, v);
+        atomicAdd(&w.size[r], 1u);
+        const uint32_t* rv = in.rec_ids + 5 * (size_t)v;
+        const bool bad = deg != 2 || rv[4] == kNone || rv[2] != in.rec_ids[5 * (size_t)r + 2];
+        if (bad) atomicOr(&w.flags[r], 1u);
+    }
+}
+
+__global__ void __launch_bounds__(kCB) k_fp_roots(CutpathInput in, const uint32_t* __restrict__ ivtx_off,
+    FloatingScratch w, int rbits, uint32_t* __restrict__ fcounts)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < in.nrec; v += gridDim.x * blockDim.x) {
+        const bool root = ivtx_off[v + 1] > ivtx_off[v] && w.parent[v] == v && w.flags[v] == 0;
+        if (root) {
+            w.k[0][v] = ((unsigned long long)in.rec_ids[5 * (size_t)v + 2] << rbits) | v;
+            atomicAdd(&fcounts[kFpPolygons], 1u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCB) k_fp_sizes(const unsigned long long* __restrict__ k,
+    const uint32_t* __restrict__ roots, uint32_t R, unsigned long long none, const uint32_t* __restrict__ size,
+    uint32_t* __restrict__ off)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < R; p += gridDim.x * blockDim.x)
+        off[p] = k[p] != none ? size[roots[p]] : 0u;
+}
+
+// one thread per polygon: its face, normal, and its cycle from its root
+__global__ void __launch_bounds__(kCB) k_fp_walk(CutpathInput in, CutpathOut cp, const unsigned long long* __restrict__ k,
+    const uint32_t* __restrict__ roots, unsigned long long none, int rbits, FloatingOut o, const uint32_t* __restrict__ size)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < in.nrec; p += gridDim.x * blockDim.x) {
+        if (k[p] == none) continue;
+        const uint32_t root = roots[p], face = (uint32_t)(k[p] >> rbits), n = size[root], base = o.off[p];
+        o.faces[p] = face;
+        double nrm[3] = { 0.0, 0.0, 0.0 };
+        int mc = -1;
+        cp_plane(in, face, nrm, mc);
+        o.normals[3 * (size_t)p] = nrm[0];
+        o.normals[3 * (size_t)p + 1] = nrm[1];
+        o.normals[3 * (size_t)p + 2] = nrm[2];
+        o.mc[p] = mc;
+        uint32_t cur = root, prev_e = kNone, i = 0;
+        do {
+            o.vtx[base + i++] = cur + in.nv;
+            const uint32_t b = cp.ivtx_off[cur];
+            const uint32_t e0 = cp.ivtx_he[b] >> 1, e1 = cp.ivtx_he[b + 1] >> 1;
+            const uint32_t e = e0 == prev_e ? e1 : e0;
+            prev_e = e;
+            const uint32_t a = cp.edges[2 * (size_t)e] - in.nv, c = cp.edges[2 * (size_t)e + 1] - in.nv;
+            cur = a == cur ? c : a;
+        } while (cur != root && i < n);
+    }
+}
+
+__global__ void k_fp_count_init(uint32_t* __restrict__ fcounts)
+{
+    if (threadIdx.x < kFpCounts) fcounts[threadIdx.x] = 0u;
+}
+
+__global__ void k_fp_vertices(const uint32_t* __restrict__ off, uint32_t R, uint32_t* __restrict__ fcounts)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) fcounts[kFpVertices] = off[R];
+}
+
 int bits_for(uint64_t n) { return n ? 64 - __builtin_clzll(n) : 1; } // 2^bits > n
 
 int grid(uint64_t n) { return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + kCB - 1) / kCB, 152 * 8)); }
 
 } // namespace
+
+size_t floating_sort_temp_bytes(uint32_t nrec) { return radix_sort_temp_bytes(std::max<uint32_t>(nrec, 1)); }
+size_t floating_scan_temp_bytes(uint32_t nrec) { return scan_temp_bytes(std::max<uint32_t>(nrec, 1)); }
+
+void launch_floating(const CutpathInput& in, const CutpathOut& cp, FloatingScratch& w, FloatingOut& o,
+    cudaStream_t s)
+{
+    const uint32_t R = in.nrec;
+    g_launches++;
+    k_fp_count_init<<<1, 32, 0, s>>>(o.counts);
+    if (R == 0) {
+        cudaMemsetAsync(o.off, 0, 4, s);
+        return;
+    }
+    const int rbits = bits_for(R), fbits = bits_for(in.nf);
+    const unsigned long long none = sentinel(rbits + fbits);
+    g_launches += 4;
+    k_fp_init<<<grid(R), kCB, 0, s>>>(R, w, none);
+    k_fp_union<<<grid(R), kCB, 0, s>>>(cp.edges, cp.counts, in.nv, w.parent, o.counts);
+    k_fp_flags<<<grid(R), kCB, 0, s>>>(in, cp.ivtx_off, w);
+    k_fp_roots<<<grid(R), kCB, 0, s>>>(in, cp.ivtx_off, w, rbits, o.counts);
+    const int b = radix_sort_pairs<unsigned long long>(w.k[0], w.v[0], w.k[1], w.v[1], R, 0, rbits + fbits,
+        w.sort_temp, s);
+    g_launches += 3;
+    k_fp_sizes<<<grid(R), kCB, 0, s>>>(w.k[b], w.v[b], R, none, w.size, o.off);
+    exclusive_scan(o.off, R, o.off + R, w.scan_temp, s);
+    k_fp_walk<<<grid(R), kCB, 0, s>>>(in, cp, w.k[b], w.v[b], none, rbits, o, w.size);
+    k_fp_vertices<<<1, 32, 0, s>>>(o.off, R, o.counts);
+}
 
 size_t cutpath_sort_temp_bytes(uint32_t n_candidates)
 {

@@ -64,6 +64,33 @@ struct CutpathOut {
     uint32_t* counts; // [kCpCounts]
 };
 
+// Floating polygons (kernel.cpp:4078-4200) from the cut path: a circular
+// cut path (every vertex on two of its edges, none on a soup border edge)
+// whose vertices all pierce the same face. Scratch and outputs for R
+// intersection vertices.
+enum { kFpPolygons = 0, kFpVertices = 1, kFpError = 2, kFpCounts = 4 };
+struct FloatingScratch {
+    uint32_t* parent;          // [R]
+    uint32_t* flags;           // [R]
+    uint32_t* size;            // [R]
+    unsigned long long* k[2];  // [R] (face, root) keys
+    uint32_t* v[2];            // [R]
+    uint32_t* sort_temp;
+    uint32_t* scan_temp;
+};
+struct FloatingOut {
+    uint32_t* faces;   // [R] each polygon's ps face (polygons by face, then smallest vertex)
+    uint32_t* off;     // [R + 1]
+    uint32_t* vtx;     // [R] m0 ids, each polygon from its smallest, first towards its lowest edge's other end
+    double* normals;   // [3R] the face's unit normal (compute_polygon_plane_coefficients)
+    int32_t* mc;       // [R] its largest component
+    uint32_t* counts;  // [kFpCounts]
+};
+size_t floating_sort_temp_bytes(uint32_t nrec);
+size_t floating_scan_temp_bytes(uint32_t nrec);
+void launch_floating(const CutpathInput& in, const CutpathOut& cp, FloatingScratch& w, FloatingOut& o,
+    cudaStream_t s);
+
 size_t cutpath_sort_temp_bytes(uint32_t n_candidates);
 size_t cutpath_scan_temp_bytes(uint32_t n_candidates);
 

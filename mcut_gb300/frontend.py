@@ -142,6 +142,15 @@ class Context:
                     ivtx_off=g(L.DATA_CUTPATH_VERTEX_OFFSETS).reshape(-1),
                     ivtx_he=g(L.DATA_CUTPATH_VERTEX_HALFEDGES).reshape(-1))
 
+    def floating_polygons(self) -> dict:
+        """The floating polygons of the last (single) dispatch (kernel.cpp:
+        4078-4200), from its cut path on the device: faces, off, vtx (m0 ids
+        around each polygon from its smallest), normals [P,3], mc."""
+        g = lambda q, dt=np.uint32, cols=1: self._get(q, dt, cols)  # noqa: E731
+        return dict(faces=g(L.DATA_FLOATING_FACES).reshape(-1), off=g(L.DATA_FLOATING_OFFSETS).reshape(-1),
+                    vtx=g(L.DATA_FLOATING_VERTICES).reshape(-1), normals=g(L.DATA_FLOATING_NORMALS, np.float64, 3),
+                    mc=g(L.DATA_FLOATING_NORMAL_COMPONENTS, np.int32).reshape(-1))
+
     def halfedge_mesh(self, mesh, device: bool = False, fetch: bool = True) -> dict:
         """MCUT's halfedge mesh of one mesh and its input checks on the device
         (mcgpu_halfedge_mesh). mesh: dict(f=indices, fs=sizes or None,

@@ -471,3 +471,108 @@ void oracle_cutpath_free(cp_result *r)
     free(r->ivtx_off); free(r->ivtx_he);
     memset(r, 0, sizeof *r);
 }
+
+/* ---- floating polygons (kernel.cpp:4078-4200) ----
+ * The cut path's connected components (through its edges); a component is a
+ * circular cut path when every vertex has two edges and none lies on a ps
+ * border edge (m0_cutpath_terminal_vertices, kernel.cpp:3850-3870: a vertex
+ * whose tested edge is a border edge); it is a floating polygon when every
+ * vertex has the same tested face -- the polygon lies inside that face. Each
+ * polygon is listed from its smallest vertex id, first towards the other end
+ * of that vertex's lowest-numbered edge; polygons ordered by face, then by
+ * their smallest vertex. */
+static uint32_t fp_find(uint32_t *parent, uint32_t v)
+{
+    while (parent[v] != v) {
+        parent[v] = parent[parent[v]];
+        v = parent[v];
+    }
+    return v;
+}
+
+typedef struct { uint32_t face, root; } fp_key;
+static int fp_cmp(const void *x, const void *y)
+{
+    const fp_key *a = (const fp_key *)x, *b = (const fp_key *)y;
+    if (a->face != b->face) return a->face < b->face ? -1 : 1;
+    return a->root < b->root ? -1 : (a->root > b->root);
+}
+
+int oracle_floating(uint32_t nv, const double *x, const uint32_t *soup_off, const uint32_t *soup_idx, uint32_t n_ivtx,
+    const uint32_t *reg, uint32_t n_edges, const uint32_t *edges, fp_result *out)
+{
+    memset(out, 0, sizeof *out);
+    uint32_t *parent = (uint32_t *)malloc(sizeof(uint32_t) * (n_ivtx ? n_ivtx : 1));
+    uint32_t *deg = (uint32_t *)calloc(n_ivtx ? n_ivtx : 1, sizeof(uint32_t));
+    uint8_t *bad = (uint8_t *)calloc(n_ivtx ? n_ivtx : 1, 1);
+    /* incident edges per vertex, ascending (CSR) */
+    uint32_t *eoff = (uint32_t *)calloc((size_t)n_ivtx + 1, sizeof(uint32_t));
+    uint32_t *einc = (uint32_t *)malloc(sizeof(uint32_t) * (2 * (size_t)n_edges + 1));
+    for (uint32_t v = 0; v < n_ivtx; ++v) parent[v] = v;
+    for (uint32_t e = 0; e < n_edges; ++e)
+        for (int s = 0; s < 2; ++s) eoff[edges[2 * e + s] - nv + 1]++;
+    for (uint32_t v = 0; v < n_ivtx; ++v) eoff[v + 1] += eoff[v];
+    uint32_t *fill = (uint32_t *)malloc(sizeof(uint32_t) * (n_ivtx ? n_ivtx : 1));
+    memcpy(fill, eoff, sizeof(uint32_t) * n_ivtx);
+    for (uint32_t e = 0; e < n_edges; ++e) {
+        const uint32_t a = edges[2 * e] - nv, b = edges[2 * e + 1] - nv;
+        einc[fill[a]++] = e;
+        einc[fill[b]++] = e;
+        deg[a]++;
+        deg[b]++;
+        uint32_t ra = fp_find(parent, a), rb = fp_find(parent, b);
+        if (ra != rb) {
+            if (ra < rb) parent[rb] = ra; else parent[ra] = rb;
+        }
+    }
+    for (uint32_t v = 0; v < n_ivtx; ++v) {
+        if (!deg[v]) continue;
+        const uint32_t r = fp_find(parent, v);
+        if (deg[v] != 2 || reg[3 * v + 2] == UINT32_MAX || reg[3 * v] != reg[3 * r]) bad[r] = 1;
+    }
+    fp_key *keys = (fp_key *)malloc(sizeof(fp_key) * (n_ivtx ? n_ivtx : 1));
+    uint32_t np = 0;
+    for (uint32_t v = 0; v < n_ivtx; ++v)
+        if (deg[v] && fp_find(parent, v) == v && !bad[v]) keys[np++] = (fp_key) { reg[3 * v], v };
+    qsort(keys, np, sizeof(fp_key), fp_cmp);
+    out->n_polygons = np;
+    out->faces = (uint32_t *)malloc(sizeof(uint32_t) * (np ? np : 1));
+    out->off = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)np + 1));
+    out->vtx = (uint32_t *)malloc(sizeof(uint32_t) * (n_ivtx ? n_ivtx : 1));
+    out->normals = (double *)calloc(3 * (size_t)(np ? np : 1), sizeof(double));
+    out->mc = (int32_t *)malloc(sizeof(int32_t) * (np ? np : 1));
+    uint32_t nvtx = 0;
+    for (uint32_t p = 0; p < np; ++p) {
+        out->faces[p] = keys[p].face;
+        /* the face's plane (ps_tested_face_to_plane_normal / _max_comp) */
+        cp_plane pl;
+        const uint32_t f = keys[p].face;
+        if (x && cp_face_plane(x, soup_idx + soup_off[f], (int)(soup_off[f + 1] - soup_off[f]), &pl) == 0) {
+            memcpy(out->normals + 3 * (size_t)p, pl.n, sizeof pl.n);
+            out->mc[p] = pl.mc;
+        } else {
+            out->mc[p] = -1;
+        }
+        out->off[p] = nvtx;
+        const uint32_t start = keys[p].root;
+        uint32_t cur = start, prev_e = UINT32_MAX;
+        do {
+            out->vtx[nvtx++] = cur + nv;
+            /* the incident edge other than the one arrived by (the lowest first) */
+            uint32_t e = einc[eoff[cur]];
+            if (e == prev_e) e = einc[eoff[cur] + 1];
+            const uint32_t a = edges[2 * e] - nv, b = edges[2 * e + 1] - nv;
+            prev_e = e;
+            cur = a == cur ? b : a;
+        } while (cur != start && nvtx < n_ivtx);
+    }
+    out->off[np] = nvtx;
+    free(parent); free(deg); free(bad); free(eoff); free(einc); free(fill); free(keys);
+    return 0;
+}
+
+void oracle_floating_free(fp_result *r)
+{
+    free(r->faces); free(r->off); free(r->vtx); free(r->normals); free(r->mc);
+    memset(r, 0, sizeof *r);
+}

@@ -11,7 +11,8 @@ kernel.cpp:2415-3206) runs only when no seam hook is installed; with a hook
 continues with its own host stages (cut-path edges, clipping, connected
 components) exactly as the reference wrote them. After the cut-path edges
 are made (kernel.cpp:3332-3632) an observer, when installed, sees them with
-their maps. The edit is anchored on source text, not line numbers, and fails
+their maps, and another sees the floating polygons detected
+(kernel.cpp:4078-4200). The edit is anchored on source text, not line numbers, and fails
 loudly if an anchor is missing.
 """
 from __future__ import annotations
@@ -29,6 +30,8 @@ mcut_seam_observer_fn g_mcut_seam_observer = nullptr;
 extern "C" void mcut_seam_observe(mcut_seam_observer_fn fn) { g_mcut_seam_observer = fn; }
 mcut_seam_cutpath_fn g_mcut_seam_cutpath_observer = nullptr;
 extern "C" void mcut_seam_observe_cutpath(mcut_seam_cutpath_fn fn) { g_mcut_seam_cutpath_observer = fn; }
+mcut_seam_floating_fn g_mcut_seam_floating_observer = nullptr;
+extern "C" void mcut_seam_observe_floating(mcut_seam_floating_fn fn) { g_mcut_seam_floating_observer = fn; }
 // ---- end seam hook ----
 
 """
@@ -66,20 +69,27 @@ HOOK_CUTPATH = """    // ---- seam cut-path observer (inserted by oracle/make_se
             m0_cutpath_edges, ps_iface_to_m0_edge_list, ivtx_to_incoming_hlist);
 """
 
+HOOK_FLOATING = """    // ---- seam floating-polygon observer (inserted by oracle/make_seam.py)
+    if (g_mcut_seam_floating_observer != nullptr)
+        g_mcut_seam_floating_observer(output.detected_floating_polygons);
+"""
+
 ANCHOR_DISPATCH = "\nvoid dispatch(output_t& output, const input_t& input)\n"
 ANCHOR_PUSH = '    TIMESTACK_PUSH("Calculate intersection points (edge-to-face)");\n'
 ANCHOR_END = "#endif\n\n    // Create edges from the new intersection points\n"
 ANCHOR_CUTPATH = "    // NOTE: at this stage we have all vertices and edges which are needed to clip\n"
+ANCHOR_FLOATING = "    if (!output.detected_floating_polygons.empty()) {\n"
 
 
 def patch_kernel(text: str) -> str:
-    for a in (ANCHOR_DISPATCH, ANCHOR_PUSH, ANCHOR_END, ANCHOR_CUTPATH):
+    for a in (ANCHOR_DISPATCH, ANCHOR_PUSH, ANCHOR_END, ANCHOR_CUTPATH, ANCHOR_FLOATING):
         if text.count(a) != 1:
             raise SystemExit(f"make_seam: anchor not found exactly once: {a.strip()[:60]!r}")
     text = text.replace(ANCHOR_DISPATCH, "\n" + HOOK_DECL + ANCHOR_DISPATCH.lstrip("\n"))
     text = text.replace(ANCHOR_PUSH, ANCHOR_PUSH + HOOK_CALL)
     text = text.replace(ANCHOR_END, "#endif\n" + HOOK_CLOSE + "\n    // Create edges from the new intersection points\n")
     text = text.replace(ANCHOR_CUTPATH, HOOK_CUTPATH + ANCHOR_CUTPATH)
+    text = text.replace(ANCHOR_FLOATING, HOOK_FLOATING + ANCHOR_FLOATING)
     return text
 
 

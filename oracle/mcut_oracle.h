@@ -156,6 +156,22 @@ int oracle_cutpath(uint32_t nv, const double *x, uint32_t nf, const uint32_t *so
     const uint32_t *key_off, const uint32_t *key_vtx, cp_result *out);
 void oracle_cutpath_free(cp_result *r);
 
+/* MCUT's floating-polygon detection (kernel.cpp:4078-4200) from the cut
+ * path: per intersection vertex (m0 id nv + i) its registry as above and the
+ * cut-path edges (first, second vertex). Polygons: their ps face ascending,
+ * each polygon's m0 vertex ids in cycle order from its smallest. */
+typedef struct fp_result {
+    uint32_t n_polygons;
+    uint32_t *faces;       /* [n_polygons] */
+    uint32_t *off;         /* [n_polygons + 1] */
+    uint32_t *vtx;
+    double *normals;       /* [3 n_polygons]: the face's unit normal (x given) */
+    int32_t *mc;           /* [n_polygons]: its largest component, -1 without x */
+} fp_result;
+int oracle_floating(uint32_t nv, const double *x, const uint32_t *soup_off, const uint32_t *soup_idx, uint32_t n_ivtx,
+    const uint32_t *reg, uint32_t n_edges, const uint32_t *edges, fp_result *out);
+void oracle_floating_free(fp_result *r);
+
 #ifdef __cplusplus
 }
 #endif

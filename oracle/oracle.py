@@ -582,3 +582,65 @@ def observe_cutpath(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, help
                         want=dict(edges=edges.reshape(-1, 2), face_keys=face_keys, face_off=face_off,
                                   face_edges=face_edges, ivtx_off=ivtx_off, ivtx_he=ivtx_he)))
     return res["result"], obs
+
+
+class FpResult(C.Structure):
+    _fields_ = [("n_polygons", C.c_uint32), ("faces", C.POINTER(C.c_uint32)), ("off", C.POINTER(C.c_uint32)),
+                ("vtx", C.POINTER(C.c_uint32)), ("normals", C.POINTER(C.c_double)), ("mc", C.POINTER(C.c_int32))]
+
+
+def floating(nv, registry, edges, x=None, soup=None):
+    """MCUT's floating-polygon detection (kernel.cpp:4078-4200,
+    oracle_floating) from the cut path: -> dict(faces, off, vtx, normals, mc)
+    with each polygon's m0 vertex ids in cycle order from its smallest; with
+    the ps coordinates x and the soup's (offsets, indices) each face's unit
+    normal and largest component."""
+    lib, _, _ = _lib("port")
+    if not hasattr(lib, "_floating_ready"):
+        lib.oracle_floating.restype = C.c_int
+        lib.oracle_floating.argtypes = [C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                        C.c_uint32, C.c_void_p, C.POINTER(FpResult)]
+        lib.oracle_floating_free.argtypes = [C.POINTER(FpResult)]
+        lib._floating_ready = True
+    reg = np.ascontiguousarray(np.asarray(registry, np.uint32).reshape(-1, 3))
+    e = np.ascontiguousarray(np.asarray(edges, np.uint32).reshape(-1, 2))
+    keep = []
+    if x is not None:
+        keep = [np.ascontiguousarray(x, np.float64).reshape(-1), np.ascontiguousarray(soup[0], np.uint32),
+                np.ascontiguousarray(soup[1], np.uint32)]
+    res = FpResult()
+    lib.oracle_floating(int(nv), *([k.ctypes.data for k in keep] if keep else [None, None, None]), len(reg),
+                        reg.ctypes.data if reg.size else None, len(e), e.ctypes.data if e.size else None,
+                        C.byref(res))
+    n = int(res.n_polygons)
+    out = dict(faces=_arr(res.faces, n, np.uint32), off=_arr(res.off, n + 1, np.uint32),
+               normals=_arr(res.normals, 3 * n, np.float64).reshape(-1, 3), mc=_arr(res.mc, n, np.int32))
+    out["vtx"] = _arr(res.vtx, int(out["off"][-1]) if n else 0, np.uint32)
+    lib.oracle_floating_free(C.byref(res))
+    return out
+
+
+def observe_floating(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: int = 0):
+    """The unmodified reference's mcDispatch with its cut path and its
+    floating-polygon detection observed, per front-end pass that reached the
+    detection: (result, cut-path observations, [dict(faces, off, mc, normals
+    [P,3], xyz [V,3])]). A pass's floating observation follows its cut-path
+    observation."""
+    result, cps = observe_cutpath(src, cut, flags=flags, helpers=helpers)
+    lib = _seam_lib()
+    if not hasattr(lib, "_floating_obs"):
+        lib.seam_floating_count.restype = C.c_int
+        lib.seam_floating_observation.restype = C.c_int
+        lib.seam_floating_observation.argtypes = [C.c_int, C.c_void_p] + [C.c_void_p] * 5
+        lib._floating_obs = True
+    obs = []
+    for k in range(lib.seam_floating_count()):
+        sz = np.zeros(2, np.uint64)
+        lib.seam_floating_observation(k, sz.ctypes.data, None, None, None, None, None)
+        p, v = int(sz[0]), int(sz[1])
+        faces, off, mc = np.zeros(p, np.uint32), np.zeros(p + 1, np.uint32), np.zeros(p, np.uint32)
+        normals, xyz = np.zeros((p, 3)), np.zeros((v, 3))
+        lib.seam_floating_observation(k, sz.ctypes.data, faces.ctypes.data, off.ctypes.data, mc.ctypes.data,
+                                      normals.ctypes.data, xyz.ctypes.data)
+        obs.append(dict(faces=faces, off=off, mc=mc, normals=normals, xyz=xyz))
+    return result, cps, obs

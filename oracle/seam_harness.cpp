@@ -393,7 +393,47 @@ void cutpath_observer(const hmesh_t& ps, const hmesh_t& m0, const std::vector<st
             if ((uint32_t)kv.first < nv || (uint32_t)kv.first >= nv + registry.size()) o.bad = 1;
 }
 
+// The floating polygons each pass detected: per polygon its ps face, normal,
+// largest normal component and vertex coordinates in the reference's order.
+struct FloatingObs {
+    std::vector<uint32_t> faces, off, mc;
+    std::vector<double> normals, xyz;
+};
+std::vector<FloatingObs> g_floating;
+void floating_observer(const std::map<fd_t, std::vector<floating_polygon_info_t>>& polygons)
+{
+    g_floating.emplace_back();
+    FloatingObs& o = g_floating.back();
+    o.off.push_back(0);
+    for (const auto& kv : polygons)
+        for (const floating_polygon_info_t& p : kv.second) {
+            o.faces.push_back((uint32_t)kv.first);
+            o.mc.push_back((uint32_t)p.polygon_normal_largest_component);
+            o.normals.insert(o.normals.end(), { p.polygon_normal.x(), p.polygon_normal.y(), p.polygon_normal.z() });
+            for (const vec3& v : p.polygon_vertices) o.xyz.insert(o.xyz.end(), { v.x(), v.y(), v.z() });
+            o.off.push_back((uint32_t)(o.xyz.size() / 3));
+        }
+}
+
 } // namespace
+
+extern "C" int seam_floating_count() { return (int)g_floating.size(); }
+
+// Floating observation k: sizes[2] = polygons, vertices; then (non-null) the arrays.
+extern "C" int seam_floating_observation(int k, uint64_t* sizes, uint32_t* faces, uint32_t* off, uint32_t* mc,
+    double* normals, double* xyz)
+{
+    if (k < 0 || k >= (int)g_floating.size()) return -1;
+    const FloatingObs& o = g_floating[k];
+    sizes[0] = o.faces.size();
+    sizes[1] = o.xyz.size() / 3;
+    if (faces && !o.faces.empty()) memcpy(faces, o.faces.data(), o.faces.size() * 4);
+    if (off) memcpy(off, o.off.data(), o.off.size() * 4);
+    if (mc && !o.mc.empty()) memcpy(mc, o.mc.data(), o.mc.size() * 4);
+    if (normals && !o.normals.empty()) memcpy(normals, o.normals.data(), o.normals.size() * 8);
+    if (xyz && !o.xyz.empty()) memcpy(xyz, o.xyz.data(), o.xyz.size() * 8);
+    return 0;
+}
 
 // The cut-path observations of the last seam_observe_reference call: how many.
 extern "C" int seam_cutpath_count() { return (int)g_cutpath.size(); }
@@ -432,9 +472,11 @@ extern "C" int seam_observe_reference(const void* sv, const uint32_t* sf, const 
     g_calls = 0;
     g_observed.clear();
     g_cutpath.clear();
+    g_floating.clear();
     mcut_seam_install(nullptr);
     mcut_seam_observe(&observer);
     mcut_seam_observe_cutpath(&cutpath_observer);
+    mcut_seam_observe_floating(&floating_observer);
     char cwd[4096];
     if (!getcwd(cwd, sizeof cwd)) return -1000;
     if (workdir && chdir(workdir) != 0) return -1001;
@@ -445,6 +487,7 @@ extern "C" int seam_observe_reference(const void* sv, const uint32_t* sf, const 
     if (ctx != MC_NULL_HANDLE) mcReleaseContext(ctx);
     mcut_seam_observe(nullptr);
     mcut_seam_observe_cutpath(nullptr);
+    mcut_seam_observe_floating(nullptr);
     if (workdir && chdir(cwd) != 0) return -1002;
     *n = (int64_t)(g_observed.size() / 3);
     for (int64_t i = 0; i < *n && i < cap; ++i) {

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "mcut/internal/hmesh.h"
+#include "mcut/internal/kernel.h"
 #include "mcut/internal/utils.h"
 
 typedef bool (*mcut_seam_front_end_fn)(const hmesh_t& ps, int sm_vtx_cnt, int sm_face_count, hmesh_t& m0,
@@ -53,3 +54,9 @@ typedef void (*mcut_seam_cutpath_fn)(const hmesh_t& ps, const hmesh_t& m0,
     const std::unordered_map<vd_t, std::vector<hd_t>>& ivtx_to_incoming_hlist);
 extern mcut_seam_cutpath_fn g_mcut_seam_cutpath_observer;
 extern "C" void mcut_seam_observe_cutpath(mcut_seam_cutpath_fn fn);
+
+// Observer of the floating-polygon detection (kernel.cpp:4078-4200): the
+// detected polygons per ps face, before dispatch() stops on them.
+typedef void (*mcut_seam_floating_fn)(const std::map<fd_t, std::vector<floating_polygon_info_t>>& polygons);
+extern mcut_seam_floating_fn g_mcut_seam_floating_observer;
+extern "C" void mcut_seam_observe_floating(mcut_seam_floating_fn fn);
