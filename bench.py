@@ -50,7 +50,7 @@ UNIT = "pairs/s"
 BYTES = {
     "bounds": ("face", 116),       # read idx 12 + positions ~12 (twice: mesh boxes, face boxes), write
                                    # fp64 box 48 + fp32 box 24 + key 4 + id 4
-    "sort": ("face", 68),          # 4 passes x (8 read + 8 write) + histogram
+    "sort": ("face", 52),          # 3 passes x (8 read + 8 write) + histogram
     "hierarchy": ("node", 184),    # node write 64 + the leaf cluster's 4 face ids and fp32 boxes 112 + keys 8
     "traverse": ("pair-of-trees", None),
     "adjacency": ("face", 40),     # incidence count + fill over indices, planes of candidates

@@ -242,7 +242,7 @@ __global__ void k_mesh_frames(const unsigned long long* __restrict__ mesh_box, u
 // Face boxes (bvh.cpp:242-314, cut boxes enlarged as preproc.cpp:2693) and
 // each face's Morton key (bvh.cpp:370-433). The code only orders leaves --
 // any order gives the same pair set -- so it is formed in fp32 from the
-// outward-rounded box: centre relative to the mesh frame, 10 bits per axis;
+// outward-rounded box: centre relative to the mesh frame, 8, 8 and 7 bits;
 // the mesh bit above the key puts every source key before every cut key so
 // one sort orders both meshes.
 template <typename K>
@@ -317,10 +317,12 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         const float c0 = (0.5f * (lo[0] + hi[0]) - fl.x) * fs.x;
         const float c1 = (0.5f * (lo[1] + hi[1]) - fl.y) * fs.y;
         const float c2 = (0.5f * (lo[2] + hi[2]) - fl.z) * fs.z;
-        const uint32_t m0 = expand_bits((uint32_t)fminf(fmaxf(c0, 0.0f), 1023.0f));
-        const uint32_t m1 = expand_bits((uint32_t)fminf(fmaxf(c1, 0.0f), 1023.0f));
-        const uint32_t m2 = expand_bits((uint32_t)fminf(fmaxf(c2, 0.0f), 1023.0f));
-        const K key = ((K)p << kMortonBits) | (K)(m0 * 4 + m1 * 2 + m2) | ((K)(is_cut ? 1 : 0) << mesh_bit);
+        constexpr float top = kMortonBits == 30 ? 1023.0f : 255.0f, scale = kMortonBits == 30 ? 1.0f : 0.25f;
+        const uint32_t m0 = expand_bits((uint32_t)fminf(fmaxf(c0 * scale, 0.0f), top));
+        const uint32_t m1 = expand_bits((uint32_t)fminf(fmaxf(c1 * scale, 0.0f), top));
+        const uint32_t m2 = expand_bits((uint32_t)fminf(fmaxf(c2 * scale, 0.0f), top));
+        const uint32_t mc = kMortonBits == 30 ? m0 * 4 + m1 * 2 + m2 : (m0 * 4 + m1 * 2 + m2) >> 1;
+        const K key = ((K)p << kMortonBits) | (K)mc | ((K)(is_cut ? 1 : 0) << mesh_bit);
         const uint32_t local = f - P.pair_fbase[p];
         if (is_cut) {
             const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);

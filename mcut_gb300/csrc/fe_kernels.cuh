@@ -12,7 +12,7 @@
 //   fbox       double[nf][6]      exact fp64 face boxes (cut boxes enlarged by eps)
 //   tree       Node[ncl-1]        LBVH over leaf clusters of `leaf_size` consecutive
 //                                 cut faces (Morton order, never across pairs),
-//                                 key = pair << 30 | Morton
+//                                 key = pair << 23 | Morton
 //   pairs      uint64[P]          (source face << 32 | cut face), global ids
 //   tests      Test[T]            culled edge-face tests
 //   records    Record[R]          intersection records, sorted by (edge, face)
@@ -24,7 +24,14 @@ namespace mcgpu {
 
 constexpr uint32_t kCutBit = 0x80000000u;
 constexpr int32_t kNoBad = 0x7F7F7F7F; // pair_bad when no face is degenerate (memset 0x7F)
-constexpr int kMortonBits = 30;
+// Morton code width: 23 (8, 8 and 7 bits per axis), which with the mesh bit
+// keeps one pair's keys within three 8-bit radix passes, or 30 (10 per axis,
+// four passes; the tree over 2 M faces is no better for the extra bits)
+#ifndef MCGPU_MORTON_BITS
+#define MCGPU_MORTON_BITS 23
+#endif
+constexpr int kMortonBits = MCGPU_MORTON_BITS;
+static_assert(kMortonBits == 30 || kMortonBits == 23, "Morton width");
 
 struct __align__(16) Node {
     float4 b0;            // left  lo.x lo.y lo.z hi.x
