@@ -358,8 +358,11 @@ int mcgpu_halfedge_mesh(mcgpu_context ctx, uint32_t flags, const mcgpu_mesh* mes
  * (double) and are recentred as mcDispatch does; like mcEnqueueDispatch,
  * the caller's arrays must stay valid until the request completes
  * (frontend.cpp:690-711). Cut meshes added with mcgpu_server_add_cut_mesh
- * stay resident on the device: a request naming one uploads only its
- * source mesh. Device memory: the resident meshes plus what every worker
+ * stay resident on the device with their own tree (built once there, over
+ * the user coordinates): a request naming one uploads only its source mesh,
+ * and its source faces walk that tree instead of the cut faces joining the
+ * batch's sort and tree. Device memory: the resident meshes (coordinates,
+ * indices and tree; the build's scratch while it runs) plus what every worker
  * may hold -- its pool while idle, its batch's cap while it runs one --
  * stay within hbm_budget_bytes. A batch's cap is its requests' estimated
  * bytes with slack; its context cannot grow past it

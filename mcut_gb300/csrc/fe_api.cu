@@ -106,7 +106,7 @@ enum BufId {
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
-    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB,
+    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB, B_RESP,
     // the cut path (built at the first query for it)
     B_CP_CAND, B_CP_INSIDE, B_CP_SORTED, B_CP_PROJ, B_CP_PK0, B_CP_PK1, B_CP_PV0, B_CP_PV1, B_CP_MADE, B_CP_FK0,
     B_CP_FK1, B_CP_FV0, B_CP_FV1, B_CP_HK0, B_CP_HK1, B_CP_HV0, B_CP_HV1, B_CP_FLAGS, B_CP_SORT, B_CP_SCAN, B_CP_OUT,
@@ -127,6 +127,7 @@ struct Layout {
     bool all_tri = true;
     uint64_t tri_stride = 0, n_poly = 0;
     uint32_t max_face = 3;
+    uint32_t res_trees = 0; // pairs whose cut tree is resident
 };
 
 } // namespace
@@ -140,7 +141,7 @@ struct mcgpu_context_t {
     DevBuf buf[B_COUNT];
     uint64_t dev_held = 0;   // bytes the pool holds (every buf)
     uint64_t dev_limit = 0;  // 0: no cap (mcgpu_context_set_memory_limit)
-    PinBuf pin_counters, pin_tab, pin_stage, pin_idx, pin_seg, pin_frames, pin_eps;
+    PinBuf pin_counters, pin_tab, pin_stage, pin_idx, pin_seg, pin_frames, pin_eps, pin_res;
     bool eps_on_device = false; // the last upload's cut-box enlargements come from the device (pin_eps)
     Layout L;
     mcgpu::Problem P {};
@@ -655,7 +656,7 @@ int grid1(uint64_t n)
 uint32_t face_size(const mcgpu_mesh& m, uint32_t f) { return m.face_sizes ? m.face_sizes[f] : 3u; }
 
 int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, const mcgpu_mesh* cuts,
-    const double* eps)
+    const double* eps, const ResidentCut* const* res)
 {
     Layout& L = c->L;
     L = Layout();
@@ -677,7 +678,10 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
         L.fbase[p] = (uint32_t)f; L.fs[p] = S.num_faces;
         L.sbase[p] = (uint32_t)sf; L.cbase[p] = (uint32_t)cf; L.ibase[p] = (uint32_t)ix;
         L.clbase[p] = (uint32_t)cl;
-        cl += (C.num_faces + L.leaf_size - 1) / L.leaf_size;
+        // a resident cut tree keeps the pair's cut faces out of the sorted list and the batch tree
+        const bool own_tree = res && res[p] && res[p]->tree_ncl > 0;
+        if (!own_tree) cl += (C.num_faces + L.leaf_size - 1) / L.leaf_size;
+        L.res_trees += own_tree ? 1 : 0;
         uint64_t is = 0, ic = 0;
         for (int side = 0; side < 2; ++side) {
             const mcgpu_mesh& m = side ? C : S;
@@ -701,7 +705,7 @@ int build_layout(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mes
         v += (uint64_t)S.num_vertices + C.num_vertices;
         f += (uint64_t)S.num_faces + C.num_faces;
         sf += S.num_faces;
-        cf += C.num_faces;
+        if (!own_tree) cf += C.num_faces;
         ix += is + ic;
         if (eps && !(flags & MCGPU_RECENTRE)) L.eps[p] = eps[p];
     }
@@ -844,6 +848,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
         uint32_t* ist = dev ? nullptr : c->pin_idx.get<uint32_t>(L.nidx);
         struct Job { double com[3], t[3]; };
         std::vector<Job> jobs(res ? n : 0);
+        // resident cut trees: the frames of their pairs, for the tree walk
+        double* hfr = L.res_trees ? c->pin_frames.get<double>(6 * (size_t)n) : nullptr;
         parallel_pairs(n, L.nv + L.nidx, [&](uint32_t p) {
             double* sx = st + (size_t)L.vbase[p] * 3;
             if (res && res[p]) {
@@ -853,6 +859,8 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
                 mesh_stats(srcs[p].vertices, fin, srcs[p].num_vertices, ss);
                 pair_frame(ss, res[p]->st, j.com, j.t);
                 apply_frame(fin, srcs[p], j.com, j.t, sx);
+                if (hfr)
+                    for (int k = 0; k < 3; ++k) { hfr[6 * (size_t)p + k] = j.com[k]; hfr[6 * (size_t)p + 3 + k] = j.t[k]; }
                 L.eps[p] = frame_eps(res[p]->st, j.t, c->gp_constant, gp_absolute);
             } else if (n == 1 && L.nv > 200000) {
                 const unsigned hw = std::max(2u, std::min(16u, std::thread::hardware_concurrency()));
@@ -996,6 +1004,36 @@ void upload(mcgpu_context_t* c, uint32_t flags, const mcgpu_mesh* srcs, const mc
     P.all_triangles = L.all_tri ? 1 : 0;
     P.leaf_size = L.leaf_size;
     P.ncl = (uint32_t)L.ncl;
+    P.res_pairs = nullptr;
+    P.pair_frames = nullptr;
+    if (L.res_trees) {
+        // each pair's resident tree (ncl 0 for the others) and frame
+        ResPair* hr = c->pin_res.get<ResPair>(n);
+        for (uint32_t p = 0; p < n; ++p) {
+            ResPair r {};
+            const ResidentCut* q = res[p];
+            if (q && q->tree_ncl) {
+                r.nodes = static_cast<const Node*>(q->tree_nodes);
+                r.leaf_face = q->tree_leaf_face;
+                r.cl_start = q->tree_cl_start;
+                r.cl_n = q->tree_cl_n;
+                r.ncl = q->tree_ncl;
+                for (int j = 0; j < 3; ++j) r.mag[j] = std::max(std::fabs(q->st.mn[j]), std::fabs(q->st.mx[j]));
+            }
+            hr[p] = r;
+        }
+        ResPair* dr = c->buf[B_RESP].get<ResPair>(n);
+        ck(cudaMemcpyAsync(dr, hr, sizeof(ResPair) * n, cudaMemcpyHostToDevice, s), "H2D resident trees");
+        P.res_pairs = dr;
+        if (gathered) {
+            P.pair_frames = c->W.frames;
+        } else {
+            double* df = c->buf[B_FRAMES].get<double>(6 * (size_t)n);
+            ck(cudaMemcpyAsync(df, c->pin_frames.get<double>(6 * (size_t)n), sizeof(double) * 6 * n,
+                   cudaMemcpyHostToDevice, s), "H2D frames");
+            P.pair_frames = df;
+        }
+    }
     // the bounds kernel's input view: one pair's raw indices, cut ones
     // offset by the source vertex count on the fly
     Problem& Pin = c->Pin;
@@ -1094,7 +1132,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     c->floating_ready = false;
     c->have_results = false;
     const unsigned long long launches0 = g_launches;
-    int rc = build_layout(c, flags, n, srcs, cuts, eps);
+    int rc = build_layout(c, flags, n, srcs, cuts, eps, res);
     if (rc != MCGPU_OK) return rc;
     Layout& L = c->L;
     cudaStream_t s = c->s;
@@ -1789,6 +1827,7 @@ int mcgpu_context_release(mcgpu_context c)
     c->pin_counters.release();
     c->pin_tab.release();
     c->pin_stage.release();
+    c->pin_res.release();
     c->pin_idx.release();
     c->pin_seg.release();
     c->pin_frames.release();

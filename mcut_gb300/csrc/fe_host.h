@@ -29,6 +29,13 @@ struct ResidentCut {
     const uint32_t* idx;
     uint32_t nv, nf;
     MeshStats st;
+    // its own tree over the user coordinates (tree_ncl == 0: none; the pair's
+    // cut faces then join the batch's tree)
+    const void* tree_nodes;
+    const uint32_t* tree_leaf_face;
+    const uint32_t* tree_cl_start;
+    const uint8_t* tree_cl_n;
+    uint32_t tree_ncl;
 };
 
 // mcgpu_dispatch_batch over host meshes with MCGPU_RECENTRE, where a non-null

@@ -239,6 +239,17 @@ __global__ void k_mesh_frames(const unsigned long long* __restrict__ mesh_box, u
     }
 }
 
+// Morton code of a box centre already in frame units (0 .. 1023 across the
+// mesh box): 8, 8 and 7 bits per axis (or 10 each with 30-bit codes)
+__device__ __forceinline__ uint32_t morton_code(float c0, float c1, float c2)
+{
+    constexpr float top = kMortonBits == 30 ? 1023.0f : 255.0f, scale = kMortonBits == 30 ? 1.0f : 0.25f;
+    const uint32_t m0 = expand_bits((uint32_t)fminf(fmaxf(c0 * scale, 0.0f), top));
+    const uint32_t m1 = expand_bits((uint32_t)fminf(fmaxf(c1 * scale, 0.0f), top));
+    const uint32_t m2 = expand_bits((uint32_t)fminf(fmaxf(c2 * scale, 0.0f), top));
+    return kMortonBits == 30 ? m0 * 4 + m1 * 2 + m2 : (m0 * 4 + m1 * 2 + m2) >> 1;
+}
+
 // Face boxes (bvh.cpp:242-314, cut boxes enlarged as preproc.cpp:2693) and
 // each face's Morton key (bvh.cpp:370-433). The code only orders leaves --
 // any order gives the same pair set -- so it is formed in fp32 from the
@@ -317,17 +328,15 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         const float c0 = (0.5f * (lo[0] + hi[0]) - fl.x) * fs.x;
         const float c1 = (0.5f * (lo[1] + hi[1]) - fl.y) * fs.y;
         const float c2 = (0.5f * (lo[2] + hi[2]) - fl.z) * fs.z;
-        constexpr float top = kMortonBits == 30 ? 1023.0f : 255.0f, scale = kMortonBits == 30 ? 1.0f : 0.25f;
-        const uint32_t m0 = expand_bits((uint32_t)fminf(fmaxf(c0 * scale, 0.0f), top));
-        const uint32_t m1 = expand_bits((uint32_t)fminf(fmaxf(c1 * scale, 0.0f), top));
-        const uint32_t m2 = expand_bits((uint32_t)fminf(fmaxf(c2 * scale, 0.0f), top));
-        const uint32_t mc = kMortonBits == 30 ? m0 * 4 + m1 * 2 + m2 : (m0 * 4 + m1 * 2 + m2) >> 1;
-        const K key = ((K)p << kMortonBits) | (K)mc | ((K)(is_cut ? 1 : 0) << mesh_bit);
+        const K key = ((K)p << kMortonBits) | (K)morton_code(c0, c1, c2) | ((K)(is_cut ? 1 : 0) << mesh_bit);
         const uint32_t local = f - P.pair_fbase[p];
         if (is_cut) {
-            const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);
-            ckey[pos] = key;
-            cval[pos] = f;
+            // a resident cut tree's faces stay out of the batch's sort and tree
+            if (!P.res_pairs || P.res_pairs[p].ncl == 0) {
+                const uint32_t pos = P.pair_cbase[p] + (local - P.pair_fs[p]);
+                ckey[pos] = key;
+                cval[pos] = f;
+            }
         } else {
             const uint32_t pos = P.pair_sbase[p] + local;
             skey[pos] = key;
@@ -569,7 +578,7 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
     {
         const uint32_t s0 = cl_start[i], cn = cl_n[i];
         const uint32_t f0 = __ldg(&leaf_face[s0]);
-        fb.plo = fb.phi = P.face_pair[f0] & ~kCutBit;
+        fb.plo = fb.phi = face_pair_of(P, f0) & ~kCutBit;
         // four faces at a time, their loads in flight together
         for (uint32_t c0 = 0; c0 < cn; c0 += 4) {
             uint32_t lf[4];
@@ -1312,6 +1321,140 @@ __global__ void __launch_bounds__(kBlock) k_traverse(Problem P, const double* __
         }
         flush();
         if (any) cand[s] = 1;
+    }
+}
+
+// Source faces of pairs with a resident cut tree (ResPair) walk that tree,
+// one thread per face. The tree's boxes are in the mesh's user coordinates;
+// the pair's cut vertices are x' = (x - com) + t, so a cut face whose
+// enlarged pair-frame box meets the query box has a user box meeting the
+// query box shifted by com - t and widened by the cut-box enlargement and a
+// margin that covers the roundings of x' and of the shift (far below the
+// fp32 boxes' own outward rounding). At the leaves the faces are tested
+// exactly on their pair-frame fp64 boxes, as every other candidate, so the
+// pair set is the one the batch tree gives.
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_traverse_resident(Problem P, const double* __restrict__ fbox,
+    const uint32_t* __restrict__ qface, unsigned long long* __restrict__ pairs, uint64_t cap,
+    uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < P.ns; t += gridDim.x * blockDim.x) {
+        const uint32_t s = qface[t];
+        const uint32_t p = face_pair_of(P, s) & ~kCutBit;
+        const ResPair R = P.res_pairs[p];
+        if (R.ncl == 0) continue;
+        const Box qb = load_box(fbox, s);
+        const double* fr = P.pair_frames + 6 * (size_t)p;
+        const double eps = P.pair_eps[p];
+        float ql[3], qh[3];
+        long long qk[6];
+        for (int j = 0; j < 3; ++j) {
+            const double sh = fr[j] - fr[3 + j];
+            const double m = 0x1p-48 * (fabs(qb.mn[j]) + fabs(qb.mx[j]) + eps + 2.0 * (fabs(fr[j]) + fabs(fr[3 + j]))
+                + 2.0 * R.mag[j]);
+            ql[j] = f32_rd(((qb.mn[j] - eps) + sh) - m);
+            qh[j] = f32_ru(((qb.mx[j] + eps) + sh) + m);
+            qk[j] = dkey(qb.mn[j]);
+            qk[3 + j] = dkey(qb.mx[j]);
+        }
+        const uint32_t cbase = P.pair_fbase[p] + P.pair_fs[p]; // the pair's first cut face (ps id)
+        unsigned long long buf[8];
+        int nb = 0;
+        bool any = false;
+        auto flush = [&]() {
+            if (nb == 0) return;
+            const uint32_t pos = atomicAdd(&counters[0], (uint32_t)nb);
+            for (int k = 0; k < nb; ++k)
+                if ((uint64_t)pos + k < cap) pairs[pos + k] = buf[k];
+            nb = 0;
+        };
+        auto leaf = [&](int li) {
+            const uint32_t s0 = __ldg(&R.cl_start[li]), cn = __ldg(&R.cl_n[li]);
+            for (uint32_t u = 0; u < cn; ++u) {
+                const uint32_t cf = cbase + __ldg(&R.leaf_face[s0 + u]);
+                longlong2 a, b, c;
+                load_key_box(fbox, cf, a, b, c);
+                if (qk[0] <= b.y && qk[3] >= a.x && qk[1] <= c.x && qk[4] >= a.y && qk[2] <= c.y && qk[5] >= b.x) {
+                    buf[nb++] = ((unsigned long long)s << 32) | cf;
+                    cand[cf] = 1;
+                    any = true;
+                    if (nb == 8) flush();
+                }
+            }
+        };
+        if (R.ncl == 1) {
+            leaf(0);
+        } else {
+            int stack[STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            bool overflow = false;
+            while (sp > 0) {
+                const int nd = stack[--sp];
+                const float4 a = __ldg(&R.nodes[nd].b0), b = __ldg(&R.nodes[nd].b1), c = __ldg(&R.nodes[nd].b2);
+                const int2 ch = __ldg(reinterpret_cast<const int2*>(&R.nodes[nd].child[0]));
+                const bool hit0 = ql[0] <= a.w && qh[0] >= a.x && ql[1] <= b.x && qh[1] >= a.y && ql[2] <= b.y
+                    && qh[2] >= a.z;
+                const bool hit1 = ql[0] <= c.y && qh[0] >= b.z && ql[1] <= c.z && qh[1] >= b.w && ql[2] <= c.w
+                    && qh[2] >= c.x;
+                if (hit0) {
+                    if (ch.x < 0) leaf(~ch.x);
+                    else if (sp < STACK) stack[sp++] = ch.x;
+                    else overflow = true;
+                }
+                if (hit1) {
+                    if (ch.y < 0) leaf(~ch.y);
+                    else if (sp < STACK) stack[sp++] = ch.y;
+                    else overflow = true;
+                }
+            }
+            if (overflow) atomicOr(&pair_status[p], ST_STACK);
+        }
+        flush();
+        if (any) cand[s] = 1;
+    }
+}
+
+// A resident mesh's faces: fp32 boxes rounded outward from its fp64 user
+// coordinates and 23-bit Morton keys in the frame of its vertex bounds
+// mn / mx; thread 0 writes the one-pair tables the cluster pass reads.
+__global__ void __launch_bounds__(kBlock) k_res_faces(const double* __restrict__ X, const uint32_t* __restrict__ idx,
+    uint32_t nv, uint32_t nf, double mn0, double mn1, double mn2, double mx0, double mx1, double mx2,
+    float* __restrict__ fbox32, uint32_t* __restrict__ key, uint32_t* __restrict__ val, uint32_t* __restrict__ tab,
+    uint32_t ncl)
+{
+    const double mn[3] = { mn0, mn1, mn2 }, mx[3] = { mx0, mx1, mx2 };
+    float flo[3], fsc[3];
+    for (int j = 0; j < 3; ++j) {
+        flo[j] = f32_rd(mn[j]);
+        const float ext = f32_ru(mx[j]) - flo[j];
+        fsc[j] = ext > 0.0f ? __fdiv_rn(1023.0f, ext) : 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        tab[0] = 0; tab[1] = nf; // pair_cbase
+        tab[2] = 0; tab[3] = ncl; // pair_clbase
+    }
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        double lo[3] = { 1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308 };
+        double hi[3] = { -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308 };
+        for (int k = 0; k < 3; ++k) {
+            uint32_t v = idx[3 * (size_t)f + k];
+            if (v >= nv) v = 0;
+            for (int j = 0; j < 3; ++j) {
+                const double x = X[3 * (size_t)v + j];
+                lo[j] = fmin(lo[j], x);
+                hi[j] = fmax(hi[j], x);
+            }
+        }
+        float b[6];
+        for (int j = 0; j < 3; ++j) { b[j] = f32_rd(lo[j]); b[3 + j] = f32_ru(hi[j]); }
+        float2* d32 = reinterpret_cast<float2*>(fbox32 + (size_t)f * 6);
+        d32[0] = make_float2(b[0], b[1]);
+        d32[1] = make_float2(b[2], b[3]);
+        d32[2] = make_float2(b[4], b[5]);
+        key[f] = morton_code((0.5f * (b[0] + b[3]) - flo[0]) * fsc[0], (0.5f * (b[1] + b[4]) - flo[1]) * fsc[1],
+            (0.5f * (b[2] + b[5]) - flo[2]) * fsc[2]);
+        val[f] = f;
     }
 }
 
@@ -2262,7 +2405,7 @@ void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)
             W.packets, W.counters, (int)W.packet_faces);
 }
 
-void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
+static void launch_traverse_tree(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
 {
     // W.traversal: 0 (default) one warp per query packet (a compact source
     // subtree of <= W.packet_faces faces), breadth-first; 1 the same
@@ -2305,6 +2448,79 @@ void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool d
                 W.cand, W.pair_status, split, (uint32_t)W.split_cap, 0);
         }
     }
+}
+
+void launch_traverse(const Problem& P, Work& W, int src_buf, int cut_buf, bool deep, cudaStream_t s)
+{
+    // the batch tree (absent when every pair's cut tree is resident), then
+    // the resident trees
+    if (P.ncl > 0) launch_traverse_tree(P, W, src_buf, cut_buf, deep, s);
+    if (P.res_pairs) {
+        const int g = grid_for(P.ns);
+        g_launches++;
+        if (deep)
+            k_traverse_resident<512><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.pairs, W.pair_cap, W.counters,
+                W.cand, W.pair_status);
+        else
+            k_traverse_resident<64><<<g, kBlock, 0, s>>>(P, W.fbox, W.svals[src_buf], W.pairs, W.pair_cap, W.counters,
+                W.cand, W.pair_status);
+    }
+}
+
+ResTreeSizes resident_tree_sizes(uint32_t nf, uint32_t leaf_size)
+{
+    auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
+    ResTreeSizes z {};
+    z.ncl = ((uint64_t)nf + leaf_size - 1) / leaf_size;
+    const uint64_t nc2 = std::max<uint64_t>(z.ncl, 2);
+    z.nodes_bytes = (nc2 - 1) * sizeof(Node);
+    z.leaf_bytes = (uint64_t)nf * 4;
+    z.start_bytes = z.ncl * 4;
+    z.n_bytes = z.ncl;
+    // fp32 boxes, keys and values (double-buffered), sort scratch, cluster
+    // keys, the build's split records, the one-pair tables
+    z.scratch_bytes = al((uint64_t)nf * 24) + 4 * al((uint64_t)nf * 4) + al(radix_sort_temp_bytes(nf))
+        + al(z.ncl * 4) + al(nc2 * 4) + al(nc2 * 64) + al(16);
+    return z;
+}
+
+void build_resident_tree(const double* X, const uint32_t* idx, uint32_t nv, uint32_t nf, const double* mn,
+    const double* mx, uint32_t leaf_size, void* scratch, const ResTreeOut& out, cudaStream_t s)
+{
+    auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
+    const ResTreeSizes z = resident_tree_sizes(nf, leaf_size);
+    const uint64_t nc2 = std::max<uint64_t>(z.ncl, 2);
+    uint8_t* b = static_cast<uint8_t*>(scratch);
+    auto take = [&](uint64_t bytes) { uint8_t* r = b; b += al(bytes); return r; };
+    float* fbox32 = reinterpret_cast<float*>(take((uint64_t)nf * 24));
+    uint32_t* keys[2] = { reinterpret_cast<uint32_t*>(take((uint64_t)nf * 4)), reinterpret_cast<uint32_t*>(take((uint64_t)nf * 4)) };
+    uint32_t* vals[2] = { reinterpret_cast<uint32_t*>(take((uint64_t)nf * 4)), reinterpret_cast<uint32_t*>(take((uint64_t)nf * 4)) };
+    uint32_t* temp = reinterpret_cast<uint32_t*>(take(radix_sort_temp_bytes(nf)));
+    uint32_t* clkey = reinterpret_cast<uint32_t*>(take(z.ncl * 4));
+    uint32_t* split_far = reinterpret_cast<uint32_t*>(take(nc2 * 4));
+    void* split_box = take(nc2 * 64);
+    uint32_t* tab = reinterpret_cast<uint32_t*>(take(16));
+    g_launches++;
+    k_res_faces<<<grid_for(nf), kBlock, 0, s>>>(X, idx, nv, nf, mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], fbox32,
+        keys[0], vals[0], tab, (uint32_t)z.ncl);
+    const int buf = radix_sort_pairs<uint32_t>(keys[0], vals[0], keys[1], vals[1], nf, 0, kMortonBits, temp, s);
+    cudaMemcpyAsync(out.leaf_face, vals[buf], (size_t)nf * 4, cudaMemcpyDeviceToDevice, s);
+    Problem P1 {};
+    P1.n_pairs = 1;
+    P1.nf = nf;
+    P1.nc = nf;
+    P1.face_split = 0; // every face a cut face of pair 0
+    P1.pair_cbase = tab;
+    P1.pair_clbase = tab + 2;
+    P1.leaf_size = leaf_size;
+    P1.ncl = (uint32_t)z.ncl;
+    const int n = (int)z.ncl;
+    g_launches++;
+    k_clusters<uint32_t><<<grid_for(n), kBlock, 0, s>>>(P1, keys[buf], clkey, out.cl_start, out.cl_n, split_far);
+    if (n < 2) return;
+    g_launches++;
+    k_build<uint32_t><<<(n + kRefitWin - 1) / kRefitWin, kRefitWin, 0, s>>>(P1, clkey, n, fbox32, vals[buf],
+        out.cl_start, out.cl_n, out.nodes, split_far, (FBox*)split_box);
 }
 
 void launch_planes(const Problem& P, Work& W, cudaStream_t s)

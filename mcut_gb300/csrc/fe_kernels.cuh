@@ -41,6 +41,21 @@ struct __align__(16) Node {
     uint32_t prange[2];   // pair-id range of each child: lo | hi << 16
 };
 
+// A pair whose cut mesh is resident with its own tree (ncl > 0): the tree
+// was built once over the mesh's user coordinates (fp32 boxes rounded
+// outward, leaves of consecutive Morton-sorted faces), and the pair's source
+// faces walk it with their boxes mapped back from the pair's frame; its cut
+// faces take no part in the batch's sort and tree. ncl == 0: not resident.
+struct __align__(16) ResPair {
+    const Node* nodes;          // [ncl - 1]
+    const uint32_t* leaf_face;  // [nf] the mesh's faces (local ids) in leaf order
+    const uint32_t* cl_start;   // [ncl] first position of each leaf in leaf_face
+    const uint8_t* cl_n;        // [ncl]
+    uint32_t ncl, pad;
+    double mag[3];              // per axis: the largest |coordinate| of the mesh
+    double pad2;
+};
+
 struct Test {
     uint32_t q, r;    // oriented edge (global vertex ids)
     uint32_t g;       // tested face (global)
@@ -75,6 +90,10 @@ struct Problem {
     int all_triangles;          // foff[f] == 3f
     uint32_t leaf_size;         // cut faces per tree leaf (consecutive in Morton order, one pair)
     uint32_t ncl;               // total leaf clusters
+    // pairs with a resident cut tree (null: none): their cut faces are not in
+    // the cut-face list, the batch tree or pair_clbase's clusters
+    const ResPair* res_pairs;   // [n_pairs]
+    const double* pair_frames;  // [n_pairs][6] com xyz, t xyz (x' = (x - com) + t), for res_pairs
 };
 
 struct Work {
@@ -172,6 +191,16 @@ void launch_incidence(const Problem& P, Work& W, cudaStream_t s);        // vert
 void launch_tests(const Problem& P, Work& W, cudaStream_t s);
 void launch_narrow(const Problem& P, Work& W, bool keep_tests, cudaStream_t s);
 int launch_records(const Problem& P, Work& W, uint32_t n_records, cudaStream_t s);
+
+// A resident cut mesh's own tree over its user coordinates (fp64 X [nv][3],
+// triangles idx [nf][3]); mn / mx: its vertex bounds. Scratch and outputs as
+// resident_tree_sizes gives them; an index past nv reads vertex 0 (a pair
+// naming the mesh reports MCGPU_INVALID_INPUT from its own index check).
+struct ResTreeSizes { uint64_t ncl, nodes_bytes, leaf_bytes, start_bytes, n_bytes, scratch_bytes; };
+ResTreeSizes resident_tree_sizes(uint32_t nf, uint32_t leaf_size);
+struct ResTreeOut { Node* nodes; uint32_t* leaf_face; uint32_t* cl_start; uint8_t* cl_n; };
+void build_resident_tree(const double* X, const uint32_t* idx, uint32_t nv, uint32_t nf, const double* mn,
+    const double* mx, uint32_t leaf_size, void* scratch, const ResTreeOut& out, cudaStream_t s);
 // clears `mask` in every pair's status bits
 void launch_clear_status(uint32_t* pair_status, uint32_t n_pairs, uint32_t mask, cudaStream_t s);
 // record ordering from the device's record count (at most cap = kRankSortMax

@@ -11,9 +11,11 @@
 // forms, and the workers' batches overlap on the device.
 //
 // Cut meshes registered once stay on the device (double user coordinates +
-// indices) with their bounds and centroid; a request naming one uploads
-// only its source mesh, and the cut is mapped into the pair's frame on the
-// device.
+// indices) with their bounds and centroid and their own tree, built once
+// over the user coordinates; a request naming one uploads only its source
+// mesh, the cut is mapped into the pair's frame on the device, and the
+// source faces walk the resident tree instead of joining its faces to the
+// batch's sort and tree.
 //
 // Device memory: each worker may hold an allowance of device bytes -- its
 // context's pool while idle, its batch's cap while it runs one -- and the
@@ -39,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include "fe_host.h"
+#include "fe_kernels.cuh"
 #include "mcut_gb300.h"
 
 namespace {
@@ -67,8 +70,20 @@ struct Resident {
     mcgpu::ResidentCut rc {};
     void* dX = nullptr;
     void* dI = nullptr;
+    void* dTree = nullptr; // nodes, leaf order, leaf starts and sizes in one allocation
     uint64_t bytes = 0;
 };
+
+// leaves of the resident trees (faces per leaf cluster)
+#ifndef MCGPU_RESIDENT_LEAF
+#define MCGPU_RESIDENT_LEAF 4
+#endif
+constexpr uint32_t kResLeaf = MCGPU_RESIDENT_LEAF;
+uint64_t al256(uint64_t b) { return (b + 255) & ~255ull; }
+uint64_t tree_bytes(const mcgpu::ResTreeSizes& z)
+{
+    return al256(z.nodes_bytes) + al256(z.leaf_bytes) + al256(z.start_bytes) + al256(z.n_bytes);
+}
 
 uint64_t mesh_faces(const mcgpu_mesh& m) { return m.num_faces; }
 
@@ -373,6 +388,7 @@ int mcgpu_server_release(mcgpu_server S)
     for (auto& r : S->cuts) {
         cudaFree(r->dX);
         cudaFree(r->dI);
+        cudaFree(r->dTree);
     }
     delete S;
     return MCGPU_OK;
@@ -386,18 +402,22 @@ int mcgpu_server_add_cut_mesh(mcgpu_server S, const mcgpu_mesh* cut, uint32_t* c
     if (cut->num_vertices < 3 || cut->num_faces < 1) return sfail(MCGPU_INVALID_INPUT, "empty cut mesh");
     std::unique_ptr<Resident> r(new Resident());
     const size_t xb = (size_t)cut->num_vertices * 24, ib = (size_t)cut->num_faces * 12;
+    const mcgpu::ResTreeSizes z = mcgpu::resident_tree_sizes(cut->num_faces, kResLeaf);
+    const uint64_t tb = tree_bytes(z);
     {
-        // the resident bytes join the budget: free idle pools if they do not fit
+        // the resident bytes join the budget (the build's scratch for the
+        // time of the build): free idle pools if they do not fit
         std::lock_guard<std::mutex> lk(S->m);
-        const uint64_t size = (uint64_t)xb + ib;
-        if (free_bytes(S, S->allow.size()) < size) trim_idle(S, S->allow.size());
-        if (free_bytes(S, S->allow.size()) < size)
+        const uint64_t size = (uint64_t)xb + ib + tb;
+        if (free_bytes(S, S->allow.size()) < size + z.scratch_bytes) trim_idle(S, S->allow.size());
+        if (free_bytes(S, S->allow.size()) < size + z.scratch_bytes)
             return sfail(MCGPU_OUT_OF_MEMORY, "resident cut mesh exceeds the device memory budget");
-        S->resident_bytes += size; // reserved now, so no batch takes these bytes meanwhile
+        S->resident_bytes += size + z.scratch_bytes; // reserved now, so no batch takes these bytes meanwhile
     }
+    bool scratch_held = true;
     auto unreserve = [&] {
         std::lock_guard<std::mutex> lk(S->m);
-        S->resident_bytes -= (uint64_t)xb + ib;
+        S->resident_bytes -= (uint64_t)xb + ib + tb + (scratch_held ? z.scratch_bytes : 0);
     };
     mcgpu::mesh_stats(cut->vertices, false, cut->num_vertices, r->rc.st);
     cudaSetDevice(S->cfg.device);
@@ -418,7 +438,43 @@ int mcgpu_server_add_cut_mesh(mcgpu_server S, const mcgpu_mesh* cut, uint32_t* c
     r->rc.idx = static_cast<const uint32_t*>(r->dI);
     r->rc.nv = cut->num_vertices;
     r->rc.nf = cut->num_faces;
-    r->bytes = xb + ib;
+    // the mesh's own tree over its user coordinates
+    void* scratch = nullptr;
+    cudaStream_t st = nullptr;
+    const bool got = cudaMalloc(&r->dTree, tb) == cudaSuccess && cudaMalloc(&scratch, z.scratch_bytes) == cudaSuccess;
+    bool ok = got && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) {
+        uint8_t* t = static_cast<uint8_t*>(r->dTree);
+        mcgpu::ResTreeOut o {};
+        o.nodes = reinterpret_cast<mcgpu::Node*>(t);
+        o.leaf_face = reinterpret_cast<uint32_t*>(t + al256(z.nodes_bytes));
+        o.cl_start = reinterpret_cast<uint32_t*>(t + al256(z.nodes_bytes) + al256(z.leaf_bytes));
+        o.cl_n = t + al256(z.nodes_bytes) + al256(z.leaf_bytes) + al256(z.start_bytes);
+        mcgpu::build_resident_tree(r->rc.X, r->rc.idx, r->rc.nv, r->rc.nf, r->rc.st.mn, r->rc.st.mx, kResLeaf,
+            scratch, o, st);
+        ok = cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(st) == cudaSuccess;
+        r->rc.tree_nodes = o.nodes;
+        r->rc.tree_leaf_face = o.leaf_face;
+        r->rc.tree_cl_start = o.cl_start;
+        r->rc.tree_cl_n = o.cl_n;
+        r->rc.tree_ncl = (uint32_t)z.ncl;
+    }
+    if (st) cudaStreamDestroy(st);
+    cudaFree(scratch);
+    {
+        std::lock_guard<std::mutex> lk(S->m);
+        S->resident_bytes -= z.scratch_bytes;
+        scratch_held = false;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        cudaFree(r->dX);
+        cudaFree(r->dI);
+        cudaFree(r->dTree);
+        unreserve();
+        return sfail(got ? MCGPU_CUDA_ERROR : MCGPU_OUT_OF_MEMORY, "resident cut tree");
+    }
+    r->bytes = xb + ib + tb;
     std::lock_guard<std::mutex> lk(S->m);
     *cut_id = (uint32_t)S->cuts.size();
     S->cuts.push_back(std::move(r));

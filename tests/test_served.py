@@ -110,10 +110,15 @@ def test_served_admission_budget(alone, mult):
     from mcut_gb300 import Server
     reqs, want, needs = alone
     # the largest request's own pool and estimate (a request whose estimate
-    # exceeds the budget is refused at submission) plus the resident mesh fit,
-    # a few requests at most beside each other
-    budget = max(int(max(needs) * mult), max(_estimate(s, c) for s, c in reqs)) \
-        + 24 * reqs[0][1]["v"].shape[0] + 12 * meshgen.num_faces(reqs[0][1])
+    # exceeds the budget is refused at submission) plus the resident mesh
+    # (coordinates, indices and its tree) fit, a few requests at most beside
+    # each other
+    probe = Server(0, workers=1)
+    probe.add_cut(reqs[0][1])
+    resident = probe.stats()["resident_bytes"]
+    probe.close()
+    assert resident > 24 * reqs[0][1]["v"].shape[0] + 12 * meshgen.num_faces(reqs[0][1])
+    budget = max(int(max(needs) * mult), max(_estimate(s, c) for s, c in reqs)) + resident
     srv = Server(0, workers=3, hbm_budget_bytes=budget)
     cid = srv.add_cut(reqs[0][1])
     tickets = [srv.submit(s, c) for s, c in reqs] + [srv.submit(reqs[0][0], cut_id=cid)]
@@ -209,3 +214,46 @@ def test_served_records_match_oracle(alone):
         wa, wb = canonical_records(w["rec_ids"], w["rec_pts"])
         assert G.same_bits(a, wa) and G.same_bits(b, wb)
     srv.close()
+
+
+def _few_faces(c, k):
+    """The first k faces of cut mesh c, with only the vertices they use."""
+    f = np.asarray(c["f"], np.uint32).reshape(-1, 3)[:k]
+    used, inv = np.unique(f, return_inverse=True)
+    return dict(c, v=c["v"][used], f=inv.astype(np.uint32).reshape(-1))
+
+
+@pytest.mark.gpu
+def test_served_resident_trees_only(alone):
+    """Batches in which every pair names a resident cut mesh (no batch tree
+    at all: every source face walks its resident mesh's own tree), several
+    requests per resident mesh, and resident meshes of one face (a one-leaf
+    tree) and of a few faces: each result equals the request alone on a
+    plain context, pairs, tests and records included."""
+    from mcut_gb300 import Context, Server
+    reqs, want, needs = alone
+    ctx = Context(0)
+    cases = []
+    for i in range(4):
+        s, c = reqs[i]
+        cases.append((s, c, want[i]))
+    # small resident meshes cut from request 0's cut mesh, against its source
+    for k in (1, 5, 40):
+        s, c0 = reqs[0]
+        c = _few_faces(c0, k)
+        cases.append((s, c, ctx.dispatch(s, c)))
+    ctx.close()
+    srv = Server(0, workers=2, max_batch_pairs=16)
+    cids = [srv.add_cut(c) for _, c, _ in cases]
+    tickets = [(srv.submit(s, cut_id=cid), w) for (s, _, w), cid in zip(cases, cids)]
+    tickets += [(srv.submit(s, cut_id=cid), w) for (s, _, w), cid in zip(cases, cids)]
+    for t, w in tickets:
+        sm, _ = srv.wait(t)
+        ids, pts = srv.records(t)
+        _same(sm, ids, pts, w)
+    st = srv.stats()
+    srv.close()
+    assert st["resident_meshes"] == len(cases)
+    # the trees are counted with the meshes: more than coordinates and indices alone
+    mesh_bytes = sum(24 * c["v"].shape[0] + 12 * meshgen.num_faces(c) for _, c, _ in cases)
+    assert st["resident_bytes"] > mesh_bytes
