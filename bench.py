@@ -542,7 +542,7 @@ def run_served(ctx, world):
     # plain: one mcgpu_dispatch per request from host arrays (recentred as
     # mcDispatch does), records read back
     n_plain = 300
-    for i, r in trace[:8]:
+    for i, r in trace[:n_plain]:  # one untimed pass over the same requests
         ctx.dispatch(*pair_of(i, r))
     lat_p = []
     t0 = time.perf_counter()
@@ -565,8 +565,12 @@ def run_served(ctx, world):
             srv.release(t)
         return n / (time.perf_counter() - t0), lat
 
-    closed(64)  # warm the worker pools
-    sat, lat_c = closed(len(trace))
+    # warm-up: one untimed pass over the whole trace (the worker pools grow to
+    # the batches' sizes, the host pages are first touched over the link),
+    # then the median of three timed passes (all three reported)
+    closed(len(trace))
+    runs = sorted((closed(len(trace)) for _ in range(3)), key=lambda x: x[0])
+    sat, lat_c = runs[1]
 
     def open_loop(rate, n):
         rng = np.random.default_rng(7)
@@ -610,7 +614,7 @@ def run_served(ctx, world):
         "workload": SERVED_WORKLOAD, "requests": len(trace), "resident_cut_meshes": len(resident),
         "plain": {"value": world * plain, "unit": UNIT, "requests": n_plain,
                   "latency_ms": {"p50": float(np.percentile(lat_p, 50)), "p99": float(np.percentile(lat_p, 99))}},
-        "served_saturated": {"value": world * sat, "unit": UNIT,
+        "served_saturated": {"value": world * sat, "unit": UNIT, "passes": [world * x[0] for x in runs],
                              "latency_ms": {"p50": float(np.percentile(lat_c, 50)),
                                             "p99": float(np.percentile(lat_c, 99))}},
         "served_over_plain": sat / plain,

@@ -45,11 +45,16 @@ inline void ck(cudaError_t e, const char* where)
 // grow-only device buffer of a context's pool; `held` sums the pool's bytes,
 // and a growth that would take it past a nonzero `limit` fails as an
 // allocation failure before anything is freed
+// A grow-only device buffer of a context's pool, allocated and freed in
+// stream order on the context's stream (cudaMallocAsync / cudaFreeAsync): a
+// context that grows its pool neither waits for nor stalls the device work
+// of other contexts, as cudaFree's device-wide synchronisation would.
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
     uint64_t* held = nullptr;
     const uint64_t* limit = nullptr;
+    const cudaStream_t* stream = nullptr;
     template <typename T>
     T* get(size_t count)
     {
@@ -59,7 +64,7 @@ struct DevBuf {
             if (limit && *limit && *held - cap + want > *limit)
                 throw CudaError { cudaErrorMemoryAllocation, "context memory limit" };
             release();
-            ck(cudaMalloc(&p, want), "cudaMalloc");
+            ck(cudaMallocAsync(&p, want, *stream), "cudaMallocAsync");
             cap = want;
             *held += want;
         }
@@ -67,7 +72,7 @@ struct DevBuf {
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, *stream);
         if (held) *held -= cap;
         p = nullptr;
         cap = 0;
@@ -1708,6 +1713,7 @@ int mcgpu_context_create(mcgpu_context* out, int device)
         for (auto& b : c->buf) {
             b.held = &c->dev_held;
             b.limit = &c->dev_limit;
+            b.stream = &c->s;
         }
         if (const char* e = getenv("MCGPU_LEAF_SIZE")) {
             const int v = atoi(e);
@@ -1815,6 +1821,8 @@ int mcgpu_context_trim(mcgpu_context c)
     c->have_results = false;
     c->W = mcgpu::Work {};
     for (auto& b : c->buf) b.release();
+    // the frees are stream-ordered: the synchronize returns the memory
+    if (cudaStreamSynchronize(c->s) != cudaSuccess) return fail(MCGPU_CUDA_ERROR, "stream synchronize after trim");
     return MCGPU_OK;
 }
 
@@ -1823,7 +1831,9 @@ int mcgpu_context_release(mcgpu_context c)
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
     cudaSetDevice(c->device);
     if (c->s) cudaStreamSynchronize(c->s);
-    for (auto& b : c->buf) b.release();
+    if (c->s)
+        for (auto& b : c->buf) b.release();
+    if (c->s) cudaStreamSynchronize(c->s);
     c->pin_counters.release();
     c->pin_tab.release();
     c->pin_stage.release();

@@ -263,7 +263,18 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
     uint8_t* __restrict__ cand, uint32_t* __restrict__ fidx_out, uint32_t* __restrict__ face_pair_out,
     uint32_t* fidx_fix)
 {
-    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < P.nf; f += gridDim.x * blockDim.x) {
+    // triangles: the next face's indices are requested before this face's
+    // work, so their latency (over the host link when the indices are the
+    // caller's host arrays) overlaps it
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t nidx[3] = { 0u, 0u, 0u };
+    const uint32_t f0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P.all_triangles && f0 < P.nf)
+        for (int k = 0; k < 3; ++k) nidx[k] = fidx_at(P, 3ull * f0 + k);
+    for (uint32_t f = f0; f < P.nf; f += stride) {
+        uint32_t cidx[3] = { nidx[0], nidx[1], nidx[2] };
+        if (P.all_triangles && f + stride < P.nf && f + stride > f)
+            for (int k = 0; k < 3; ++k) nidx[k] = fidx_at(P, 3ull * (f + stride) + k);
         cand[f] = 0; // no candidate pair yet (the traversal sets it)
         const uint32_t fp = face_pair_of(P, f);
         if (face_pair_out) face_pair_out[f] = fp;
@@ -289,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_face_bounds(Problem P, double* __res
         }
         bool bad = false;
         for (uint32_t k = 0; k < n; ++k) {
-            uint32_t v = fidx_at(P, o + k);
+            uint32_t v = P.all_triangles ? cidx[k < 3 ? k : 0] : fidx_at(P, o + k);
             if (v < vlo || v >= vhi) {
                 // the pair's outcome is MCGPU_INVALID_INPUT; every later kernel
                 // reads the index table, so it gets the mesh's first vertex in place
