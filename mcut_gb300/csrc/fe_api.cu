@@ -111,7 +111,7 @@ enum BufId {
     B_PSTAT, B_PBAD, B_PNREC, B_TRI, B_SEG, B_CLKEY, B_CLSTART, B_CLN, B_LKB, B_PACKETS, B_PFLAG, B_PLIST, B_TOP, B_NRANGE, B_SPLIT, B_FRAME, B_XPERT, B_FIDXG,
     // the record hand-over (built at the first query for it)
     B_DCK0, B_DCK1, B_DCV0, B_DCV1, B_DFK0, B_DFK1, B_DFV0, B_DFV1, B_DFLAGS, B_DSORT, B_DSCAN, B_DOUT,
-    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB, B_RESP,
+    B_X32, B_PCNT, B_XRAW, B_GSEG, B_FRAMES, B_COM, B_RAWB, B_RESP, B_PROOT,
     // the cut path (built at the first query for it)
     B_CP_CAND, B_CP_INSIDE, B_CP_SORTED, B_CP_PROJ, B_CP_PK0, B_CP_PK1, B_CP_PV0, B_CP_PV1, B_CP_MADE, B_CP_FK0,
     B_CP_FK1, B_CP_FV0, B_CP_FV1, B_CP_HK0, B_CP_HK1, B_CP_HV0, B_CP_HV1, B_CP_FLAGS, B_CP_SORT, B_CP_SCAN, B_CP_OUT,
@@ -637,7 +637,7 @@ __global__ void k_prep(uint32_t n_pairs, const uint32_t* __restrict__ tab, uint3
 // statuses and record ranges, no degenerate face
 __global__ void k_init_dispatch(unsigned long long* __restrict__ mb, uint32_t n_pairs, uint32_t* __restrict__ counters,
     uint32_t* __restrict__ pair_status, int32_t* __restrict__ pair_bad, uint32_t* __restrict__ pair_nrec,
-    uint32_t* __restrict__ pair_cnt)
+    uint32_t* __restrict__ pair_cnt, int32_t* __restrict__ pair_root)
 {
     const uint64_t n12 = (uint64_t)n_pairs * 12;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n12 + 16; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -649,6 +649,7 @@ __global__ void k_init_dispatch(unsigned long long* __restrict__ mb, uint32_t n_
         }
         if (i <= n_pairs) pair_nrec[i] = 0u;
         if (pair_cnt && i < (uint64_t)n_pairs * 5) pair_cnt[i] = 0u;
+        if (pair_root && i < n_pairs) pair_root[i] = kNoRoot;
     }
 }
 
@@ -1185,6 +1186,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
     W.pair_bad = c->buf[B_PBAD].get<int32_t>(n);
     W.pair_nrec = c->buf[B_PNREC].get<uint32_t>(n + 1);
     W.pair_cnt = n > 1 ? c->buf[B_PCNT].get<uint32_t>((size_t)n * 5) : nullptr;
+    W.pair_root = n > 1 ? c->buf[B_PROOT].get<int32_t>(n) : nullptr;
     W.scan_temp = c->buf[B_SCANTMP].get<uint32_t>(scan_temp_bytes((uint32_t)L.nv + 1) / 4 + 64);
     if (W.pair_cap == 0) W.pair_cap = std::max<uint64_t>(1 << 16, 2 * (L.ns + L.nc));
     W.pairs = c->buf[B_PAIRS].get<unsigned long long>(W.pair_cap);
@@ -1205,7 +1207,7 @@ int run(mcgpu_context_t* c, uint32_t flags, uint32_t n, const mcgpu_mesh* srcs, 
         rec(c, 2 * MCGPU_STAGE_BOUNDS);
         g_launches++;
         k_init_dispatch<<<grid1((uint64_t)n * 12 + 16), 256, 0, s>>>(W.mesh_box, n, W.counters, W.pair_status,
-            W.pair_bad, W.pair_nrec, W.pair_cnt); // the candidate-face flags are cleared by the bounds kernel
+            W.pair_bad, W.pair_nrec, W.pair_cnt, W.pair_root); // the candidate-face flags are cleared by the bounds kernel
         launch_bounds_morton(P, c->Pin, W, wide, key_bits, s);
         rec(c, 2 * MCGPU_STAGE_BOUNDS + 1);
         rec(c, 2 * MCGPU_STAGE_SORT);

@@ -543,7 +543,7 @@ template <typename K>
 __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restrict__ key, int n,
     const float* __restrict__ fbox32, const uint32_t* __restrict__ leaf_face, const uint32_t* __restrict__ cl_start,
     const uint8_t* __restrict__ cl_n, Node* __restrict__ nodes, uint32_t* __restrict__ split_far,
-    FBox* __restrict__ split_box)
+    FBox* __restrict__ split_box, int32_t* __restrict__ pair_root)
 {
     using D = DltOf<K>;
     constexpr int kW = kRefitWin / 32;
@@ -647,6 +647,10 @@ __global__ void __launch_bounds__(kRefitWin) k_build(Problem P, const K* __restr
         }
         fb.plo = min(fb.plo, o.plo);
         fb.phi = max(fb.phi, o.phi);
+        // the node that holds exactly one pair's clusters is that pair's root
+        if (pair_root && fb.plo == fb.phi && (uint32_t)pl == P.pair_clbase[fb.plo]
+            && (uint32_t)pr + 1u == P.pair_clbase[fb.plo + 1])
+            pair_root[fb.plo] = pidx;
         if (root) return;
         l = pl;
         r = pr;
@@ -918,7 +922,7 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
     const uint32_t* __restrict__ cl_start, const uint8_t* __restrict__ cl_n, const WaveTop* __restrict__ top,
     int nleaf, const Node* __restrict__ nodes, unsigned long long* __restrict__ pairs, uint64_t cap,
     uint32_t* __restrict__ counters, uint8_t* __restrict__ cand, uint32_t* __restrict__ pair_status,
-    SplitEntry* __restrict__ split, uint32_t split_cap, int split_round)
+    SplitEntry* __restrict__ split, uint32_t split_cap, int split_round, const int32_t* __restrict__ pair_root)
 {
     extern __shared__ __align__(16) unsigned char wave_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1109,8 +1113,19 @@ __global__ void __launch_bounds__(kBlock) k_traverse_wave(Problem P, const doubl
                 if (lane < cnt) stk[lane] = split[it].nodes[lane];
                 sp = cnt;
             }
-            // first: the listed top cut of the tree
-            const int ntop = SPLIT ? 0 : (int)counters[13];
+            // first: the listed top cut of the tree -- or, for a packet of one
+            // pair in a batch, that pair's own subtree (the levels above it hold
+            // other pairs' clusters only)
+            int ntop = SPLIT ? 0 : (int)counters[13];
+            if (!SPLIT && pair_root && pmin == pmax) {
+                const int r0 = __ldg(&pair_root[pmin]);
+                if (r0 >= 0) {
+                    if (lane == 0) stk[0] = r0;
+                    __syncwarp();
+                    sp = 1;
+                    ntop = 0;
+                }
+            }
             for (int base = 0; base < ntop; base += 32) {
                 const int i = base + lane;
                 bool hit = false;
@@ -2399,10 +2414,10 @@ void launch_hierarchy(const Problem& P, Work& W, bool wide, int cut_buf, cudaStr
     const int g = (n + kRefitWin - 1) / kRefitWin;
     if (wide)
         k_build<unsigned long long><<<g, kRefitWin, 0, s>>>(P, (const unsigned long long*)W.cl_key, n, W.fbox32,
-            W.cvals[cut_buf], W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box);
+            W.cvals[cut_buf], W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box, W.pair_root);
     else
         k_build<uint32_t><<<g, kRefitWin, 0, s>>>(P, (const uint32_t*)W.cl_key, n, W.fbox32, W.cvals[cut_buf],
-            W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box);
+            W.cl_start, W.cl_n, W.nodes, W.split_far, (FBox*)W.split_box, W.pair_root);
 }
 
 void launch_packets(const Problem& P, Work& W, int src_buf, cudaStream_t s)
@@ -2451,12 +2466,12 @@ static void launch_traverse_tree(const Problem& P, Work& W, int src_buf, int cut
         k_top_cut<<<1, 32, 0, s>>>(W.nodes, (int)P.ncl, top, W.counters);
         k_traverse_wave<false><<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
             W.cvals[cut_buf], W.cl_start, W.cl_n, top, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters, W.cand,
-            W.pair_status, split, (uint32_t)W.split_cap, (int)W.split_round);
+            W.pair_status, split, (uint32_t)W.split_cap, (int)W.split_round, W.pair_root);
         if (W.split_round > 0) {
             g_launches++;
             k_traverse_wave<true><<<grid_for(P.ns), kBlock, kWaveSmem, s>>>(P, W.fbox, W.svals[src_buf], W.packets,
                 W.cvals[cut_buf], W.cl_start, W.cl_n, top, (int)P.ncl, W.nodes, W.pairs, W.pair_cap, W.counters,
-                W.cand, W.pair_status, split, (uint32_t)W.split_cap, 0);
+                W.cand, W.pair_status, split, (uint32_t)W.split_cap, 0, nullptr);
         }
     }
 }
@@ -2531,7 +2546,7 @@ void build_resident_tree(const double* X, const uint32_t* idx, uint32_t nv, uint
     if (n < 2) return;
     g_launches++;
     k_build<uint32_t><<<(n + kRefitWin - 1) / kRefitWin, kRefitWin, 0, s>>>(P1, clkey, n, fbox32, vals[buf],
-        out.cl_start, out.cl_n, out.nodes, split_far, (FBox*)split_box);
+        out.cl_start, out.cl_n, out.nodes, split_far, (FBox*)split_box, nullptr);
 }
 
 void launch_planes(const Problem& P, Work& W, cudaStream_t s)

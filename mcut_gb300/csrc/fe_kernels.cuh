@@ -24,6 +24,7 @@ namespace mcgpu {
 
 constexpr uint32_t kCutBit = 0x80000000u;
 constexpr int32_t kNoBad = 0x7F7F7F7F; // pair_bad when no face is degenerate (memset 0x7F)
+constexpr int32_t kNoRoot = (int32_t)0x80000000; // pair_root of a pair without an internal tree node
 // Morton code width: 23 (8, 8 and 7 bits per axis), which with the mesh bit
 // keeps one pair's keys within three 8-bit radix passes, or 30 (10 per axis,
 // four passes; the tree over 2 M faces is no better for the extra bits)
@@ -163,6 +164,8 @@ struct Work {
     uint32_t* pair_status;            // [n_pairs] ST_* bits
     int32_t* pair_bad;                // [n_pairs] lowest degenerate ps face (local), INT_MAX if none
     uint32_t* pair_nrec;              // [n_pairs+1] first sorted record of each pair (+ total)
+    int32_t* pair_root;               // [n_pairs] a batch's node whose subtree holds exactly the pair's leaf
+                                      //   clusters (kNoRoot: none, the pair has one cluster or none); null: one pair
     uint32_t* pair_cnt;               // [n_pairs*5] a batch's per-pair counts: candidate pairs, tests,
                                       //   escalations (fp32 / fp64 / exact); null: one pair (counters only)
     double* tri_scratch;              // polygon triplet scratch (24-byte entries)

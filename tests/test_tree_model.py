@@ -144,3 +144,32 @@ def test_bottom_up_build_gives_the_karras_tree(seed):
         assert len(got) == n - 1
         for i in range(n - 1):
             assert expect[i] == got[i], (n, window, i)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_every_pair_of_a_batch_has_its_own_subtree(seed):
+    """A batch's cut keys carry the pair above the Morton code (pair << 23 |
+    code), so each pair with two or more leaf clusters owns exactly one node
+    whose leaf range is the pair's clusters: the node k_build records as the
+    pair's root, where a one-pair query packet starts its walk (the nodes
+    above it hold other pairs' clusters only)."""
+    rng = random.Random(100 + seed)
+    for _ in range(10):
+        npairs = rng.choice([2, 3, 7, 40])
+        keys, ranges = [], []
+        for p in range(npairs):
+            cnt = rng.choice([0, 1, 2, 3, 9, 33, 150])
+            codes = sorted(rng.randrange(16 if rng.random() < 0.3 else 2 ** 23) for _ in range(cnt))
+            ranges.append((len(keys), len(keys) + cnt - 1))
+            keys += [(p << 23) | c for c in codes]
+        if len(keys) < 2:
+            continue
+        nodes = karras(keys)
+        for lo, hi in ranges:
+            if hi - lo + 1 < 2:
+                continue
+            owners = [i for i, (_, _, a, b) in nodes.items() if (a, b) == (lo, hi)]
+            assert len(owners) == 1, (lo, hi, owners)
+            # the same node from the bottom-up build's merge rule
+            built = bottom_up(keys, 32, rng)
+            assert built[owners[0]][2:] == (lo, hi)
