@@ -256,6 +256,22 @@ def run_single():
                       "kernel_launches_per_dispatch": int(sm.kernel_launches)}))
 
 
+def run_single_host():
+    """Two dispatches of the workload through the e2e call (the caller's host
+    arrays in internal coordinates, read by the bounds kernels over the host
+    link, records read back): the second one's launches are what a profiler
+    capture should select."""
+    from mcut_gb300 import Context, recentre
+    src, cut = make_workload()
+    sx, cx, eps = recentre(src, cut)
+    ctx = Context(0)
+    si, ci = dict(v=sx, f=src["f"], fs=None), dict(v=cx, f=cut["f"], fs=None)
+    for _ in range(2):
+        r = ctx.dispatch(si, ci, cut_eps=eps, recentre=False)
+    print(json.dumps({"single_host": True, "status": r.status_name, "records": int(r.num_records),
+                      "kernel_launches_per_dispatch": int(r.kernel_launches)}))
+
+
 BATCH_WORKLOAD = ("fracture batch: 4096 independent pairs, icosphere level U{2..5} r U(0.5,1.5) noise N(0,0.005) "
                   "vs n x n crack grid n U{8..128}, random rotation, offset U(-0.3,0.3), z noise N(0,0.02)")
 
@@ -797,10 +813,14 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (4096 pairs) and served (request stream) measurements")
     ap.add_argument("--single", action="store_true",
                     help="one warm-up dispatch + one dispatch of the workload, nothing else (for ncu captures)")
+    ap.add_argument("--single-host", action="store_true",
+                    help="the same through the e2e call: host arrays in internal coordinates (for ncu captures)")
     args = ap.parse_args()
     world, rank, local = dist_init(args)
     if args.single:
         run_single()
+    elif args.single_host:
+        run_single_host()
     elif args.impl == "reference":
         run_reference(args, world, rank)
     else:

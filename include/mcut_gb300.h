@@ -298,7 +298,9 @@ int mcgpu_recentre(uint32_t flags, const mcgpu_mesh* src, const mcgpu_mesh* cut,
  * file-scope __device__ array of about 12 MB that every GPU loading this
  * library keeps until exit. The call reads counters back into host variables
  * between its stages, so it waits for `stream` three or four times and
- * returns when its GPU work is done.
+ * returns when its GPU work is done; it cannot be recorded into a CUDA
+ * graph, and on a stream that is being captured it returns
+ * MCGPU_INVALID_VALUE before any GPU call (the capture stays valid).
  * Limits: triangles only; at most 16384 vertices and 16384 faces over both
  * meshes, 32768 candidate pairs, 65536 edge-face tests -- anything larger
  * returns MCGPU_TOO_LARGE. Every call shares that array and it keeps the

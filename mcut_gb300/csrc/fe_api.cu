@@ -257,14 +257,10 @@ void vertex_bounds(const void* v, bool fin, uint32_t n, double* mn_out, double* 
 // three independent chains
 void mesh_sums(const void* v, bool fin, uint32_t n, double* out)
 {
-    // one core streams the array: software prefetches ahead of the hardware
-    // prefetcher keep more lines in flight (the pass is bound by that core's reads)
-    constexpr uint32_t kAhead = 512; // vertices
     double a = 0.0, b = 0.0, c = 0.0;
     if (fin) {
         const float* p = (const float*)v;
         for (uint32_t i = 0; i < n; ++i) {
-            if ((i & 3) == 0 && i + kAhead < n) __builtin_prefetch(p + 3 * (size_t)(i + kAhead), 0, 0);
             a += (double)p[3 * (size_t)i];
             b += (double)p[3 * (size_t)i + 1];
             c += (double)p[3 * (size_t)i + 2];
@@ -272,7 +268,6 @@ void mesh_sums(const void* v, bool fin, uint32_t n, double* out)
     } else {
         const double* p = (const double*)v;
         for (uint32_t i = 0; i < n; ++i) {
-            if ((i & 1) == 0 && i + kAhead < n) __builtin_prefetch(p + 3 * (size_t)(i + kAhead), 0, 0);
             a += p[3 * (size_t)i];
             b += p[3 * (size_t)i + 1];
             c += p[3 * (size_t)i + 2];

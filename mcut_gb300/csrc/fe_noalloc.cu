@@ -149,6 +149,15 @@ extern "C" int mcgpu_dispatch_noalloc(void* stream, const mcgpu_mesh* src, const
         return na_fail(out, MCGPU_INVALID_VALUE);
     // an error left by the caller's earlier, unrelated work is not this call's
     (void)cudaGetLastError();
+    // the call waits for its stream between stages, which a stream being
+    // captured into a CUDA graph cannot do: refuse before any GPU call, so
+    // the caller's capture stays valid
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess
+        || cap != cudaStreamCaptureStatusNone) {
+        (void)cudaGetLastError();
+        return na_fail(out, MCGPU_INVALID_VALUE);
+    }
     if (src->face_sizes || cut->face_sizes) return na_fail(out, MCGPU_TOO_LARGE); // triangles only
     const uint64_t nv = (uint64_t)src->num_vertices + cut->num_vertices;
     const uint64_t nf = (uint64_t)src->num_faces + cut->num_faces;

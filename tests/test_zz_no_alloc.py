@@ -190,3 +190,34 @@ def test_noalloc_null_argument_sets_status():
     sm.status = 12345
     rc = lib.mcgpu_dispatch_noalloc(None, None, None, 1e-4, None, None, 0, C.byref(sm))
     assert rc == L.INVALID_VALUE and sm.status == L.INVALID_VALUE
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call waits for its stream between stages, which a stream being
+    captured into a CUDA graph cannot do: on such a stream it returns
+    MCGPU_INVALID_VALUE before any GPU work, the caller's capture stays valid
+    (it ends without error and replays), and the next call outside the
+    capture gives the allocating entry point's records."""
+    import torch
+    from mcut_gb300 import _lib as L
+    lib = L.load()
+    c = CASES["two_spheres"]
+    sx, cx, eps, want = _reference_result(c["src"], c["cut"])
+    ms, k1 = _device_mesh(torch, sx, c["src"]["f"])
+    mc, k2 = _device_mesh(torch, cx, c["cut"]["f"])
+    ids = torch.zeros(5 * 4096, dtype=torch.int32, device="cuda")
+    pts = torch.zeros(3 * 4096, dtype=torch.float64, device="cuda")
+    x = torch.zeros(8, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    sm = L.Summary()
+    with torch.cuda.graph(g):
+        x += 1.0  # the caller's own captured work
+        rc = lib.mcgpu_dispatch_noalloc(C.c_void_p(torch.cuda.current_stream().cuda_stream), C.byref(ms),
+                                        C.byref(mc), eps, ids.data_ptr(), pts.data_ptr(), 4096, C.byref(sm))
+    assert rc == L.INVALID_VALUE and sm.status == L.INVALID_VALUE
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0
+    rc, sm, got_ids, got_pts = _noalloc(torch, lib, ms, mc, eps, 4096)
+    assert rc == L.OK and sm.status == want.status
+    assert np.array_equal(got_ids, want.record_ids) and G.same_bits(got_pts, want.record_points)
