@@ -476,6 +476,26 @@ def run_hmesh(ctx, cpu=True):
             oracle.hmesh(m["f"], None, len(m["v"]), "port")
             row["cpu_port_1_thread_ms"] = 1e3 * (time.perf_counter() - t0)
         res[name] = row
+    # a connected component's wire arrays (mcGetConnectedComponentData: faces,
+    # face adjacency and counts, edges, float vertices), the cut mesh taken as
+    # one component, from device arrays to host arrays
+    f = torch.from_numpy(np.ascontiguousarray(c["f"], np.uint32).view(np.int32)).cuda()
+    v = torch.from_numpy(np.ascontiguousarray(c["v"], np.float64)).cuda()
+    for _ in range(2):
+        w = ctx.cc_wire(dict(v=v, f=f, fs=None), device=True)
+    ts = []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w = ctx.cc_wire(dict(v=v, f=f, fs=None), device=True)
+        ts.append(1e3 * (time.perf_counter() - t0))
+    row = {"faces": int(len(c["f"]) // 3), "adjacent_faces": int(len(w["adj"])), "gpu_ms": float(np.median(ts))}
+    if cpu:
+        t0 = time.perf_counter()
+        h = oracle.hmesh(c["f"], None, len(c["v"]), "port")
+        oracle.cc_wire_of_hmesh(h, np.full(len(c["f"]) // 3, 3, np.uint32), c["v"])
+        row["cpu_port_1_thread_ms"] = 1e3 * (time.perf_counter() - t0)
+    res["cc_wire"] = row
     return res
 
 

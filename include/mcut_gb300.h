@@ -185,7 +185,17 @@ typedef enum mcgpu_data {
     MCGPU_DATA_FLOATING_OFFSETS = 33,    /* uint32[P+1] */
     MCGPU_DATA_FLOATING_VERTICES = 34,   /* uint32[o[P]]: m0 ids around each polygon, from its smallest */
     MCGPU_DATA_FLOATING_NORMALS = 35,    /* double[3P]: the face's unit normal (floating_polygon_info_t) */
-    MCGPU_DATA_FLOATING_NORMAL_COMPONENTS = 36 /* int32[P]: its largest component */
+    MCGPU_DATA_FLOATING_NORMAL_COMPONENTS = 36, /* int32[P]: its largest component */
+    /* A connected component's arrays as mcGetConnectedComponentData hands them to the caller
+     * (frontend.cpp:2006-2832), from the halfedge mesh of the last mcgpu_halfedge_mesh call over
+     * the component's faces in its corner order (F faces, E edges, V vertices) */
+    MCGPU_DATA_CC_FACE = 37,             /* uint32[corners]: vertices around each face, the targets of
+                                            its halfedges (MC_CONNECTED_COMPONENT_DATA_FACE) */
+    MCGPU_DATA_CC_FACE_ADJACENT_FACE_SIZE = 38, /* uint32[F]: faces across each face's halfedges */
+    MCGPU_DATA_CC_FACE_ADJACENT_FACE = 39, /* uint32[sum]: those faces, face by face, halfedge order */
+    MCGPU_DATA_CC_EDGE = 40,             /* uint32[2E]: vertex(e, 0), vertex(e, 1) of each edge */
+    MCGPU_DATA_CC_VERTEX_FLOAT = 41      /* float[3V]: the call's double vertices rounded to float
+                                            (needs the vertices at the mcgpu_halfedge_mesh call) */
 } mcgpu_data;
 
 /* Context with its own stream and device memory pool on `device`.
@@ -342,10 +352,13 @@ typedef struct mcgpu_hmesh_report {
  * check_input_mesh (preproc.cpp:505-579) and mesh_is_closed
  * (preproc.cpp:1957-1994): the same status and failing face as that
  * face-by-face loop, the same edge and halfedge numbering, next / prev links
- * and per-vertex halfedge lists. Only the indices and face sizes are read
- * (vertices may be NULL); with MCGPU_DEVICE_POINTERS they are device arrays.
- * The arrays stay in the context until its next mcgpu_halfedge_mesh call
- * (mcgpu_get_data queries 18-24). Returns MCGPU_OK when it ran; the
+ * and per-vertex halfedge lists. The connectivity reads the indices and face
+ * sizes only; double vertices, when given (float input is not), are rounded
+ * to float for MCGPU_DATA_CC_VERTEX_FLOAT. With MCGPU_DEVICE_POINTERS the
+ * arrays are device arrays. The results stay in the context until its next
+ * mcgpu_halfedge_mesh call (mcgpu_get_data queries 18-24; 37-41, a
+ * connected component's arrays as MCUT serialises them, when the mesh is a
+ * component given in its corner order). Returns MCGPU_OK when it ran; the
  * mesh's outcome is out->status. */
 int mcgpu_halfedge_mesh(mcgpu_context ctx, uint32_t flags, const mcgpu_mesh* mesh, mcgpu_hmesh_report* out);
 

@@ -43,6 +43,9 @@ DATA_CUTPATH_STATUS, DATA_CUTPATH_EDGES, DATA_CUTPATH_FACE_KEYS, DATA_CUTPATH_FA
 # its floating polygons
 DATA_FLOATING_FACES, DATA_FLOATING_OFFSETS, DATA_FLOATING_VERTICES, DATA_FLOATING_NORMALS, \
     DATA_FLOATING_NORMAL_COMPONENTS = range(32, 37)
+# a connected component's arrays as MCUT serialises them, from the last halfedge mesh
+DATA_CC_FACE, DATA_CC_FACE_ADJACENT_FACE_SIZE, DATA_CC_FACE_ADJACENT_FACE, DATA_CC_EDGE, \
+    DATA_CC_VERTEX_FLOAT = range(37, 42)
 # mcgpu_hmesh_status (the oracle's HM_* values)
 HMESH_OK, HMESH_FACE_SIZE, HMESH_INDEX_RANGE, HMESH_DUPLICATE_INDEX, HMESH_NON_MANIFOLD, HMESH_TOO_SMALL, \
     HMESH_COMPONENTS = range(7)

@@ -119,7 +119,7 @@ enum BufId {
     // the halfedge mesh (mcgpu_halfedge_mesh)
     B_HM_IDX, B_HM_FOFF, B_HM_KEY, B_HM_FIRST, B_HM_DIR, B_HM_SLOTFACE, B_HM_BUCKET, B_HM_EID, B_HM_VCUR,
     B_HM_PARENT, B_HM_SCAN, B_HM_SMALL, B_HM_TGT, B_HM_FACE, B_HM_NEXT, B_HM_PREV, B_HM_CORNER, B_HM_VOFF,
-    B_HM_VHE, B_COUNT
+    B_HM_VHE, B_CW_FACE, B_CW_POS, B_CW_ADJ, B_CW_ADJN, B_CW_SCAN, B_CW_VF, B_CW_XD, B_COUNT
 };
 
 // host per-pair tables and results of the last dispatch
@@ -200,6 +200,13 @@ struct mcgpu_context_t {
     bool hm_ready = false;
     uint32_t hm_ne = 0, hm_nv = 0;
     uint64_t hm_nidx = 0;
+    // the last halfedge mesh's face offsets (null: triangles) and face count,
+    // and the component wire arrays derived from it (built at the first query)
+    const uint32_t* hm_foff = nullptr;
+    uint32_t hm_nf = 0;
+    bool cw_ready = false, hm_has_vf = false;
+    mcgpu::CcWireOut cw {};
+    uint32_t cw_total = 0;
     mcgpu::HmeshOut hm {};
 };
 
@@ -1642,6 +1649,28 @@ int ensure_cutpath(mcgpu_context_t* c)
     return MCGPU_OK;
 }
 
+// The wire arrays of the last halfedge mesh (a connected component given in
+// its corner order): its faces' vertices and face adjacency.
+void ensure_cc_wire(mcgpu_context_t* c)
+{
+    if (c->cw_ready) return;
+    const uint64_t nidx = c->hm_nidx;
+    CcWireOut& w = c->cw;
+    w.face = c->buf[B_CW_FACE].get<uint32_t>(std::max<uint64_t>(nidx, 1));
+    w.pos = c->buf[B_CW_POS].get<uint32_t>(nidx + 1);
+    w.adj = c->buf[B_CW_ADJ].get<uint32_t>(std::max<uint64_t>(nidx, 1));
+    w.adj_n = c->buf[B_CW_ADJN].get<uint32_t>(std::max<uint32_t>(c->hm_nf, 1));
+    // the scan's block sums, then one word for the adjacency count
+    const size_t sw = cc_wire_scan_bytes(nidx) / 4;
+    uint32_t* scan = c->buf[B_CW_SCAN].get<uint32_t>(sw + 64);
+    uint32_t* total = scan + sw + 32;
+    launch_cc_wire(c->hm, c->hm_foff, c->hm_nf, nidx, w, scan, total, c->s);
+    ck(cudaMemcpyAsync(&c->cw_total, total, 4, cudaMemcpyDeviceToHost, c->s), "D2H adjacency count");
+    ck(cudaStreamSynchronize(c->s), "sync wire arrays");
+    ck(cudaGetLastError(), "wire arrays");
+    c->cw_ready = true;
+}
+
 // The floating polygons of the last dispatch (one pair), from its cut path.
 int ensure_floating(mcgpu_context_t* c)
 {
@@ -2004,7 +2033,9 @@ int mcgpu_autotune(mcgpu_context c, uint32_t flags, const mcgpu_batch* sample, u
 int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, uint64_t* bytes_out)
 {
     if (!c) return fail(MCGPU_INVALID_VALUE, "null context");
-    if ((query < MCGPU_DATA_HE_TARGET || query >= MCGPU_DATA_CUTPATH_STATUS) && !c->have_results)
+    const bool hm_query = (query >= MCGPU_DATA_HE_TARGET && query < MCGPU_DATA_CUTPATH_STATUS)
+        || (query >= MCGPU_DATA_CC_FACE && query <= MCGPU_DATA_CC_VERTEX_FLOAT);
+    if (!hm_query && !c->have_results)
         return fail(MCGPU_INVALID_VALUE, "no dispatch results (none completed, or the pool was trimmed)");
     try {
         const Work& W = c->W;
@@ -2177,6 +2208,24 @@ int mcgpu_get_data(mcgpu_context c, uint32_t query, uint64_t bytes, void* mem, u
             default: return copy_out(c, c->hm.v_he, 4 * nhe, bytes, mem, bytes_out);
             }
         }
+        case MCGPU_DATA_CC_FACE:
+        case MCGPU_DATA_CC_FACE_ADJACENT_FACE_SIZE:
+        case MCGPU_DATA_CC_FACE_ADJACENT_FACE:
+        case MCGPU_DATA_CC_EDGE:
+        case MCGPU_DATA_CC_VERTEX_FLOAT: {
+            if (!c->hm_ready) return fail(MCGPU_INVALID_VALUE, "no halfedge mesh (mcgpu_halfedge_mesh) built");
+            if (query == MCGPU_DATA_CC_EDGE) return copy_out(c, c->hm.he_target, 8ull * c->hm_ne, bytes, mem, bytes_out);
+            if (query == MCGPU_DATA_CC_VERTEX_FLOAT) {
+                if (!c->hm_has_vf) return fail(MCGPU_INVALID_VALUE, "no double vertices given to mcgpu_halfedge_mesh");
+                return copy_out(c, c->buf[B_CW_VF].get<float>(3ull * c->hm_nv), 12ull * c->hm_nv, bytes, mem, bytes_out);
+            }
+            ensure_cc_wire(c);
+            switch (query) {
+            case MCGPU_DATA_CC_FACE: return copy_out(c, c->cw.face, 4 * c->hm_nidx, bytes, mem, bytes_out);
+            case MCGPU_DATA_CC_FACE_ADJACENT_FACE_SIZE: return copy_out(c, c->cw.adj_n, 4ull * c->hm_nf, bytes, mem, bytes_out);
+            default: return copy_out(c, c->cw.adj, 4ull * c->cw_total, bytes, mem, bytes_out);
+            }
+        }
         case MCGPU_DATA_RECORD_OFFSETS: {
             const uint64_t need = c->rec_begin.size() * 8;
             if (bytes_out) *bytes_out = need;
@@ -2330,6 +2379,23 @@ int mcgpu_halfedge_mesh(mcgpu_context c, uint32_t flags, const mcgpu_mesh* m, mc
         c->hm_ne = ne;
         c->hm_nv = nv;
         c->hm_nidx = nidx;
+        c->hm_nf = nf;
+        c->hm_foff = foff;
+        c->cw_ready = false;
+        c->hm_has_vf = false;
+        if (m->vertices && !(flags & MCGPU_VERTEX_ARRAY_FLOAT) && nv) {
+            // MC_CONNECTED_COMPONENT_DATA_VERTEX_FLOAT: static_cast<float> of each coordinate
+            const double* x = static_cast<const double*>(m->vertices);
+            if (!dev) {
+                double* d = c->buf[B_CW_XD].get<double>(3ull * nv);
+                ck(cudaMemcpyAsync(d, m->vertices, 24ull * nv, cudaMemcpyHostToDevice, s), "H2D vertices");
+                x = d;
+            }
+            launch_to_float(x, 3ull * nv, c->buf[B_CW_VF].get<float>(3ull * nv), s);
+            ck(cudaStreamSynchronize(s), "sync vertices");
+            ck(cudaGetLastError(), "vertex rounding");
+            c->hm_has_vf = true;
+        }
         out->num_edges = ne;
         out->closed = hs[2 + kHmBorder] ? 0 : 1;
         // check_input_mesh (preproc.cpp:505-579): after the conversion

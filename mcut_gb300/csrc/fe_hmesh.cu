@@ -270,4 +270,60 @@ void launch_hmesh_build(const HmeshInput& in, const HmeshTable& t, HmeshScratch&
     k_hm_cc_count<<<hgrid(in.nv), kHBlock, 0, s>>>(in.nv, w.parent, w.counts + kHmComponents);
 }
 
+namespace {
+__global__ void __launch_bounds__(kHBlock) k_cw_corners(uint64_t nidx, const uint32_t* __restrict__ corner_he,
+    const uint32_t* __restrict__ he_target, const int32_t* __restrict__ he_face, uint32_t* __restrict__ face,
+    uint32_t* __restrict__ flag)
+{
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s <= nidx; s += (uint64_t)gridDim.x * blockDim.x) {
+        if (s == nidx) { flag[s] = 0u; continue; }
+        const uint32_t h = corner_he[s];
+        face[s] = he_target[h];
+        flag[s] = he_face[h ^ 1u] >= 0 ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kHBlock) k_cw_adjacent(uint64_t nidx, const uint32_t* __restrict__ corner_he,
+    const int32_t* __restrict__ he_face, const uint32_t* __restrict__ pos, uint32_t* __restrict__ adj)
+{
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < nidx; s += (uint64_t)gridDim.x * blockDim.x) {
+        const int32_t f = he_face[corner_he[s] ^ 1u];
+        if (f >= 0) adj[pos[s]] = (uint32_t)f;
+    }
+}
+
+__global__ void __launch_bounds__(kHBlock) k_cw_counts(uint32_t nf, const uint32_t* __restrict__ foff,
+    const uint32_t* __restrict__ pos, uint32_t* __restrict__ adj_n)
+{
+    for (uint32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += gridDim.x * blockDim.x) {
+        const uint64_t a = foff ? foff[f] : 3ull * f, b = foff ? foff[f + 1] : 3ull * f + 3;
+        adj_n[f] = pos[b] - pos[a];
+    }
+}
+
+__global__ void __launch_bounds__(kHBlock) k_to_float(const double* __restrict__ x, uint64_t n, float* __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(x[i]);
+}
+} // namespace
+
+size_t cc_wire_scan_bytes(uint64_t nidx) { return scan_temp_bytes((uint32_t)(nidx + 1)); }
+
+void launch_cc_wire(const HmeshOut& o, const uint32_t* foff, uint32_t nf, uint64_t nidx, CcWireOut& w,
+    uint32_t* scan_temp, uint32_t* total, cudaStream_t s)
+{
+    g_launches += 3;
+    k_cw_corners<<<hgrid(nidx + 1), kHBlock, 0, s>>>(nidx, o.corner_he, o.he_target, o.he_face, w.face, w.pos);
+    exclusive_scan(w.pos, (uint32_t)(nidx + 1), total, scan_temp, s);
+    k_cw_adjacent<<<hgrid(nidx), kHBlock, 0, s>>>(nidx, o.corner_he, o.he_face, w.pos, w.adj);
+    k_cw_counts<<<hgrid(nf), kHBlock, 0, s>>>(nf, foff, w.pos, w.adj_n);
+}
+
+void launch_to_float(const double* x, uint64_t n, float* out, cudaStream_t s)
+{
+    g_launches++;
+    k_to_float<<<hgrid(n), kHBlock, 0, s>>>(x, n, out);
+}
+
 } // namespace mcgpu

@@ -65,4 +65,23 @@ void launch_hmesh_edges(const HmeshInput& in, HmeshTable& t, HmeshScratch& w, cu
 void launch_hmesh_build(const HmeshInput& in, const HmeshTable& t, HmeshScratch& w, HmeshOut& o, uint32_t ne,
     cudaStream_t s);
 
+// A connected component's arrays as mcGetConnectedComponentData serialises
+// them (frontend.cpp:2006-2832) from its halfedge mesh: vertices around each
+// face (the targets of its halfedges, hmesh.cpp:705-733), the faces across
+// its halfedges (get_faces_around_face, hmesh.cpp:796-818) with their
+// counts. Edges are he_target itself (vertex(e, 0) / vertex(e, 1) are the
+// targets of halfedges 2e / 2e + 1, hmesh.cpp:234-256).
+struct CcWireOut {
+    uint32_t* face;    // [nidx]
+    uint32_t* pos;     // [nidx + 1] exclusive scan of "a face across this corner's halfedge"
+    uint32_t* adj;     // [pos[nidx]]
+    uint32_t* adj_n;   // [nf]
+};
+size_t cc_wire_scan_bytes(uint64_t nidx);
+// returns the adjacency count through *total (a readback)
+void launch_cc_wire(const HmeshOut& o, const uint32_t* foff, uint32_t nf, uint64_t nidx, CcWireOut& w,
+    uint32_t* scan_temp, uint32_t* total, cudaStream_t s);
+// static_cast<float> of n doubles (IEEE round to nearest)
+void launch_to_float(const double* x, uint64_t n, float* out, cudaStream_t s);
+
 } // namespace mcgpu

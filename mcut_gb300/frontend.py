@@ -179,6 +179,32 @@ class Context:
                        v_he=g(L.DATA_VERTEX_HE, np.uint32))
         return out
 
+    def cc_wire(self, cc, device: bool = False) -> dict:
+        """A connected component's arrays as mcGetConnectedComponentData
+        serialises them (frontend.cpp:2006-2832), computed on the device from
+        the component's halfedge mesh. cc: dict(v=double vertices [V,3],
+        f=indices in the component's corner order, fs=sizes or None). ->
+        dict(status, face, adjsize, adj, edge, vf)."""
+        ptr = (lambda a: a.data_ptr()) if device else (lambda a: a.ctypes.data)
+        v = cc["v"] if device else np.ascontiguousarray(cc["v"], dtype=np.float64)
+        f = cc["f"] if device else np.ascontiguousarray(cc["f"], dtype=np.uint32)
+        fs = cc.get("fs")
+        if fs is not None and not device:
+            fs = np.ascontiguousarray(fs, dtype=np.uint32)
+        nv = int(v.shape[0])
+        nf = int(fs.shape[0]) if fs is not None else int(f.shape[0] // 3)
+        cm = L.Mesh(ptr(v), ptr(f) if nf else None, None if fs is None else ptr(fs), nv, nf)
+        rep = L.HmeshReport()
+        L.check(self._lib.mcgpu_halfedge_mesh(self._h, L.DEVICE_POINTERS if device else 0, C.byref(cm),
+                                              C.byref(rep)), "mcgpu_halfedge_mesh")
+        out = dict(status=rep.status)
+        if rep.status in (L.HMESH_OK, L.HMESH_TOO_SMALL, L.HMESH_COMPONENTS):
+            g = lambda q, dt: self._get(q, dt, 1).reshape(-1)  # noqa: E731
+            out.update(face=g(L.DATA_CC_FACE, np.uint32), adjsize=g(L.DATA_CC_FACE_ADJACENT_FACE_SIZE, np.uint32),
+                       adj=g(L.DATA_CC_FACE_ADJACENT_FACE, np.uint32), edge=g(L.DATA_CC_EDGE, np.uint32),
+                       vf=g(L.DATA_CC_VERTEX_FLOAT, np.float32).reshape(-1, 3))
+        return out
+
     def memory(self) -> dict:
         """Device bytes the context's pool holds and its cap (0: none)."""
         held, cap = C.c_uint64(0), C.c_uint64(0)

@@ -423,6 +423,75 @@ def dispatch(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE, helpers: in
     return dict(result=rc, ccs=info[:ncc.value].copy(), n_ivtx=int(niv.value))
 
 
+class CcWire(C.Structure):
+    _fields_ = [("type", C.c_int32), ("nv", C.c_uint32), ("nf", C.c_uint32), ("nidx", C.c_uint32),
+                ("nadj", C.c_uint32), ("ne", C.c_uint32), ("vd", C.POINTER(C.c_double)),
+                ("vf", C.POINTER(C.c_float)), ("face", C.POINTER(C.c_uint32)), ("fsize", C.POINTER(C.c_uint32)),
+                ("adj", C.POINTER(C.c_uint32)), ("adjsize", C.POINTER(C.c_uint32)), ("edge", C.POINTER(C.c_uint32))]
+
+
+def cc_wire(src, cut, flags: int = MC_DISPATCH_VERTEX_ARRAY_DOUBLE):
+    """Full reference mcDispatch, then every connected component's arrays as
+    mcGetConnectedComponentData returns them (frontend.cpp:2006-2832):
+    (result, [dict(type, vd, vf, face, fsize, adj, adjsize, edge)])."""
+    lib, _, _ = _lib("ref")
+    lib.ref_cc_wire.restype = C.c_int
+    lib.ref_cc_wire.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                C.c_uint32, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.POINTER(CcWire))]
+    lib.ref_cc_wire_free.argtypes = [C.POINTER(CcWire), C.c_int]
+    fin = bool(flags & MC_DISPATCH_VERTEX_ARRAY_FLOAT)
+    ks, sa = _mesh_args(src, fin)
+    kc, ca = _mesh_args(cut, fin)
+    n = C.c_int(0)
+    w = C.POINTER(CcWire)()
+    with tempfile.TemporaryDirectory() as td:
+        rc = lib.ref_cc_wire(*sa, *ca, int(flags), td.encode(), C.byref(n), C.byref(w))
+    del ks, kc
+    out = []
+    for i in range(n.value):
+        c = w[i]
+        out.append(dict(type=int(c.type), vd=_arr(c.vd, 3 * c.nv, np.float64).reshape(-1, 3),
+                        vf=_arr(c.vf, 3 * c.nv, np.float32).reshape(-1, 3), face=_arr(c.face, c.nidx, np.uint32),
+                        fsize=_arr(c.fsize, c.nf, np.uint32), adj=_arr(c.adj, c.nadj, np.uint32),
+                        adjsize=_arr(c.adjsize, c.nf, np.uint32), edge=_arr(c.edge, 2 * c.ne, np.uint32)))
+    if n.value:
+        lib.ref_cc_wire_free(w, n.value)
+    return rc, out
+
+
+def cc_corners(face, fsize):
+    """A component's faces in its halfedge mesh's corner order: the serialised
+    face lists are the targets of each face's halfedges (get_vertices_around_face,
+    hmesh.cpp:705-733), so corner i of the mesh is serialised entry i - 1."""
+    off = np.concatenate([[0], np.cumsum(fsize.astype(np.int64))])
+    out = np.empty_like(face)
+    for i in range(len(fsize)):
+        a, b = off[i], off[i + 1]
+        out[a:b] = np.roll(face[a:b], 1)
+    return out
+
+
+def cc_wire_of_hmesh(h, fsize, vd):
+    """Restatement of the wire arrays from a halfedge mesh (oracle.hmesh's dict
+    over a component's faces in corner order): vertices around each face (the
+    targets of its corner halfedges), the faces across each of its halfedges
+    that have one (get_faces_around_face, hmesh.cpp:796-818) with their counts,
+    each edge's vertex(e, 0) / vertex(e, 1) (the targets of halfedges 2e and
+    2e + 1, hmesh.cpp:234-256), and the float vertices (static_cast<float>)."""
+    ch = h["corner_he"].astype(np.int64)
+    face = h["he_target"][ch]
+    across = h["he_face"][ch ^ 1]
+    off = np.concatenate([[0], np.cumsum(fsize.astype(np.int64))])
+    fid = np.repeat(np.arange(len(fsize)), fsize.astype(np.int64))
+    keep = across >= 0
+    adj = across[keep].astype(np.uint32)
+    adjsize = np.bincount(fid[keep], minlength=len(fsize)).astype(np.uint32)
+    edge = h["he_target"].astype(np.uint32)  # 2e then 2e + 1: vertex(e, 0), vertex(e, 1)
+    return dict(face=face.astype(np.uint32), adj=adj, adjsize=adjsize, edge=edge,
+                vf=np.asarray(vd, dtype=np.float64).astype(np.float32))
+
+
 HM_OK, HM_FACE_SIZE, HM_INDEX_RANGE, HM_DUPLICATE_INDEX, HM_NON_MANIFOLD, HM_TOO_SMALL, HM_COMPONENTS = range(7)
 
 

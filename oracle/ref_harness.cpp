@@ -19,6 +19,9 @@
 //                   returning status and per-CC type / vertex / face counts,
 //                   plus the intersection-point count read back from the
 //                   reference's own verbose dumps (kernel.cpp:1736-1738,3260-3266).
+//   ref_cc_wire   : the full public API, then each connected component's
+//                   arrays as mcGetConnectedComponentData returns them
+//                   (vertices, faces, face sizes, face adjacency, edges).
 //   ref_hmesh     : one mesh's halfedge mesh as the reference builds it (its
 //                   own hmesh_t::add_vertex / add_face, preceded by the face
 //                   checks of client_input_arrays_to_hmesh, preproc.cpp:390-460)
@@ -430,6 +433,99 @@ extern "C" int ref_dispatch(const void* sv, const uint32_t* sf, const uint32_t* 
     if (workdir && chdir(cwd) != 0)
         return -1002;
     return (int)err;
+}
+
+// One connected component as mcGetConnectedComponentData hands it to the
+// caller (frontend.cpp:2006-2832): vertices as doubles and floats, faces
+// (vertices around each face) with their sizes, the faces around each face
+// with their counts, and the edges' vertex pairs.
+struct cc_wire {
+    int32_t type;
+    uint32_t nv, nf, nidx, nadj, ne;
+    double* vd;
+    float* vf;
+    uint32_t *face, *fsize, *adj, *adjsize, *edge;
+};
+
+template <typename T>
+static T* cc_query(McContext ctx, McConnectedComponent cc, McFlags q, uint32_t* count)
+{
+    McSize nb = 0;
+    if (mcGetConnectedComponentData(ctx, cc, q, 0, NULL, &nb) != MC_NO_ERROR)
+        return nullptr;
+    T* p = (T*)malloc(nb ? nb : sizeof(T));
+    if (nb && mcGetConnectedComponentData(ctx, cc, q, nb, p, NULL) != MC_NO_ERROR) {
+        free(p);
+        return nullptr;
+    }
+    *count = (uint32_t)(nb / sizeof(T));
+    return p;
+}
+
+// Full public-API dispatch, then every connected component's wire arrays
+// through the reference's own mcGetConnectedComponentData. *out: n_cc
+// entries (free with ref_cc_wire_free).
+extern "C" int ref_cc_wire(const void* sv, const uint32_t* sf, const uint32_t* sfs, uint32_t nsv, uint32_t nsf,
+    const void* cv, const uint32_t* cf, const uint32_t* cfs, uint32_t ncv, uint32_t ncf, uint32_t flags,
+    const char* workdir, int* n_cc, cc_wire** out)
+{
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd))
+        return -1000;
+    if (workdir && chdir(workdir) != 0)
+        return -1001;
+    *n_cc = 0;
+    *out = nullptr;
+    McContext ctx = MC_NULL_HANDLE;
+    McResult err = mcCreateContext(&ctx, MC_NULL_HANDLE);
+    if (err == MC_NO_ERROR)
+        err = mcDispatch(ctx, flags, sv, sf, sfs, nsv, nsf, cv, cf, cfs, ncv, ncf);
+    if (err == MC_NO_ERROR) {
+        McUint32 n = 0;
+        mcGetConnectedComponents(ctx, MC_CONNECTED_COMPONENT_TYPE_ALL, 0, NULL, &n);
+        std::vector<McConnectedComponent> ccs(n);
+        if (n)
+            mcGetConnectedComponents(ctx, MC_CONNECTED_COMPONENT_TYPE_ALL, n, ccs.data(), NULL);
+        cc_wire* w = (cc_wire*)calloc(n ? n : 1, sizeof(cc_wire));
+        for (McUint32 i = 0; i < n; ++i) {
+            McConnectedComponentType t;
+            mcGetConnectedComponentData(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_TYPE, sizeof(t), &t, NULL);
+            w[i].type = (int32_t)t;
+            uint32_t k = 0;
+            w[i].vd = cc_query<double>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_VERTEX_DOUBLE, &k);
+            w[i].nv = k / 3;
+            w[i].vf = cc_query<float>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_VERTEX_FLOAT, &k);
+            w[i].face = cc_query<uint32_t>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_FACE, &w[i].nidx);
+            w[i].fsize = cc_query<uint32_t>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_FACE_SIZE, &w[i].nf);
+            w[i].adj = cc_query<uint32_t>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_FACE_ADJACENT_FACE, &w[i].nadj);
+            w[i].adjsize = cc_query<uint32_t>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_FACE_ADJACENT_FACE_SIZE, &k);
+            w[i].edge = cc_query<uint32_t>(ctx, ccs[i], MC_CONNECTED_COMPONENT_DATA_EDGE, &k);
+            w[i].ne = k / 2;
+        }
+        *n_cc = (int)n;
+        *out = w;
+        if (n)
+            mcReleaseConnectedComponents(ctx, 0, NULL);
+    }
+    if (ctx != MC_NULL_HANDLE)
+        mcReleaseContext(ctx);
+    if (workdir && chdir(cwd) != 0)
+        return -1002;
+    return (int)err;
+}
+
+extern "C" void ref_cc_wire_free(cc_wire* w, int n)
+{
+    for (int i = 0; i < n; ++i) {
+        free(w[i].vd);
+        free(w[i].vf);
+        free(w[i].face);
+        free(w[i].fsize);
+        free(w[i].adj);
+        free(w[i].adjsize);
+        free(w[i].edge);
+    }
+    free(w);
 }
 
 // One mesh's halfedge mesh and input checks, step for step as the
