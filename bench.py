@@ -158,9 +158,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload():
+def make_workload(name="c2"):
+    """C2x16 (the headline pair) or C3x16 (the coplanar lattice cube)."""
     from mcut_gb300 import meshgen
-    return meshgen.sphere_heightfield(16.0)
+    return meshgen.cube_coplanar(16.0) if name == "c3" else meshgen.sphere_heightfield(16.0)
 
 
 def dist_init(args):
@@ -233,7 +234,7 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_single():
+def run_single(workload="c2"):
     """Two dispatches of the workload from device-resident inputs: the launches
     of the second one are what a profiler capture should select (-s skips the
     first dispatch's launches)."""
@@ -241,7 +242,7 @@ def run_single():
     import torch
     from mcut_gb300 import Context, recentre
     from mcut_gb300 import _lib as L
-    src, cut = make_workload()
+    src, cut = make_workload(workload)
     sx, cx, eps = recentre(src, cut)
     ctx = Context(0)
     lib = L.load()
@@ -833,12 +834,14 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (4096 pairs) and served (request stream) measurements")
     ap.add_argument("--single", action="store_true",
                     help="one warm-up dispatch + one dispatch of the workload, nothing else (for ncu captures)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="the pair --single dispatches (C2x16 or C3x16)")
     ap.add_argument("--single-host", action="store_true",
                     help="the same through the e2e call: host arrays in internal coordinates (for ncu captures)")
     args = ap.parse_args()
     world, rank, local = dist_init(args)
     if args.single:
-        run_single()
+        run_single(args.workload)
     elif args.single_host:
         run_single_host()
     elif args.impl == "reference":
