@@ -10,7 +10,7 @@
  * component of its own), and whether the mesh is closed (mesh_is_closed,
  * preproc.cpp:1957-1994).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for a device edge table and validity
+ * TEST INFRASTRUCTURE ONLY: the oracle for the device edge table and validity
  * pass; the product library never links it. tests/test_hmesh_oracle.py pins
  * every array against the reference's own hmesh_t (oracle/ref_harness.cpp).
  *

@@ -1,7 +1,7 @@
 /*
  * Plain-C restatement of the MCUT (v1.2.0) intersection front end.
  *
- * TEST INFRASTRUCTURE ONLY. It is the checker the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY. It is the oracle the CUDA path is compared
  * against and the CPU baseline that bench.py times; the product library never
  * links, loads or calls it.
  *
