@@ -277,6 +277,64 @@ static __device__ __noinline__ int orient3d_exact_sign(const double* pa, const d
     return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
 }
 
+// Shewchuk's adaptive stages B and C (orient3dadapt, shewchuk.c:1962-2085),
+// between the fp64 filter and the full exact expansion. B: the determinant of
+// the rounded differences as an exact expansion (three 2x2 minors, each
+// scaled by a z difference, summed); its estimate decides past
+// o3derrboundB * permanent, and when all nine differences were exact (zero
+// tails) the expansion is the determinant itself, so its top component's
+// sign is the exact sign. C: the tails' first-order terms added to the
+// estimate, deciding past o3derrboundC * permanent + resulterrbound * |det|
+// (shewchuk.c:394-400 for the bounds, epsilon = 2^-53). Returns 2 when
+// neither decides. Same comparisons as the reference (>=), whose value's sign
+// is what it reads.
+static __device__ __noinline__ int orient3d_sign_bc(const double* pa, const double* pb, const double* pc,
+    const double* pd, double perm)
+{
+    const double EPS = 1.1102230246251565e-16;
+    const double O3D_B = (3.0 + 28.0 * EPS) * EPS, O3D_C = (26.0 + 288.0 * EPS) * EPS * EPS,
+                 RES = (3.0 + 8.0 * EPS) * EPS;
+    const double adx = pa[0] - pd[0], bdx = pb[0] - pd[0], cdx = pc[0] - pd[0];
+    const double ady = pa[1] - pd[1], bdy = pb[1] - pd[1], cdy = pc[1] - pd[1];
+    const double adz = pa[2] - pd[2], bdz = pb[2] - pd[2], cdz = pc[2] - pd[2];
+    double bc[4], ca[4], ab[4], adet[8], bdet[8], cdet[8], abdet[16], fin[24];
+    auto minor2 = [](double p, double q, double r, double s, double* o) { // p q - r s, exactly
+        double a1, a0, b1, b0;
+        two_product(p, q, a1, a0);
+        two_product(r, s, b1, b0);
+        two_two_diff(a1, a0, b1, b0, o);
+    };
+    minor2(bdx, cdy, cdx, bdy, bc);
+    minor2(cdx, ady, adx, cdy, ca);
+    minor2(adx, bdy, bdx, ady, ab);
+    const int al = scale_expansion_zeroelim(4, bc, adz, adet);
+    const int bl = scale_expansion_zeroelim(4, ca, bdz, bdet);
+    const int cl = scale_expansion_zeroelim(4, ab, cdz, cdet);
+    const int abl = fast_expansion_sum_zeroelim(al, adet, bl, bdet, abdet);
+    const int n = fast_expansion_sum_zeroelim(abl, abdet, cl, cdet, fin);
+    double det = fin[0];
+    for (int i = 1; i < n; ++i) det += fin[i];
+    double eb = O3D_B * perm;
+    if (det >= eb || -det >= eb) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+    const double adxt = two_diff_tail(pa[0], pd[0], adx), bdxt = two_diff_tail(pb[0], pd[0], bdx),
+                 cdxt = two_diff_tail(pc[0], pd[0], cdx);
+    const double adyt = two_diff_tail(pa[1], pd[1], ady), bdyt = two_diff_tail(pb[1], pd[1], bdy),
+                 cdyt = two_diff_tail(pc[1], pd[1], cdy);
+    const double adzt = two_diff_tail(pa[2], pd[2], adz), bdzt = two_diff_tail(pb[2], pd[2], bdz),
+                 cdzt = two_diff_tail(pc[2], pd[2], cdz);
+    if (adxt == 0.0 && bdxt == 0.0 && cdxt == 0.0 && adyt == 0.0 && bdyt == 0.0 && cdyt == 0.0 && adzt == 0.0
+        && bdzt == 0.0 && cdzt == 0.0) {
+        const double top = fin[n - 1];
+        return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
+    }
+    eb = O3D_C * perm + RES * fabs(det);
+    det += (adz * ((bdx * cdyt + cdy * bdxt) - (bdy * cdxt + cdx * bdyt)) + adzt * (bdx * cdy - bdy * cdx))
+        + (bdz * ((cdx * adyt + ady * cdxt) - (cdy * adxt + adx * cdyt)) + bdzt * (cdx * ady - cdy * adx))
+        + (cdz * ((adx * bdyt + bdy * adxt) - (ady * bdxt + bdx * adyt)) + cdzt * (adx * bdy - ady * bdx));
+    if (det >= eb || -det >= eb) return det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+    return 2;
+}
+
 // Which stage decided a sign (escalation counters).
 enum { ESC_F32 = 0, ESC_F64 = 1, ESC_EXACT = 2 };
 
@@ -403,6 +461,8 @@ __device__ __forceinline__ int orient3d_sign_filtered(const double* pa, const do
     if (det > eb) { stage = ESC_F64; return 1; }
     if (-det > eb) { stage = ESC_F64; return -1; }
     stage = ESC_EXACT;
+    const int s = orient3d_sign_bc(pa, pb, pc, pd, perm);
+    if (s != 2) return s;
     return orient3d_exact_sign(pa, pb, pc, pd);
 }
 
