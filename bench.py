@@ -440,7 +440,7 @@ def run_configs(ctx, lib, world, cpu=True):
                  "status": r.status_name, "pairs": int(r.num_pairs), "tests": int(r.num_tests),
                  "records": int(r.num_records), "ms_per_dispatch": float(np.median(t)),
                  "ms_per_dispatch_e2e": float(np.median(te)),
-                 "escalations": {"fp32_filter": esc[0], "fp64_filter": esc[1], "exact": esc[2],
+                 "escalations": {"fp32_filter": esc[0], "fp64_filter": esc[1], "adaptive_or_exact": esc[2],
                                  "rates": [e / tot for e in esc]}}
     out["hmesh"] = run_hmesh(ctx, cpu)
     out["cutpath"] = run_cutpath(ctx, cpu)

@@ -113,7 +113,8 @@ typedef struct mcgpu_summary {
     uint64_t num_pairs;       /* candidate (source face, cut face) pairs */
     uint64_t num_tests;       /* culled edge-face tests */
     uint64_t num_records;     /* intersection records (type '1', point inside) */
-    uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, exact stage
+    uint64_t escalations[3];  /* orient3d signs decided by: fp32 filter, fp64 filter, the later
+                                 stages (adaptive B/C, then the exact expansion)
                                  (in a batch, these four counts are the pair's own) */
     float stage_ms[8];        /* per-stage device time of the call (MCGPU_PROFILE; a batch's
                                  summaries all carry the batch's times) */
